@@ -1,0 +1,253 @@
+/*
+ * ref_harness.c -- drives the unmodified reference library as an oracle.
+ *
+ * Test infrastructure only. This translation unit includes the reference's
+ * own src/pumas.c (compiled from its source tree by oracle/Makefile, never
+ * copied) so that the per-context Box-Muller cache of the reference
+ * (`struct simulation_context`, pumas.c:426-477) can be reset between events.
+ * Each event then starts from the same state as with a freshly created
+ * context (pumas.c:2607-2609), which is what the GPU engine does.
+ *
+ * Random numbers come from the Philox stream of philox.h, keyed by
+ * (seed, event id); geometry comes from gpumas_geometry.h. Events are
+ * processed independently, optionally over OpenMP threads with one context
+ * per thread, as the reference's threading model prescribes
+ * (pumas.h:596-635).
+ */
+#include "pumas.c"
+
+#include <stdint.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "oracle.h"
+#include "philox.h"
+
+/* The loaded physics shared by all calls. */
+static struct pumas_physics * ref_physics = NULL;
+
+/* A medium with an optional uniform density override. */
+struct ref_medium {
+        struct pumas_medium api;
+        double density;
+};
+
+/* Per event data stored in the context's user memory. */
+struct ref_event {
+        struct oracle_stream stream;
+        const struct gpumas_geometry * geometry;
+        struct ref_medium * media;
+        int steps;
+};
+
+static double ref_locals(struct pumas_medium * medium,
+    struct pumas_state * state, struct pumas_locals * locals)
+{
+        (void)state;
+        const struct ref_medium * m = (const struct ref_medium *)medium;
+        locals->density = m->density;
+        return 0.;
+}
+
+static enum pumas_step ref_medium_cb(struct pumas_context * context,
+    struct pumas_state * state, struct pumas_medium ** medium_ptr,
+    double * step_ptr)
+{
+        struct ref_event * data = context->user_data;
+        const int m = gpumas_geometry_locate(data->geometry, state->position);
+        if (medium_ptr != NULL)
+                *medium_ptr = (m < 0) ? NULL : &data->media[m].api;
+        if (step_ptr != NULL) {
+                const double sgn =
+                    (context->mode.direction == PUMAS_MODE_FORWARD) ? 1. : -1.;
+                const double u[3] = { sgn * state->direction[0],
+                        sgn * state->direction[1], sgn * state->direction[2] };
+                *step_ptr = gpumas_geometry_step(
+                    data->geometry, state->position, u, m);
+                data->steps++;
+        }
+        return PUMAS_STEP_CHECK;
+}
+
+static double ref_random(struct pumas_context * context)
+{
+        struct ref_event * data = context->user_data;
+        return oracle_stream_draw(&data->stream);
+}
+
+/* Create the physics from a MDF and dump it. */
+int oracle_ref_physics_create(
+    const char * mdf, const char * dedx, const char * dump_path)
+{
+        pumas_error_handler_set(NULL);
+        struct pumas_physics * physics = NULL;
+        enum pumas_return rc = pumas_physics_create(
+            &physics, PUMAS_PARTICLE_MUON, mdf, dedx, NULL);
+        if (rc != PUMAS_RETURN_SUCCESS) return rc;
+        FILE * stream = fopen(dump_path, "wb");
+        if (stream == NULL) {
+                pumas_physics_destroy(&physics);
+                return PUMAS_RETURN_PATH_ERROR;
+        }
+        rc = pumas_physics_dump(physics, stream);
+        fclose(stream);
+        pumas_physics_destroy(&physics);
+        return rc;
+}
+
+/* Load a physics dump as the oracle's physics. */
+int oracle_ref_load(const char * dump_path)
+{
+        pumas_error_handler_set(NULL);
+        if (ref_physics != NULL) pumas_physics_destroy(&ref_physics);
+        FILE * stream = fopen(dump_path, "rb");
+        if (stream == NULL) return PUMAS_RETURN_PATH_ERROR;
+        const enum pumas_return rc = pumas_physics_load(&ref_physics, stream);
+        fclose(stream);
+        return rc;
+}
+
+int oracle_ref_material_index(const char * name, int * index)
+{
+        if (ref_physics == NULL) return PUMAS_RETURN_PHYSICS_ERROR;
+        return pumas_physics_material_index(ref_physics, name, index);
+}
+
+/* Tabulated properties, for known answer tests (pumas.h property API). */
+int oracle_ref_property(int property, int scheme, int material,
+    double kinetic, double * value)
+{
+        if (ref_physics == NULL) return PUMAS_RETURN_PHYSICS_ERROR;
+        switch (property) {
+        case 0:
+                return pumas_physics_property_range(
+                    ref_physics, scheme, material, kinetic, value);
+        case 1:
+                return pumas_physics_property_proper_time(
+                    ref_physics, scheme, material, kinetic, value);
+        case 2:
+                return pumas_physics_property_kinetic_energy(
+                    ref_physics, scheme, material, kinetic, value);
+        case 3:
+                return pumas_physics_property_stopping_power(
+                    ref_physics, scheme, material, kinetic, value);
+        case 4:
+                return pumas_physics_property_energy_straggling(
+                    ref_physics, material, kinetic, value);
+        case 5:
+                return pumas_physics_property_elastic_cutoff_angle(
+                    ref_physics, material, kinetic, value);
+        case 6:
+                return pumas_physics_property_elastic_path(
+                    ref_physics, material, kinetic, value);
+        case 7:
+                return pumas_physics_property_transport_path(
+                    ref_physics, scheme, material, kinetic, value);
+        case 8:
+                return pumas_physics_property_cross_section(
+                    ref_physics, material, kinetic, value);
+        default:
+                return PUMAS_RETURN_INDEX_ERROR;
+        }
+}
+
+int oracle_ref_max_threads(void)
+{
+#ifdef _OPENMP
+        return omp_get_max_threads();
+#else
+        return 1;
+#endif
+}
+
+/* Transport a batch of events, one transport call per event. */
+int oracle_ref_transport(const struct oracle_config * cfg,
+    const struct gpumas_geometry * geometry, int64_t n, uint64_t first_event,
+    struct oracle_state * states, struct oracle_result * results,
+    int n_threads)
+{
+        if (ref_physics == NULL) return PUMAS_RETURN_PHYSICS_ERROR;
+        pumas_error_handler_set(NULL);
+
+        struct ref_medium * media =
+            calloc(geometry->n_media > 0 ? geometry->n_media : 1,
+                sizeof(*media));
+        if (media == NULL) return PUMAS_RETURN_MEMORY_ERROR;
+        int i;
+        for (i = 0; i < geometry->n_media; i++) {
+                media[i].api.material = geometry->media[i].material;
+                media[i].density = geometry->media[i].density;
+                media[i].api.locals =
+                    (media[i].density > 0.) ? &ref_locals : NULL;
+        }
+
+        int rc_all = PUMAS_RETURN_SUCCESS;
+#ifdef _OPENMP
+        if (n_threads <= 0) n_threads = omp_get_max_threads();
+#pragma omp parallel num_threads(n_threads)
+#endif
+        {
+                struct pumas_context * context = NULL;
+                const int rc = pumas_context_create(
+                    &context, ref_physics, sizeof(struct ref_event));
+                if (rc != PUMAS_RETURN_SUCCESS) {
+#ifdef _OPENMP
+#pragma omp atomic write
+#endif
+                        rc_all = rc;
+                } else {
+                        context->medium = &ref_medium_cb;
+                        context->random = &ref_random;
+                        context->mode.energy_loss = cfg->energy_loss;
+                        context->mode.decay = cfg->decay;
+                        context->mode.direction = cfg->direction;
+                        context->mode.scattering = cfg->scattering;
+                        context->event = cfg->event;
+                        context->limit.energy = cfg->limit_energy;
+                        context->limit.distance = cfg->limit_distance;
+                        context->limit.grammage = cfg->limit_grammage;
+                        context->limit.time = cfg->limit_time;
+                        context->accuracy = cfg->accuracy;
+                        struct ref_event * data = context->user_data;
+                        data->geometry = geometry;
+                        data->media = media;
+                        struct simulation_context * context_ =
+                            (struct simulation_context *)context;
+                        int64_t k;
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 256)
+#endif
+                        for (k = 0; k < n; k++) {
+                                data->stream.seed = cfg->seed;
+                                data->stream.event = first_event + k;
+                                data->stream.n = 0;
+                                data->stream.next = 0.;
+                                data->steps = 0;
+                                context_->randn_done = 0;
+                                context_->randn_next = 0.;
+
+                                enum pumas_event event = PUMAS_EVENT_NONE;
+                                struct pumas_medium * m[2] = { NULL, NULL };
+                                struct pumas_state * s =
+                                    (struct pumas_state *)(states + k);
+                                const enum pumas_return rck =
+                                    pumas_context_transport(
+                                        context, s, &event, m);
+                                struct oracle_result * r = results + k;
+                                r->event = event;
+                                r->medium_in = (m[0] == NULL) ? -1 :
+                                    (int)((struct ref_medium *)m[0] - media);
+                                r->medium_out = (m[1] == NULL) ? -1 :
+                                    (int)((struct ref_medium *)m[1] - media);
+                                r->status = rck;
+                                r->steps = data->steps;
+                                r->pad = 0;
+                                r->draws = data->stream.n;
+                        }
+                        pumas_context_destroy(&context);
+                }
+        }
+        free(media);
+        return rc_all;
+}
