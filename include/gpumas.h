@@ -1,0 +1,276 @@
+/*
+ * gpumas.h -- C ABI of the GB300 muon transport engine (libgpumas.so).
+ *
+ * This library runs the hot path of the reference library PUMAS 1.2.3,
+ * `pumas_context_transport` (pumas.h:1046-1048), on an NVIDIA GB300 GPU for
+ * whole batches of events: forward and backward Monte Carlo with CSDA, mixed
+ * or straggled energy loss, discrete energy losses (bremsstrahlung, pair
+ * production, photonuclear, delta rays), mixed Coulomb multiple scattering,
+ * decay weighting or randomisation and geometry stepping.
+ *
+ * The API mirrors pumas.h: the physics tables are the reference's own
+ * (produced by `pumas_physics_create` and serialised by
+ * `pumas_physics_dump`), contexts carry the same mode / event / limit /
+ * accuracy settings, and states use the layout of `struct pumas_state`. What
+ * differs is what a GPU needs instead of host callbacks:
+ *   - the medium callback is replaced by a geometry descriptor
+ *     (gpumas_geometry.h);
+ *   - the random callback is replaced by a Philox-4x32-10 stream keyed by
+ *     (seed, event id), see `gpumas_context.seed`;
+ *   - the transport call takes arrays of events.
+ *
+ * All functions return an `enum pumas_return` value (pumas.h:143-196) as an
+ * int. The library never exits the process; there is no CPU fallback, and
+ * every transport entry point returns PUMAS_RETURN_PHYSICS_ERROR-like codes
+ * (GPUMAS_RETURN_DEVICE_ERROR) if no CUDA device is usable.
+ */
+#ifndef GPUMAS_H
+#define GPUMAS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "gpumas_geometry.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Return codes: same values as enum pumas_return (pumas.h:143-196). */
+#define GPUMAS_RETURN_SUCCESS 0
+#define GPUMAS_RETURN_ACCURACY_ERROR 1
+#define GPUMAS_RETURN_END_OF_FILE 2
+#define GPUMAS_RETURN_DECAY_ERROR 3
+#define GPUMAS_RETURN_DENSITY_ERROR 4
+#define GPUMAS_RETURN_DIRECTION_ERROR 5
+#define GPUMAS_RETURN_INCOMPLETE_FILE 6
+#define GPUMAS_RETURN_INDEX_ERROR 7
+#define GPUMAS_RETURN_PHYSICS_ERROR 8
+#define GPUMAS_RETURN_INTERNAL_ERROR 9
+#define GPUMAS_RETURN_IO_ERROR 10
+#define GPUMAS_RETURN_FORMAT_ERROR 11
+#define GPUMAS_RETURN_MEDIUM_ERROR 12
+#define GPUMAS_RETURN_MEMORY_ERROR 13
+#define GPUMAS_RETURN_MODEL_ERROR 14
+#define GPUMAS_RETURN_MISSING_LIMIT 15
+#define GPUMAS_RETURN_MISSING_RANDOM 16
+#define GPUMAS_RETURN_PATH_ERROR 17
+#define GPUMAS_RETURN_RAISE_ERROR 18
+#define GPUMAS_RETURN_TOO_LONG 19
+#define GPUMAS_RETURN_UNDEFINED_MDF 20
+#define GPUMAS_RETURN_UNKNOWN_ELEMENT 21
+#define GPUMAS_RETURN_UNKNOWN_MATERIAL 22
+#define GPUMAS_RETURN_UNKNOWN_PARTICLE 23
+#define GPUMAS_RETURN_VALUE_ERROR 24
+/* Codes beyond the reference's: a CUDA call failed. */
+#define GPUMAS_RETURN_DEVICE_ERROR 64
+
+/* Modes and events: same values as enum pumas_mode and pumas_event. */
+#define GPUMAS_MODE_DISABLED -1
+#define GPUMAS_MODE_CSDA 0
+#define GPUMAS_MODE_MIXED 1
+#define GPUMAS_MODE_STRAGGLED 2
+#define GPUMAS_MODE_WEIGHTED 0
+#define GPUMAS_MODE_RANDOMISED 1
+#define GPUMAS_MODE_FORWARD 0
+#define GPUMAS_MODE_BACKWARD 1
+
+#define GPUMAS_EVENT_NONE 0
+#define GPUMAS_EVENT_LIMIT_ENERGY 1
+#define GPUMAS_EVENT_LIMIT_DISTANCE 2
+#define GPUMAS_EVENT_LIMIT_GRAMMAGE 4
+#define GPUMAS_EVENT_LIMIT_TIME 8
+#define GPUMAS_EVENT_LIMIT 15
+#define GPUMAS_EVENT_MEDIUM 16
+#define GPUMAS_EVENT_VERTEX_BREMSSTRAHLUNG 32
+#define GPUMAS_EVENT_VERTEX_PAIR_CREATION 64
+#define GPUMAS_EVENT_VERTEX_PHOTONUCLEAR 128
+#define GPUMAS_EVENT_VERTEX_DELTA_RAY 256
+#define GPUMAS_EVENT_VERTEX_DEL 480
+#define GPUMAS_EVENT_VERTEX_COULOMB 512
+#define GPUMAS_EVENT_VERTEX_DECAY 1024
+#define GPUMAS_EVENT_VERTEX 2016
+#define GPUMAS_EVENT_WEIGHT 2048
+
+/** A Monte Carlo state: same layout as struct pumas_state
+ * (pumas.h:289-309), so that arrays of either type can be passed. */
+struct gpumas_state {
+        double charge;
+        double energy;
+        double distance;
+        double grammage;
+        double time;
+        double weight;
+        double position[3];
+        double direction[3];
+        int decayed;
+};
+
+/** Per event outputs besides the state. */
+struct gpumas_result {
+        /** The transport end event (pumas_context_transport `event`). */
+        int event;
+        /** Start and end medium indices in the geometry (`media[2]`),
+         * -1 for no medium. */
+        int medium_in;
+        int medium_out;
+        /** The per event return code (pumas_context_transport's return). */
+        int status;
+        /** Number of geometric step proposals (medium callback calls with a
+         * step argument, pumas.c:3182, 5281). */
+        int steps;
+        int pad;
+        /** Number of random draws consumed. */
+        uint64_t draws;
+};
+
+/** Structure of arrays view of events in device memory. Every pointer
+ * holds `n` values; `result` may be NULL. */
+struct gpumas_soa {
+        double * charge;
+        double * energy;
+        double * distance;
+        double * grammage;
+        double * time;
+        double * weight;
+        double * position[3];
+        double * direction[3];
+        int * decayed;
+        struct gpumas_result * result;
+};
+
+/* ------------------------------------------------------------------------ */
+/* Physics.                                                                 */
+/* ------------------------------------------------------------------------ */
+
+/** Device image of the physics tables. */
+struct gpumas_physics;
+
+/**
+ * Load physics tables from the bytes of a `pumas_physics_dump` stream
+ * (pumas.c:2167-2196; replaces pumas_physics_load, pumas.h:948-949) and
+ * upload them to the current CUDA device. The dump must come from an LP64
+ * little-endian host (tag 13) with the default DCS models (SSR, SSR, DRSS)
+ * for muons; otherwise GPUMAS_RETURN_FORMAT_ERROR or
+ * GPUMAS_RETURN_MODEL_ERROR is returned.
+ */
+int gpumas_physics_load(
+    struct gpumas_physics ** physics, const void * dump, size_t size);
+
+/**
+ * Upload a live `struct pumas_physics` (returned by the reference's
+ * pumas_physics_create or pumas_physics_load, pumas.h:898-949) of this
+ * process. Same checks as gpumas_physics_load.
+ */
+int gpumas_physics_upload(
+    struct gpumas_physics ** physics, const void * pumas_physics);
+
+/** Release the device image (pumas_physics_destroy, pumas.h:908). */
+void gpumas_physics_destroy(struct gpumas_physics ** physics);
+
+/** Index of a material from its name (pumas_physics_material_index,
+ * pumas.h:1468-1469). */
+int gpumas_physics_material_index(const struct gpumas_physics * physics,
+    const char * name, int * index);
+
+/** Number of materials and elements, the cutoff and the particle mass. */
+int gpumas_physics_info(const struct gpumas_physics * physics,
+    int * n_materials, int * n_elements, double * cutoff, double * mass);
+
+/* ------------------------------------------------------------------------ */
+/* Contexts.                                                                */
+/* ------------------------------------------------------------------------ */
+
+/** Mode flags (struct pumas_context_mode, pumas.h:554-579). */
+struct gpumas_context_mode {
+        int energy_loss;
+        int decay;
+        int direction;
+        int scattering;
+};
+
+/** External limits (struct pumas_context_limit, pumas.h:582-594). */
+struct gpumas_context_limit {
+        double energy;
+        double distance;
+        double grammage;
+        double time;
+};
+
+/**
+ * A simulation context. The public fields have the meaning and defaults of
+ * struct pumas_context (pumas.h:636-672; defaults pumas.c:2592-2612):
+ * STRAGGLED energy loss, MIXED scattering, FORWARD, WEIGHTED decay,
+ * no stop event, null limits and an accuracy of 1E-02.
+ */
+struct gpumas_context {
+        struct gpumas_context_mode mode;
+        int event;
+        struct gpumas_context_limit limit;
+        double accuracy;
+        /** Key of the Philox random stream (replaces `random`). */
+        uint64_t seed;
+        /** A pointer to user memory of `extra_memory` bytes, or NULL. */
+        void * user_data;
+};
+
+/** Create a context (pumas_context_create, pumas.h:1214-1216). */
+int gpumas_context_create(struct gpumas_context ** context,
+    const struct gpumas_physics * physics, int extra_memory);
+
+/** Destroy a context and its device buffers (pumas_context_destroy). */
+void gpumas_context_destroy(struct gpumas_context ** context);
+
+/**
+ * Set the geometry (replaces the `medium` callback). The descriptor and its
+ * arrays are copied to the device; media materials are checked against the
+ * physics.
+ */
+int gpumas_context_geometry_set(
+    struct gpumas_context * context, const struct gpumas_geometry * geometry);
+
+/**
+ * Transport n events held in host memory (the batched form of
+ * pumas_context_transport, pumas.h:1046-1048). States are updated in place;
+ * `results` (n entries, may be NULL) receives the per event end event,
+ * media, return code and counters. Event k uses the random stream of event
+ * id `first_event + k`. The return value is GPUMAS_RETURN_SUCCESS if the
+ * configuration is valid and every event succeeded, the first failing
+ * event's code otherwise (context level checks mirror pumas.c:3120-3177).
+ */
+int gpumas_context_transport(struct gpumas_context * context, size_t n,
+    struct gpumas_state * states, struct gpumas_result * results,
+    uint64_t first_event);
+
+/**
+ * Transport n events held in device memory as a structure of arrays, on a
+ * CUDA stream (cudaStream_t, or NULL for the default stream). Asynchronous:
+ * only the configuration is checked before returning.
+ */
+int gpumas_context_transport_device(struct gpumas_context * context,
+    size_t n, const struct gpumas_soa * events, uint64_t first_event,
+    void * stream);
+
+/** Engine statistics of the last transport call on this context. */
+struct gpumas_stats {
+        /** Kernel launches of the call. */
+        int launches;
+        /** Total device time of the transport kernels, in ms. */
+        double kernel_ms;
+};
+int gpumas_context_stats(
+    const struct gpumas_context * context, struct gpumas_stats * stats);
+
+/* ------------------------------------------------------------------------ */
+/* Random stream.                                                           */
+/* ------------------------------------------------------------------------ */
+
+/** Fill `out` with draws first .. first + n - 1 of the stream of
+ * (seed, domain, event), computed on the device (for checking). */
+int gpumas_random_fill(uint64_t seed, uint32_t domain, uint64_t event,
+    uint64_t first, size_t n, double * out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GPUMAS_H */

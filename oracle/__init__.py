@@ -80,7 +80,8 @@ def make_geometry(kind, media, **kw):
     g.uniform_medium = int(kw.get("uniform_medium", 0))
     if "slab_z" in kw:
         z = np.ascontiguousarray(kw["slab_z"], dtype=np.float64)
-        sm = np.ascontiguousarray(kw["slab_medium"], dtype=np.int32)
+        sm = np.ascontiguousarray(
+            kw.get("slab_medium", kw.get("slab_media")), dtype=np.int32)
         keep += [z, sm]
         g.n_slabs = len(sm)
         g.slab_z = z.ctypes.data_as(ctypes.POINTER(ctypes.c_double))

@@ -1,0 +1,347 @@
+"""pumas_gb300 -- GB300 engine for the PUMAS muon transport hot path.
+
+Python mirror of the reference's transport API (include/pumas.h) over the C
+ABI of libgpumas.so (include/gpumas.h):
+
+* ``Physics``: the physics tables, loaded from a ``pumas_physics_dump``
+  stream as produced by the reference's ``pumas_physics_create`` (the
+  package ships one for the materials of data/materials.xml);
+* ``Context``: the ``pumas_context`` settings (``mode.energy_loss``,
+  ``mode.decay``, ``mode.direction``, ``mode.scattering``, ``event``,
+  ``limit.*``, ``accuracy``) plus a geometry descriptor and a Philox seed in
+  place of the medium and random callbacks;
+* ``Context.transport(states)``: ``pumas_context_transport`` over an array
+  of ``pumas_state`` records, on the GPU.
+
+There is no CPU fallback: if the CUDA library is not built or no device is
+usable, the calls raise.
+"""
+import ctypes
+import gzip
+import os
+
+import numpy as np
+
+from . import build as _build
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+DATA = os.path.join(HERE, "data")
+DEFAULT_DUMP = os.path.join(DATA, "muon.pumas.gz")
+
+# enum pumas_mode / pumas_event / pumas_return values (pumas.h:90-196).
+MODE_DISABLED, MODE_CSDA, MODE_MIXED, MODE_STRAGGLED = -1, 0, 1, 2
+MODE_WEIGHTED, MODE_RANDOMISED = 0, 1
+MODE_FORWARD, MODE_BACKWARD = 0, 1
+EVENT_NONE, EVENT_LIMIT_ENERGY, EVENT_LIMIT_DISTANCE = 0, 1, 2
+EVENT_LIMIT_GRAMMAGE, EVENT_LIMIT_TIME, EVENT_LIMIT = 4, 8, 15
+EVENT_MEDIUM = 16
+EVENT_VERTEX_BREMSSTRAHLUNG, EVENT_VERTEX_PAIR_CREATION = 32, 64
+EVENT_VERTEX_PHOTONUCLEAR, EVENT_VERTEX_DELTA_RAY = 128, 256
+EVENT_VERTEX_DEL, EVENT_VERTEX_COULOMB, EVENT_VERTEX_DECAY = 480, 512, 1024
+EVENT_VERTEX, EVENT_WEIGHT = 2016, 2048
+RETURN_SUCCESS, RETURN_ACCURACY_ERROR, RETURN_DECAY_ERROR = 0, 1, 3
+RETURN_DENSITY_ERROR, RETURN_DIRECTION_ERROR = 4, 5
+RETURN_INDEX_ERROR, RETURN_PHYSICS_ERROR, RETURN_INTERNAL_ERROR = 7, 8, 9
+RETURN_FORMAT_ERROR, RETURN_MEDIUM_ERROR, RETURN_MEMORY_ERROR = 11, 12, 13
+RETURN_MODEL_ERROR, RETURN_MISSING_LIMIT = 14, 15
+RETURN_UNKNOWN_MATERIAL, RETURN_VALUE_ERROR = 22, 24
+RETURN_DEVICE_ERROR = 64
+
+GEOMETRY_UNIFORM, GEOMETRY_SLABS, GEOMETRY_HEIGHTMAP = 0, 1, 2
+
+# struct pumas_state (pumas.h:289-309), padded to 8 bytes.
+STATE_DTYPE = np.dtype([
+    ("charge", "f8"), ("energy", "f8"), ("distance", "f8"),
+    ("grammage", "f8"), ("time", "f8"), ("weight", "f8"),
+    ("position", "f8", 3), ("direction", "f8", 3), ("decayed", "i4"),
+    ("pad", "i4")])
+RESULT_DTYPE = np.dtype([
+    ("event", "i4"), ("medium_in", "i4"), ("medium_out", "i4"),
+    ("status", "i4"), ("steps", "i4"), ("pad", "i4"), ("draws", "u8")])
+
+
+class PumasError(RuntimeError):
+    """A non-success return code of the engine."""
+
+    def __init__(self, code, where=""):
+        self.code = code
+        super().__init__("%s: return code %d" % (where, code))
+
+
+class _Medium(ctypes.Structure):
+    _fields_ = [("material", ctypes.c_int), ("density", ctypes.c_double)]
+
+
+class _Geometry(ctypes.Structure):
+    _fields_ = [
+        ("kind", ctypes.c_int), ("n_media", ctypes.c_int),
+        ("media", ctypes.POINTER(_Medium)),
+        ("uniform_medium", ctypes.c_int),
+        ("n_slabs", ctypes.c_int),
+        ("slab_z", ctypes.POINTER(ctypes.c_double)),
+        ("slab_medium", ctypes.POINTER(ctypes.c_int)),
+        ("hm_nx", ctypes.c_int), ("hm_ny", ctypes.c_int),
+        ("hm_x0", ctypes.c_double), ("hm_y0", ctypes.c_double),
+        ("hm_dx", ctypes.c_double), ("hm_dy", ctypes.c_double),
+        ("hm_z", ctypes.POINTER(ctypes.c_double)),
+        ("hm_below", ctypes.c_int), ("hm_above", ctypes.c_int),
+        ("hm_ztop", ctypes.c_double)]
+
+
+class _Mode(ctypes.Structure):
+    _fields_ = [("energy_loss", ctypes.c_int), ("decay", ctypes.c_int),
+                ("direction", ctypes.c_int), ("scattering", ctypes.c_int)]
+
+
+class _Limit(ctypes.Structure):
+    _fields_ = [("energy", ctypes.c_double), ("distance", ctypes.c_double),
+                ("grammage", ctypes.c_double), ("time", ctypes.c_double)]
+
+
+class _Context(ctypes.Structure):
+    _fields_ = [("mode", _Mode), ("event", ctypes.c_int), ("limit", _Limit),
+                ("accuracy", ctypes.c_double), ("seed", ctypes.c_uint64),
+                ("user_data", ctypes.c_void_p)]
+
+
+class _Stats(ctypes.Structure):
+    _fields_ = [("launches", ctypes.c_int), ("kernel_ms", ctypes.c_double)]
+
+
+class _Soa(ctypes.Structure):
+    _fields_ = [
+        ("charge", ctypes.c_void_p), ("energy", ctypes.c_void_p),
+        ("distance", ctypes.c_void_p), ("grammage", ctypes.c_void_p),
+        ("time", ctypes.c_void_p), ("weight", ctypes.c_void_p),
+        ("position", ctypes.c_void_p * 3),
+        ("direction", ctypes.c_void_p * 3),
+        ("decayed", ctypes.c_void_p), ("result", ctypes.c_void_p)]
+
+
+_lib = None
+
+
+def library(build=False):
+    """The loaded libgpumas.so (built first if `build`)."""
+    global _lib
+    if _lib is None:
+        if build:
+            _build.build()
+        if not os.path.exists(_build.LIB):
+            raise RuntimeError(
+                "libgpumas.so is not built (pumas_gb300.build.build())")
+        lib = ctypes.CDLL(_build.LIB)
+        vp, sz, i, d = ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int, \
+            ctypes.c_double
+        u64 = ctypes.c_uint64
+        pp = ctypes.POINTER(ctypes.c_void_p)
+        lib.gpumas_physics_load.argtypes = [pp, ctypes.c_char_p, sz]
+        lib.gpumas_physics_upload.argtypes = [pp, vp]
+        lib.gpumas_physics_destroy.argtypes = [pp]
+        lib.gpumas_physics_destroy.restype = None
+        lib.gpumas_physics_material_index.argtypes = [
+            vp, ctypes.c_char_p, ctypes.POINTER(i)]
+        lib.gpumas_physics_info.argtypes = [
+            vp, ctypes.POINTER(i), ctypes.POINTER(i), ctypes.POINTER(d),
+            ctypes.POINTER(d)]
+        lib.gpumas_context_create.argtypes = [
+            ctypes.POINTER(ctypes.POINTER(_Context)), vp, i]
+        lib.gpumas_context_destroy.argtypes = [
+            ctypes.POINTER(ctypes.POINTER(_Context))]
+        lib.gpumas_context_destroy.restype = None
+        lib.gpumas_context_geometry_set.argtypes = [
+            ctypes.POINTER(_Context), ctypes.POINTER(_Geometry)]
+        lib.gpumas_context_transport.argtypes = [
+            ctypes.POINTER(_Context), sz, vp, vp, u64]
+        lib.gpumas_context_transport_device.argtypes = [
+            ctypes.POINTER(_Context), sz, ctypes.POINTER(_Soa), u64, vp]
+        lib.gpumas_context_stats.argtypes = [
+            ctypes.POINTER(_Context), ctypes.POINTER(_Stats)]
+        lib.gpumas_random_fill.argtypes = [
+            u64, ctypes.c_uint32, u64, u64, sz, vp]
+        for f in ("gpumas_physics_load", "gpumas_physics_upload",
+                  "gpumas_physics_material_index", "gpumas_physics_info",
+                  "gpumas_context_create", "gpumas_context_geometry_set",
+                  "gpumas_context_transport",
+                  "gpumas_context_transport_device", "gpumas_context_stats",
+                  "gpumas_random_fill"):
+            getattr(lib, f).restype = i
+        _lib = lib
+    return _lib
+
+
+def _check(rc, where):
+    if rc != RETURN_SUCCESS:
+        raise PumasError(rc, where)
+
+
+def default_dump():
+    """Bytes of the shipped physics dump (StandardRock, Water, Air, Iron)."""
+    with gzip.open(DEFAULT_DUMP, "rb") as f:
+        return f.read()
+
+
+class Physics:
+    """Device physics tables (pumas_physics)."""
+
+    def __init__(self, dump=None):
+        if dump is None:
+            dump = default_dump()
+        lib = library()
+        self._lib = lib
+        self._ptr = ctypes.c_void_p()
+        _check(lib.gpumas_physics_load(ctypes.byref(self._ptr), dump,
+                                       len(dump)), "gpumas_physics_load")
+        nm, ne = ctypes.c_int(), ctypes.c_int()
+        cut, mass = ctypes.c_double(), ctypes.c_double()
+        lib.gpumas_physics_info(self._ptr, ctypes.byref(nm), ctypes.byref(ne),
+                                ctypes.byref(cut), ctypes.byref(mass))
+        self.n_materials, self.n_elements = nm.value, ne.value
+        self.cutoff, self.mass = cut.value, mass.value
+
+    def material_index(self, name):
+        idx = ctypes.c_int(-1)
+        _check(self._lib.gpumas_physics_material_index(
+            self._ptr, name.encode(), ctypes.byref(idx)),
+            "gpumas_physics_material_index")
+        return idx.value
+
+    def __del__(self):
+        if getattr(self, "_ptr", None):
+            self._lib.gpumas_physics_destroy(ctypes.byref(self._ptr))
+
+
+class Geometry:
+    """A geometry descriptor (include/gpumas_geometry.h).
+
+    `media` is a list of (material index, density in kg/m^3 or 0 for the
+    material's default)."""
+
+    def __init__(self, kind, media, **kw):
+        self._keep = []
+        g = _Geometry()
+        g.kind = kind
+        m = (_Medium * len(media))(*[_Medium(int(a), float(b))
+                                     for a, b in media])
+        self._keep.append(m)
+        g.n_media, g.media = len(media), m
+        g.uniform_medium = int(kw.get("medium", 0))
+        if kind == GEOMETRY_SLABS:
+            z = np.ascontiguousarray(kw["z"], dtype=np.float64)
+            sm = np.ascontiguousarray(kw["slab_media"], dtype=np.int32)
+            self._keep += [z, sm]
+            g.n_slabs = len(sm)
+            g.slab_z = z.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+            g.slab_medium = sm.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+        elif kind == GEOMETRY_HEIGHTMAP:
+            hz = np.ascontiguousarray(kw["heights"], dtype=np.float64)
+            self._keep.append(hz)
+            g.hm_ny, g.hm_nx = hz.shape
+            g.hm_x0, g.hm_y0 = kw["x0"], kw["y0"]
+            g.hm_dx, g.hm_dy = kw["dx"], kw["dy"]
+            g.hm_z = hz.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+            g.hm_below, g.hm_above = kw["below"], kw["above"]
+            g.hm_ztop = kw["ztop"]
+        self.c = g
+
+    @classmethod
+    def uniform(cls, material, density=0.):
+        return cls(GEOMETRY_UNIFORM, [(material, density)], medium=0)
+
+    @classmethod
+    def slabs(cls, z, materials, densities=None):
+        densities = densities or [0.] * len(materials)
+        media = list(zip(materials, densities))
+        return cls(GEOMETRY_SLABS, media, z=z,
+                   slab_media=list(range(len(materials))))
+
+    @classmethod
+    def heightmap(cls, heights, x0, y0, dx, dy, below, above, ztop):
+        media = [below, above]
+        return cls(GEOMETRY_HEIGHTMAP, media, heights=heights, x0=x0, y0=y0,
+                   dx=dx, dy=dy, below=0, above=1, ztop=ztop)
+
+
+def new_states(n):
+    """A zeroed array of pumas_state records with unit weight."""
+    s = np.zeros(n, dtype=STATE_DTYPE)
+    s["weight"] = 1.
+    return s
+
+
+class Context:
+    """A simulation context (pumas_context) on the GPU."""
+
+    def __init__(self, physics):
+        self.physics = physics
+        self._lib = physics._lib
+        self._ptr = ctypes.POINTER(_Context)()
+        _check(self._lib.gpumas_context_create(
+            ctypes.byref(self._ptr), physics._ptr, 0),
+            "gpumas_context_create")
+        self._c = self._ptr.contents
+        self.mode = self._c.mode
+        self.limit = self._c.limit
+        self.geometry = None
+
+    event = property(lambda self: self._c.event,
+                     lambda self, v: setattr(self._c, "event", int(v)))
+    accuracy = property(lambda self: self._c.accuracy,
+                        lambda self, v: setattr(self._c, "accuracy",
+                                                float(v)))
+    seed = property(lambda self: self._c.seed,
+                    lambda self, v: setattr(self._c, "seed", int(v)))
+
+    def set_geometry(self, geometry):
+        _check(self._lib.gpumas_context_geometry_set(
+            self._ptr, ctypes.byref(geometry.c)),
+            "gpumas_context_geometry_set")
+        self.geometry = geometry
+
+    def transport(self, states, first_event=0, check=False):
+        """Transport a copy of `states`; returns (states, results). With
+        `check`, a non-success per event return code raises."""
+        s = np.array(states, dtype=STATE_DTYPE, copy=True, order="C")
+        r = np.zeros(len(s), dtype=RESULT_DTYPE)
+        rc = self._lib.gpumas_context_transport(
+            self._ptr, len(s), s.ctypes.data, r.ctypes.data, first_event)
+        if rc != RETURN_SUCCESS and (check or rc >= RETURN_DEVICE_ERROR or
+                                     not np.any(r["status"] == rc)):
+            raise PumasError(rc, "gpumas_context_transport")
+        return s, r
+
+    def transport_raw(self, n, states_ptr, results_ptr, first_event=0):
+        """Transport n states at a host address (in place)."""
+        return self._lib.gpumas_context_transport(
+            self._ptr, n, states_ptr, results_ptr, first_event)
+
+    def transport_device(self, n, soa, first_event=0, stream=None):
+        """Transport n events of a device SoA (dict of device pointers)."""
+        c = _Soa()
+        for k in ("charge", "energy", "distance", "grammage", "time",
+                  "weight", "decayed"):
+            setattr(c, k, soa[k])
+        for k in range(3):
+            c.position[k] = soa["position"][k]
+            c.direction[k] = soa["direction"][k]
+        c.result = soa.get("result", None)
+        return self._lib.gpumas_context_transport_device(
+            self._ptr, n, ctypes.byref(c), first_event, stream)
+
+    def stats(self):
+        st = _Stats()
+        self._lib.gpumas_context_stats(self._ptr, ctypes.byref(st))
+        return {"launches": st.launches, "kernel_ms": st.kernel_ms}
+
+    def __del__(self):
+        if getattr(self, "_ptr", None):
+            self._lib.gpumas_context_destroy(ctypes.byref(self._ptr))
+
+
+def random_fill(seed, domain, event, first, n):
+    """Draws first .. first + n - 1 of a Philox stream, computed on the GPU."""
+    out = np.zeros(n, dtype=np.float64)
+    _check(library().gpumas_random_fill(seed, domain, event, first, n,
+                                        out.ctypes.data),
+           "gpumas_random_fill")
+    return out

@@ -1,0 +1,2837 @@
+/*
+ * gp_device.cuh -- device side muon transport physics for sm_103a.
+ *
+ * A GPU restatement of the reference transport (PUMAS 1.2.3, src/pumas.c):
+ * table interpolants, CEL / DEL / EHS samplers, Coulomb scattering, the
+ * default DCS models and the polar angle samplers. Floating point
+ * expressions keep the reference's evaluation order; the CUDA double
+ * precision libm differs from glibc by at most an ulp or two, which the
+ * parity tests bound. Differences in structure, all result preserving:
+ *
+ *   - no per context index cache in table lookups (pumas.c:4174-4210): the
+ *     cache never changes the bracketing index;
+ *   - per element constants come precomputed from the host (gp_internal.h);
+ *   - the FP32 DCS interpolation (pumas.c:11276-11346) uses
+ *     (float)log((double)x) and (float)exp((double)x), which agree with
+ *     glibc's logf / expf far more often than CUDA's single precision ones;
+ *   - the x87 extended precision of the Coulomb pole reduction
+ *     (pumas.c:7524-7683) is replaced by double precision. It only enters
+ *     the choice of the hard scatterer in compound materials and is skipped
+ *     altogether for single element ones, where the choice is forced;
+ *   - every rejection loop, unbounded in the reference (pumas.c:5839, 6115,
+ *     6241, 6918, 6973, 11208), has an iteration cap after which the event
+ *     stops with PUMAS_RETURN_INTERNAL_ERROR, so that no GPU thread can
+ *     spin forever.
+ */
+#ifndef GP_DEVICE_CUH
+#define GP_DEVICE_CUH
+
+#include <stdint.h>
+
+#include "gpumas.h"
+#include "gp_internal.h"
+
+#define GP_EPSILON_X 3E-03
+#define GP_STEP_MIN 1E-07
+#define GP_ALPHA_EM 7.2973525693E-03
+#define GP_HBAR_C 1.973269804E-16
+#define GP_ELECTRON_MASS 0.510998910E-03
+#define GP_ELECTRON_RADIUS 2.817940285E-15
+#define GP_PROTON_MASS 0.938272
+#define GP_NEUTRON_MASS 0.939565
+#define GP_PION_MASS 0.13957018
+#define GP_AVOGADRO 6.02214076E+23
+#define GP_PI 3.14159265358979323846
+#define GP_FLT_EPSILON 1.19209290E-07
+#define GP_DBL_EPSILON 2.2204460492503131E-16
+#define GP_DBL_MAX 1.7976931348623157E+308
+
+/* Iteration cap of the reference's unbounded rejection loops. */
+#define GP_MAX_REJECTIONS 100000
+
+#define GPD __device__ __forceinline__
+
+/* Transport settings of a launch (the public fields of pumas_context). */
+struct gp_config {
+        int energy_loss, decay, direction, scattering;
+        int event;
+        double limit_energy, limit_distance, limit_grammage, limit_time;
+        double accuracy;
+        uint64_t seed;
+};
+
+/* ------------------------------------------------------------------------ */
+/* Philox-4x32-10 stream, keyed by (seed, event id): draw n of an event     */
+/* uses block n / 2 of counter (block, 0, event), 64 bits per draw mapped   */
+/* to ((w >> 12) + 0.5) 2^-52.                                              */
+/* ------------------------------------------------------------------------ */
+GPD void gp_philox(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
+    uint32_t k0, uint32_t k1, uint32_t * out)
+{
+#pragma unroll
+        for (int round = 0; round < 10; round++) {
+                const uint32_t hi0 = __umulhi(0xD2511F53u, c0);
+                const uint32_t lo0 = 0xD2511F53u * c0;
+                const uint32_t hi1 = __umulhi(0xCD9E8D57u, c2);
+                const uint32_t lo1 = 0xCD9E8D57u * c2;
+                c0 = hi1 ^ c1 ^ k0;
+                c1 = lo1;
+                c2 = hi0 ^ c3 ^ k1;
+                c3 = lo0;
+                k0 += 0x9E3779B9u;
+                k1 += 0xBB67AE85u;
+        }
+        out[0] = c0;
+        out[1] = c1;
+        out[2] = c2;
+        out[3] = c3;
+}
+
+/* Exact map of a 64 bit word to ]0, 1[: 1.m - (1 - 2^-53). */
+GPD double gp_word_to_uniform(uint32_t lo, uint32_t hi)
+{
+        const uint64_t w = ((uint64_t)hi << 32) | lo;
+        const double one_m = __longlong_as_double(
+            (long long)(0x3FF0000000000000ull | (w >> 12)));
+        return __dsub_rn(one_m, 0x1.fffffffffffffp-1);
+}
+
+/* Per event state: the pumas_state, the per event part of the reference's
+ * simulation_context (pumas.c:426-477) and the random stream. */
+struct gp_event {
+        double charge, energy, distance, grammage, time, weight;
+        double pos[3], dir[3];
+        int decayed;
+        int step_first, step_event, step_foreseen;
+        double step_X_limit, step_invlb1;
+        int randn_done;
+        double randn_next;
+        double lifetime;
+        uint64_t id;
+        uint32_t n;
+        double rnext;
+        uint32_t k0, k1;
+        int steps;
+        int status;
+};
+
+GPD double gp_random(gp_event & e)
+{
+        double u;
+        if (e.n & 1u) {
+                u = e.rnext;
+        } else {
+                uint32_t x[4];
+                gp_philox(e.n >> 1, 0u, (uint32_t)e.id,
+                    (uint32_t)(e.id >> 32), e.k0, e.k1, x);
+                u = gp_word_to_uniform(x[0], x[1]);
+                e.rnext = gp_word_to_uniform(x[2], x[3]);
+        }
+        e.n++;
+        return u;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Tables (pumas.c:3644-4752).                                              */
+/* ------------------------------------------------------------------------ */
+GPD int gp_sch(int scheme) { return (scheme > 1) ? 1 : scheme; }
+GPD int gp_sch_el(int scheme) { return (scheme >= 1) ? 1 : 0; }
+
+/* table_index (pumas.c:4174-4233), bracketing from below. */
+GPD int gp_index(const gp_tables & T, const double * __restrict__ table,
+    double value)
+{
+        const int imax = T.n_energies - 1;
+        if (value < __ldg(table)) return -1;
+        if (value >= __ldg(table + imax)) return imax;
+        int i1 = 0, i2 = imax;
+        do {
+                const int i3 = (i1 + i2) >> 1;
+                if (value >= __ldg(table + i3))
+                        i1 = i3;
+                else
+                        i2 = i3;
+        } while (i2 - i1 >= 2);
+        return i1;
+}
+
+/* math_pchip_interpolate (pumas.c:4118-4125). */
+GPD double gp_pchip(double t, double p0, double p1, double m0, double m1)
+{
+        const double c2 = -3 * (p0 - p1) - 2 * m0 - m1;
+        const double c3 = 2 * (p0 - p1) + m0 + m1;
+        return p0 + t * (m0 + t * (c2 + t * c3));
+}
+
+/* table_interpolate_pchip (pumas.c:4146-4157). */
+GPD double gp_interpolate(const gp_tables & T, const double * __restrict__ X,
+    const double * __restrict__ Y, const double * __restrict__ M, double x)
+{
+        const int i1 = gp_index(T, X, x);
+        const int i2 = i1 + 1;
+        const double x1 = __ldg(X + i1);
+        const double dX = __ldg(X + i2) - x1;
+        const double t = (x - x1) / dX;
+        const double m1 = __ldg(M + i1) * dX;
+        const double m2 = (i2 > 1) ? __ldg(M + i2) * dX : m1;
+        return gp_pchip(t, __ldg(Y + i1), __ldg(Y + i2), m1, m2);
+}
+
+#define GP_ROW(s, m) ((long)((s) * T.n_materials + (m)) * T.n_energies)
+#define GP_MROW(m) ((long)(m) * T.n_energies)
+
+GPD double gp_cel_grammage(
+    const gp_tables & T, int scheme, int material, double kinetic)
+{
+        const int imax = T.n_energies - 1;
+        if (kinetic < __ldg(T.K)) return 0.;
+        const int s = gp_sch(scheme);
+        if (kinetic >= __ldg(T.K + imax)) {
+                const double a = __ldg(T.a_max + material);
+                const double b = __ldg(T.b_max + s * T.n_materials + material);
+                const double K0 = __ldg(T.K + imax);
+                const double K1 = a / b + T.mass;
+                return __ldg(T.X + GP_ROW(s, material) + imax) +
+                    1. / b * log((kinetic + K1) / (K0 + K1));
+        }
+        return gp_interpolate(T, T.K, T.X + GP_ROW(s, material),
+            T.X_dK + GP_ROW(s, material), kinetic);
+}
+
+GPD double gp_cel_grammage_as_time(
+    const gp_tables & T, int scheme, int material, double time)
+{
+        const int imax = T.n_energies - 1;
+        const int s = gp_sch(scheme);
+        const double * Tt = T.T + GP_ROW(s, material);
+        if (time < __ldg(Tt)) return 0.;
+        if (time >= __ldg(Tt + imax)) {
+                const double a = __ldg(T.a_max + material);
+                const double b = __ldg(T.b_max + s * T.n_materials + material);
+                const double E0 = __ldg(T.K + imax) + T.mass;
+                const double tmax = __ldg(Tt + imax);
+                const double r =
+                    E0 / (a + b * E0) * exp(a * (time - tmax) / T.mass);
+                const double kinetic = a * r / (1. - b * r) - T.mass;
+                const double K1 = a / b + T.mass;
+                return __ldg(T.X + GP_ROW(s, material) + imax) +
+                    1. / b * log((kinetic + K1) / (E0 - T.mass + K1));
+        }
+        return gp_interpolate(T, Tt, T.X + GP_ROW(s, material),
+            T.X_dT + GP_ROW(s, material), time);
+}
+
+GPD double gp_cel_proper_time(
+    const gp_tables & T, int scheme, int material, double kinetic)
+{
+        const int imax = T.n_energies - 1;
+        if (kinetic < __ldg(T.K)) return 0.;
+        const int s = gp_sch(scheme);
+        if (kinetic >= __ldg(T.K + imax)) {
+                const double a = __ldg(T.a_max + material);
+                const double b = __ldg(T.b_max + s * T.n_materials + material);
+                const double E0 = __ldg(T.K + imax) + T.mass;
+                const double E1 = kinetic + T.mass;
+                return __ldg(T.T + GP_ROW(s, material) + imax) +
+                    T.mass / a * log((E1 / E0) * (a + b * E0) / (a + b * E1));
+        }
+        return gp_interpolate(T, T.K, T.T + GP_ROW(s, material),
+            T.T_dK + GP_ROW(s, material), kinetic);
+}
+
+GPD double gp_cel_kinetic_energy(
+    const gp_tables & T, int scheme, int material, double grammage)
+{
+        const int imax = T.n_energies - 1;
+        const int s = gp_sch(scheme);
+        const double * X = T.X + GP_ROW(s, material);
+        if (grammage < __ldg(X)) return 0.;
+        if (grammage >= __ldg(X + imax)) {
+                const double a = __ldg(T.a_max + material);
+                const double b = __ldg(T.b_max + s * T.n_materials + material);
+                const double K0 = __ldg(T.K + imax);
+                const double K1 = a / b + T.mass;
+                return (K0 + K1) * exp(b * (grammage - __ldg(X + imax))) - K1;
+        }
+        return gp_interpolate(
+            T, X, T.K, T.K_dX + GP_ROW(s, material), grammage);
+}
+
+GPD double gp_cel_energy_loss(
+    const gp_tables & T, int scheme, int material, double kinetic)
+{
+        const int imax = T.n_energies - 1;
+        if (kinetic < __ldg(T.K)) return 0.;
+        const int s = gp_sch(scheme);
+        if (kinetic >= __ldg(T.K + imax)) {
+                return __ldg(T.a_max + material) +
+                    __ldg(T.b_max + s * T.n_materials + material) *
+                    (kinetic + T.mass);
+        }
+        return gp_interpolate(T, T.K, T.dE + GP_ROW(s, material),
+            T.dE_dK + GP_ROW(s, material), kinetic);
+}
+
+GPD double gp_cel_straggling(const gp_tables & T, int material, double kinetic)
+{
+        const int imax = T.n_energies - 1;
+        if (kinetic < __ldg(T.K)) return 0.;
+        const double Kmax = __ldg(T.K + imax);
+        if (kinetic >= Kmax) {
+                const double r = (kinetic + T.mass) / (Kmax + T.mass);
+                return __ldg(T.Omega + GP_MROW(material) + imax) * r * r;
+        }
+        return gp_interpolate(T, T.K, T.Omega + GP_MROW(material),
+            T.Omega_dK + GP_MROW(material), kinetic);
+}
+
+GPD double gp_del_cross_section(
+    const gp_tables & T, int material, double kinetic)
+{
+        const int imax = T.n_energies - 1;
+        if (kinetic < __ldg(T.K)) return 0.;
+        if (kinetic >= __ldg(T.K + imax))
+                return __ldg(T.CS + GP_MROW(material) + imax);
+        return gp_interpolate(T, T.K, T.CS + GP_MROW(material),
+            T.CS_dK + GP_MROW(material), kinetic);
+}
+
+GPD double gp_del_interaction_length(
+    const gp_tables & T, int material, double kinetic)
+{
+        const int imax = T.n_energies - 1;
+        if (kinetic < __ldg(T.K)) return 0.;
+        if (kinetic >= __ldg(T.K + imax)) {
+                const double k0 = __ldg(T.K + imax);
+                const double a0 = __ldg(T.a_max + material);
+                const double b0 = __ldg(T.b_max + T.n_materials + material);
+                const double cs = __ldg(T.CS + GP_MROW(material) + imax);
+                const double dZ =
+                    cs / b0 * log((a0 + b0 * (kinetic + T.mass)) /
+                                  (a0 + b0 * (k0 + T.mass)));
+                return __ldg(T.NI_in + GP_MROW(material) + imax) + dZ;
+        }
+        return gp_interpolate(T, T.K, T.NI_in + GP_MROW(material),
+            T.NI_in_dK + GP_MROW(material), kinetic);
+}
+
+GPD double gp_del_kinetic_from_interaction_length(
+    const gp_tables & T, int material, double nI)
+{
+        const int imax = T.n_energies - 1;
+        const double * NI = T.NI_in + GP_MROW(material);
+        if (nI < __ldg(NI)) return 0.;
+        if (nI >= __ldg(NI + imax)) {
+                const double k0 = __ldg(T.K + imax);
+                const double a0 = __ldg(T.a_max + material);
+                const double b0 = __ldg(T.b_max + T.n_materials + material);
+                const double cs = __ldg(T.CS + GP_MROW(material) + imax);
+                const double nI0 = __ldg(NI + imax);
+                return ((a0 + b0 * (k0 + T.mass)) * exp(b0 * (nI - nI0) / cs) -
+                           a0) / b0 - T.mass;
+        }
+        return gp_interpolate(T, NI, T.K, T.K_dNI_in + GP_MROW(material), nI);
+}
+
+GPD double gp_ehs_interaction_length(
+    const gp_tables & T, int scheme, int material, double kinetic)
+{
+        const int imax = T.n_energies - 1;
+        if (kinetic < __ldg(T.K)) return 0.;
+        const double * NI = T.NI_el + GP_ROW(gp_sch_el(scheme), material);
+        if (kinetic >= __ldg(T.K + imax)) {
+                const double k0 = __ldg(T.K + imax - 1);
+                const double k1 = __ldg(T.K + imax);
+                const double nI0 = __ldg(NI + imax - 1);
+                const double nI1 = __ldg(NI + imax);
+                return nI1 + (kinetic - k1) * (nI1 - nI0) / (k1 - k0);
+        }
+        return gp_interpolate(T, T.K, NI,
+            T.NI_el_dK + GP_ROW(gp_sch_el(scheme), material), kinetic);
+}
+
+GPD double gp_ehs_kinetic_from_interaction_length(
+    const gp_tables & T, int scheme, int material, double nI)
+{
+        const int imax = T.n_energies - 1;
+        const double * NI = T.NI_el + GP_ROW(gp_sch_el(scheme), material);
+        if (nI < __ldg(NI)) return 0.;
+        if (nI >= __ldg(NI + imax)) {
+                const double k0 = __ldg(T.K + imax - 1);
+                const double k1 = __ldg(T.K + imax);
+                const double nI0 = __ldg(NI + imax - 1);
+                const double nI1 = __ldg(NI + imax);
+                return k1 + (nI - nI1) * (k1 - k0) / (nI1 - nI0);
+        }
+        return gp_interpolate(T, NI, T.K,
+            T.K_dNI_el + GP_ROW(gp_sch_el(scheme), material), nI);
+}
+
+/* table_get_msc (pumas.c:4077-4111). */
+GPD void gp_table_get_msc(const gp_tables & T, int energy_loss, int material,
+    double kinetic, double & mu0, double & invlb1)
+{
+        const int imax = T.n_energies - 1;
+        const int s = gp_sch(energy_loss);
+        const double * Mu0 = T.Mu0 + GP_MROW(material);
+        const double * Ms1 = T.Ms1 + GP_ROW(s + 1, material);
+        const double K1 = __ldg(T.K + 1);
+        if (kinetic < K1) {
+                mu0 = __ldg(Mu0 + 1);
+                invlb1 = __ldg(Ms1 + 1) * sqrt(K1 / kinetic);
+        } else if (kinetic >= __ldg(T.K + imax)) {
+                mu0 = __ldg(Mu0 + imax);
+                invlb1 = __ldg(Ms1 + imax) * __ldg(T.K + imax) / kinetic;
+        } else {
+                const int i1 = gp_index(T, T.K, kinetic);
+                const double x0 = __ldg(T.K + i1);
+                const double dx = __ldg(T.K + i1 + 1) - x0;
+                const double t = (kinetic - x0) / dx;
+                const double * m0 = T.Mu0_dK + GP_MROW(material) + i1;
+                const double * m1 = T.Ms1_dK + GP_ROW(s + 1, material) + i1;
+                mu0 = gp_pchip(t, __ldg(Mu0 + i1), __ldg(Mu0 + i1 + 1),
+                    __ldg(m0) * dx, __ldg(m0 + 1) * dx);
+                invlb1 = gp_pchip(t, __ldg(Ms1 + i1), __ldg(Ms1 + i1 + 1),
+                    __ldg(m1) * dx, __ldg(m1 + 1) * dx);
+        }
+}
+
+/* coulomb_ehs_length (pumas.c:7446-7466). */
+GPD double gp_coulomb_ehs_length(
+    const gp_tables & T, int material, double kinetic)
+{
+        const double p2 = kinetic * (kinetic + 2. * T.mass);
+        const int imax = T.n_energies - 1;
+        const double * Lb = T.Lb + GP_MROW(material);
+        if (kinetic < __ldg(T.K + 1)) {
+                return __ldg(Lb + 1) / p2;
+        } else if (kinetic >= __ldg(T.K + imax)) {
+                return __ldg(Lb + imax) / p2;
+        } else {
+                const int i1 = gp_index(T, T.K, kinetic);
+                const int i2 = i1 + 1;
+                const double k1 = __ldg(T.K + i1);
+                double h = (kinetic - k1) / (__ldg(T.K + i2) - k1);
+                const double l1 = __ldg(Lb + i1);
+                return (l1 + h * (__ldg(Lb + i2) - l1)) / p2;
+        }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Coulomb scattering (pumas.c:7203-7683).                                  */
+/* ------------------------------------------------------------------------ */
+
+/* coulomb_screening_parameters (pumas.c:7203-7387) with the element's
+ * Salvat amplitudes and exponents from the host. */
+GPD int gp_coulomb_screening(const gp_element & el, double mass,
+    double kinetic, double kinetic0, double * amplitude, double * screening)
+{
+        const double Z = el.Z;
+        const double aZE = GP_ALPHA_EM * Z * (kinetic + mass);
+        const double p2 = kinetic * (kinetic + 2. * mass);
+        const double zeta2 = aZE * aZE / p2;
+        double f;
+        if (zeta2 < 1) {
+                f = 1. / (1. + zeta2) + 0.20205690315959424 -
+                    0.03692775514336999 * zeta2 +
+                    0.008349277381922926 * zeta2 * zeta2;
+                f *= zeta2;
+        } else {
+                const double r2i = 1. / (1. + zeta2);
+                const double phi = -atan(sqrt(zeta2));
+                f = -0.5 * log(r2i) + 0.5 * (1. - r2i) +
+                    1. / 12. * (1. - cos(2 * phi) * r2i) -
+                    1. / 120. * (1. - cos(4 * phi) * r2i * r2i) +
+                    1. / 252. * (1. - cos(6 * phi) * r2i * r2i * r2i);
+        }
+        const double ktv = exp(2 * f);
+        const double p02 = kinetic0 * (kinetic0 + 2. * mass);
+        const double d = 0.25 * GP_HBAR_C * GP_HBAR_C / p02 * ktv;
+        const int n = el.n_screen;
+        for (int i = 0; i < 3; i++) {
+                if (i < n) {
+                        amplitude[i] = el.amplitude[i];
+                        const double a = el.a_screen[i];
+                        screening[i] = d * a * a;
+                }
+        }
+        screening[n] = 12. * d / (el.RN * el.RN);
+        return n + 1;
+}
+
+/* coulomb_nuclear_form_factor (pumas.c:7396-7416). */
+GPD double gp_coulomb_nuclear_form_factor(double mu, double N)
+{
+        if (mu <= 0.)
+                return 1.;
+        else if (mu > 1.)
+                return 0.;
+        const double x2 = 10. * mu / N;
+        double d;
+        if (x2 <= 1E-04) {
+                d = 1. / (1. + 0.1 * x2);
+        } else {
+                const double x = sqrt(x2);
+                double sx, cx;
+                sincos(x, &sx, &cx);
+                d = 3 * (sx - x * cx) / (x2 * x);
+        }
+        return d * d;
+}
+
+/* coulomb_normalisation (pumas.c:7428-7435). */
+GPD double gp_coulomb_normalisation(
+    double Z, double A, double mass, double kinetic, double kinetic0)
+{
+        const double p2 = kinetic * (kinetic + 2. * mass);
+        const double p02 = kinetic0 * (kinetic0 + 2. * mass);
+        double d = GP_ALPHA_EM * Z * GP_HBAR_C * (kinetic + mass);
+        return A * 1E-03 * p2 * p02 / (d * d * GP_PI * GP_AVOGADRO);
+}
+
+/* coulomb_spin_factor (pumas.c:7475-7479). */
+GPD double gp_coulomb_spin_factor(double mass, double kinetic)
+{
+        const double e = kinetic + mass;
+        return kinetic * (e + mass) / (e * e);
+}
+
+/* coulomb_frame_parameters (pumas.c:7492-7508). */
+GPD void gp_coulomb_frame_parameters(double Ma, double mass, double kinetic,
+    double & kinetic0, double * parameters)
+{
+        double M2 = mass + Ma;
+        M2 *= M2;
+        const double sCM12i = 1. / sqrt(M2 + 2. * Ma * kinetic);
+        parameters[0] = (kinetic + mass + Ma) * sCM12i;
+        kinetic0 = (kinetic * Ma + mass * (mass + Ma)) * sCM12i - mass;
+        if (kinetic0 < 1E-09) kinetic0 = 1E-09;
+        const double etot = kinetic + mass + Ma;
+        const double betaCM2 = kinetic * (kinetic + 2. * mass) / (etot * etot);
+        double rM2 = mass / Ma;
+        rM2 *= rM2;
+        parameters[1] = sqrt(rM2 * (1. - betaCM2) + betaCM2);
+}
+
+/* coulomb_pole_reduction (pumas.c:7524-7576). */
+GPD void gp_coulomb_pole_reduction(int n_parameters, const double * amplitude,
+    const double * screening, double * a, double * b, double * c)
+{
+        const int n = n_parameters - 1;
+        for (int i = 0; i < 3; i++) a[i] = b[i] = 0.;
+        for (int i = 0; i < 4; i++) c[i] = 0.;
+        for (int i = 0; i < 3; i++) {
+                if (i >= n) break;
+                const double Ai = amplitude[i];
+                const double Bi = screening[i];
+                b[i] = Ai * Ai;
+                for (int j = i + 1; j < 3; j++) {
+                        if (j >= n) break;
+                        const double d =
+                            2 * Ai * amplitude[j] / (screening[j] - Bi);
+                        a[i] += d;
+                        a[j] -= d;
+                }
+        }
+        const double N = screening[n];
+        double Sa[4] = { 0, 0, 0, 0 }, Sb[4] = { 0, 0, 0, 0 };
+        for (int i = 0; i < 3; i++) {
+                if (i >= n) break;
+                const double x = 1. - screening[i] / N;
+                double r = x;
+                for (int j = 0; j < 4; j++) {
+                        Sa[j] += a[i] / r;
+                        r *= x;
+                        Sb[j] += b[i] / r;
+                }
+        }
+        double tmp = 1;
+        for (int i = 0; i < 4; i++) {
+                c[i] = ((4 - i) * Sb[3 - i] / N - Sa[3 - i]) * tmp;
+                tmp *= N;
+        }
+        for (int i = 0; i < 3; i++) {
+                if (i >= n) break;
+                const double Bi = screening[i];
+                double d = 1. - Bi / N;
+                d *= d;
+                d *= d;
+                a[i] = (a[i] - 4 * b[i] / (N - Bi)) / d;
+                b[i] /= d;
+        }
+}
+
+/* coulomb_transport_coefficients, order 0 only (pumas.c:7623-7683). */
+GPD double gp_coulomb_cs0(double mu, double S, int n_parameters,
+    const double * screening, const double * a, const double * b,
+    const double * c)
+{
+        const int n = n_parameters - 1;
+        double cs0 = 0.;
+        for (int i = 0; i < 3; i++) {
+                if (i >= n) break;
+                const double alp = screening[i];
+                const double r = mu / (mu + alp);
+                const double L = log(1. + mu / alp);
+                const double I0 = r / alp;
+                const double J0 = L;
+                const double I1 = L - r;
+                const double J1 = -alp * L;
+                cs0 += a[i] * (J0 - S * J1) + b[i] * (I0 - S * I1);
+        }
+        const double N = screening[n];
+        const double r = mu / (mu + N);
+        const double L = log(1. + mu / N);
+        const double I0 = r / N;
+        const double J0 = L;
+        const double I1 = L - r;
+        const double J1 = -N * L;
+        const double rn = 1. / (1. + mu / N);
+        const double K0 = (1. - rn) * (1. + rn) / (2 * N * N);
+        const double L0 =
+            (1. - rn) * ((1. + rn) * (1. + rn) - rn) / (3 * N * N * N);
+        const double K1 = I0 - N * K0;
+        const double L1 = K0 - N * L0;
+        cs0 += c[0] * (J0 - S * J1) + c[1] * (I0 - S * I1) +
+            c[2] * (K0 - S * K1) + c[3] * (L0 - S * L1);
+        return cs0;
+}
+
+/* coulomb_restricted_cs (pumas.c:7591-7609). */
+GPD double gp_coulomb_restricted_cs(double mu, double fspin, int n_parameters,
+    const double * screening, const double * a, const double * b,
+    const double * c)
+{
+        if ((mu >= 1.) || (mu >= 1E+06 * screening[n_parameters - 1]))
+                return 0.;
+        const double cs0 =
+            gp_coulomb_cs0(1., fspin, n_parameters, screening, a, b, c);
+        const double cs = gp_coulomb_cs0(mu, fspin, n_parameters, screening,
+            a, b, c);
+        if (cs > cs0)
+                return 0;
+        else
+                return cs0 - cs;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Numerical helpers and default DCS models.                                */
+/* ------------------------------------------------------------------------ */
+
+/* Gauss-Legendre nodes and weights on [0, 1], 9 and 12 points, as in
+ * math_gauss_quad_coefficients (pumas.c:12463-12561). */
+__constant__ double gp_gl9_x[9] = {
+        0.0159198802461870, 0.0819844463366821, 0.1933142836497048,
+        0.3378732882980955, 0.5000000000000000, 0.6621267117019045,
+        0.8066857163502952, 0.9180155536633179, 0.9840801197538130,
+};
+__constant__ double gp_gl9_w[9] = {
+        0.0406371941807872, 0.0903240803474287, 0.1303053482014677,
+        0.1561735385200015, 0.1651196775006299, 0.1561735385200015,
+        0.1303053482014677, 0.0903240803474287, 0.0406371941807872,
+};
+__constant__ double gp_gl12_x[12] = {
+        0.0092196828766404, 0.0479413718147625, 0.1150486629028477,
+        0.2063410228566913, 0.3160842505009099, 0.4373832957442655,
+        0.5626167042557344, 0.6839157494990901, 0.7936589771433087,
+        0.8849513370971523, 0.9520586281852375, 0.9907803171233596,
+};
+__constant__ double gp_gl12_w[12] = {
+        0.0235876681932559, 0.0534696629976592, 0.0800391642716731,
+        0.1015837133615330, 0.1167462682691774, 0.1245735229067014,
+        0.1245735229067014, 0.1167462682691774, 0.1015837133615330,
+        0.0800391642716731, 0.0534696629976592, 0.0235876681932559,
+};
+
+/* Chebyshev coefficients of CERNLIB RDILOG (C332), math_dilog
+ * (pumas.c:12609-12673). */
+__constant__ double gp_dilog_c[20] = {
+        0.42996693560813697, 0.40975987533077105, -0.01858843665014592,
+        0.00145751084062268, -0.00014304184442340, 0.00001588415541880,
+        -0.00000190784959387, 0.00000024195180854, -0.00000003193341274,
+        0.00000000434545063, -0.00000000060578480, 0.00000000008612098,
+        -0.00000000001244332, 0.00000000000182256, -0.00000000000027007,
+        0.00000000000004042, -0.00000000000000610, 0.00000000000000093,
+        -0.00000000000000014, 0.00000000000000002,
+};
+
+GPD double gp_sq(double x) { return x * x; }
+
+/* math_dilog (pumas.c:12609-12673); pow(y, 2.) is exactly y * y. */
+__device__ double gp_dilog(double x)
+{
+        const double PI3 = GP_PI * GP_PI / 3.;
+        const double PI6 = GP_PI * GP_PI / 6.;
+        const double PI12 = GP_PI * GP_PI / 12.;
+        if (x == 10) {
+                return PI6;
+        } else if ((x == -1.) || (1. - x == 0.)) {
+                return -PI12;
+        }
+        double T = -x;
+        double A, S, Y;
+        if (T <= -2) {
+                Y = -1. / (1. + T);
+                S = 1.;
+                A = -PI3 + 0.5 * (gp_sq(log(-T)) - gp_sq(log(1. + 1. / T)));
+        } else if (T < -1.) {
+                Y = -1. - T;
+                S = -1.;
+                A = log(-T);
+                A = -PI6 + A * (A + log(1. + 1. / T));
+        } else if (T <= -0.5) {
+                Y = -(1. + T) / T;
+                S = 1.;
+                A = log(-T);
+                A = -PI6 + A * (-0.5 * A + log(1. + T));
+        } else if (T < 0.) {
+                Y = -T / (1. + T);
+                S = -1.;
+                A = 0.5 * gp_sq(log(1 + T));
+        } else if (T <= 1.) {
+                Y = T;
+                S = 1.;
+                A = 0.;
+        } else {
+                Y = 1. / T;
+                S = -1.;
+                A = PI6 + 0.5 * gp_sq(log(T));
+        }
+        const double H = Y + Y - 1;
+        const double ALFA = H + H;
+        double B0 = 0., B1 = 0., B2 = 0.;
+#pragma unroll
+        for (int i = 19; i >= 0; i--) {
+                B0 = gp_dilog_c[i] + ALFA * B1 - B2;
+                B2 = B1;
+                B1 = B0;
+        }
+        return -(S * (B0 - H * B2) + A);
+}
+
+#define GP_SSR_SQRTE 1.648721270700128
+#define GP_SSR_ME 0.5109989461
+#define GP_SSR_RE 2.8179403227E-13
+
+/* dcs_bremsstrahlung_SSR (pumas.c:13915-14005), in m^2/GeV. */
+__device__ double gp_dcs_bremsstrahlung(const gp_tables & T,
+    const gp_element & el, double K, double q)
+{
+        double m = T.mass;
+        const double Z = el.Z;
+        if ((Z <= 0) || (el.A <= 0) || (m <= 0) || (K <= 0) || (q <= 0))
+                return 0.;
+        if (q >= K + m * el.qmax_m_brems) return 0.;
+        const double energy = (K + m) * 1E+03;
+        const double v = q * 1E+03 / energy;
+        m *= 1E+03;
+        const double Z13 = el.z13_inv;
+        const double rad_log = el.rad_log;
+        const double rad_log_inel = (Z == 1.) ? 446. : 1429.;
+        const double delta = m * m * v / (2. * energy * (1. - v));
+        double phi1 = log(rad_log * Z13 * (m / GP_SSR_ME) /
+            (1. + rad_log * Z13 * T.k.exp_half * delta / GP_SSR_ME));
+        double phi2 = log(rad_log * Z13 * T.k.exp_m16 * (m / GP_SSR_ME) /
+            (1. + rad_log * Z13 * T.k.exp_13 * delta / GP_SSR_ME));
+        phi1 -= el.ssr_delta1 * (1. - 1. / Z);
+        phi2 -= el.ssr_delta2 * (1. - 1. / Z);
+        const double s_atomic_1 = log(
+            m / delta / (m * delta / (GP_SSR_ME * GP_SSR_ME) + GP_SSR_SQRTE));
+        const double s_atomic_2 = log(1. + GP_SSR_ME /
+            (delta * rad_log_inel * Z13 * Z13 * GP_SSR_SQRTE));
+        const double s_atomic =
+            (4. / 3. * (1. - v) + v * v) * (s_atomic_1 - s_atomic_2);
+        double s_rad;
+        if (v < .0 || v > 1.) {
+                s_rad = 0.;
+        } else if (v < 0.02) {
+                s_rad = -0.00349 + 148.84 * v + -987.531 * v * v;
+        } else if (v >= 0.02 && v < 0.1) {
+                s_rad = 0.1642 + 132.573 * v + -585.361 * v * v +
+                    1407.77 * v * v * v;
+        } else if (v >= 0.01 && v < 0.9) {
+                s_rad = -2.8922 + -19.0156 * v + 57.698 * v * v;
+                const double tmp = log(1. - v);
+                s_rad += -63.418 * v * log(v) + 14.1166 * tmp +
+                    1.84206 * tmp * tmp;
+        } else {
+                s_rad = 2134.19 + 581.823 * v + -2708.85 * v * v;
+                const double tmp = log(1. - v);
+                s_rad += 4767.05 * v * log(v) + 1.52918 * tmp +
+                    0.361933 * tmp * tmp;
+        }
+        const double result =
+            ((2. - 2. * v + v * v) * phi1 - 2. / 3. * (1. - v) * phi2) +
+            1. / Z * s_atomic + 0.25 * GP_ALPHA_EM * phi1 * s_rad;
+        if (result <= 0.) return 0.;
+        const double aux = 2 * (GP_SSR_ME / m) * GP_SSR_RE * Z;
+        return aux * aux * (GP_ALPHA_EM / q) * result * 1E-04;
+}
+
+/* dcs_pair_production_d2_SSR (pumas.c:14394-14544). */
+__device__ double gp_dcs_pair_d2(const gp_tables & T, const gp_element & el,
+    double K, double q, double rho)
+{
+        double m = T.mass;
+        const double Z = el.Z;
+        if ((Z <= 0) || (el.A <= 0) || (m <= 0) || (K <= 0) || (q <= 0))
+                return 0.;
+        const double qmin = 4. * GP_ELECTRON_MASS;
+        const double qmax = K + m * el.qmax_m_pair;
+        if ((q < qmin) || (q > qmax)) return 0.;
+        const double energy = (K + m) * 1E+03;
+        const double v = q / (K + m);
+        m *= 1E+03;
+        const double rad_log = el.rad_log;
+        const double const_prefactor = el.pair_pref;
+        const double Z13 = el.zm13;
+        const double d_n = el.dn;
+        rho = 1 - rho;
+        const double rho2 = rho * rho;
+        double g1, g2;
+        if (Z == 1.) {
+                g1 = 4.4E-05;
+                g2 = 4.8E-05;
+        } else {
+                g1 = 1.95E-05;
+                g2 = 5.3E-05;
+        }
+        const double zeta1 =
+            (0.073 * log(energy / m / (1. + g1 * el.z23 * energy / m)) - 0.26);
+        const double zeta2 =
+            (0.058 * log(energy / m / (1 + g2 / Z13 * energy / m)) - 0.14);
+        double zeta;
+        if ((zeta1 > 0.) && (zeta2 > 0.))
+                zeta = zeta1 / zeta2;
+        else
+                zeta = 0.;
+        const double beta = v * v / (2. * (1. - v));
+        const double xi =
+            gp_sq(m * v / (2. * GP_SSR_ME)) * (1. - rho2) / (1. - v);
+        const double lxi = log(1. + 1. / xi);
+        const double Be = ((2. + rho2) * (1. + beta) + xi * (3. + rho2)) * lxi +
+            (1. - rho2 - beta) / (1. + xi) - (3. + rho2);
+        const double Ce2 = ((1. - rho2) * (1. + beta) + xi * (3. - rho2)) * lxi +
+            2. * (1. - beta - rho2) / (1. + xi) - (3. - rho2);
+        const double Ce1 = Be - Ce2;
+        const double De = ((2. + rho2) * (1. + beta) + xi * (3. + rho2)) *
+                gp_dilog(1. / (1. + xi)) -
+            (2. + rho2) * xi * lxi - (xi + rho2 + beta) / (1. + xi);
+        const double sxi = sqrt(1. + xi);
+        const double ev = energy * v * (1. - rho2);
+        double Le1, Le2;
+        if (De / Be > 0.) {
+                const double tmp = De / Be;
+                const double Xe = (tmp < 100) ? exp(-tmp) : 0.;
+                Le1 = log(rad_log * Z13 * sxi /
+                          (Xe + 2. * GP_SSR_ME * T.k.exp_half * rad_log * Z13 *
+                                  (1. + xi) / ev)) - tmp -
+                    0.5 * log(Xe + el.pair_medn2 * (1. + xi));
+                Le2 = log(rad_log * Z13 * T.k.exp_m16 * sxi /
+                          (Xe + 2. * GP_SSR_ME * T.k.exp_13 * rad_log * Z13 *
+                                  (1. + xi) / ev)) - tmp -
+                    0.5 * log(Xe + el.pair_medn2 * T.k.exp_m13 * (1. + xi));
+        } else {
+                const double tmp = De / Be;
+                const double Xe_inv = (tmp > -100) ? exp(De / Be) : 0;
+                Le1 = log(rad_log * Z13 * sxi /
+                          (1. + Xe_inv * 2. * GP_SSR_ME * T.k.exp_half *
+                                    rad_log * Z13 * (1. + xi) / ev)) -
+                    0.5 * De / Be -
+                    0.5 * log(1. + Xe_inv * el.pair_medn2 * (1. + xi));
+                Le2 = log(rad_log * Z13 * T.k.exp_m16 * sxi /
+                          (1. + Xe_inv * 2. * GP_SSR_ME * T.k.exp_13 *
+                                    rad_log * Z13 * (1. + xi) / ev)) -
+                    0.5 * De / Be -
+                    0.5 * log(1. + Xe_inv * el.pair_medn2 * T.k.exp_m13 *
+                                       (1. + xi));
+        }
+        double diagram_e = const_prefactor * (Z + zeta) * (1. - v) / v *
+            (Ce1 * Le1 + Ce2 * Le2);
+        if (diagram_e < 0.) diagram_e = 0.;
+
+        const double lxi1 = log(1. + xi);
+        const double Bm = ((1. + rho2) * (1. + (3. * beta) / 2) -
+                              1. / xi * (1. + 2. * beta) * (1. - rho2)) * lxi1 +
+            xi * (1. - rho2 - beta) / (1. + xi) +
+            (1. + 2. * beta) * (1. - rho2);
+        const double Cm2 =
+            ((1. - beta) * (1. - rho2) - xi * (1. + rho2)) * lxi1 / xi -
+            2. * (1. - beta - rho2) / (1. + xi) + 1. - beta -
+            (1. + beta) * rho2;
+        const double Cm1 = Bm - Cm2;
+        const double Dm = ((1. + rho2) * (1. + (3. * beta) / 2.) -
+                              1. / xi * (1. + 2. * beta) * (1. - rho2)) *
+                gp_dilog(xi / (1. + xi)) +
+            (1. + (3. * beta) / 2.) * (1. - rho2) / xi * lxi1 +
+            (1. - rho2 - beta / 2. * (1. + rho2) +
+                (1. - rho2) / (2. * xi) * beta) * xi / (1. + xi);
+        double Lm1, Lm2;
+        if (Dm / Bm > 0.) {
+                const double tmp = Dm / Bm;
+                const double Xm = (tmp < 100) ? exp(-tmp) : 0.;
+                Lm1 = log(m / GP_SSR_ME * rad_log * Z13 / d_n /
+                          (Xm + 2. * GP_SSR_ME * T.k.exp_half * rad_log * Z13 *
+                                  (1. + xi) / ev)) - tmp;
+                Lm2 = log(m / GP_SSR_ME * rad_log * Z13 / d_n /
+                          (Xm + 2. * GP_SSR_ME * T.k.exp_13 * rad_log * Z13 *
+                                  (1. + xi) / ev)) - tmp;
+        } else {
+                const double tmp = Dm / Bm;
+                const double Xmv = (tmp > -100) ? exp(tmp) : 0.;
+                Lm1 = log(m / GP_SSR_ME * rad_log * Z13 / d_n /
+                    (1. + 2. * GP_SSR_ME * T.k.exp_half * rad_log * Z13 *
+                            (1. + xi) / ev * Xmv));
+                Lm2 = log(m / GP_SSR_ME * rad_log * Z13 / d_n /
+                    (1. + 2. * GP_SSR_ME * T.k.exp_13 * rad_log * Z13 *
+                            (1. + xi) / ev * Xmv));
+        }
+        double diagram_mu = const_prefactor * (Z + zeta) * (1. - v) / v *
+            T.k.pair_me_m2 * (Cm1 * Lm1 + Cm2 * Lm2);
+        if (diagram_mu < 0.) diagram_mu = 0.;
+        return (diagram_e + diagram_mu) * 1E-01 / energy;
+}
+
+/* dcs_pair_production_SSR (pumas.c:14560-14604). */
+__device__ double gp_dcs_pair_production(const gp_tables & T,
+    const gp_element & el, double K, double q)
+{
+        const double mass = T.mass;
+        if ((el.Z <= 0) || (el.A <= 0) || (mass <= 0) || (K <= 0) || (q <= 0))
+                return 0.;
+        if (q <= 4. * GP_ELECTRON_MASS) return 0.;
+        if (q >= K + mass * el.qmax_m_pair) return 0.;
+        const double gamma = 1. + K / mass;
+        const double x0 = 1. - 4. * GP_ELECTRON_MASS / q;
+        const double x1 = 1. - 6. / (gamma * (gamma - q / mass));
+        double rmax;
+        if ((x0 > 0) && (x1 > 0))
+                rmax = sqrt(x0) * x1;
+        else
+                return 0.;
+        const double ri = 1. - rmax;
+        if ((ri <= 0.) || (ri >= 1.)) return 0.;
+        const double tmin = log(ri);
+        double I = 0.;
+        for (int i = 0; i < 12; i++) {
+                const double rho = exp(gp_gl12_x[i] * tmin);
+                I -= gp_dcs_pair_d2(T, el, K, q, rho) * rho * gp_gl12_w[i] *
+                    tmin;
+        }
+        return (I < 0) ? 0. : I;
+}
+
+/* dcs_photonuclear_f2p_ALLM97 (pumas.c:14626-14673). */
+GPD double gp_f2p_allm97(const gp_tables & T, double x, double Q2)
+{
+        const double m02 = 0.31985;
+        const double mP2 = 49.457;
+        const double mR2 = 0.15052;
+        const double Q02 = 0.52544;
+        const double Lambda2 = 0.06527;
+        const double M = 0.5 * (GP_PROTON_MASS + GP_NEUTRON_MASS);
+        const double M2 = M * M;
+        const double W2 = M2 + Q2 * (1.0 / x - 1.0);
+        const double t = log(log((Q2 + Q02) / Lambda2) / T.k.allm_lq0);
+        const double xP = (Q2 + mP2) / (Q2 + mP2 + W2 - M2);
+        const double xR = (Q2 + mR2) / (Q2 + mR2 + W2 - M2);
+        const double cP =
+            0.28067 + (0.28067 - 0.22291) * (1.0 / (1.0 + pow(t, 2.1979)) - 1.0);
+        const double aP =
+            -0.0808 + (-0.0808 - -0.44812) * (1.0 / (1.0 + pow(t, 1.1709)) - 1.0);
+        const double bP = 0.36292 + 1.8917 * pow(t, 1.8439);
+        const double cR = 0.80107 + 0.97307 * pow(t, 3.4942);
+        const double aR = 0.58400 + 0.37888 * pow(t, 2.6063);
+        const double bR = 0.01147 + 3.7582 * pow(t, 0.49338);
+        const double l1x = log(1 - x);
+        const double F2P = cP * exp(aP * log(xP) + bP * l1x);
+        const double F2R = cR * exp(aR * log(xR) + bR * l1x);
+        return Q2 / (Q2 + m02) * (F2P + F2R);
+}
+
+/* dcs_photonuclear_d2_DRSS (pumas.c:14923-14943) with the shadowing and F2
+ * of pumas.c:14688-14721. */
+__device__ double gp_photonuclear_d2(const gp_tables & T,
+    const gp_element & el, double K, double q, double Q2)
+{
+        const double ml = T.mass;
+        const double cf = 4 * GP_PI * GP_ALPHA_EM * GP_ALPHA_EM * GP_HBAR_C *
+            GP_HBAR_C;
+        const double M = 0.5 * (GP_PROTON_MASS + GP_NEUTRON_MASS);
+        const double E = K + ml;
+        const double y = q / E;
+        const double x = 0.5 * Q2 / (M * q);
+        const double F2p = gp_f2p_allm97(T, x, Q2);
+        const double Z = el.Z, A = el.A;
+        double shadowing;
+        if (Z == 1.)
+                shadowing = 1.;
+        else if (x < 0.0014)
+                shadowing = el.shadow_low;
+        else if (x < 0.04)
+                shadowing = exp((0.069 * log10(x) + 0.097) * el.log_A);
+        else
+                shadowing = 1.;
+        const double F2A = F2p * shadowing *
+            (Z + (A - Z) * (1.0 + x * (-1.85 + x * (2.45 + x * (-2.35 + x)))));
+        const double R = 0.;
+        const double dds = (1 - y +
+                               0.5 * (1 - 2 * ml * ml / Q2) *
+                                   (y * y + Q2 / (E * E)) / (1 + R)) /
+                (Q2 * Q2) -
+            0.25 / (E * E * Q2);
+        return cf * F2A * dds / q;
+}
+
+/* dcs_photonuclear_DRSS (pumas.c:15002-15083, mode 0). */
+__device__ double gp_dcs_photonuclear(const gp_tables & T,
+    const gp_element & el, double K, double q)
+{
+        const double ml = T.mass;
+        if ((el.Z <= 0) || (el.A <= 0) || (ml <= 0) || (K <= 0)) return 0.;
+        const double M = 0.5 * (GP_NEUTRON_MASS + GP_PROTON_MASS);
+        const double mpi = GP_PION_MASS;
+        if ((q <= mpi + 0.5 * mpi * mpi / M) ||
+            (q >= K + ml - 0.5 * (M + ml * ml / M)))
+                return 0.;
+        const double E = K + ml;
+        const double ml2 = ml * ml;
+        const double Q2min = ml2 * (q * q - 0.5 * ml2) / (E * (E - q));
+        const double Q2max = 2.0 * M * (q - mpi) - mpi * mpi;
+        if ((Q2max < Q2min) | (Q2min < 0)) return 0.;
+        const double xmin = log(Q2min);
+        const double xmax = log(Q2max);
+        const double dx = xmax - xmin;
+        double ds = 0.;
+        for (int i = 0; i < 9; i++) {
+                const double Q2 = exp(xmin + dx * gp_gl9_x[i]);
+                const double w = gp_gl9_w[i] * (dx * Q2);
+                const double tmp = gp_photonuclear_d2(T, el, K, q, Q2);
+                if (tmp <= 0.) continue;
+                ds += tmp * w;
+        }
+        return (ds < 0.) ? 0. : ds;
+}
+
+GPD void gp_photonuclear_range(
+    double m, double K, double & qmin, double & qmax)
+{
+        const double M = 0.5 * (GP_NEUTRON_MASS + GP_PROTON_MASS);
+        const double mpi = GP_PION_MASS;
+        qmin = mpi + 0.5 * mpi * mpi / M;
+        qmax = K + m - 0.5 * (M + m * m / M);
+}
+
+/* pumas_electronic_dcs (pumas.c:11082-11101). */
+GPD double gp_electronic_dcs(double Z, double I, double m, double K, double q)
+{
+        const double P2 = K * (K + 2. * m);
+        const double E = K + m;
+        const double Wmax = 2. * GP_ELECTRON_MASS * P2 /
+            (m * m + GP_ELECTRON_MASS * (GP_ELECTRON_MASS + 2. * E));
+        if (q > Wmax) return 0.;
+        const double Wmin = (13.6 / 19.2) * I;
+        if (q <= Wmin) return 0.;
+        const double E2 = E * E;
+        const double beta2 = P2 / E2;
+        const double a0 = 0.5 / E2;
+        const double a1 = beta2 / Wmax;
+        return 2 * GP_PI * GP_ELECTRON_MASS * GP_ELECTRON_RADIUS *
+            GP_ELECTRON_RADIUS * Z * (a0 + 1. / q * (1 / q - a1)) / beta2;
+}
+
+/* Process DCS wrappers (pumas.c:11003-11122), in m^2/kg. */
+__device__ double gp_dcs_process(const gp_tables & T, int process,
+    const gp_element & el, double K, double q)
+{
+        const double m = T.mass;
+        if (process == 0) {
+                return gp_dcs_bremsstrahlung(T, el, K, q) * 1E+03 *
+                    GP_AVOGADRO * (m + K) / el.A;
+        } else if (process == 1) {
+                return gp_dcs_pair_production(T, el, K, q) * 1E+03 *
+                    GP_AVOGADRO * (m + K) / el.A;
+        } else if (process == 2) {
+                double qmin, qmax;
+                gp_photonuclear_range(m, K, qmin, qmax);
+                if ((q < qmin) || (q > qmax)) return 0.;
+                return gp_dcs_photonuclear(T, el, K, q) * 1E+03 *
+                    GP_AVOGADRO * (m + K) / el.A;
+        } else {
+                return gp_electronic_dcs(el.Z, el.I, m, K, q) * (m + K) *
+                    GP_AVOGADRO / (el.A * 1E-03);
+        }
+}
+
+/* Single precision log and exp, rounded from double precision. */
+GPD float gp_logf(float x) { return (float)log((double)x); }
+GPD float gp_expf(float x) { return (float)exp((double)x); }
+
+/* dcs_evaluate (pumas.c:11243-11347). */
+__device__ double gp_dcs_evaluate(const gp_tables & T, int process,
+    const gp_element & el, double K, double q)
+{
+        const double wj = K / (K + T.mass);
+        if (process == 3) return gp_dcs_process(T, 3, el, K, q) * wj;
+        double qlow = 0;
+        if (process == 2) {
+                double qmin, qmax;
+                gp_photonuclear_range(T.mass, K, qmin, qmax);
+                if ((q < qmin) || (q > qmax))
+                        return 0.;
+                else
+                        qlow = 2 * qmin;
+        } else {
+                double qmin = 4. * GP_ELECTRON_MASS;
+                const double qmax = K + T.mass * el.qmax_m_pair;
+                if (process == 1)
+                        qlow = 4 * qmin;
+                else
+                        qmin = 0.;
+                if ((q < qmin) || (q > qmax)) return 0.;
+        }
+        if (q < qlow) return gp_dcs_process(T, process, el, K, q) * wj;
+
+        const int nx = T.n_table_dcs;
+        const float xmin = __ldg(T.DCS_x);
+        const float xmax = __ldg(T.DCS_x + nx - 1);
+        const float x = gp_logf((float)(q / K));
+        if ((x < xmin) || (x >= xmax))
+                return gp_dcs_process(T, process, el, K, q) * wj;
+        int ix = 0, tmpi = nx - 1;
+        do {
+                const int i3 = (ix + tmpi) >> 1;
+                if (x >= __ldg(T.DCS_x + i3))
+                        ix = i3;
+                else
+                        tmpi = i3;
+        } while (tmpi - ix >= 2);
+        if ((ix < 0) || (ix >= nx - 1))
+                return gp_dcs_process(T, process, el, K, q) * wj;
+
+        float p00, p01, m00, m01, p10, p11, m10, m11, h0, h1;
+        const int imax = T.n_energies - 1;
+        const double Kmax = __ldg(T.K + imax);
+        const long stride = (long)nx * 2;
+        const float * base = T.DCS +
+            stride * ((long)(process * T.n_elements + el.index) * T.n_energies);
+        int i0 = 0;
+        if ((K >= Kmax) || ((i0 = gp_index(T, T.K, K)) >= imax)) {
+                const float * data = base + stride * imax;
+                p00 = p10 = __ldg(data + 2 * ix);
+                m00 = m10 = __ldg(data + 2 * ix + 1);
+                p01 = p11 = __ldg(data + 2 * ix + 2);
+                m01 = m11 = __ldg(data + 2 * ix + 3);
+                h0 = 1.f;
+                h1 = 0.f;
+        } else {
+                const float * data = base + stride * i0;
+                p00 = __ldg(data + 2 * ix);
+                m00 = __ldg(data + 2 * ix + 1);
+                p01 = __ldg(data + 2 * ix + 2);
+                m01 = __ldg(data + 2 * ix + 3);
+                data += 2 * nx;
+                p10 = __ldg(data + 2 * ix);
+                m10 = __ldg(data + 2 * ix + 1);
+                p11 = __ldg(data + 2 * ix + 2);
+                m11 = __ldg(data + 2 * ix + 3);
+                const float K0 = (float)__ldg(T.K + i0);
+                const float K1 = (float)__ldg(T.K + i0 + 1);
+                h1 = __fdiv_rn(gp_logf(__fdiv_rn((float)K, K0)),
+                    gp_logf(__fdiv_rn(K1, K0)));
+                h0 = __fsub_rn(1.f, h1);
+        }
+        if (((p00 == 0.f) && (m00 == 0.f)) || ((p01 == 0.f) && (m01 == 0.f)) ||
+            ((p10 == 0.f) && (m10 == 0.f)) || ((p11 == 0.f) && (m11 == 0.f)))
+                return gp_dcs_process(T, process, el, K, q) * wj;
+
+        /* Single precision interpolation, without fused multiply-adds as
+         * the reference's SSE evaluation. */
+        const float x0 = __ldg(T.DCS_x + ix);
+        const float x1 = __ldg(T.DCS_x + ix + 1);
+        const float dx = __fsub_rn(x1, x0);
+        m00 = __fmul_rn(m00, dx);
+        m01 = __fmul_rn(m01, dx);
+        const float t = __fdiv_rn(__fsub_rn(x, x0), dx);
+        const float d0 = __fsub_rn(p00, p01);
+        const float c02 = __fsub_rn(__fsub_rn(__fmul_rn(-3.f, d0),
+            __fmul_rn(2.f, m00)), m01);
+        const float c03 = __fadd_rn(__fadd_rn(__fmul_rn(2.f, d0), m00), m01);
+        float r = __fmul_rn(gp_expf(__fadd_rn(p00, __fmul_rn(t, __fadd_rn(m00,
+            __fmul_rn(t, __fadd_rn(c02, __fmul_rn(t, c03))))))), h0);
+        if (h1 > 0.f) {
+                m10 = __fmul_rn(m10, dx);
+                m11 = __fmul_rn(m11, dx);
+                const float d1 = __fsub_rn(p10, p11);
+                const float c12 = __fsub_rn(__fsub_rn(__fmul_rn(-3.f, d1),
+                    __fmul_rn(2.f, m10)), m11);
+                const float c13 =
+                    __fadd_rn(__fadd_rn(__fmul_rn(2.f, d1), m10), m11);
+                r = __fadd_rn(r, __fmul_rn(gp_expf(__fadd_rn(p10,
+                    __fmul_rn(t, __fadd_rn(m10, __fmul_rn(t, __fadd_rn(c12,
+                    __fmul_rn(t, c13))))))), h1));
+        }
+        return r * wj;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Event context helpers.                                                   */
+/* ------------------------------------------------------------------------ */
+
+/* Medium of a geometry region: material and density (transport_set_locals,
+ * pumas.c:5528-5552, for a uniform density override). */
+GPD int gp_medium_material(const gpumas_geometry & g, int medium)
+{
+        return __ldg(&g.media[medium].material);
+}
+
+GPD double gp_medium_density(
+    const gp_tables & T, const gpumas_geometry & g, int medium)
+{
+        const double d = __ldg(&g.media[medium].density);
+        return (d > 0.) ? d : __ldg(T.material_density +
+                                  __ldg(&g.media[medium].material));
+}
+
+GPD int gp_locate(const gpumas_geometry & g, const gp_event & e)
+{
+        return gpumas_geometry_locate(&g, e.pos);
+}
+
+GPD double gp_step_proposal(const gp_config & cfg, const gpumas_geometry & g,
+    gp_event & e, int medium)
+{
+        const double sgn = (cfg.direction == GPUMAS_MODE_FORWARD) ? 1. : -1.;
+        const double u[3] = { sgn * e.dir[0], sgn * e.dir[1], sgn * e.dir[2] };
+        e.steps++;
+        return gpumas_geometry_step(&g, e.pos, u, medium);
+}
+
+/* step_randn (pumas.c:7016-7029): Box-Muller pairs cached per event. */
+GPD double gp_randn(gp_event & e)
+{
+        e.randn_done = !e.randn_done;
+        if (!e.randn_done) return e.randn_next;
+        const double r = sqrt(-2. * log(gp_random(e)));
+        const double phi = 2. * GP_PI * gp_random(e);
+        double s, c;
+        sincos(phi, &s, &c);
+        e.randn_next = r * c;
+        return r * s;
+}
+
+/* step_rotate_direction (pumas.c:7042-7095). */
+__device__ void gp_rotate(gp_event & e, double mu)
+{
+        double * const direction = e.dir;
+        const double cos_theta = 1 - 2 * mu;
+        const double stsq = 4 * mu * (1. - mu);
+        if (stsq <= 0.) return;
+        const double st = sqrt(stsq);
+        double u0x = 0., u0y = 0., u0z = 0.;
+        const double a0 = fabs(direction[0]);
+        const double a1 = fabs(direction[1]);
+        const double a2 = fabs(direction[2]);
+        if (a0 > a1) {
+                if (a0 > a2) {
+                        const double nrm =
+                            1. / sqrt(direction[0] * direction[0] +
+                                     direction[2] * direction[2]);
+                        u0x = -direction[2] * nrm, u0z = direction[0] * nrm;
+                } else {
+                        const double nrm =
+                            1. / sqrt(direction[1] * direction[1] +
+                                     direction[2] * direction[2]);
+                        u0y = direction[2] * nrm, u0z = -direction[1] * nrm;
+                }
+        } else {
+                if (a1 > a2) {
+                        const double nrm =
+                            1. / sqrt(direction[0] * direction[0] +
+                                     direction[1] * direction[1]);
+                        u0x = direction[1] * nrm, u0y = -direction[0] * nrm;
+                } else {
+                        const double nrm =
+                            1. / sqrt(direction[1] * direction[1] +
+                                     direction[2] * direction[2]);
+                        u0y = direction[2] * nrm, u0z = -direction[1] * nrm;
+                }
+        }
+        const double u1x = u0y * direction[2] - u0z * direction[1];
+        const double u1y = u0z * direction[0] - u0x * direction[2];
+        const double u1z = u0x * direction[1] - u0y * direction[0];
+        const double phi = GP_PI * (1. - 2. * gp_random(e));
+        double sp, cp;
+        sincos(phi, &sp, &cp);
+        direction[0] = cos_theta * direction[0] + st * (cp * u0x + sp * u1x);
+        direction[1] = cos_theta * direction[1] + st * (cp * u0y + sp * u1y);
+        direction[2] = cos_theta * direction[2] + st * (cp * u0z + sp * u1z);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Polar angles of DELs (pumas.c:11736-11976).                              */
+/* ------------------------------------------------------------------------ */
+
+/* polar_bremsstrahlung (pumas.c:11759-11830), also for pair production. */
+__device__ double gp_polar_bremsstrahlung(const gp_tables & T, gp_event & e,
+    const gp_element & el, double ki, double kf)
+{
+        const double m = T.mass;
+        const double E = ki + m;
+        const double nu = ki - kf;
+        const double y = nu / E;
+        const double tmp = 0.5 * m * nu / (E * (E - nu));
+        const double mu0 = tmp * tmp;
+        const double c1 = (2 * (1. - y) + y * y) * mu0;
+        const double c2 = 4 * (1. - y) * mu0 * mu0;
+        const double muni = el.muni;
+        const double muc = sqrt(mu0) - mu0;
+        if (muc < 0) return 0;
+        double x0;
+        {
+                const double q = muni;
+                const double r = mu0;
+                const double qr = q * r;
+                x0 = (1. + 2 * qr) * log((1. + qr) / (r + qr)) -
+                    (1. - r) * (1 + 2 * q) / (1 + q);
+        }
+        for (int i = 0; i < 100; i++) {
+                const double r0 = gp_random(e);
+                const double r1 = gp_random(e);
+                const double mu = r0 * mu0 / (mu0 + 1. - r0);
+                const double mus = mu0 + mu;
+                const double mu2 = mus * mus;
+                const double d1 = 1 / mu2;
+                const double d2 = d1 * d1;
+                const double score = r1 * c1 * d1;
+                double pdf = c1 * d1 - mu * c2 * d2;
+                if (score > pdf) continue;
+                const double l2 = mu2 / (mu0 * mu0);
+                const double q = muni * l2;
+                const double r = mu0 * l2;
+                const double qr = q * r;
+                if (qr > 1E+05) continue;
+                const double x = (1. + 2 * qr) * log((1. + qr) / (r + qr)) -
+                    (1. - r) * (1 + 2 * q) / (1 + q);
+                pdf *= x / x0;
+                if (score <= pdf) return mu;
+        }
+        return 0.;
+}
+
+/* Objective of the photonuclear polar sampling (pumas.c:11855-11862). */
+GPD double gp_polar_objective(const gp_tables & T, const gp_element & el,
+    double K, double q, double lnQ2)
+{
+        const double Q2 = exp(lnQ2);
+        return -gp_photonuclear_d2(T, el, K, q, Q2) * Q2;
+}
+
+/* math_find_minimum_brent (pumas.c:12233-12325); as in the reference the
+ * upper bracket of the search is the initial minimiser xb. */
+__device__ int gp_find_minimum_brent(const gp_tables & T,
+    const gp_element & el, double K, double q, double xa, double xb,
+    double xc, double fb, double tol, int max_iter, double & xopt,
+    double & fopt)
+{
+        const double EPS = 1E-15;
+        const double GOLD = 0.3819660;
+        tol *= fabs(xc - xa);
+        double x = xb, w = xb, v = xb;
+        double fw = fb, fv = fb, fx = fb;
+        double d = 0., ee = 0.;
+        int i;
+        for (i = 0; i < max_iter; i++) {
+                const double xm = 0.5 * (xa + xb);
+                const double tol1 = tol * fabs(x) + EPS;
+                const double tol2 = 2 * tol1;
+                if (fabs(x - xm) <= (tol2 - 0.5 * (xb - xa))) break;
+                if (fabs(ee) > tol1) {
+                        const double r = (x - w) * (fx - fv);
+                        double qq = (x - v) * (fx - fw);
+                        double p = (x - v) * qq - (x - w) * r;
+                        qq = 2. * (qq - r);
+                        if (qq > 0.) p = -p;
+                        qq = fabs(qq);
+                        const double etemp = ee;
+                        ee = d;
+                        if (fabs(p) >= fabs(0.5 * qq * etemp) ||
+                            (p <= qq * (xa - x)) || (p >= qq * (xb - x))) {
+                                ee = (x >= xm) ? xa - x : xb - x;
+                                d = GOLD * ee;
+                        } else {
+                                d = p / qq;
+                                const double u = x + d;
+                                if ((u - xa < tol2) || (xb - u < tol2))
+                                        d = ((xm - x) >= 0.0) ? fabs(tol1) :
+                                                                -fabs(tol1);
+                        }
+                } else {
+                        ee = (x >= xm) ? xa - x : xb - x;
+                        d = GOLD * ee;
+                }
+                const double u = (fabs(d) >= tol1) ? x + d :
+                    x + ((d >= 0.0) ? fabs(tol1) : -fabs(tol1));
+                const double fu = gp_polar_objective(T, el, K, q, u);
+                if (fu <= fx) {
+                        if (u >= x)
+                                xa = x;
+                        else
+                                xb = x;
+                        v = w, w = x, x = u;
+                        fv = fw, fw = fx, fx = fu;
+                } else {
+                        if (u < x)
+                                xa = u;
+                        else
+                                xb = u;
+                        if ((fu <= fw) || (w == x)) {
+                                v = w;
+                                w = u;
+                                fv = fw;
+                                fw = fu;
+                        } else if ((fu <= fv) || (v == x) || (v == w)) {
+                                v = u;
+                                fv = fu;
+                        }
+                }
+        }
+        xopt = x;
+        fopt = fx;
+        return (i < max_iter) ? i : -1;
+}
+
+/* math_find_minimum with Brent refinement (pumas.c:12105-12206). */
+__device__ int gp_find_minimum(const gp_tables & T, const gp_element & el,
+    double K, double q, double xa, double xc, double tol, int max_iter,
+    double & xopt, double & fopt)
+{
+        double fa = gp_polar_objective(T, el, K, q, xa);
+        double fc = gp_polar_objective(T, el, K, q, xc);
+        const double atol = tol * fabs(xc - xa);
+        double xb = 0, fb = 0;
+        int i;
+        for (i = 0; i < max_iter; i++) {
+                xb = 0.5 * (xa + xc);
+                fb = gp_polar_objective(T, el, K, q, xb);
+                if ((fb < fa) && (fb < fc)) break;
+                if (fabs(xc - xa) <= atol) {
+                        xopt = xb;
+                        fopt = fb;
+                        return i;
+                }
+                if (fb < fc) {
+                        xc = xb;
+                        fc = fb;
+                } else {
+                        xa = xb;
+                        fa = fb;
+                }
+        }
+        if (i == max_iter) {
+                if (fa < fb) {
+                        fb = fa;
+                        xb = xa;
+                } else if (fc < fb) {
+                        fb = fc;
+                        xb = xc;
+                }
+                xopt = xb;
+                fopt = fb;
+                return -1;
+        }
+        const int status = gp_find_minimum_brent(
+            T, el, K, q, xa, xb, xc, fb, tol, max_iter - i, xopt, fopt);
+        return (status < 0) ? -2 : status + i;
+}
+
+/* polar_photonuclear (pumas.c:11874-11950). */
+__device__ double gp_polar_photonuclear(const gp_tables & T, gp_event & e,
+    const gp_element & el, double ki, double kf)
+{
+        const double M = 0.5 * (GP_PROTON_MASS + GP_NEUTRON_MASS);
+        const double q = ki - kf;
+        const double ml = T.mass;
+        const double E = ki + ml;
+        const double ml2 = ml * ml;
+        const double Q2min = ml2 * (q * q - 0.5 * ml2) / (E * (E - q));
+        const double Q2max =
+            2.0 * M * (q - GP_PION_MASS) - GP_PION_MASS * GP_PION_MASS;
+        if ((Q2max < Q2min) | (Q2min < 0)) return 0.;
+        double fopt = 0., xopt = 0.;
+        const double lnQ2min = log(Q2min);
+        const double lnQ2max = log(Q2max);
+        const int status = gp_find_minimum(
+            T, el, ki, q, lnQ2min, lnQ2max, 1E-06, 100, xopt, fopt);
+        fopt = -fopt;
+        if (status == -2) return 0.;
+        const double x = exp(xopt) / (2 * q * M);
+        const double lne = 0.1;
+        if ((x <= 0.04) && (xopt + lne < lnQ2max)) {
+                double f2, x2;
+                const int status2 = gp_find_minimum(
+                    T, el, ki, q, xopt + lne, lnQ2max, 1E-06, 100, x2, f2);
+                if (status2 >= 0) {
+                        f2 = -f2;
+                        if (f2 > fopt) {
+                                xopt = x2;
+                                fopt = f2;
+                        }
+                }
+        }
+        const double rQ2 = lnQ2max - lnQ2min;
+        double Q2 = 0.;
+        int i;
+        for (i = 0; i < 100; i++) {
+                const double u = gp_random(e);
+                Q2 = Q2min * exp(rQ2 * u);
+                const double r = gp_photonuclear_d2(T, el, ki, q, Q2) * Q2;
+                if (gp_random(e) * fopt <= r) break;
+        }
+        if (i == 100) return 0.;
+        const double p = sqrt(ki * (ki + 2 * ml));
+        const double E1 = E - q;
+        const double eps = ml / E1;
+        const double p1 = E1 * sqrt((1. + eps) * (1. - eps));
+        const double p2 = p * p1;
+        double tmp = p2 + ml * ml - E * E1;
+        if (fabs(tmp) <= 3 * GP_DBL_EPSILON * p2) tmp = 0.;
+        const double a_mu = 0.5 * tmp / p2;
+        const double b_mu = 0.25 / p2;
+        double mu = a_mu + b_mu * Q2;
+        if (mu < 0)
+                mu = 0.;
+        else if (mu > 1.)
+                mu = 1.;
+        return mu;
+}
+
+/* polar_ionisation (pumas.c:11965-11976). */
+GPD double gp_polar_ionisation(const gp_tables & T, double ki, double kf)
+{
+        const double nu = ki - kf;
+        const double p2 = ki * (ki + 2 * T.mass);
+        const double E = ki + T.mass;
+        const double c = (p2 - nu * (E + GP_ELECTRON_MASS)) /
+            sqrt(p2 * (p2 + nu * nu - 2 * nu * E));
+        return 0.5 * (1. - c);
+}
+
+__device__ double gp_polar(const gp_tables & T, gp_event & e, int process,
+    const gp_element & el, double ki, double kf)
+{
+        if (process <= 1)
+                return gp_polar_bremsstrahlung(T, e, el, ki, kf);
+        else if (process == 2)
+                return gp_polar_photonuclear(T, e, el, ki, kf);
+        else
+                return gp_polar_ionisation(T, ki, kf);
+}
+
+/* ------------------------------------------------------------------------ */
+/* DEL sampling (pumas.c:5706-6270, 11185-11226).                           */
+/* ------------------------------------------------------------------------ */
+
+/* dcs_ionisation_randomise (pumas.c:11185-11226). */
+__device__ double gp_ionisation_randomise(const gp_tables & T, gp_event & e,
+    const gp_element & el, double K, double xlow)
+{
+        const double P2 = K * (K + 2. * T.mass);
+        const double E = K + T.mass;
+        const double Wmax = 2. * GP_ELECTRON_MASS * P2 /
+            (T.mass * T.mass +
+                GP_ELECTRON_MASS * (GP_ELECTRON_MASS + 2. * E));
+        if (Wmax < T.cutoff * K) return K;
+        double Wmin = (13.6 / 19.2) * el.I;
+        const double qlow = K * xlow;
+        if (qlow >= Wmin) Wmin = qlow;
+        const double E2 = E * E;
+        const double beta2 = P2 / E2;
+        const double a0 = 0.5 / E2;
+        const double a1 = beta2 / Wmax;
+        const double p0 = a0 * (Wmax - Wmin);
+        const double p2 = 1. / Wmin - 1. / Wmax;
+        double q = 0.;
+        int trials;
+        for (trials = 0; trials < GP_MAX_REJECTIONS; trials++) {
+                double z = gp_random(e) * (p0 + p2);
+                if (z <= p0) {
+                        z /= p0;
+                        q = (Wmax - Wmin) * z;
+                } else {
+                        z = (z - p0) / p2;
+                        q = Wmin * Wmax / (Wmax - z * (Wmax - Wmin));
+                }
+                const double r0 = a0 + 1 / (q * q);
+                const double r1 = r0 - a1 / q;
+                if (gp_random(e) * r0 <= r1) break;
+        }
+        if (trials == GP_MAX_REJECTIONS) e.status = GPUMAS_RETURN_INTERNAL_ERROR;
+        return K - q;
+}
+
+GPD double gp_envelope_norm(double a, double xmin, double xmax)
+{
+        if (a == 1)
+                return log(xmax / xmin);
+        else
+                return (pow(xmin, 1. - a) - pow(xmax, 1. - a)) / (a - 1.);
+}
+
+/* del_randomise_target (pumas.c:6154-6270). Returns the process and sets the
+ * target element; in backward mode also the DCS sum as *weight. */
+__device__ void gp_del_target(const gp_tables & T, const gp_config & cfg,
+    gp_event & e, int material, double Q, int & process, int & element,
+    double & weight)
+{
+        int i1;
+        double h, dk;
+        i1 = gp_index(T, T.K, e.energy);
+        if (i1 < 0) {
+                i1 = 0;
+                h = dk = 0.;
+        } else if (i1 >= T.n_energies - 1) {
+                i1 = T.n_energies - 1;
+                h = dk = 0.;
+        } else {
+                const double K1 = __ldg(T.K + i1);
+                dk = __ldg(T.K + i1 + 1) - K1;
+                h = (e.energy - K1) / dk;
+        }
+        const int ic0 = __ldg(T.comp_start + material);
+        const int nc = __ldg(T.elements_in + material);
+        if (cfg.direction == GPUMAS_MODE_FORWARD) {
+                const double zeta = gp_random(e);
+                for (int ic = ic0; ic < ic0 + nc; ic++) {
+                        for (int ip = 0; ip < GP_N_DEL; ip++) {
+                                const long o =
+                                    (long)(ip * T.n_components + ic) *
+                                        T.n_energies + i1;
+                                const double csf = gp_pchip(h,
+                                    __ldg(T.CSf + o), __ldg(T.CSf + o + 1),
+                                    __ldg(T.CSf_dK + o) * dk,
+                                    __ldg(T.CSf_dK + o + 1) * dk);
+                                if (!(zeta > csf)) {
+                                        element = __ldg(T.comp_element + ic);
+                                        process = ip;
+                                        return;
+                                }
+                        }
+                }
+                /* Not reached for consistent tables (pumas.c:6209). */
+                element = __ldg(T.comp_element + ic0 + nc - 1);
+                process = GP_N_DEL - 1;
+                e.status = GPUMAS_RETURN_INTERNAL_ERROR;
+                return;
+        }
+        double stot = 0.;
+        for (int ip = 0; ip < GP_N_DEL; ip++) {
+                for (int ic = ic0; ic < ic0 + nc; ic++) {
+                        const gp_element & el =
+                            T.element[__ldg(T.comp_element + ic)];
+                        const double d = gp_dcs_evaluate(T, ip, el, e.energy, Q);
+                        stot += d * __ldg(T.comp_fraction + ic);
+                }
+        }
+        if (stot == 0.) {
+                weight = 0.;
+                return;
+        }
+        weight = stot;
+        if (cfg.scattering == GPUMAS_MODE_DISABLED) {
+                element = T.n_elements;
+                process = GP_N_DEL;
+                return;
+        }
+        double zeta = 0.;
+        int trials;
+        for (trials = 0; trials < GP_MAX_REJECTIONS; trials++) {
+                zeta = gp_random(e) * stot;
+                if ((zeta > 0.) && (zeta < stot)) break;
+        }
+        if (trials == GP_MAX_REJECTIONS) e.status = GPUMAS_RETURN_INTERNAL_ERROR;
+        /* The energy transfer and the weight share a union in the reference
+         * (struct del_info, pumas.c:643-655): the selection below evaluates
+         * the DCS at an energy transfer equal to stot (pumas.c:6250). */
+        const double Q_union = stot;
+        double s = 0.;
+        for (int ic = ic0; ic < ic0 + nc; ic++) {
+                const int iel = __ldg(T.comp_element + ic);
+                const gp_element & el = T.element[iel];
+                for (int ip = 0; ip < GP_N_DEL; ip++) {
+                        const double si =
+                            gp_dcs_evaluate(T, ip, el, e.energy, Q_union) *
+                            __ldg(T.comp_fraction + ic);
+                        s += si;
+                        if (!(zeta > s)) {
+                                element = iel;
+                                process = ip;
+                                return;
+                        }
+                }
+        }
+        element = __ldg(T.comp_element + ic0 + nc - 1);
+        process = GP_N_DEL - 1;
+        e.status = GPUMAS_RETURN_INTERNAL_ERROR;
+}
+
+/* del_randomise_forward (pumas.c:5912-6017). Returns true if a polar angle
+ * is to be sampled. */
+__device__ bool gp_del_forward(const gp_tables & T, const gp_config & cfg,
+    gp_event & e, int material, int & process, int & target)
+{
+        if (e.energy <= __ldg(T.Kt + material)) return false;
+        int ip = 0, iel = 0;
+        double w = 0.;
+        gp_del_target(T, cfg, e, material, 0., ip, iel, w);
+        const gp_element & el = T.element[iel];
+        target = iel;
+        process = ip;
+        if (ip == 3) {
+                e.energy = gp_ionisation_randomise(
+                    T, e, el, e.energy, T.cutoff);
+                return true;
+        }
+        double qmin, qmax;
+        if (ip == 2) {
+                gp_photonuclear_range(T.mass, e.energy, qmin, qmax);
+        } else {
+                qmax = e.energy + T.mass * el.qmax_m_pair;
+                qmin = (ip == 0) ? 0. : 4. * GP_ELECTRON_MASS;
+        }
+        double xmin = qmin / e.energy;
+        if (xmin < T.cutoff) xmin = T.cutoff;
+        const double xmax = qmax / e.energy;
+        if (xmin >= xmax) return false;
+
+        double a0, a1, b0, b1, p0;
+        const int imax = T.n_energies - 1;
+        const float * env = T.DCS_env +
+            2 * ((long)(ip * T.n_elements + el.index) * T.n_energies);
+        if (e.energy >= __ldg(T.K + imax)) {
+                a0 = (double)__ldg(env + 2 * imax);
+                b0 = (double)__ldg(env + 2 * imax + 1);
+                p0 = 1.;
+                a1 = b1 = 0.;
+        } else {
+                const int row = gp_index(T, T.K, e.energy);
+                a0 = (double)__ldg(env + 2 * row);
+                b0 = (double)__ldg(env + 2 * row + 1);
+                a1 = (double)__ldg(env + 2 * row + 2);
+                b1 = (double)__ldg(env + 2 * row + 3);
+                const double k0 = __ldg(T.K + row);
+                const double k1 = __ldg(T.K + row + 1);
+                const double h1 = (e.energy - k0) / (k1 - k0);
+                const double h0 = 1. - h1;
+                b0 *= h0;
+                b1 *= h1;
+                p0 = gp_envelope_norm(a0, xmin, xmax) * b0;
+                const double p1 = gp_envelope_norm(a1, xmin, xmax) * b1;
+                p0 /= p0 + p1;
+        }
+        double x = 0.;
+        int i;
+        for (i = 0; i < 100; i++) {
+                double u = gp_random(e);
+                double a;
+                if (u < p0) {
+                        a = a0;
+                        u = u / p0;
+                } else {
+                        a = a1;
+                        u = (u - p0) / (1. - p0);
+                }
+                if (a == 1) {
+                        x = xmin * exp(u * log(xmax / xmin));
+                } else {
+                        const double am = a - 1.;
+                        const double pmin = pow(xmin, -am);
+                        const double pmax = pow(xmax, -am);
+                        x = pow(pmin - u * (pmin - pmax), -1. / am);
+                }
+                const double penv = b0 * pow(x, -a0) + b1 * pow(x, -a1);
+                const double d = gp_dcs_evaluate(T, ip, el, e.energy,
+                    e.energy * x);
+                if (gp_random(e) * penv <= d) break;
+        }
+        if (i == 100) return false;
+        e.energy *= (1. - x);
+        return true;
+}
+
+/* del_randomise_reverse (pumas.c:6036-6093) with the power law sampling
+ * of del_randomise_power_law (pumas.c:6109-6138), alpha = 2. */
+__device__ bool gp_del_reverse(const gp_tables & T, const gp_config & cfg,
+    gp_event & e, int material, int & process, int & target)
+{
+        const double lnq0 = -log(T.cutoff);
+        const double kt = __ldg(T.Kt + material);
+        const double kf = e.energy;
+        const double pCEL =
+            (kf >= kt) ? 0. : lnq0 / (lnq0 + log(kt / (kt - kf)));
+        if (pCEL && (gp_random(e) < pCEL)) {
+                e.weight /= pCEL;
+                return false;
+        }
+        const double xf =
+            (kf >= kt * (1. - T.cutoff)) ? T.cutoff : 1. - kf / kt;
+        double xmax;
+        const double m1 = T.mass - GP_ELECTRON_MASS;
+        if (e.energy < 0.5 * m1 * m1 / GP_ELECTRON_MASS) {
+                const double m2 = T.mass + GP_ELECTRON_MASS;
+                xmax = 2. * GP_ELECTRON_MASS * (e.energy + 2. * T.mass) /
+                    (m2 * m2);
+                if (xmax < xf)
+                        return false;
+                else if (xmax > 1.)
+                        xmax = 1.;
+        } else {
+                xmax = 1.;
+        }
+        double r = 0., w_bias = 0.;
+        {
+                const double alpha = 2.0;
+                const double a1 = 1. - alpha;
+                const double x0 = pow(xf, a1);
+                const double x1 = pow(xmax, a1);
+                int trials;
+                for (trials = 0; trials < GP_MAX_REJECTIONS; trials++) {
+                        const double z = gp_random(e);
+                        const double tmp = x0 + z * (x1 - x0);
+                        r = pow(tmp, 1. / a1);
+                        if ((r < xf) || (r >= xmax)) continue;
+                        w_bias = (x1 - x0) * r / (a1 * tmp);
+                        break;
+                }
+                if (trials == GP_MAX_REJECTIONS) {
+                        e.status = GPUMAS_RETURN_INTERNAL_ERROR;
+                        return false;
+                }
+                r = 1. - r;
+        }
+        w_bias /= r;
+        e.energy /= r;
+        int ip = 0, iel = 0;
+        double weight = 0.;
+        gp_del_target(T, cfg, e, material, e.energy - kf, ip, iel, weight);
+        if (weight <= 0) {
+                e.weight = 0.;
+                return false;
+        }
+        e.weight *= w_bias * weight /
+            (gp_del_cross_section(T, material, kf) * (1. - pCEL));
+        process = ip;
+        if (cfg.scattering == GPUMAS_MODE_DISABLED) return false;
+        target = iel;
+        return true;
+}
+
+/* transport_do_del (pumas.c:5706-5757). */
+__device__ void gp_do_del(const gp_tables & T, const gp_config & cfg,
+    gp_event & e, int material)
+{
+        double ki, kf;
+        int process = -1, target = 0;
+        bool polar;
+        if (cfg.direction == GPUMAS_MODE_FORWARD) {
+                ki = e.energy;
+                polar = gp_del_forward(T, cfg, e, material, process, target);
+                kf = e.energy;
+        } else {
+                kf = e.energy;
+                polar = gp_del_reverse(T, cfg, e, material, process, target);
+                ki = e.energy;
+        }
+        if (process < 0) {
+                e.step_event = (e.weight > 0) ? GPUMAS_EVENT_NONE :
+                                                GPUMAS_EVENT_WEIGHT;
+        } else {
+                e.step_event = (process == 0) ?
+                    GPUMAS_EVENT_VERTEX_BREMSSTRAHLUNG :
+                    (process == 1) ? GPUMAS_EVENT_VERTEX_PAIR_CREATION :
+                    (process == 2) ? GPUMAS_EVENT_VERTEX_PHOTONUCLEAR :
+                    (process == 3) ? GPUMAS_EVENT_VERTEX_DELTA_RAY :
+                                     GPUMAS_EVENT_VERTEX;
+        }
+        if ((cfg.scattering == GPUMAS_MODE_MIXED) && polar) {
+                if (kf > ki) {
+                        const double tmp = kf;
+                        kf = ki;
+                        ki = tmp;
+                }
+                const double mu = gp_polar(T, e, process, T.element[target],
+                    ki, kf);
+                gp_rotate(e, mu);
+        }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Elastic hard scattering (transport_do_ehs, pumas.c:5768-5885).           */
+/* ------------------------------------------------------------------------ */
+__device__ void gp_do_ehs(const gp_tables & T, const gp_config & cfg,
+    gp_event & e, int material)
+{
+        const double kinetic = e.energy;
+        double mu0 = 0., invlb1 = 0.;
+        gp_table_get_msc(T, cfg.energy_loss, material, kinetic, mu0, invlb1);
+        const int n_el = __ldg(T.elements_in + material);
+        const int ic0 = __ldg(T.comp_start + material);
+        const double fspin = gp_coulomb_spin_factor(T.mass, kinetic);
+
+        /* Choice of the hard scatterer: the restricted cross sections are
+         * only needed for compound materials. */
+        int ihard = n_el - 1;
+        if (n_el > 1) {
+                double cs_hard[GP_MAX_COMPONENTS];
+                double cs_tot = 0.;
+                for (int i = 0; i < n_el; i++) {
+                        const gp_element & el =
+                            T.element[__ldg(T.comp_element + ic0 + i)];
+                        double kinetic0, fCM[2], amplitude[3], screening[4];
+                        double a[3], b[3], c[4];
+                        gp_coulomb_frame_parameters(
+                            el.Ma, T.mass, kinetic, kinetic0, fCM);
+                        const int np = gp_coulomb_screening(el, T.mass,
+                            kinetic, kinetic0, amplitude, screening);
+                        gp_coulomb_pole_reduction(
+                            np, amplitude, screening, a, b, c);
+                        const double normalisation =
+                            __ldg(T.comp_fraction + ic0 + i) /
+                            gp_coulomb_normalisation(
+                                el.Z, el.A, T.mass, kinetic, kinetic0);
+                        cs_hard[i] = normalisation *
+                            gp_coulomb_restricted_cs(
+                                mu0, fspin, np, screening, a, b, c);
+                        cs_tot += cs_hard[i];
+                }
+                const double cc0 = gp_random(e) * cs_tot;
+                double cs = 0.;
+                for (int i = 0; i < n_el; i++) {
+                        cs += cs_hard[i];
+                        if (cs >= cc0) {
+                                ihard = i;
+                                break;
+                        }
+                }
+        } else {
+                /* One element: the draw is consumed, the choice forced. */
+                gp_random(e);
+        }
+
+        const gp_element & el = T.element[__ldg(T.comp_element + ic0 + ihard)];
+        double kinetic0, fCM[2], amplitude[3], screening[4];
+        gp_coulomb_frame_parameters(el.Ma, T.mass, kinetic, kinetic0, fCM);
+        const int np = gp_coulomb_screening(
+            el, T.mass, kinetic, kinetic0, amplitude, screening);
+        const int n = np - 1;
+        double A = screening[0];
+        for (int i = 1; i < 3; i++) {
+                if (i >= n) break;
+                if (screening[i] < A) A = screening[i];
+        }
+        double mu1 = mu0;
+        int trials;
+        for (trials = 0; trials < GP_MAX_REJECTIONS; trials++) {
+                const double zeta = gp_random(e);
+                const double tmp = 1. + A - zeta * (1 - mu0);
+                if (tmp <= 0.) continue;
+                mu1 = (A + mu0) * (A + 1.) / tmp - A;
+                if (mu1 < mu0)
+                        mu1 = mu0;
+                else if (mu1 > 1.)
+                        mu1 = 1;
+                double ratio = 0.;
+                for (int k = 0; k < 3; k++) {
+                        if (k >= n) break;
+                        ratio += amplitude[k] * (A + mu1) / (screening[k] + mu1);
+                }
+                ratio *= gp_coulomb_nuclear_form_factor(mu1, screening[n]);
+                ratio *= ratio * (1. - fspin * mu1);
+                if (gp_random(e) <= ratio) break;
+        }
+        if (trials == GP_MAX_REJECTIONS) e.status = GPUMAS_RETURN_INTERNAL_ERROR;
+        const double gamma = fCM[0];
+        const double tau = fCM[1];
+        double mu;
+        if (mu1 > 1E-06) {
+                const double a = gamma * (tau + 1. - 2. * mu1);
+                const double ct_h = a / sqrt(4. * mu1 * (1. - mu1) + a * a);
+                mu = 0.5 * (1. - ct_h);
+        } else {
+                const double d = gamma * (1. + tau);
+                mu = mu1 / (d * d);
+        }
+        gp_rotate(e, mu);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Stepping (pumas.c:5194-5696, 6296-7005).                                 */
+/* ------------------------------------------------------------------------ */
+
+/* step_fluctuate (pumas.c:6943-7005). */
+__device__ void gp_fluctuate(const gp_tables & T, const gp_config & cfg,
+    gp_event & e, int material, double Xtot, double dX, double & kf,
+    double & ratio)
+{
+        const int scheme = cfg.energy_loss;
+        const double sgn = (cfg.direction == GPUMAS_MODE_FORWARD) ? 1. : -1.;
+        double k1, r = 0.;
+        k1 = gp_cel_kinetic_energy(T, scheme, material, Xtot - sgn * dX);
+        const double dk0 = fabs(e.energy - k1);
+        if ((k1 > 0.) && (dk0 > 0.)) {
+                const double Omega0 = gp_cel_straggling(T, material, e.energy);
+                const double Omega1 = gp_cel_straggling(T, material, k1);
+                double dk12 = 0.5 * dX * (Omega0 + Omega1);
+                const double tmp = dX / Xtot;
+                if (tmp > 5E-02) {
+                        const double de1 =
+                            gp_cel_energy_loss(T, scheme, material, k1);
+                        const double de0 =
+                            gp_cel_energy_loss(T, scheme, material, e.energy);
+                        dk12 *= 1. + sgn * dX / dk0 * (de1 - de0);
+                }
+                const double dk1 = sqrt(dk12);
+                if (dk0 >= 3. * dk1) {
+                        double u;
+                        int trials = 0;
+                        do {
+                                u = gp_randn(e);
+                        } while ((fabs(u) > 3.) &&
+                            (++trials < GP_MAX_REJECTIONS));
+                        if (trials == GP_MAX_REJECTIONS)
+                                e.status = GPUMAS_RETURN_INTERNAL_ERROR;
+                        u /= 1.015387;
+                        k1 += u * dk1;
+                } else if (dk0 >= 1.7320508 * dk1) {
+                        const double u = 1.7320508 * (1. - 2. * gp_random(e));
+                        k1 += u * dk1;
+                } else {
+                        const double dk32 = 3. * dk12;
+                        const double dk02 = dk0 * dk0;
+                        const double a =
+                            1. - (dk32 - dk02) / (dk32 + 3. * dk02);
+                        if (gp_random(e) <= a) {
+                                const double b =
+                                    0.5 * (dk32 + 3. * dk02) / dk0;
+                                const double u = gp_random(e);
+                                k1 = e.energy - sgn * b * u;
+                                if (k1 < 0.) k1 = 0.;
+                        } else {
+                                k1 = e.energy;
+                        }
+                }
+                r = fabs(e.energy - k1) / dk0;
+        }
+        if (r == 0.) r = 1.;
+        kf = k1;
+        ratio = r;
+}
+
+/* transport_limit (pumas.c:5569-5696). */
+__device__ void gp_limit(const gp_tables & T, const gp_config & cfg,
+    gp_event & e, int material, double Xi, double Xf, double & grammage_max)
+{
+        e.step_event = e.step_foreseen = GPUMAS_EVENT_NONE;
+        if (e.weight <= 0.) {
+                e.step_event = GPUMAS_EVENT_WEIGHT;
+                return;
+        }
+        if (cfg.direction == GPUMAS_MODE_FORWARD) {
+                const double kinetic_min =
+                    (cfg.event & GPUMAS_EVENT_LIMIT_ENERGY) ?
+                    cfg.limit_energy : 0.;
+                if (e.energy <= kinetic_min) {
+                        e.step_event = GPUMAS_EVENT_LIMIT_ENERGY;
+                        return;
+                }
+        } else if ((cfg.event & GPUMAS_EVENT_LIMIT_ENERGY) &&
+            (e.energy >= cfg.limit_energy)) {
+                e.step_event = GPUMAS_EVENT_LIMIT_ENERGY;
+                return;
+        }
+        if (cfg.event & GPUMAS_EVENT_LIMIT_GRAMMAGE) {
+                grammage_max = cfg.limit_grammage;
+                e.step_foreseen = GPUMAS_EVENT_LIMIT_GRAMMAGE;
+        } else {
+                grammage_max = 0.;
+        }
+        const int scheme = cfg.energy_loss;
+        if (scheme == GPUMAS_MODE_DISABLED) {
+                if (cfg.scattering == GPUMAS_MODE_MIXED) {
+                        const double X = Xi -
+                            gp_coulomb_ehs_length(T, material, e.energy) *
+                                log(gp_random(e));
+                        if ((grammage_max == 0.) || (X < grammage_max)) {
+                                grammage_max = X;
+                                e.step_foreseen = GPUMAS_EVENT_VERTEX_COULOMB;
+                                return;
+                        }
+                }
+                return;
+        }
+        const double sgn = (cfg.direction == GPUMAS_MODE_FORWARD) ? 1. : -1.;
+        int foreseen = GPUMAS_EVENT_NONE;
+        double kinetic_limit = 0.;
+        if (scheme == GPUMAS_MODE_MIXED) {
+                for (int i = 0; i < 1000; i++) {
+                        const double zeta = gp_random(e);
+                        if ((zeta <= 0.) || (zeta >= 1.)) continue;
+                        const double nI =
+                            gp_del_interaction_length(T, material, e.energy) +
+                            sgn * log(zeta);
+                        if (nI <= 0.) break;
+                        const double k = gp_del_kinetic_from_interaction_length(
+                            T, material, nI);
+                        if (cfg.direction == GPUMAS_MODE_FORWARD) {
+                                if (k >= e.energy) continue;
+                        } else {
+                                if (k <= e.energy) continue;
+                        }
+                        if ((cfg.direction == GPUMAS_MODE_BACKWARD) ||
+                            (k > __ldg(T.Kt + material))) {
+                                kinetic_limit = k;
+                                foreseen = GPUMAS_EVENT_VERTEX_DEL;
+                        }
+                        break;
+                }
+        }
+        if ((scheme < GPUMAS_MODE_STRAGGLED) &&
+            (cfg.scattering == GPUMAS_MODE_MIXED)) {
+                const double nI = gp_ehs_interaction_length(
+                                      T, scheme, material, e.energy) +
+                    sgn * log(gp_random(e));
+                if (nI > 0.) {
+                        const double k = gp_ehs_kinetic_from_interaction_length(
+                            T, scheme, material, nI);
+                        if ((kinetic_limit <= 0.) ||
+                            ((cfg.direction == GPUMAS_MODE_FORWARD) &&
+                                (k > kinetic_limit)) ||
+                            ((cfg.direction == GPUMAS_MODE_BACKWARD) &&
+                                (k < kinetic_limit))) {
+                                kinetic_limit = k;
+                                foreseen = GPUMAS_EVENT_VERTEX_COULOMB;
+                        }
+                }
+        }
+        if (foreseen == GPUMAS_EVENT_NONE) return;
+        const double X = Xi + sgn * (Xf - gp_cel_grammage(
+                                            T, scheme, material, kinetic_limit));
+        if ((grammage_max <= 0) || (X < grammage_max)) {
+                grammage_max = X;
+                e.step_foreseen = foreseen;
+        }
+}
+
+/* step_transport (pumas.c:6296-6925) for uniform media without magnetic
+ * field. Sets e.step_event and returns the end step medium. */
+__device__ int gp_step(const gp_tables & T, const gp_config & cfg,
+    const gpumas_geometry & g, gp_event & e, int straight, int medium,
+    int material, double density, double grammage_max,
+    double step_max_medium)
+{
+        const int scheme = cfg.energy_loss;
+        const double density_i = 1. / density;
+        const double momentum = sqrt(e.energy * (e.energy + 2. * T.mass));
+        const int tmp_scheme =
+            (scheme == GPUMAS_MODE_DISABLED) ? GPUMAS_MODE_CSDA : scheme;
+        const double Xtot = gp_cel_grammage(T, tmp_scheme, material, e.energy);
+
+        double step_loc;
+        double invlb1 = 0.;
+        if (!straight) {
+                double r = cfg.accuracy;
+                const double k_threshold = 1E+09;
+                if ((scheme == GPUMAS_MODE_STRAGGLED) &&
+                    (e.energy > k_threshold)) {
+                        double f = k_threshold / e.energy;
+                        if (f < 0.1) f = 0.1;
+                        r *= f;
+                }
+                step_loc = r * density_i * Xtot;
+                if (cfg.scattering == GPUMAS_MODE_MIXED) {
+                        if (e.step_first != 0) {
+                                double mu0;
+                                gp_table_get_msc(T, scheme, material,
+                                    e.energy, mu0, invlb1);
+                                invlb1 *= density;
+                        } else
+                                invlb1 = e.step_invlb1;
+                        const double stepT = cfg.accuracy / invlb1;
+                        if (stepT < step_loc) step_loc = stepT;
+                }
+        } else {
+                if (grammage_max <= 0.)
+                        step_loc = 1E+09 * density_i;
+                else
+                        step_loc = grammage_max * density_i;
+        }
+        e.step_first = 0;
+        if (step_loc < GP_STEP_MIN) step_loc = GP_STEP_MIN;
+        double step = (step_max_medium <= 0) ?
+            step_loc :
+            (step_max_medium < step_loc ? step_max_medium : step_loc);
+
+        int out_medium = medium;
+        int event = GPUMAS_EVENT_NONE;
+        if (cfg.event & GPUMAS_EVENT_LIMIT_DISTANCE) {
+                const double d = cfg.limit_distance - e.distance;
+                if (d <= step) {
+                        step = d;
+                        event = GPUMAS_EVENT_LIMIT_DISTANCE;
+                }
+        }
+        const double sgn = (cfg.direction == GPUMAS_MODE_FORWARD) ? 1. : -1.;
+        const double sd0 = sgn * e.dir[0], sd1 = sgn * e.dir[1],
+                     sd2 = sgn * e.dir[2];
+        e.pos[0] += step * sd0;
+        e.pos[1] += step * sd1;
+        e.pos[2] += step * sd2;
+
+        int end_medium = gp_locate(g, e);
+        if (end_medium != medium) {
+                /* Boundary check of a PUMAS_STEP_CHECK geometry
+                 * (pumas.c:6425-6485). */
+                const double step_min = (step < GP_STEP_MIN) ? step : GP_STEP_MIN;
+                const double pi0 = e.pos[0], pi1 = e.pos[1], pi2 = e.pos[2];
+                double s1 = 0., s2 = -step_min;
+                e.pos[0] = pi0 + s2 * sd0;
+                e.pos[1] = pi1 + s2 * sd1;
+                e.pos[2] = pi2 + s2 * sd2;
+                int tmp_medium = gp_locate(g, e);
+                if (tmp_medium != medium) {
+                        if (tmp_medium != end_medium) end_medium = tmp_medium;
+                        s1 = s2;
+                        s2 = -step;
+                        while (fabs(s1 - s2) > GP_STEP_MIN) {
+                                double s3 = 0.5 * (s1 + s2);
+                                e.pos[0] = pi0 + s3 * sd0;
+                                e.pos[1] = pi1 + s3 * sd1;
+                                e.pos[2] = pi2 + s3 * sd2;
+                                tmp_medium = gp_locate(g, e);
+                                if (tmp_medium == medium) {
+                                        s2 = s3;
+                                } else {
+                                        s1 = s3;
+                                        if (tmp_medium != end_medium)
+                                                end_medium = tmp_medium;
+                                }
+                        }
+                        step += s1;
+                        e.pos[0] = pi0 + s1 * sd0;
+                        e.pos[1] = pi1 + s1 * sd1;
+                        e.pos[2] = pi2 + s1 * sd2;
+                } else {
+                        e.pos[0] = pi0;
+                        e.pos[1] = pi1;
+                        e.pos[2] = pi2;
+                }
+                event = GPUMAS_EVENT_MEDIUM;
+                out_medium = end_medium;
+        }
+
+        const double density1 = density;
+        double k1 = e.energy, dk = 0.;
+        const double dX = 0.5 * step * (density + density1);
+        if ((scheme >= GPUMAS_MODE_CSDA) && (scheme <= GPUMAS_MODE_MIXED)) {
+                const double X = Xtot - sgn * dX;
+                if ((cfg.direction == GPUMAS_MODE_FORWARD) &&
+                    (X <= e.step_X_limit)) {
+                        k1 = (cfg.event & GPUMAS_EVENT_LIMIT_ENERGY) ?
+                            cfg.limit_energy : 0.;
+                        const double grammage =
+                            e.grammage + Xtot - e.step_X_limit;
+                        if ((grammage_max <= 0.) || (grammage < grammage_max)) {
+                                grammage_max = grammage;
+                                event = GPUMAS_EVENT_LIMIT_ENERGY;
+                        }
+                } else if ((cfg.direction == GPUMAS_MODE_BACKWARD) &&
+                    (e.step_X_limit > 0.) && (X > e.step_X_limit)) {
+                        k1 = (cfg.event & GPUMAS_EVENT_LIMIT_ENERGY) ?
+                            cfg.limit_energy : 0.;
+                        const double grammage =
+                            e.grammage + e.step_X_limit - Xtot;
+                        if ((grammage_max <= 0.) || (grammage < grammage_max)) {
+                                grammage_max = grammage;
+                                event = GPUMAS_EVENT_LIMIT_ENERGY;
+                        }
+                } else if (dX < GP_EPSILON_X * Xtot) {
+                        k1 -= sgn * gp_cel_energy_loss(T, scheme, material, k1) *
+                            dX;
+                        if ((cfg.event & GPUMAS_EVENT_LIMIT_ENERGY) &&
+                            (cfg.limit_energy > 0.)) {
+                                if (((cfg.direction == GPUMAS_MODE_FORWARD) &&
+                                        (k1 < cfg.limit_energy)) ||
+                                    ((cfg.direction == GPUMAS_MODE_BACKWARD) &&
+                                        (k1 > cfg.limit_energy))) {
+                                        k1 = cfg.limit_energy;
+                                        event = GPUMAS_EVENT_LIMIT_ENERGY;
+                                }
+                        } else if (k1 < 0.) {
+                                k1 = 0.;
+                        }
+                } else {
+                        k1 = gp_cel_kinetic_energy(T, scheme, material, X);
+                }
+        } else if (scheme == GPUMAS_MODE_STRAGGLED) {
+                double ratio;
+                gp_fluctuate(T, cfg, e, material, Xtot, dX, k1, ratio);
+                dk = fabs(e.energy - k1);
+                double kinetic_limit = -1.;
+                if (cfg.direction == GPUMAS_MODE_FORWARD) {
+                        const double kinetic_min =
+                            (cfg.event & GPUMAS_EVENT_LIMIT_ENERGY) ?
+                            cfg.limit_energy : 0.;
+                        if (k1 <= kinetic_min) kinetic_limit = kinetic_min;
+                } else {
+                        if ((cfg.event & GPUMAS_EVENT_LIMIT_ENERGY) &&
+                            (k1 >= cfg.limit_energy))
+                                kinetic_limit = cfg.limit_energy;
+                }
+                if (kinetic_limit >= 0.) {
+                        const double grammage = e.grammage +
+                            fabs(e.energy - kinetic_limit) / dk * dX;
+                        k1 = kinetic_limit;
+                        if ((grammage_max <= 0.) || (grammage < grammage_max)) {
+                                grammage_max = grammage;
+                                event = GPUMAS_EVENT_LIMIT_ENERGY;
+                        }
+                }
+                double Xmax = dX;
+                if (grammage_max > 0.) {
+                        const double dX1 = grammage_max - e.grammage;
+                        if (Xmax > dX1) Xmax = dX1;
+                }
+                double k_x = -1.;
+                do {
+                        /* DEL candidate, thinned (pumas.c:6600-6621). */
+                        double xs_del =
+                            gp_del_cross_section(T, material, e.energy);
+                        const double tmp_del =
+                            gp_del_cross_section(T, material, k1);
+                        if (tmp_del > xs_del) xs_del = tmp_del;
+                        if (xs_del <= 0.) break;
+                        const double X_del = -log(gp_random(e)) / xs_del;
+                        if (X_del >= Xmax) break;
+                        const double k_h = gp_cel_kinetic_energy(
+                            T, scheme, material, Xtot - sgn * X_del);
+                        const double k_del =
+                            e.energy - sgn * ratio * fabs(e.energy - k_h);
+                        if (k_del <= 0.) break;
+                        const double r =
+                            gp_del_cross_section(T, material, k_del) / xs_del;
+                        if (gp_random(e) > r) break;
+                        k_x = k_del;
+                        Xmax = X_del;
+                        event = GPUMAS_EVENT_VERTEX_DEL;
+                } while (0);
+                if (cfg.scattering == GPUMAS_MODE_MIXED) do {
+                        /* EHS candidate, thinned (pumas.c:6623-6656). */
+                        double kmin, kmax;
+                        if (k1 <= e.energy)
+                                kmin = k1, kmax = e.energy;
+                        else
+                                kmax = k1, kmin = e.energy;
+                        if (kmin < __ldg(T.K + 1)) {
+                                const double tmp = kmin;
+                                kmin = kmax, kmax = tmp;
+                        }
+                        const double lb_ehs =
+                            gp_coulomb_ehs_length(T, material, kmin);
+                        if (lb_ehs <= 0.) break;
+                        const double X_ehs = -log(gp_random(e)) * lb_ehs;
+                        if (X_ehs >= Xmax) break;
+                        const double k_h = gp_cel_kinetic_energy(
+                            T, scheme, material, Xtot - sgn * X_ehs);
+                        const double k_ehs =
+                            e.energy - sgn * ratio * fabs(e.energy - k_h);
+                        if (k_ehs <= 0.) break;
+                        const double r =
+                            gp_coulomb_ehs_length(T, material, k_ehs) / lb_ehs;
+                        if ((r <= 0.) || (gp_random(e) > 1. / r)) break;
+                        k_x = k_ehs;
+                        Xmax = X_ehs;
+                        event = GPUMAS_EVENT_VERTEX_COULOMB;
+                } while (0);
+                if (k_x >= 0.) {
+                        k1 = k_x;
+                        grammage_max = e.grammage + Xmax;
+                }
+        }
+
+        const double Xi = e.grammage;
+        e.grammage += dX;
+        const double sf0 = step;
+        if ((grammage_max > 0.) && (e.grammage >= grammage_max)) {
+                const double dX_ = grammage_max - Xi;
+                step = dX_ * density_i;
+                e.grammage = grammage_max;
+                if (!(event & GPUMAS_EVENT_LIMIT_ENERGY)) {
+                        if (scheme <= GPUMAS_MODE_MIXED) {
+                                if (scheme != GPUMAS_MODE_DISABLED)
+                                        k1 = gp_cel_kinetic_energy(T, scheme,
+                                            material,
+                                            Xtot - sgn * (e.grammage - Xi));
+                                event = e.step_foreseen;
+                        } else if (!(event & (GPUMAS_EVENT_VERTEX_COULOMB |
+                                                 GPUMAS_EVENT_VERTEX_DEL))) {
+                                k1 = e.energy -
+                                    sgn * (e.grammage - Xi) * dk / dX;
+                                if (k1 < 0.) k1 = 0.;
+                                event = GPUMAS_EVENT_LIMIT_GRAMMAGE;
+                        }
+                }
+                const double ds_ = step - sf0;
+                e.pos[0] += ds_ * sd0;
+                e.pos[1] += ds_ * sd1;
+                e.pos[2] += ds_ * sd2;
+        }
+
+        int decayed = 0;
+        double time_max =
+            (cfg.event & GPUMAS_EVENT_LIMIT_TIME) ? cfg.limit_time : 0.;
+        if (cfg.decay == GPUMAS_MODE_RANDOMISED) {
+                if ((time_max <= 0.) || (e.lifetime < time_max)) {
+                        time_max = e.lifetime;
+                        decayed = 1;
+                }
+        }
+        const double sf1 = step;
+        if (straight && (scheme != GPUMAS_MODE_DISABLED)) {
+                const double Ti =
+                    gp_cel_proper_time(T, scheme, material, e.energy);
+                if (time_max > 0.) {
+                        const double Tf =
+                            Ti - sgn * (time_max - e.time) * density;
+                        if (Tf > 0.) {
+                                const double dxT = fabs(Xtot -
+                                    gp_cel_grammage_as_time(
+                                        T, scheme, material, Tf));
+                                if (Xi + dxT < e.grammage) {
+                                        event = GPUMAS_EVENT_LIMIT_TIME;
+                                        e.time = time_max;
+                                        e.decayed = decayed;
+                                        step = dxT * density_i;
+                                        if (step > sf1) step = sf1;
+                                        e.grammage = Xi + dxT;
+                                        const double xf = Xtot - sgn * dxT;
+                                        k1 = gp_cel_kinetic_energy(
+                                            T, scheme, material, xf);
+                                }
+                        }
+                }
+                if (event != GPUMAS_EVENT_LIMIT_TIME) {
+                        const double Tf =
+                            gp_cel_proper_time(T, scheme, material, k1);
+                        e.time += fabs(Tf - Ti) * density_i;
+                }
+        } else {
+                const double p_f =
+                    (k1 <= 0) ? momentum : sqrt(k1 * (k1 + 2. * T.mass));
+                const double ti = e.time;
+                e.time += 0.5 * step * T.mass * (1. / momentum + 1. / p_f);
+                if ((time_max > 0.) && (e.time >= time_max)) {
+                        event = GPUMAS_EVENT_LIMIT_TIME;
+                        e.time = time_max;
+                        e.decayed = decayed;
+                        const double a = (momentum / p_f - 1.) / sf1;
+                        const double c =
+                            -2. * (time_max - ti) * momentum / T.mass;
+                        if (a != 0.) {
+                                double delta = 1. - a * c;
+                                if (delta < 0.) delta = 0.;
+                                step = 1. / a * (sqrt(delta) - 1.);
+                        } else {
+                                step = -0.5 * c;
+                        }
+                        if (step < 0.) step = 0.;
+                        if (scheme != GPUMAS_MODE_DISABLED) {
+                                const double p1 = momentum / (1 + a * step);
+                                k1 = sqrt(p1 * p1 - T.mass * T.mass) - T.mass;
+                                if (k1 < 0.) k1 = 0.;
+                        }
+                        const double Xf = Xi + dX;
+                        e.grammage = Xi + step * density;
+                        if (e.grammage > Xf) e.grammage = Xf;
+                }
+        }
+        if (event == GPUMAS_EVENT_LIMIT_TIME) {
+                const double ds_ = step - sf1;
+                e.pos[0] += ds_ * sd0;
+                e.pos[1] += ds_ * sd1;
+                e.pos[2] += ds_ * sd2;
+        }
+
+        e.step_event = event;
+        e.energy = k1;
+        e.distance += step;
+
+        if (cfg.scattering == GPUMAS_MODE_MIXED) {
+                if (e.energy <= 0.) {
+                        e.step_invlb1 = invlb1;
+                } else {
+                        double mu0, invlb1_;
+                        gp_table_get_msc(
+                            T, scheme, material, e.energy, mu0, invlb1_);
+                        e.step_invlb1 = density1 * invlb1_;
+                }
+        }
+        if ((invlb1 > 0.) || (e.step_invlb1 > 0.)) {
+                double ilb1 = 0.25 * step * (invlb1 + e.step_invlb1);
+                if (ilb1 > 1.) ilb1 = 1.;
+                double mu;
+                int trials = 0;
+                do {
+                        mu = -ilb1 * log(gp_random(e));
+                } while ((mu > 1.) && (++trials < GP_MAX_REJECTIONS));
+                if (trials == GP_MAX_REJECTIONS)
+                        e.status = GPUMAS_RETURN_INTERNAL_ERROR;
+                gp_rotate(e, mu);
+        }
+        return out_medium;
+}
+
+/* Cap on the number of steps of one transport call; the reference has
+ * none, the engine stops the event with an internal error instead. */
+#define GP_MAX_STEPS 100000000
+
+/* transport_with_stepping (pumas.c:5194-5514), uniform media. */
+__device__ int gp_transport_stepping(const gp_tables & T,
+    const gp_config & cfg, const gpumas_geometry & g, gp_event & e,
+    int & medium, double density, double step_max_medium)
+{
+        int material = gp_medium_material(g, medium);
+        const int scheme = cfg.energy_loss;
+        const int straight = ((cfg.scattering == GPUMAS_MODE_DISABLED) &&
+                                 (scheme <= GPUMAS_MODE_MIXED)) ? 1 : 0;
+        e.step_event = GPUMAS_EVENT_NONE;
+        double ti = e.time, wi = e.weight, Xi = e.grammage;
+        double dei, Xf;
+        if (scheme > GPUMAS_MODE_DISABLED) {
+                Xf = gp_cel_grammage(T, scheme, material, e.energy);
+                dei = 1. / gp_cel_energy_loss(T, scheme, material, e.energy);
+        } else {
+                Xf = dei = 0.;
+        }
+        if ((cfg.event & GPUMAS_EVENT_LIMIT_DISTANCE) &&
+            (e.distance >= cfg.limit_distance))
+                return GPUMAS_EVENT_LIMIT_DISTANCE;
+        if ((cfg.event & GPUMAS_EVENT_LIMIT_GRAMMAGE) &&
+            (e.grammage >= cfg.limit_grammage))
+                return GPUMAS_EVENT_LIMIT_GRAMMAGE;
+        if ((cfg.event & GPUMAS_EVENT_LIMIT_TIME) &&
+            (e.time >= cfg.limit_time))
+                return GPUMAS_EVENT_LIMIT_TIME;
+        if (e.weight <= 0.) return GPUMAS_EVENT_WEIGHT;
+
+        double grammage_max = 0.;
+        e.step_event = GPUMAS_EVENT_NONE;
+        e.step_first = 1;
+        e.step_X_limit = (cfg.event & GPUMAS_EVENT_LIMIT_ENERGY) ?
+            gp_cel_grammage(T,
+                (scheme > GPUMAS_MODE_DISABLED) ? scheme : GPUMAS_MODE_CSDA,
+                material, cfg.limit_energy) :
+            0.;
+        e.step_invlb1 = 0;
+        gp_limit(T, cfg, e, material, Xi, Xf, grammage_max);
+        if (e.step_event) return e.step_event;
+
+        for (int step_index = 1; step_index < GP_MAX_STEPS; step_index++) {
+                if (e.status != GPUMAS_RETURN_SUCCESS) break;
+                if (step_index > 1) {
+                        const int m = gp_locate(g, e);
+                        step_max_medium = gp_step_proposal(cfg, g, e, m);
+                        if (step_max_medium > 0.)
+                                step_max_medium += 0.5 * GP_STEP_MIN;
+                }
+                const int new_medium = gp_step(T, cfg, g, e, straight, medium,
+                    material, density, grammage_max, step_max_medium);
+                if (!e.step_event) continue;
+
+                if ((cfg.direction == GPUMAS_MODE_BACKWARD) &&
+                    (cfg.energy_loss >= GPUMAS_MODE_CSDA)) {
+                        const double wt = (cfg.decay == GPUMAS_MODE_WEIGHTED) ?
+                            exp(-fabs(e.time - ti) / T.ctau) : 1.;
+                        e.weight = wi * wt * dei *
+                            gp_cel_energy_loss(T, scheme, material, e.energy);
+                } else if (cfg.decay == GPUMAS_MODE_WEIGHTED) {
+                        e.weight = wi * exp(-fabs(e.time - ti) / T.ctau);
+                }
+
+                if (e.step_event & (GPUMAS_EVENT_LIMIT | GPUMAS_EVENT_WEIGHT |
+                                       GPUMAS_EVENT_VERTEX_DECAY)) {
+                        break;
+                } else if (e.step_event & GPUMAS_EVENT_VERTEX_DEL) {
+                        gp_do_del(T, cfg, e, material);
+                        if ((cfg.event & e.step_event) ||
+                            (e.step_event == GPUMAS_EVENT_WEIGHT))
+                                break;
+                        e.step_first = 1;
+                        e.step_invlb1 = 0;
+                } else if (e.step_event & GPUMAS_EVENT_VERTEX_COULOMB) {
+                        gp_do_ehs(T, cfg, e, material);
+                        if (cfg.event & e.step_event) break;
+                } else if (e.step_event & GPUMAS_EVENT_MEDIUM) {
+                        medium = new_medium;
+                        if ((medium < 0) || (cfg.event & GPUMAS_EVENT_MEDIUM))
+                                break;
+                        material = gp_medium_material(g, medium);
+                        density = gp_medium_density(T, g, medium);
+                        if (density <= 0.) {
+                                e.status = GPUMAS_RETURN_DENSITY_ERROR;
+                                break;
+                        }
+                        e.step_X_limit =
+                            (cfg.event & GPUMAS_EVENT_LIMIT_ENERGY) ?
+                            gp_cel_grammage(T,
+                                scheme > GPUMAS_MODE_DISABLED ? scheme :
+                                                                GPUMAS_MODE_CSDA,
+                                material, cfg.limit_energy) :
+                            0.;
+                        e.step_first = 1;
+                        e.step_invlb1 = 0;
+                } else {
+                        e.status = GPUMAS_RETURN_INTERNAL_ERROR;
+                        break;
+                }
+                ti = e.time;
+                wi = e.weight;
+                Xi = e.grammage;
+                if (cfg.energy_loss >= GPUMAS_MODE_CSDA) {
+                        Xf = gp_cel_grammage(T, scheme, material, e.energy);
+                        dei = 1. /
+                            gp_cel_energy_loss(T, scheme, material, e.energy);
+                }
+                gp_limit(T, cfg, e, material, Xi, Xf, grammage_max);
+                if (e.step_event) break;
+                if (step_index == GP_MAX_STEPS - 1)
+                        e.status = GPUMAS_RETURN_INTERNAL_ERROR;
+        }
+
+        if (cfg.direction == GPUMAS_MODE_FORWARD) {
+                const double kinetic_min =
+                    (cfg.event & GPUMAS_EVENT_LIMIT_ENERGY) ?
+                    cfg.limit_energy : 0.;
+                if (fabs(e.energy - kinetic_min) < GP_FLT_EPSILON)
+                        e.energy = kinetic_min;
+        } else {
+                if ((cfg.event & GPUMAS_EVENT_LIMIT_ENERGY) &&
+                    (fabs(e.energy - cfg.limit_energy) < GP_FLT_EPSILON))
+                        e.energy = cfg.limit_energy;
+        }
+        return e.step_event;
+}
+
+/* transport_with_csda (pumas.c:4777-4949), no magnetic field. */
+__device__ int gp_transport_csda(const gp_tables & T, const gp_config & cfg,
+    gp_event & e, int material, double density)
+{
+        const double ki = e.energy;
+        const double di = e.distance;
+        const double ti = e.time;
+        const double xi = gp_cel_grammage(T, GPUMAS_MODE_CSDA, material, ki);
+        const double Ti = gp_cel_proper_time(T, GPUMAS_MODE_CSDA, material, ki);
+        int event = GPUMAS_EVENT_NONE;
+        double xB;
+        if (cfg.event & GPUMAS_EVENT_LIMIT_GRAMMAGE) {
+                xB = cfg.limit_grammage - e.grammage;
+                event = GPUMAS_EVENT_LIMIT_GRAMMAGE;
+        } else
+                xB = GP_DBL_MAX;
+        if (cfg.event & GPUMAS_EVENT_LIMIT_DISTANCE) {
+                const double xD = density * (cfg.limit_distance - di);
+                if (xD < xB) {
+                        xB = xD;
+                        event = GPUMAS_EVENT_LIMIT_DISTANCE;
+                }
+        }
+        int decayed = 0;
+        double time_max =
+            (cfg.event & GPUMAS_EVENT_LIMIT_TIME) ? cfg.limit_time : 0.;
+        if (cfg.decay == GPUMAS_MODE_RANDOMISED) {
+                if ((time_max <= 0.) || (e.lifetime < time_max)) {
+                        time_max = e.lifetime;
+                        decayed = 1;
+                }
+        }
+        if (time_max > 0.) {
+                const double dt = time_max - ti;
+                if (dt <= 0.) {
+                        xB = 0.;
+                        event = GPUMAS_EVENT_LIMIT_TIME;
+                } else {
+                        const double sgn =
+                            (cfg.direction == GPUMAS_MODE_FORWARD) ? 1. : -1.;
+                        const double Tf = Ti - sgn * dt * density;
+                        if (Tf > 0.) {
+                                const double xT = fabs(xi -
+                                    gp_cel_grammage_as_time(
+                                        T, GPUMAS_MODE_CSDA, material, Tf));
+                                if (xT < xB) {
+                                        xB = xT;
+                                        event = GPUMAS_EVENT_LIMIT_TIME;
+                                }
+                        }
+                }
+        }
+        if (xB <= 0.) return event;
+        double xf, kf;
+        if (cfg.direction == GPUMAS_MODE_FORWARD) {
+                if (xi > xB) {
+                        xf = xi - xB;
+                        if (xB < GP_EPSILON_X * xi) {
+                                kf = ki - gp_cel_energy_loss(T,
+                                    GPUMAS_MODE_CSDA, material, ki) * xB;
+                                if (kf < 0.) kf = 0.;
+                        } else {
+                                kf = gp_cel_kinetic_energy(
+                                    T, GPUMAS_MODE_CSDA, material, xf);
+                        }
+                } else {
+                        xf = kf = 0.;
+                        event = GPUMAS_EVENT_LIMIT_ENERGY;
+                }
+                if (cfg.event & GPUMAS_EVENT_LIMIT_ENERGY) {
+                        if (ki <= cfg.limit_energy)
+                                return GPUMAS_EVENT_LIMIT_ENERGY;
+                        if (kf < cfg.limit_energy) {
+                                kf = cfg.limit_energy;
+                                xf = gp_cel_grammage(
+                                    T, GPUMAS_MODE_CSDA, material, kf);
+                                event = GPUMAS_EVENT_LIMIT_ENERGY;
+                        }
+                }
+        } else {
+                if (xB == GP_DBL_MAX) {
+                        xf = xB;
+                        kf = GP_DBL_MAX;
+                } else {
+                        xf = xB + xi;
+                        if (xB < GP_EPSILON_X * xi) {
+                                kf = ki + gp_cel_energy_loss(T,
+                                    GPUMAS_MODE_CSDA, material, ki) * xB;
+                        } else {
+                                kf = gp_cel_kinetic_energy(
+                                    T, GPUMAS_MODE_CSDA, material, xf);
+                        }
+                }
+                if (cfg.event & GPUMAS_EVENT_LIMIT_ENERGY) {
+                        if (ki >= cfg.limit_energy)
+                                return GPUMAS_EVENT_LIMIT_ENERGY;
+                        if (kf > cfg.limit_energy) {
+                                kf = cfg.limit_energy;
+                                xf = gp_cel_grammage(
+                                    T, GPUMAS_MODE_CSDA, material, kf);
+                                event = GPUMAS_EVENT_LIMIT_ENERGY;
+                        }
+                }
+        }
+        const double distance = fabs(xf - xi) / density;
+        e.energy = kf;
+        if (event == GPUMAS_EVENT_LIMIT_DISTANCE)
+                e.distance = cfg.limit_distance;
+        else
+                e.distance += distance;
+        if (event == GPUMAS_EVENT_LIMIT_GRAMMAGE)
+                e.grammage = cfg.limit_grammage;
+        else
+                e.grammage += distance * density;
+        if (event == GPUMAS_EVENT_LIMIT_TIME) {
+                e.time = time_max;
+                e.decayed = decayed;
+                if (decayed) event = GPUMAS_EVENT_VERTEX_DECAY;
+        } else
+                e.time += fabs(Ti - gp_cel_proper_time(
+                                        T, GPUMAS_MODE_CSDA, material, kf)) /
+                    density;
+        if (cfg.direction == GPUMAS_MODE_BACKWARD)
+                e.weight *=
+                    gp_cel_energy_loss(T, GPUMAS_MODE_CSDA, material, kf) /
+                    gp_cel_energy_loss(T, GPUMAS_MODE_CSDA, material, ki);
+        if (cfg.decay == GPUMAS_MODE_WEIGHTED)
+                e.weight *= exp(-fabs(ti - e.time) / T.ctau);
+        const double path =
+            (cfg.direction == GPUMAS_MODE_FORWARD) ? distance : -distance;
+        e.pos[0] += path * e.dir[0];
+        e.pos[1] += path * e.dir[1];
+        e.pos[2] += path * e.dir[2];
+        return event;
+}
+
+/* Prepare the event context for a new transport call. */
+GPD void gp_event_init(gp_event & e, uint64_t seed, uint64_t id)
+{
+        e.step_first = 0;
+        e.step_event = e.step_foreseen = 0;
+        e.step_X_limit = e.step_invlb1 = 0.;
+        e.randn_done = 0;
+        e.randn_next = 0.;
+        e.lifetime = 0.;
+        e.id = id;
+        e.n = 0;
+        e.rnext = 0.;
+        e.k0 = (uint32_t)seed;
+        e.k1 = (uint32_t)(seed >> 32);
+        e.steps = 0;
+        e.status = GPUMAS_RETURN_SUCCESS;
+}
+
+/* pumas_context_transport (pumas.c:3114-3251) for one event. The context
+ * level checks are done on the host before the launch. */
+__device__ void gp_transport(const gp_tables & T, const gp_config & cfg,
+    const gpumas_geometry & g, gp_event & e, int & event, int & medium_in,
+    int & medium_out)
+{
+        event = GPUMAS_EVENT_NONE;
+        medium_in = medium_out = -1;
+        if (e.decayed) {
+                event = GPUMAS_EVENT_VERTEX_DECAY;
+                return;
+        }
+        {
+                const double * const u = e.dir;
+                const double norm2 = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
+                if (fabs(norm2 - 1) > GP_FLT_EPSILON) {
+                        e.status = GPUMAS_RETURN_DIRECTION_ERROR;
+                        return;
+                }
+        }
+        int medium = gp_locate(g, e);
+        double step_max_medium = gp_step_proposal(cfg, g, e, medium);
+        medium_in = medium;
+        if (medium < 0) {
+                event = GPUMAS_EVENT_MEDIUM;
+                return;
+        } else if (step_max_medium > 0.)
+                step_max_medium += 0.5 * GP_STEP_MIN;
+        const double density = gp_medium_density(T, g, medium);
+        if (density <= 0.) {
+                e.status = GPUMAS_RETURN_DENSITY_ERROR;
+                return;
+        }
+        if (cfg.decay == GPUMAS_MODE_RANDOMISED) {
+                const double u = gp_random(e);
+                e.lifetime = e.time - T.ctau * log(u);
+        }
+        int do_stepping = 1;
+        if ((step_max_medium <= 0.) &&
+            (cfg.energy_loss <= GPUMAS_MODE_CSDA)) {
+                if ((cfg.energy_loss == GPUMAS_MODE_DISABLED) &&
+                    ((cfg.event & GPUMAS_EVENT_LIMIT) == 0)) {
+                        e.status = GPUMAS_RETURN_MISSING_LIMIT;
+                        return;
+                } else if ((cfg.scattering == GPUMAS_MODE_DISABLED) &&
+                    (cfg.energy_loss == GPUMAS_MODE_CSDA)) {
+                        do_stepping = 0;
+                }
+        }
+        if (do_stepping) {
+                event = gp_transport_stepping(
+                    T, cfg, g, e, medium, density, step_max_medium);
+        } else {
+                event = gp_transport_csda(
+                    T, cfg, e, gp_medium_material(g, medium), density);
+        }
+        medium_out = medium;
+}
+
+#endif /* GP_DEVICE_CUH */

@@ -1,0 +1,103 @@
+/*
+ * gp_internal.h -- device image of the physics tables and engine internals.
+ *
+ * The tables of `struct pumas_physics` (pumas.c:660-806) are copied to one
+ * device allocation with the reference's row layouts: FP64 rows of
+ * n_energies values indexed as [scheme][material][row] or [material][row],
+ * and the FP32 DCS tables as [process][element][row][n_table_dcs][2]. At
+ * 1.8 MB for four materials the whole image stays resident in the 129 MB L2
+ * and its hot rows in L1.
+ *
+ * Per element constants that the reference recomputes inside the stepping
+ * (screening exponents of Salvat et al., nuclear radii, Z^1/3, radiation
+ * logarithms, pow(A, 0.27), ...) are evaluated once on the host at upload
+ * time with the same expressions, which removes FP64 work from the device
+ * and keeps the host libm values of the reference.
+ */
+#ifndef GP_INTERNAL_H
+#define GP_INTERNAL_H
+
+#include <stdint.h>
+
+#define GP_N_DEL 4
+#define GP_MAX_COMPONENTS 8
+
+/* Per element constants. */
+struct gp_element {
+        double Z, A, I;
+        int index;          /* element index in the DCS tables */
+        int n_screen;       /* number of atomic screening terms, 1 to 3 */
+        double amplitude[3];/* Salvat amplitudes (pumas.c:7348-7365) */
+        double a_screen[3]; /* exponent / BOHR_RADIUS (pumas.c:7369) */
+        double RN;          /* data_nuclear_radius (pumas.c:7143-7175) */
+        double Ma;          /* Z M_p + (A - Z) M_n (pumas.c:7495) */
+        double z13;         /* pow(Z, 1/3) */
+        double z13_inv;     /* 1 / pow(Z, 1/3) (SSR bremsstrahlung) */
+        double zm13;        /* pow(Z, -1/3) (SSR pair production) */
+        double z23;         /* pow(Z, 2/3) */
+        double dn;          /* 1.54 pow(A, 0.27) */
+        double rad_log;     /* radiation_logarithm(Z) */
+        double qmax_m_pair; /* 1 - 0.75 sqrt(e) Z^1/3, pair range */
+        double qmax_m_brems;/* 1 - 0.75 SQRTE Z^1/3, SSR brems bound */
+        double muni;        /* (m RN / hbar c)^2 / 6, polar brems */
+        double mu_qc;       /* SSR bremsstrahlung nuclear factor */
+        double ssr_delta1;  /* SSR bremsstrahlung delta1(mu_qc) */
+        double ssr_delta2;  /* SSR bremsstrahlung delta2(mu_qc) */
+        double pair_pref;   /* 4 / (3 pi) Z (alpha_em r_e)^2, SSR pairs */
+        double pair_medn2;  /* (m_e / m d_n)^2, SSR pairs (MeV units) */
+        double log_A;       /* log(A), DRSS shadowing */
+        double shadow_low;  /* exp(-0.1 log(A)), DRSS shadowing */
+};
+
+/* Numerical constants evaluated on the host with the reference's
+ * expressions (constant folded or libm). */
+struct gp_constants {
+        double exp1;        /* exp(1.) */
+        double exp_half;    /* exp(0.5) */
+        double exp_m16;     /* exp(-1. / 6.) */
+        double exp_13;      /* exp(1. / 3.) */
+        double exp_m13;     /* exp(-1. / 3.) */
+        double allm_lq0;    /* log(Q02 / Lambda2) in ALLM97 */
+        double pair_me_m2;  /* pow(ME / m, 2.) with m in MeV, SSR pairs */
+};
+
+struct gp_tables {
+        int n_energies, n_materials, n_elements, n_components, n_table_dcs;
+        double ctau, mass, cutoff, elastic_ratio;
+        const double *K, *K_dX, *K_dNI_in, *K_dNI_el;
+        const double *X, *X_dK, *X_dT, *T, *T_dK, *dE, *dE_dK;
+        const double *Omega, *Omega_dK, *NI_el, *NI_el_dK, *NI_in, *NI_in_dK;
+        const double *CS, *CS_dK, *CSf, *CSf_dK, *CSn, *CSn_dK;
+        const float *DCS, *DCS_x, *DCS_env;
+        const double *Kt, *a_max, *b_max, *Mu0, *Mu0_dK, *Lb, *Lb_dK;
+        const double *Ms1, *Ms1_dK;
+        const int * elements_in;
+        const int * comp_start;
+        const int * comp_element;
+        const double * comp_fraction;
+        const double * material_density;
+        const struct gp_element * element;
+        struct gp_constants k;
+};
+
+/* Host side handle. */
+struct gpumas_physics {
+        struct gp_tables tables; /* device pointers */
+        void * device_blob;
+        size_t device_size;
+        int n_materials;
+        int n_elements;
+        char ** material_name;
+        int device;
+};
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+int gp_physics_tables(const struct gpumas_physics * physics,
+    struct gp_tables * tables);
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,517 @@
+/*
+ * gp_transport.cu -- transport kernels and the context C ABI.
+ *
+ * Replaces the per event `pumas_context_transport` loop of a user program
+ * (e.g. the reference's examples/pumas/straight.c:133-179) by batched
+ * launches: one GPU thread per event, the event state in registers, the
+ * physics image and the geometry descriptor read through the L1 / L2
+ * caches. Context level checks mirror pumas.c:3120-3177 and are done on the
+ * host before any launch; per event checks (direction norm, density) are
+ * done on the device and reported in the per event status.
+ */
+#include <cuda_runtime.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "gp_device.cuh"
+
+/* ------------------------------------------------------------------------ */
+/* Event I/O: array of pumas_state structures or structure of arrays.       */
+/* ------------------------------------------------------------------------ */
+struct gp_io_aos {
+        gpumas_state * states;
+        gpumas_result * results;
+        __device__ void load(size_t i, gp_event & e) const
+        {
+                const gpumas_state & s = states[i];
+                e.charge = s.charge;
+                e.energy = s.energy;
+                e.distance = s.distance;
+                e.grammage = s.grammage;
+                e.time = s.time;
+                e.weight = s.weight;
+                for (int k = 0; k < 3; k++) {
+                        e.pos[k] = s.position[k];
+                        e.dir[k] = s.direction[k];
+                }
+                e.decayed = s.decayed;
+        }
+        __device__ void store(size_t i, const gp_event & e, int event,
+            int m_in, int m_out) const
+        {
+                gpumas_state & s = states[i];
+                s.charge = e.charge;
+                s.energy = e.energy;
+                s.distance = e.distance;
+                s.grammage = e.grammage;
+                s.time = e.time;
+                s.weight = e.weight;
+                for (int k = 0; k < 3; k++) {
+                        s.position[k] = e.pos[k];
+                        s.direction[k] = e.dir[k];
+                }
+                s.decayed = e.decayed;
+                if (results != NULL) {
+                        gpumas_result r;
+                        r.event = event;
+                        r.medium_in = m_in;
+                        r.medium_out = m_out;
+                        r.status = e.status;
+                        r.steps = e.steps;
+                        r.pad = 0;
+                        r.draws = e.n;
+                        results[i] = r;
+                }
+        }
+};
+
+struct gp_io_soa {
+        gpumas_soa a;
+        __device__ void load(size_t i, gp_event & e) const
+        {
+                e.charge = a.charge[i];
+                e.energy = a.energy[i];
+                e.distance = a.distance[i];
+                e.grammage = a.grammage[i];
+                e.time = a.time[i];
+                e.weight = a.weight[i];
+                for (int k = 0; k < 3; k++) {
+                        e.pos[k] = a.position[k][i];
+                        e.dir[k] = a.direction[k][i];
+                }
+                e.decayed = a.decayed[i];
+        }
+        __device__ void store(size_t i, const gp_event & e, int event,
+            int m_in, int m_out) const
+        {
+                a.charge[i] = e.charge;
+                a.energy[i] = e.energy;
+                a.distance[i] = e.distance;
+                a.grammage[i] = e.grammage;
+                a.time[i] = e.time;
+                a.weight[i] = e.weight;
+                for (int k = 0; k < 3; k++) {
+                        a.position[k][i] = e.pos[k];
+                        a.direction[k][i] = e.dir[k];
+                }
+                a.decayed[i] = e.decayed;
+                if (a.result != NULL) {
+                        gpumas_result r;
+                        r.event = event;
+                        r.medium_in = m_in;
+                        r.medium_out = m_out;
+                        r.status = e.status;
+                        r.steps = e.steps;
+                        r.pad = 0;
+                        r.draws = e.n;
+                        a.result[i] = r;
+                }
+        }
+};
+
+/* ------------------------------------------------------------------------ */
+/* Kernels.                                                                 */
+/* ------------------------------------------------------------------------ */
+
+/* Event I/O of a launch: AoS (pumas_state array) when `aos.states` is set,
+ * SoA otherwise. */
+struct gp_io {
+        gp_io_aos aos;
+        gp_io_soa soa;
+        __device__ void load(size_t i, gp_event & e) const
+        {
+                if (aos.states != NULL)
+                        aos.load(i, e);
+                else
+                        soa.load(i, e);
+        }
+        __device__ void store(size_t i, const gp_event & e, int event,
+            int m_in, int m_out) const
+        {
+                if (aos.states != NULL)
+                        aos.store(i, e, event, m_in, m_out);
+                else
+                        soa.store(i, e, event, m_in, m_out);
+        }
+};
+
+/* One thread per event, the whole transport call in one launch. */
+__global__ void __launch_bounds__(128) gp_kernel_plain(
+    const gp_tables * __restrict__ Tp, const gp_config cfg,
+    const gpumas_geometry * __restrict__ gp, const gp_io io, size_t n,
+    uint64_t first_event)
+{
+        const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+        if (i >= n) return;
+        const gp_tables & T = *Tp;
+        const gpumas_geometry & g = *gp;
+        gp_event e;
+        io.load(i, e);
+        gp_event_init(e, cfg.seed, first_event + i);
+        int event, m_in, m_out;
+        gp_transport(T, cfg, g, e, event, m_in, m_out);
+        io.store(i, e, event, m_in, m_out);
+}
+
+/* Draws of the Philox stream, for checking against other implementations. */
+__global__ void gp_kernel_random(uint64_t seed, uint32_t domain,
+    uint64_t event, uint64_t first, size_t n, double * out)
+{
+        const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+        if (i >= n) return;
+        const uint64_t k = first + i;
+        uint32_t x[4];
+        gp_philox((uint32_t)(k >> 1), domain, (uint32_t)event,
+            (uint32_t)(event >> 32), (uint32_t)seed, (uint32_t)(seed >> 32),
+            x);
+        out[i] = (k & 1) ? gp_word_to_uniform(x[2], x[3]) :
+                           gp_word_to_uniform(x[0], x[1]);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Contexts.                                                                */
+/* ------------------------------------------------------------------------ */
+struct gp_context {
+        struct gpumas_context api; /* first member: public view */
+        const struct gpumas_physics * physics;
+        gp_tables * d_tables;
+        gpumas_geometry * d_geometry;
+        void * d_geometry_data;
+        int has_geometry;
+        int n_media;
+        void * d_io;
+        size_t io_size;
+        cudaStream_t stream;
+        cudaEvent_t t0, t1;
+        struct gpumas_stats stats;
+        void * extra;
+};
+
+static int gp_check(cudaError_t rc)
+{
+        return (rc == cudaSuccess) ? GPUMAS_RETURN_SUCCESS :
+                                     GPUMAS_RETURN_DEVICE_ERROR;
+}
+
+extern "C" int gpumas_context_create(struct gpumas_context ** context,
+    const struct gpumas_physics * physics, int extra_memory)
+{
+        if (context == NULL) return GPUMAS_RETURN_VALUE_ERROR;
+        *context = NULL;
+        if (physics == NULL) return GPUMAS_RETURN_PHYSICS_ERROR;
+        gp_context * c = (gp_context *)calloc(1, sizeof(*c));
+        if (c == NULL) return GPUMAS_RETURN_MEMORY_ERROR;
+        c->physics = physics;
+        /* Defaults of pumas_context_create (pumas.c:2592-2612). */
+        c->api.mode.energy_loss = GPUMAS_MODE_STRAGGLED;
+        c->api.mode.decay = GPUMAS_MODE_WEIGHTED;
+        c->api.mode.direction = GPUMAS_MODE_FORWARD;
+        c->api.mode.scattering = GPUMAS_MODE_MIXED;
+        c->api.event = GPUMAS_EVENT_NONE;
+        c->api.accuracy = 1E-02;
+        c->api.seed = 0;
+        if (extra_memory > 0) {
+                c->extra = calloc(1, extra_memory);
+                c->api.user_data = c->extra;
+        }
+        gp_tables tables;
+        gp_physics_tables(physics, &tables);
+        int rc = gp_check(cudaMalloc(&c->d_tables, sizeof(gp_tables)));
+        if (rc == GPUMAS_RETURN_SUCCESS)
+                rc = gp_check(cudaMemcpy(c->d_tables, &tables,
+                    sizeof(gp_tables), cudaMemcpyHostToDevice));
+        if (rc == GPUMAS_RETURN_SUCCESS)
+                rc = gp_check(cudaMalloc(&c->d_geometry,
+                    sizeof(gpumas_geometry)));
+        if (rc == GPUMAS_RETURN_SUCCESS)
+                rc = gp_check(cudaStreamCreateWithFlags(
+                    &c->stream, cudaStreamNonBlocking));
+        if (rc == GPUMAS_RETURN_SUCCESS)
+                rc = gp_check(cudaEventCreate(&c->t0));
+        if (rc == GPUMAS_RETURN_SUCCESS)
+                rc = gp_check(cudaEventCreate(&c->t1));
+        if (rc != GPUMAS_RETURN_SUCCESS) {
+                struct gpumas_context * tmp = &c->api;
+                gpumas_context_destroy(&tmp);
+                return rc;
+        }
+        *context = &c->api;
+        return GPUMAS_RETURN_SUCCESS;
+}
+
+extern "C" void gpumas_context_destroy(struct gpumas_context ** context)
+{
+        if ((context == NULL) || (*context == NULL)) return;
+        gp_context * c = (gp_context *)(*context);
+        if (c->d_tables != NULL) cudaFree(c->d_tables);
+        if (c->d_geometry != NULL) cudaFree(c->d_geometry);
+        if (c->d_geometry_data != NULL) cudaFree(c->d_geometry_data);
+        if (c->d_io != NULL) cudaFree(c->d_io);
+        if (c->stream != NULL) cudaStreamDestroy(c->stream);
+        if (c->t0 != NULL) cudaEventDestroy(c->t0);
+        if (c->t1 != NULL) cudaEventDestroy(c->t1);
+        free(c->extra);
+        free(c);
+        *context = NULL;
+}
+
+/* Copy a geometry descriptor and its arrays to one device allocation. */
+extern "C" int gp_geometry_upload(const struct gpumas_physics * physics,
+    const struct gpumas_geometry * geometry, gpumas_geometry * d_geometry,
+    void ** d_data)
+{
+        if (geometry == NULL) return GPUMAS_RETURN_MEDIUM_ERROR;
+        const gpumas_geometry & g = *geometry;
+        if ((g.n_media <= 0) || (g.media == NULL))
+                return GPUMAS_RETURN_MEDIUM_ERROR;
+        for (int i = 0; i < g.n_media; i++) {
+                if ((g.media[i].material < 0) ||
+                    (g.media[i].material >= physics->n_materials))
+                        return GPUMAS_RETURN_INDEX_ERROR;
+        }
+        size_t sz_media = g.n_media * sizeof(gpumas_medium);
+        size_t sz_z = 0, sz_m = 0, sz_h = 0;
+        if (g.kind == GPUMAS_GEOMETRY_UNIFORM) {
+                if ((g.uniform_medium < 0) || (g.uniform_medium >= g.n_media))
+                        return GPUMAS_RETURN_INDEX_ERROR;
+        } else if (g.kind == GPUMAS_GEOMETRY_SLABS) {
+                if ((g.n_slabs <= 0) || (g.slab_z == NULL) ||
+                    (g.slab_medium == NULL))
+                        return GPUMAS_RETURN_MEDIUM_ERROR;
+                for (int i = 0; i < g.n_slabs; i++) {
+                        if (!(g.slab_z[i] < g.slab_z[i + 1]))
+                                return GPUMAS_RETURN_VALUE_ERROR;
+                        if ((g.slab_medium[i] < -1) ||
+                            (g.slab_medium[i] >= g.n_media))
+                                return GPUMAS_RETURN_INDEX_ERROR;
+                }
+                sz_z = (g.n_slabs + 1) * sizeof(double);
+                sz_m = g.n_slabs * sizeof(int);
+        } else if (g.kind == GPUMAS_GEOMETRY_HEIGHTMAP) {
+                if ((g.hm_nx < 2) || (g.hm_ny < 2) || (g.hm_z == NULL) ||
+                    !(g.hm_dx > 0.) || !(g.hm_dy > 0.))
+                        return GPUMAS_RETURN_VALUE_ERROR;
+                if ((g.hm_below < -1) || (g.hm_below >= g.n_media) ||
+                    (g.hm_above < -1) || (g.hm_above >= g.n_media))
+                        return GPUMAS_RETURN_INDEX_ERROR;
+                sz_h = (size_t)g.hm_nx * g.hm_ny * sizeof(double);
+        } else {
+                return GPUMAS_RETURN_VALUE_ERROR;
+        }
+        const size_t o_media = 0;
+        const size_t o_z = (o_media + sz_media + 255) & ~(size_t)255;
+        const size_t o_m = (o_z + sz_z + 255) & ~(size_t)255;
+        const size_t o_h = (o_m + sz_m + 255) & ~(size_t)255;
+        const size_t total = o_h + sz_h;
+        char * host = (char *)calloc(1, total);
+        if (host == NULL) return GPUMAS_RETURN_MEMORY_ERROR;
+        memcpy(host + o_media, g.media, sz_media);
+        if (sz_z) memcpy(host + o_z, g.slab_z, sz_z);
+        if (sz_m) memcpy(host + o_m, g.slab_medium, sz_m);
+        if (sz_h) memcpy(host + o_h, g.hm_z, sz_h);
+        char * d = NULL;
+        int rc = gp_check(cudaMalloc(&d, total));
+        if (rc == GPUMAS_RETURN_SUCCESS)
+                rc = gp_check(
+                    cudaMemcpy(d, host, total, cudaMemcpyHostToDevice));
+        free(host);
+        if (rc != GPUMAS_RETURN_SUCCESS) {
+                if (d != NULL) cudaFree(d);
+                return rc;
+        }
+        gpumas_geometry dg = g;
+        dg.media = (const gpumas_medium *)(d + o_media);
+        dg.slab_z = sz_z ? (const double *)(d + o_z) : NULL;
+        dg.slab_medium = sz_m ? (const int *)(d + o_m) : NULL;
+        dg.hm_z = sz_h ? (const double *)(d + o_h) : NULL;
+        rc = gp_check(cudaMemcpy(
+            d_geometry, &dg, sizeof(dg), cudaMemcpyHostToDevice));
+        if (rc != GPUMAS_RETURN_SUCCESS) {
+                cudaFree(d);
+                return rc;
+        }
+        *d_data = d;
+        return GPUMAS_RETURN_SUCCESS;
+}
+
+extern "C" int gpumas_context_geometry_set(
+    struct gpumas_context * context, const struct gpumas_geometry * geometry)
+{
+        if (context == NULL) return GPUMAS_RETURN_VALUE_ERROR;
+        gp_context * c = (gp_context *)context;
+        void * data = NULL;
+        const int rc =
+            gp_geometry_upload(c->physics, geometry, c->d_geometry, &data);
+        if (rc != GPUMAS_RETURN_SUCCESS) return rc;
+        if (c->d_geometry_data != NULL) cudaFree(c->d_geometry_data);
+        c->d_geometry_data = data;
+        c->has_geometry = 1;
+        c->n_media = geometry->n_media;
+        return GPUMAS_RETURN_SUCCESS;
+}
+
+/* Context level checks of pumas_context_transport (pumas.c:3120-3177). */
+extern "C" int gp_config_check(const struct gpumas_context * context,
+    const struct gpumas_physics * physics, gp_config * cfg)
+{
+        if (context->mode.direction != GPUMAS_MODE_FORWARD &&
+            context->mode.direction != GPUMAS_MODE_BACKWARD)
+                return GPUMAS_RETURN_VALUE_ERROR;
+        if ((context->mode.energy_loss < GPUMAS_MODE_DISABLED) ||
+            (context->mode.energy_loss > GPUMAS_MODE_STRAGGLED))
+                return GPUMAS_RETURN_VALUE_ERROR;
+        if ((context->mode.scattering != GPUMAS_MODE_DISABLED) &&
+            (context->mode.scattering != GPUMAS_MODE_MIXED))
+                return GPUMAS_RETURN_VALUE_ERROR;
+        if ((context->mode.decay < GPUMAS_MODE_DISABLED) ||
+            (context->mode.decay > GPUMAS_MODE_RANDOMISED))
+                return GPUMAS_RETURN_DECAY_ERROR;
+        if ((context->accuracy <= 0) || (context->accuracy > 1))
+                return GPUMAS_RETURN_ACCURACY_ERROR;
+        if ((context->mode.direction == GPUMAS_MODE_BACKWARD) &&
+            (context->mode.energy_loss > GPUMAS_MODE_CSDA) &&
+            (physics->tables.cutoff < 1E-02))
+                return GPUMAS_RETURN_ACCURACY_ERROR;
+        cfg->energy_loss = context->mode.energy_loss;
+        cfg->decay = context->mode.decay;
+        cfg->direction = context->mode.direction;
+        cfg->scattering = context->mode.scattering;
+        cfg->event = context->event;
+        cfg->limit_energy = context->limit.energy;
+        cfg->limit_distance = context->limit.distance;
+        cfg->limit_grammage = context->limit.grammage;
+        cfg->limit_time = context->limit.time;
+        cfg->accuracy = context->accuracy;
+        cfg->seed = context->seed;
+        return GPUMAS_RETURN_SUCCESS;
+}
+
+static const int gp_block = 128;
+
+extern "C" int gpumas_context_transport_device(struct gpumas_context * context,
+    size_t n, const struct gpumas_soa * events, uint64_t first_event,
+    void * stream)
+{
+        if ((context == NULL) || (events == NULL))
+                return GPUMAS_RETURN_VALUE_ERROR;
+        gp_context * c = (gp_context *)context;
+        if (!c->has_geometry) return GPUMAS_RETURN_MEDIUM_ERROR;
+        gp_config cfg;
+        int rc = gp_config_check(context, c->physics, &cfg);
+        if (rc != GPUMAS_RETURN_SUCCESS) return rc;
+        if (n == 0) return GPUMAS_RETURN_SUCCESS;
+        cudaStream_t s = (cudaStream_t)stream;
+        gp_io io;
+        memset(&io, 0, sizeof(io));
+        io.soa.a = *events;
+        const unsigned int grid = (unsigned int)((n + gp_block - 1) / gp_block);
+        cudaEventRecord(c->t0, s);
+        gp_kernel_plain<<<grid, gp_block, 0, s>>>(
+            c->d_tables, cfg, c->d_geometry, io, n, first_event);
+        cudaEventRecord(c->t1, s);
+        c->stats.launches = 1;
+        c->stats.kernel_ms = -1.;
+        return gp_check(cudaGetLastError());
+}
+
+extern "C" int gpumas_context_transport(struct gpumas_context * context,
+    size_t n, struct gpumas_state * states, struct gpumas_result * results,
+    uint64_t first_event)
+{
+        if (context == NULL) return GPUMAS_RETURN_VALUE_ERROR;
+        gp_context * c = (gp_context *)context;
+        if (!c->has_geometry) return GPUMAS_RETURN_MEDIUM_ERROR;
+        gp_config cfg;
+        int rc = gp_config_check(context, c->physics, &cfg);
+        if (rc != GPUMAS_RETURN_SUCCESS) return rc;
+        if (n == 0) return GPUMAS_RETURN_SUCCESS;
+        if (states == NULL) return GPUMAS_RETURN_VALUE_ERROR;
+
+        const size_t sz_s = n * sizeof(gpumas_state);
+        const size_t sz_r = n * sizeof(gpumas_result);
+        const size_t o_r = (sz_s + 255) & ~(size_t)255;
+        const size_t need = o_r + sz_r;
+        if (need > c->io_size) {
+                if (c->d_io != NULL) cudaFree(c->d_io);
+                c->d_io = NULL;
+                c->io_size = 0;
+                rc = gp_check(cudaMalloc(&c->d_io, need));
+                if (rc != GPUMAS_RETURN_SUCCESS) return rc;
+                c->io_size = need;
+        }
+        gp_io io;
+        memset(&io, 0, sizeof(io));
+        io.aos.states = (gpumas_state *)c->d_io;
+        io.aos.results = (gpumas_result *)((char *)c->d_io + o_r);
+        cudaStream_t s = c->stream;
+        rc = gp_check(cudaMemcpyAsync(
+            io.aos.states, states, sz_s, cudaMemcpyHostToDevice, s));
+        if (rc != GPUMAS_RETURN_SUCCESS) return rc;
+        const unsigned int grid = (unsigned int)((n + gp_block - 1) / gp_block);
+        cudaEventRecord(c->t0, s);
+        gp_kernel_plain<<<grid, gp_block, 0, s>>>(
+            c->d_tables, cfg, c->d_geometry, io, n, first_event);
+        cudaEventRecord(c->t1, s);
+        rc = gp_check(cudaGetLastError());
+        if (rc != GPUMAS_RETURN_SUCCESS) return rc;
+        rc = gp_check(cudaMemcpyAsync(
+            states, io.aos.states, sz_s, cudaMemcpyDeviceToHost, s));
+        if (rc != GPUMAS_RETURN_SUCCESS) return rc;
+        gpumas_result * hr = results;
+        gpumas_result * tmp = NULL;
+        if (hr == NULL) {
+                tmp = (gpumas_result *)malloc(sz_r);
+                if (tmp == NULL) return GPUMAS_RETURN_MEMORY_ERROR;
+                hr = tmp;
+        }
+        rc = gp_check(cudaMemcpyAsync(
+            hr, io.aos.results, sz_r, cudaMemcpyDeviceToHost, s));
+        if (rc == GPUMAS_RETURN_SUCCESS)
+                rc = gp_check(cudaStreamSynchronize(s));
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, c->t0, c->t1);
+        c->stats.launches = 1;
+        c->stats.kernel_ms = ms;
+        if (rc == GPUMAS_RETURN_SUCCESS) {
+                for (size_t i = 0; i < n; i++) {
+                        if (hr[i].status != GPUMAS_RETURN_SUCCESS) {
+                                rc = hr[i].status;
+                                break;
+                        }
+                }
+        }
+        free(tmp);
+        return rc;
+}
+
+extern "C" int gpumas_context_stats(
+    const struct gpumas_context * context, struct gpumas_stats * stats)
+{
+        if ((context == NULL) || (stats == NULL))
+                return GPUMAS_RETURN_VALUE_ERROR;
+        const gp_context * c = (const gp_context *)context;
+        *stats = c->stats;
+        if (stats->kernel_ms < 0.) {
+                float ms = 0.f;
+                if (cudaEventElapsedTime(&ms, c->t0, c->t1) == cudaSuccess)
+                        stats->kernel_ms = ms;
+        }
+        return GPUMAS_RETURN_SUCCESS;
+}
+
+extern "C" int gpumas_random_fill(uint64_t seed, uint32_t domain,
+    uint64_t event, uint64_t first, size_t n, double * out)
+{
+        if ((out == NULL) || (n == 0)) return GPUMAS_RETURN_VALUE_ERROR;
+        double * d = NULL;
+        int rc = gp_check(cudaMalloc(&d, n * sizeof(double)));
+        if (rc != GPUMAS_RETURN_SUCCESS) return rc;
+        gp_kernel_random<<<(unsigned int)((n + 255) / 256), 256>>>(
+            seed, domain, event, first, n, d);
+        rc = gp_check(cudaGetLastError());
+        if (rc == GPUMAS_RETURN_SUCCESS)
+                rc = gp_check(cudaMemcpy(
+                    out, d, n * sizeof(double), cudaMemcpyDeviceToHost));
+        cudaFree(d);
+        return rc;
+}

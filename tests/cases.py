@@ -1,0 +1,123 @@
+"""Parity cases shared by the golden fixture generator and the tests.
+
+Each case is a transport configuration (the public pumas_context settings),
+a geometry made of named materials and a generator of initial states. The
+same case runs on the reference (to make the golden fixtures), on the C
+restatement oracle and on the GPU engine.
+"""
+import numpy as np
+
+from pumas_gb300 import workloads as W
+from pumas_gb300 import STATE_DTYPE
+
+FWD, BWD = 0, 1
+CSDA, MIXED, STRAGGLED, DISABLED = 0, 1, 2, -1
+WEIGHTED, RANDOMISED = 0, 1
+LIMIT_ENERGY, LIMIT_DISTANCE, LIMIT_GRAMMAGE, LIMIT_TIME = 1, 2, 4, 8
+
+
+def _cfg(energy_loss, scattering, direction, decay=WEIGHTED, event=0,
+         **limits):
+    c = dict(energy_loss=energy_loss, scattering=scattering,
+             direction=direction, decay=decay, event=event,
+             limit_energy=0., limit_distance=0., limit_grammage=0.,
+             limit_time=0., accuracy=1E-02)
+    c.update(limits)
+    return c
+
+
+def _states(n, seed, first, emin, emax, z0=0., uz=1., alt=True):
+    ev = np.arange(first, first + n, dtype=np.uint64)
+    s = np.zeros(n, dtype=STATE_DTYPE)
+    s["charge"] = np.where(ev % 2 == 1, 1., -1.) if alt else -1.
+    s["energy"] = emin * (emax / emin) ** W.uniform(seed, 1, ev, 0)
+    s["weight"] = 1.
+    s["position"][:, 2] = z0
+    s["direction"][:, 2] = uz
+    return s
+
+
+STACK = dict(kind=1, media=[("StandardRock", 0.), ("Water", 0.),
+                            ("Iron", 0.), ("Air", 0.), ("StandardRock", 2000.)],
+             slab_z=[0., 10., 30., 31., 200., 400.],
+             slab_media=[0, 1, 2, 3, 4])
+ROCK_SLAB = dict(kind=1, media=[("StandardRock", 0.)], slab_z=[0., 1000.],
+                 slab_media=[0])
+ROCK = dict(kind=0, media=[("StandardRock", 0.)])
+WATER = dict(kind=0, media=[("Water", 0.)])
+
+CASES = {
+    # Plain forward CSDA in infinite rock (pumas.c:4777-4949).
+    "plain_csda": dict(
+        config=_cfg(CSDA, DISABLED, FWD, decay=DISABLED, event=LIMIT_ENERGY,
+                    limit_energy=1.),
+        geometry=ROCK, n=2000, seed=1,
+        states=lambda n, s, f: W.plain_csda(n, s, f)),
+    # Forward straggled + mixed scattering through 1 km of rock.
+    "rock_slab": dict(
+        config=_cfg(STRAGGLED, MIXED, FWD, event=LIMIT_ENERGY,
+                    limit_energy=1.),
+        geometry=ROCK_SLAB, n=300, seed=7,
+        states=lambda n, s, f: W.rock_slab(n, s, f)),
+    # Backward straggled + mixed, up through the rock slab.
+    "rock_slab_backward": dict(
+        config=_cfg(STRAGGLED, MIXED, BWD),
+        geometry=ROCK_SLAB, n=200, seed=9,
+        states=lambda n, s, f: _states(n, s, f, 10., 1E+04, z0=999.999)),
+    # Forward mixed (no straggling): DEL and EHS pre-sampled as limits.
+    "stack_forward_mixed": dict(
+        config=_cfg(MIXED, MIXED, FWD, event=LIMIT_ENERGY, limit_energy=1.),
+        geometry=STACK, n=200, seed=11,
+        states=lambda n, s, f: _states(n, s, f, 1., 1E+04)),
+    # Forward straggled through the multi-material stack.
+    "stack_forward_straggled": dict(
+        config=_cfg(STRAGGLED, MIXED, FWD, event=LIMIT_ENERGY,
+                    limit_energy=1.),
+        geometry=STACK, n=200, seed=12,
+        states=lambda n, s, f: _states(n, s, f, 1., 1E+04)),
+    # Backward mixed and straggled through the stack.
+    "stack_backward_mixed": dict(
+        config=_cfg(MIXED, MIXED, BWD),
+        geometry=STACK, n=200, seed=13,
+        states=lambda n, s, f: _states(n, s, f, 1., 1E+04, z0=399.99)),
+    "stack_backward_straggled": dict(
+        config=_cfg(STRAGGLED, MIXED, BWD),
+        geometry=STACK, n=200, seed=14,
+        states=lambda n, s, f: _states(n, s, f, 1., 1E+04, z0=399.99)),
+    # Randomised decay, CSDA stepping without scattering.
+    "stack_csda_randomised": dict(
+        config=_cfg(CSDA, DISABLED, FWD, decay=RANDOMISED,
+                    event=LIMIT_ENERGY, limit_energy=1.),
+        geometry=STACK, n=300, seed=15,
+        states=lambda n, s, f: _states(n, s, f, 1., 1E+03)),
+    # External limits in water (pumas.c:5250-5259, 6389-6397, 6713-6809).
+    "water_distance_limit": dict(
+        config=_cfg(STRAGGLED, MIXED, FWD, event=LIMIT_ENERGY |
+                    LIMIT_DISTANCE, limit_energy=1., limit_distance=50.),
+        geometry=WATER, n=200, seed=16,
+        states=lambda n, s, f: _states(n, s, f, 1., 1E+03)),
+    "water_grammage_limit": dict(
+        config=_cfg(MIXED, MIXED, FWD, event=LIMIT_GRAMMAGE,
+                    limit_grammage=3E+05),
+        geometry=WATER, n=200, seed=17,
+        states=lambda n, s, f: _states(n, s, f, 1., 1E+04)),
+    "water_time_limit": dict(
+        config=_cfg(CSDA, MIXED, FWD, event=LIMIT_TIME, limit_time=1E+02),
+        geometry=WATER, n=200, seed=18,
+        states=lambda n, s, f: _states(n, s, f, 1., 1E+03)),
+    # CSDA in infinite rock, backward, grammage limit.
+    "rock_csda_backward": dict(
+        config=_cfg(CSDA, DISABLED, BWD, event=LIMIT_GRAMMAGE,
+                    limit_grammage=1E+05),
+        geometry=ROCK, n=500, seed=19,
+        states=lambda n, s, f: _states(n, s, f, 1., 1E+04)),
+}
+
+
+def make_states(name, n=None, first_event=0):
+    c = CASES[name]
+    return c["states"](c["n"] if n is None else n, c["seed"], first_event)
+
+
+def material_indices(index_of, geometry):
+    return [(index_of(m), d) for m, d in geometry["media"]]

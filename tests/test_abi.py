@@ -1,0 +1,57 @@
+"""The C ABI library: builds, loads and exports every declared symbol.
+
+CPU only: no CUDA call is made (loading libgpumas.so needs libcudart only).
+"""
+import ctypes
+import os
+import re
+import shutil
+
+import pytest
+
+from conftest import ROOT
+
+HEADERS = [os.path.join(ROOT, "include", h)
+           for h in ("gpumas.h", "gpumas_geometry.h")]
+
+
+def declared_functions():
+    names = []
+    for h in HEADERS:
+        text = open(h).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"^\s*(?:int|void|double)\s+\**\s*(gpumas_\w+)\s*\(",
+                             text, flags=re.M):
+            names.append(m.group(1))
+    return names
+
+
+@pytest.mark.skipif(shutil.which("nvcc") is None and
+                    not os.path.exists("/usr/local/cuda/bin/nvcc"),
+                    reason="no nvcc")
+def test_library_exports_declared_symbols():
+    import pumas_gb300
+    from pumas_gb300 import build
+    lib = ctypes.CDLL(build.build())
+    names = declared_functions()
+    assert "gpumas_context_transport" in names
+    assert "gpumas_physics_load" in names
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+    # The geometry header's functions are inline host/device code, not
+    # exported symbols.
+    assert pumas_gb300.library() is not None
+
+
+def test_no_product_import_of_oracle():
+    """The product package never imports or links the oracle."""
+    pkg = os.path.join(ROOT, "pumas_gb300")
+    for dirpath, _, files in os.walk(pkg):
+        if "_build" in dirpath or "data" in dirpath:
+            continue
+        for f in files:
+            if f.endswith((".py", ".cu", ".cuh", ".h", ".cpp")):
+                text = open(os.path.join(dirpath, f)).read()
+                assert "import oracle" not in text
+                assert "oracle/" not in text
+                assert "liboracle" not in text

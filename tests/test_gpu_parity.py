@@ -1,0 +1,97 @@
+"""Parity of the GPU engine with the reference (GPU).
+
+The CUDA path is compared, through the C ABI, with
+* the golden fixtures made by the unmodified reference (tests/golden), and
+* the C restatement oracle on fresh seeded events.
+Tolerance: 1E-09 relative on energy, distance, grammage, time, weight,
+position and direction (absolute floor of 1E-09 near zero), identical end
+events, media and status; at least 99.9 % of events within tolerance, all
+of them for deterministic CSDA.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from cases import CASES, make_states
+from conftest import (GOLDEN, compare, gpu_context, gpu_geometry,
+                      oracle_config, oracle_geometry)
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1E-09
+
+
+def run_gpu(physics, name, states, first_event=0, seed=None):
+    case = CASES[name]
+    geo = gpu_geometry(physics, case["geometry"])
+    ctx = gpu_context(physics, case["config"],
+                      case["seed"] if seed is None else seed, geo)
+    return ctx.transport(states, first_event)
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_gpu_matches_reference_golden(gpu_physics, name):
+    data = np.load(os.path.join(GOLDEN, name + ".npz"))
+    s1, r1 = run_gpu(gpu_physics, name, data["initial"])
+    same, close = compare(s1, r1, data["final"], data["results"], RTOL)
+    n = len(close)
+    frac = close.mean()
+    if CASES[name]["config"]["energy_loss"] == 0 and \
+            CASES[name]["config"]["scattering"] == -1:
+        assert close.all(), "%d / %d CSDA events differ" % (n - close.sum(), n)
+    else:
+        assert frac >= 0.999 or n - close.sum() <= 1, \
+            "%s: %d / %d events outside 1e-9" % (name, n - close.sum(), n)
+    assert np.all(r1["status"] == 0)
+
+
+@pytest.mark.parametrize("name", ["plain_csda", "rock_slab",
+                                  "stack_backward_straggled",
+                                  "stack_forward_mixed"])
+def test_gpu_matches_port_fresh_events(gpu_physics, port, name):
+    case = CASES[name]
+    n = 20000 if name == "plain_csda" else 2000
+    s0 = make_states(name, n=n, first_event=5000)
+    a, ra = run_gpu(gpu_physics, name, s0, 5000, seed=case["seed"] + 3)
+    geo = oracle_geometry(port, case["geometry"])
+    cfg = oracle_config(case["config"], case["seed"] + 3)
+    b, rb = port.transport(cfg, geo, s0, 5000, 0)
+    same, close = compare(a, ra, b, rb, RTOL)
+    assert close.mean() >= 0.999, "%d / %d outside 1e-9" % (
+        (~close).sum(), n)
+
+
+def test_gpu_random_stream_matches_oracle(gpu_physics, port):
+    import pumas_gb300 as pg
+    for event in (0, 1, 2**33 + 5):
+        u = pg.random_fill(0x0123456789ABCDEF, 0, event, 0, 257)
+        v = [port.uniform(0x0123456789ABCDEF, 0, event, k) for k in range(257)]
+        assert np.array_equal(u, v)
+
+
+def test_gpu_edge_cases(gpu_physics):
+    import pumas_gb300 as pg
+    rock = gpu_physics.material_index("StandardRock")
+    ctx = pg.Context(gpu_physics)
+    ctx.event = pg.EVENT_LIMIT_ENERGY
+    ctx.limit.energy = 1.
+    ctx.seed = 1
+    ctx.set_geometry(pg.Geometry.slabs([0., 10.], [rock]))
+    s, r = ctx.transport(pg.new_states(0))
+    assert len(s) == 0
+    s0 = pg.new_states(4)
+    s0["energy"] = 10.
+    s0["direction"][:, 2] = 1.
+    s0["direction"][1] = (0., 0., 1.1)
+    s0["position"][2, 2] = -1.
+    s0["decayed"][3] = 1
+    s, r = ctx.transport(s0)
+    assert r["status"][0] == 0 and r["event"][0] == pg.EVENT_MEDIUM
+    assert r["status"][1] == pg.RETURN_DIRECTION_ERROR
+    assert r["event"][2] == pg.EVENT_MEDIUM and r["medium_in"][2] == -1
+    assert r["event"][3] == pg.EVENT_VERTEX_DECAY and s["energy"][3] == 10.
+    ctx.accuracy = 0.
+    with pytest.raises(pg.PumasError) as err:
+        ctx.transport(s0[:1])
+    assert err.value.code == pg.RETURN_ACCURACY_ERROR
