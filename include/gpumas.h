@@ -262,6 +262,15 @@ int gpumas_context_stats(
     const struct gpumas_context * context, struct gpumas_stats * stats);
 
 /* ------------------------------------------------------------------------ */
+/* Diagnostics.                                                             */
+/* ------------------------------------------------------------------------ */
+
+/** Measured FP64 fused multiply-add throughput of the current device, in
+ * TFLOP/s (2 flops per DFMA), from a register-resident microbenchmark. It
+ * is the denominator of the engine's FP64 roofline. */
+int gpumas_bench_dfma(double * tflops);
+
+/* ------------------------------------------------------------------------ */
 /* Random stream.                                                           */
 /* ------------------------------------------------------------------------ */
 

@@ -499,6 +499,50 @@ extern "C" int gpumas_context_stats(
         return GPUMAS_RETURN_SUCCESS;
 }
 
+/* FP64 throughput microbenchmark: 8 independent DFMA chains per thread. */
+__global__ void gp_kernel_dfma(double * out, int iters, double a, double b)
+{
+        double x[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++) x[k] = threadIdx.x * 1E-03 + k;
+        for (int i = 0; i < iters; i++) {
+#pragma unroll
+                for (int k = 0; k < 8; k++) x[k] = fma(x[k], a, b);
+        }
+        double s = 0.;
+#pragma unroll
+        for (int k = 0; k < 8; k++) s += x[k];
+        if (s == 12345.678) out[0] = s;
+}
+
+extern "C" int gpumas_bench_dfma(double * tflops)
+{
+        if (tflops == NULL) return GPUMAS_RETURN_VALUE_ERROR;
+        int device, sms = 0;
+        cudaGetDevice(&device);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+        double * d = NULL;
+        int rc = gp_check(cudaMalloc(&d, sizeof(double)));
+        if (rc != GPUMAS_RETURN_SUCCESS) return rc;
+        const int threads = 256, blocks = 8 * sms, iters = 4096;
+        cudaEvent_t t0, t1;
+        cudaEventCreate(&t0);
+        cudaEventCreate(&t1);
+        gp_kernel_dfma<<<blocks, threads>>>(d, iters, 0.999999, 1E-07);
+        cudaEventRecord(t0);
+        gp_kernel_dfma<<<blocks, threads>>>(d, iters, 0.999999, 1E-07);
+        cudaEventRecord(t1);
+        rc = gp_check(cudaEventSynchronize(t1));
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, t0, t1);
+        cudaEventDestroy(t0);
+        cudaEventDestroy(t1);
+        cudaFree(d);
+        const double flops = 2. * 8. * iters * (double)threads * blocks;
+        *tflops = (ms > 0.f) ? flops / (ms * 1E-03) * 1E-12 : 0.;
+        return rc;
+}
+
 extern "C" int gpumas_random_fill(uint64_t seed, uint32_t domain,
     uint64_t event, uint64_t first, size_t n, double * out)
 {
