@@ -51,6 +51,11 @@ def parse():
     p.add_argument("--no-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--cpu-events", type=int, default=0)
+    p.add_argument("--engine", type=int, default=2,
+                   help="1: one thread per event, 2: slot pool")
+    p.add_argument("--pool-slots", type=int, default=0)
+    p.add_argument("--max-inner", type=int, default=0)
+    p.add_argument("--batch", type=int, default=0)
     return p.parse_args()
 
 
@@ -213,6 +218,8 @@ def main():
     W.rock_slab_config(ctx)
     ctx.seed = args.seed
     ctx.set_geometry(W.rock_slab_geometry(physics))
+    tuning = ctx.tuning(engine=args.engine, pool_slots=args.pool_slots,
+                        max_inner=args.max_inner, batch=args.batch)
 
     n = args.events
     first = rank * 10 ** 12
@@ -267,9 +274,10 @@ def main():
     if world > 1:
         torch.distributed.barrier()
     total_ms = ev0.elapsed_time(ev1)
-    # Kernel-only time of the last step (CUDA events around the launch on
-    # the same stream, recorded by the library).
-    last_kernel_ms = ctx.stats()["kernel_ms"]
+    # Device time of the last step's transport (CUDA events on the same
+    # stream around the engine's launches, recorded by the library).
+    st = ctx.stats()
+    last_kernel_ms = st["kernel_ms"]
     res = np.frombuffer(results.cpu().numpy().tobytes(),
                         dtype=pg.RESULT_DTYPE)
     steps_per_event = float(res["steps"].mean())
@@ -342,7 +350,8 @@ def main():
         "steps_per_event": steps_per_event,
         "kernel_ms": last_kernel_ms,
         "event_errors": bad,
-        "gpu_launches": args.steps,
+        "gpu_launches": args.steps * st["launches"],
+        "engine": tuning,
         "e2e": e2e, "roofline": roofline, "cpu_baseline": base,
         "clocks": clocks.summary(),
     }

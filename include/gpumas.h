@@ -251,6 +251,27 @@ int gpumas_context_transport_device(struct gpumas_context * context,
     size_t n, const struct gpumas_soa * events, uint64_t first_event,
     void * stream);
 
+/**
+ * Engine parameters of a context. `engine` selects the execution scheme:
+ * 0 automatic, 1 one GPU thread per event for the whole transport call,
+ * 2 the slot pool, where events are refilled into `pool_slots` resident
+ * slots and stepped by kernels regrouped by step kind (continuous step,
+ * DEL, hard elastic scatter), with `max_inner` continuous steps per slot and
+ * iteration and `batch` iterations per captured CUDA graph. Results do not
+ * depend on these parameters. Zero fields keep the current value.
+ */
+struct gpumas_tuning {
+        int engine;
+        int pool_slots;
+        int max_inner;
+        int batch;
+};
+
+int gpumas_context_tuning_set(
+    struct gpumas_context * context, const struct gpumas_tuning * tuning);
+int gpumas_context_tuning_get(
+    const struct gpumas_context * context, struct gpumas_tuning * tuning);
+
 /** Engine statistics of the last transport call on this context. */
 struct gpumas_stats {
         /** Kernel launches of the call. */

@@ -108,6 +108,14 @@ class _Stats(ctypes.Structure):
     _fields_ = [("launches", ctypes.c_int), ("kernel_ms", ctypes.c_double)]
 
 
+class _Tuning(ctypes.Structure):
+    _fields_ = [("engine", ctypes.c_int), ("pool_slots", ctypes.c_int),
+                ("max_inner", ctypes.c_int), ("batch", ctypes.c_int)]
+
+
+ENGINE_AUTO, ENGINE_PLAIN, ENGINE_POOL = 0, 1, 2
+
+
 class _Soa(ctypes.Structure):
     _fields_ = [
         ("charge", ctypes.c_void_p), ("energy", ctypes.c_void_p),
@@ -157,6 +165,11 @@ def library(build=False):
             ctypes.POINTER(_Context), sz, ctypes.POINTER(_Soa), u64, vp]
         lib.gpumas_context_stats.argtypes = [
             ctypes.POINTER(_Context), ctypes.POINTER(_Stats)]
+        lib.gpumas_context_tuning_set.argtypes = [
+            ctypes.POINTER(_Context), ctypes.POINTER(_Tuning)]
+        lib.gpumas_context_tuning_get.argtypes = [
+            ctypes.POINTER(_Context), ctypes.POINTER(_Tuning)]
+        lib.gpumas_bench_dfma.argtypes = [ctypes.POINTER(ctypes.c_double)]
         lib.gpumas_random_fill.argtypes = [
             u64, ctypes.c_uint32, u64, u64, sz, vp]
         for f in ("gpumas_physics_load", "gpumas_physics_upload",
@@ -164,7 +177,8 @@ def library(build=False):
                   "gpumas_context_create", "gpumas_context_geometry_set",
                   "gpumas_context_transport",
                   "gpumas_context_transport_device", "gpumas_context_stats",
-                  "gpumas_random_fill"):
+                  "gpumas_context_tuning_set", "gpumas_context_tuning_get",
+                  "gpumas_bench_dfma", "gpumas_random_fill"):
             getattr(lib, f).restype = i
         _lib = lib
     return _lib
@@ -327,6 +341,17 @@ class Context:
         c.result = soa.get("result", None)
         return self._lib.gpumas_context_transport_device(
             self._ptr, n, ctypes.byref(c), first_event, stream)
+
+    def tuning(self, engine=0, pool_slots=0, max_inner=0, batch=0):
+        """Set engine parameters (zero keeps a value); returns the current
+        ones as a dict."""
+        t = _Tuning(engine, pool_slots, max_inner, batch)
+        _check(self._lib.gpumas_context_tuning_set(self._ptr,
+                                                   ctypes.byref(t)),
+               "gpumas_context_tuning_set")
+        self._lib.gpumas_context_tuning_get(self._ptr, ctypes.byref(t))
+        return {"engine": t.engine, "pool_slots": t.pool_slots,
+                "max_inner": t.max_inner, "batch": t.batch}
 
     def stats(self):
         st = _Stats()

@@ -1,0 +1,511 @@
+/*
+ * gp_batch.cu -- the slot pool engine: stepping regrouped by step kind.
+ *
+ * The reference transports one event per call, in a loop over steps
+ * (transport_with_stepping, pumas.c:5194-5514) whose iterations differ
+ * widely in cost: a continuous step, a discrete energy loss (DEL) with its
+ * rejection sampling and polar angle, a hard elastic scatter (EHS) with its
+ * Coulomb setup, a boundary crossing. Running one event per GPU thread from
+ * start to end makes a warp wait on its slowest lane at every such branch.
+ *
+ * This engine keeps a pool of P event slots in device memory (structure of
+ * arrays, sized to stay resident in L2) and advances all of them one
+ * iteration at a time with one kernel per step kind:
+ *
+ *   1. gp_pool_step: every slot makes its continuous step(s). Empty slots are
+ *      first refilled from the input (a device work queue: an atomic cursor
+ *      over the events). Slots whose step ended on a DEL or an EHS are
+ *      appended to the DEL or EHS list with warp aggregated atomics (a
+ *      ballot and prefix count per warp), so that the lists are compact.
+ *   2. gp_pool_del: one thread per listed DEL, full warps.
+ *   3. gp_pool_ehs: one thread per listed EHS, full warps.
+ *
+ * Finished events are written back to the caller's arrays at their input
+ * index and their slot is refilled at the next iteration. Per event results
+ * are identical to the one thread per event kernel: the random stream of an
+ * event depends only on (seed, event id), and an event's draws are consumed
+ * in the same order whichever slot, warp or kernel executes them.
+ *
+ * The host runs the iterations in batches captured in a CUDA graph and reads
+ * two counters (input cursor, active slots) after each batch to stop.
+ */
+#include <cooperative_groups.h>
+#include <cuda_runtime.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "gp_context.h"
+#include "gp_io.cuh"
+
+namespace cg = cooperative_groups;
+
+/* Field layout of a slot: doubles, ints and 64 bit integers, each as an
+ * array of P values. */
+enum gp_slot_double {
+        SD_CHARGE, SD_ENERGY, SD_DISTANCE, SD_GRAMMAGE, SD_TIME, SD_WEIGHT,
+        SD_POS0, SD_POS1, SD_POS2, SD_DIR0, SD_DIR1, SD_DIR2,
+        SD_STEP_X_LIMIT, SD_STEP_INVLB1, SD_RANDN_NEXT, SD_LIFETIME, SD_RNEXT,
+        SD_DENSITY, SD_TI, SD_WI, SD_XI, SD_XF, SD_DEI, SD_GRAMMAGE_MAX,
+        SD_STEP_MAX_MEDIUM, SD_N
+};
+enum gp_slot_int {
+        SI_DECAYED, SI_STEP_FIRST, SI_STEP_EVENT, SI_STEP_FORESEEN,
+        SI_RANDN_DONE, SI_STEPS, SI_STATUS, SI_MEDIUM, SI_MATERIAL,
+        SI_STRAIGHT, SI_STEP_INDEX, SI_NEW_MEDIUM, SI_PHASE, SI_MEDIUM_IN,
+        SI_N_DRAWS, SI_N
+};
+enum gp_slot_u64 { SU_ID, SU_SRC, SU_N };
+
+#define GP_EMPTY 0
+
+struct gp_pool {
+        double * d;
+        int * i;
+        uint64_t * u;
+        int P;
+};
+
+struct gp_counters {
+        unsigned long long cursor;
+        int active;
+        int pad;
+        int n_del[2];
+        int n_ehs[2];
+};
+
+/* Per call launch parameters, read by the kernels from device memory so
+ * that one instantiated graph serves every call. */
+struct gp_launch {
+        gp_config cfg;
+        gp_io io;
+        size_t n;
+        uint64_t first_event;
+        int max_inner;
+};
+
+struct gp_pool_state {
+        gp_pool pool;
+        gp_counters * d_counters;
+        gp_counters * h_counters;
+        int * del_list[2];
+        int * ehs_list[2];
+        void * d_mem;
+        size_t capacity;
+        gp_launch * d_launch;
+        gp_launch * h_launch;
+        cudaGraph_t graph;
+        cudaGraphExec_t exec;
+        int graph_batch;
+        const void * graph_tables;
+        const void * graph_geometry;
+};
+
+#define PD(f) pool.d[(size_t)(f) * pool.P + slot]
+#define PI(f) pool.i[(size_t)(f) * pool.P + slot]
+#define PU(f) pool.u[(size_t)(f) * pool.P + slot]
+
+__device__ __forceinline__ void gp_slot_load(const gp_pool & pool, int slot,
+    const gp_config & cfg, gp_event & e, gp_loop & L)
+{
+        e.charge = PD(SD_CHARGE);
+        e.energy = PD(SD_ENERGY);
+        e.distance = PD(SD_DISTANCE);
+        e.grammage = PD(SD_GRAMMAGE);
+        e.time = PD(SD_TIME);
+        e.weight = PD(SD_WEIGHT);
+        e.pos[0] = PD(SD_POS0);
+        e.pos[1] = PD(SD_POS1);
+        e.pos[2] = PD(SD_POS2);
+        e.dir[0] = PD(SD_DIR0);
+        e.dir[1] = PD(SD_DIR1);
+        e.dir[2] = PD(SD_DIR2);
+        e.step_X_limit = PD(SD_STEP_X_LIMIT);
+        e.step_invlb1 = PD(SD_STEP_INVLB1);
+        e.randn_next = PD(SD_RANDN_NEXT);
+        e.lifetime = PD(SD_LIFETIME);
+        e.rnext = PD(SD_RNEXT);
+        e.decayed = PI(SI_DECAYED);
+        e.step_first = PI(SI_STEP_FIRST);
+        e.step_event = PI(SI_STEP_EVENT);
+        e.step_foreseen = PI(SI_STEP_FORESEEN);
+        e.randn_done = PI(SI_RANDN_DONE);
+        e.steps = PI(SI_STEPS);
+        e.status = PI(SI_STATUS);
+        e.n = (uint32_t)PI(SI_N_DRAWS);
+        e.id = PU(SU_ID);
+        e.k0 = (uint32_t)cfg.seed;
+        e.k1 = (uint32_t)(cfg.seed >> 32);
+        L.density = PD(SD_DENSITY);
+        L.ti = PD(SD_TI);
+        L.wi = PD(SD_WI);
+        L.Xi = PD(SD_XI);
+        L.Xf = PD(SD_XF);
+        L.dei = PD(SD_DEI);
+        L.grammage_max = PD(SD_GRAMMAGE_MAX);
+        L.step_max_medium = PD(SD_STEP_MAX_MEDIUM);
+        L.medium = PI(SI_MEDIUM);
+        L.material = PI(SI_MATERIAL);
+        L.straight = PI(SI_STRAIGHT);
+        L.step_index = PI(SI_STEP_INDEX);
+        L.new_medium = PI(SI_NEW_MEDIUM);
+}
+
+__device__ __forceinline__ void gp_slot_store(const gp_pool & pool, int slot,
+    const gp_event & e, const gp_loop & L)
+{
+        PD(SD_CHARGE) = e.charge;
+        PD(SD_ENERGY) = e.energy;
+        PD(SD_DISTANCE) = e.distance;
+        PD(SD_GRAMMAGE) = e.grammage;
+        PD(SD_TIME) = e.time;
+        PD(SD_WEIGHT) = e.weight;
+        PD(SD_POS0) = e.pos[0];
+        PD(SD_POS1) = e.pos[1];
+        PD(SD_POS2) = e.pos[2];
+        PD(SD_DIR0) = e.dir[0];
+        PD(SD_DIR1) = e.dir[1];
+        PD(SD_DIR2) = e.dir[2];
+        PD(SD_STEP_X_LIMIT) = e.step_X_limit;
+        PD(SD_STEP_INVLB1) = e.step_invlb1;
+        PD(SD_RANDN_NEXT) = e.randn_next;
+        PD(SD_LIFETIME) = e.lifetime;
+        PD(SD_RNEXT) = e.rnext;
+        PI(SI_DECAYED) = e.decayed;
+        PI(SI_STEP_FIRST) = e.step_first;
+        PI(SI_STEP_EVENT) = e.step_event;
+        PI(SI_STEP_FORESEEN) = e.step_foreseen;
+        PI(SI_RANDN_DONE) = e.randn_done;
+        PI(SI_STEPS) = e.steps;
+        PI(SI_STATUS) = e.status;
+        PI(SI_N_DRAWS) = (int)e.n;
+        PU(SU_ID) = e.id;
+        PD(SD_DENSITY) = L.density;
+        PD(SD_TI) = L.ti;
+        PD(SD_WI) = L.wi;
+        PD(SD_XI) = L.Xi;
+        PD(SD_XF) = L.Xf;
+        PD(SD_DEI) = L.dei;
+        PD(SD_GRAMMAGE_MAX) = L.grammage_max;
+        PD(SD_STEP_MAX_MEDIUM) = L.step_max_medium;
+        PI(SI_MEDIUM) = L.medium;
+        PI(SI_MATERIAL) = L.material;
+        PI(SI_STRAIGHT) = L.straight;
+        PI(SI_STEP_INDEX) = L.step_index;
+        PI(SI_NEW_MEDIUM) = L.new_medium;
+}
+
+/* Append `slot` to a compact list with one atomic per warp. */
+__device__ __forceinline__ void gp_append(int * count, int * list, int slot)
+{
+        cg::coalesced_group g = cg::coalesced_threads();
+        int base = 0;
+        if (g.thread_rank() == 0) base = atomicAdd(count, (int)g.size());
+        base = g.shfl(base, 0);
+        list[base + g.thread_rank()] = slot;
+}
+
+/* Finish an event: write its state and results back at its input index
+ * and free the slot. */
+__device__ __forceinline__ void gp_finish(const gp_pool & pool, int slot,
+    const gp_config & cfg, const gp_io & io, gp_counters * cnt, gp_event & e,
+    int event, int medium_out)
+{
+        gp_stepping_end(cfg, e);
+        io.store((size_t)PU(SU_SRC), e, event, PI(SI_MEDIUM_IN), medium_out);
+        PI(SI_PHASE) = GP_EMPTY;
+        atomicSub(&cnt->active, 1);
+}
+
+/* Route a slot to its next phase. */
+__device__ __forceinline__ void gp_route(const gp_pool & pool, int slot,
+    const gp_config & cfg, const gp_io & io, gp_counters * cnt,
+    int * del_list, int * ehs_list, int parity, int next, gp_event & e,
+    gp_loop & L, int event)
+{
+        if (next == GP_NEXT_DONE) {
+                gp_finish(pool, slot, cfg, io, cnt, e, event, L.medium);
+                return;
+        }
+        gp_slot_store(pool, slot, e, L);
+        PI(SI_PHASE) = next;
+        if (next == GP_NEXT_DEL)
+                gp_append(&cnt->n_del[parity], del_list, slot);
+        else if (next == GP_NEXT_EHS)
+                gp_append(&cnt->n_ehs[parity], ehs_list, slot);
+}
+
+__global__ void __launch_bounds__(128) gp_pool_step(
+    const gp_tables * __restrict__ Tp, const gpumas_geometry * __restrict__ gp,
+    const gp_launch * __restrict__ X, const gp_pool pool, gp_counters * cnt,
+    int * del_list, int * ehs_list, int parity)
+{
+        const gp_config & cfg = X->cfg;
+        const gp_io & io = X->io;
+        const size_t n = X->n;
+        const uint64_t first_event = X->first_event;
+        const int max_inner = X->max_inner;
+        const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+        if (slot == 0) {
+                /* The other parity's lists were consumed by the previous
+                 * iteration's kernels, which precede this one. */
+                cnt->n_del[parity ^ 1] = 0;
+                cnt->n_ehs[parity ^ 1] = 0;
+        }
+        if (slot >= pool.P) return;
+        const gp_tables & T = *Tp;
+        const gpumas_geometry & g = *gp;
+        gp_event e;
+        gp_loop L;
+        int event = GPUMAS_EVENT_NONE;
+        int next;
+        if (PI(SI_PHASE) == GP_EMPTY) {
+                /* Refill from the input queue. Events that end before their
+                 * first step are finished here and the next one is taken. */
+                next = GP_EMPTY;
+                for (;;) {
+                        if (*(volatile unsigned long long *)&cnt->cursor >= n)
+                                break;
+                        cg::coalesced_group w = cg::coalesced_threads();
+                        unsigned long long base = 0;
+                        if (w.thread_rank() == 0)
+                                base = atomicAdd(&cnt->cursor,
+                                    (unsigned long long)w.size());
+                        base = w.shfl(base, 0);
+                        const unsigned long long idx = base + w.thread_rank();
+                        if (idx >= n) break;
+                        io.load((size_t)idx, e);
+                        gp_event_init(e, cfg.seed, first_event + idx);
+                        int medium_in;
+                        next = gp_transport_begin(
+                            T, cfg, g, e, L, event, medium_in);
+                        if (next == GP_NEXT_DONE) {
+                                io.store((size_t)idx, e, event, medium_in,
+                                    L.medium);
+                                next = GP_EMPTY;
+                                continue;
+                        }
+                        PU(SU_SRC) = idx;
+                        PI(SI_MEDIUM_IN) = medium_in;
+                        atomicAdd(&cnt->active, 1);
+                        break;
+                }
+                if (next == GP_EMPTY) return;
+        } else {
+                gp_slot_load(pool, slot, cfg, e, L);
+        }
+        next = GP_NEXT_STEP;
+        for (int k = 0; k < max_inner; k++) {
+                next = gp_stepping_step(T, cfg, g, e, L, event);
+                if (next != GP_NEXT_STEP) break;
+        }
+        gp_route(pool, slot, cfg, io, cnt, del_list, ehs_list, parity, next,
+            e, L, event);
+}
+
+__global__ void __launch_bounds__(128) gp_pool_del(
+    const gp_tables * __restrict__ Tp, const gp_launch * __restrict__ X,
+    const gp_pool pool, gp_counters * cnt, const int * __restrict__ list,
+    int parity)
+{
+        const gp_config & cfg = X->cfg;
+        const gp_io & io = X->io;
+        const int count = cnt->n_del[parity];
+        const gp_tables & T = *Tp;
+        for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < count;
+             j += gridDim.x * blockDim.x) {
+                const int slot = list[j];
+                gp_event e;
+                gp_loop L;
+                gp_slot_load(pool, slot, cfg, e, L);
+                int event = GPUMAS_EVENT_NONE;
+                const int next = gp_stepping_del(T, cfg, e, L, event);
+                if (next == GP_NEXT_DONE) {
+                        gp_finish(pool, slot, cfg, io, cnt, e, event,
+                            L.medium);
+                } else {
+                        gp_slot_store(pool, slot, e, L);
+                        PI(SI_PHASE) = GP_NEXT_STEP;
+                }
+        }
+}
+
+__global__ void __launch_bounds__(128) gp_pool_ehs(
+    const gp_tables * __restrict__ Tp, const gp_launch * __restrict__ X,
+    const gp_pool pool, gp_counters * cnt, const int * __restrict__ list,
+    int parity)
+{
+        const gp_config & cfg = X->cfg;
+        const gp_io & io = X->io;
+        const int count = cnt->n_ehs[parity];
+        const gp_tables & T = *Tp;
+        for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < count;
+             j += gridDim.x * blockDim.x) {
+                const int slot = list[j];
+                gp_event e;
+                gp_loop L;
+                gp_slot_load(pool, slot, cfg, e, L);
+                int event = GPUMAS_EVENT_NONE;
+                const int next = gp_stepping_ehs(T, cfg, e, L, event);
+                if (next == GP_NEXT_DONE) {
+                        gp_finish(pool, slot, cfg, io, cnt, e, event,
+                            L.medium);
+                } else {
+                        gp_slot_store(pool, slot, e, L);
+                        PI(SI_PHASE) = GP_NEXT_STEP;
+                }
+        }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Host driver.                                                             */
+/* ------------------------------------------------------------------------ */
+extern "C" void gp_pool_free(struct gp_pool_state * ps)
+{
+        if (ps == NULL) return;
+        if (ps->exec != NULL) cudaGraphExecDestroy(ps->exec);
+        if (ps->graph != NULL) cudaGraphDestroy(ps->graph);
+        if (ps->d_mem != NULL) cudaFree(ps->d_mem);
+        if (ps->h_counters != NULL) cudaFreeHost(ps->h_counters);
+        if (ps->h_launch != NULL) cudaFreeHost(ps->h_launch);
+        free(ps);
+}
+
+static int gp_pool_alloc(gp_context * c, int P)
+{
+        gp_pool_state * ps = c->pool;
+        if ((ps != NULL) && (ps->capacity == (size_t)P)) return 0;
+        gp_pool_free(ps);
+        c->pool = NULL;
+        ps = (gp_pool_state *)calloc(1, sizeof(*ps));
+        if (ps == NULL) return GPUMAS_RETURN_MEMORY_ERROR;
+        const size_t sd = (size_t)SD_N * P * sizeof(double);
+        const size_t si = (size_t)SI_N * P * sizeof(int);
+        const size_t su = (size_t)SU_N * P * sizeof(uint64_t);
+        const size_t sl = (size_t)P * sizeof(int);
+        const size_t total = sd + si + su + 4 * sl + 256 + sizeof(gp_launch);
+        int rc = gp_check(cudaMalloc(&ps->d_mem, total));
+        if (rc == 0)
+                rc = gp_check(cudaMallocHost(
+                    (void **)&ps->h_counters, sizeof(gp_counters)));
+        if (rc == 0)
+                rc = gp_check(cudaMallocHost(
+                    (void **)&ps->h_launch, sizeof(gp_launch)));
+        if (rc != 0) {
+                gp_pool_free(ps);
+                return rc;
+        }
+        char * p = (char *)ps->d_mem;
+        ps->pool.d = (double *)p;
+        ps->pool.u = (uint64_t *)(p + sd);
+        ps->pool.i = (int *)(p + sd + su);
+        ps->del_list[0] = (int *)(p + sd + su + si);
+        ps->del_list[1] = ps->del_list[0] + P;
+        ps->ehs_list[0] = ps->del_list[1] + P;
+        ps->ehs_list[1] = ps->ehs_list[0] + P;
+        ps->d_counters = (gp_counters *)(ps->ehs_list[1] + P);
+        ps->d_launch = (gp_launch *)((char *)ps->d_counters + 256);
+        ps->pool.P = P;
+        ps->capacity = P;
+        c->pool = ps;
+        return 0;
+}
+
+static void gp_iteration(gp_context * c, int parity, int block,
+    cudaStream_t s)
+{
+        gp_pool_state * ps = c->pool;
+        const int P = ps->pool.P;
+        const unsigned int grid = (P + block - 1) / block;
+        gp_pool_step<<<grid, block, 0, s>>>(c->d_tables, c->d_geometry,
+            ps->d_launch, ps->pool, ps->d_counters, ps->del_list[parity],
+            ps->ehs_list[parity], parity);
+        const unsigned int grid2 = (grid + 3) / 4;
+        gp_pool_del<<<grid2, block, 0, s>>>(c->d_tables, ps->d_launch,
+            ps->pool, ps->d_counters, ps->del_list[parity], parity);
+        gp_pool_ehs<<<grid2, block, 0, s>>>(c->d_tables, ps->d_launch,
+            ps->pool, ps->d_counters, ps->ehs_list[parity], parity);
+}
+
+/* Transport n events of `io` with the slot pool. Returns the number of
+ * kernel launches in *launches. */
+extern "C" int gp_pool_transport(gp_context * c, const gp_config * cfg_,
+    const gp_io * io_, size_t n, uint64_t first, cudaStream_t s,
+    const gp_tuning * tuning, int * launches)
+{
+        const gp_config cfg = *cfg_;
+        const gp_io io = *io_;
+        int P = tuning->pool_slots;
+        if ((size_t)P > n) P = (int)((n + 127) / 128 * 128);
+        if (P < 128) P = 128;
+        int rc = gp_pool_alloc(c, P);
+        if (rc != 0) return rc;
+        gp_pool_state * ps = c->pool;
+        const int block = 128;
+        const int batch = (tuning->batch > 0) ? tuning->batch : 16;
+        const int inner = (tuning->max_inner > 0) ? tuning->max_inner : 1;
+
+        rc = gp_check(cudaMemsetAsync(ps->pool.i + (size_t)SI_PHASE * P, 0,
+            (size_t)P * sizeof(int), s));
+        if (rc == 0)
+                rc = gp_check(cudaMemsetAsync(
+                    ps->d_counters, 0, sizeof(gp_counters), s));
+        if (rc != 0) return rc;
+
+        /* Launch parameters of this call. */
+        ps->h_launch->cfg = cfg;
+        ps->h_launch->io = io;
+        ps->h_launch->n = n;
+        ps->h_launch->first_event = first;
+        ps->h_launch->max_inner = inner;
+        rc = gp_check(cudaMemcpyAsync(ps->d_launch, ps->h_launch,
+            sizeof(gp_launch), cudaMemcpyHostToDevice, s));
+        if (rc != 0) return rc;
+
+        /* A batch of iterations as a CUDA graph (an even number, for the
+         * list parity), rebuilt only when the pool or the context changes. */
+        const int iters = 2 * ((batch + 1) / 2);
+        const int same = (ps->exec != NULL) && (ps->graph_batch == iters) &&
+            (ps->graph_tables == c->d_tables) &&
+            (ps->graph_geometry == c->d_geometry);
+        if (!same) {
+                if (ps->exec != NULL) cudaGraphExecDestroy(ps->exec);
+                if (ps->graph != NULL) cudaGraphDestroy(ps->graph);
+                ps->exec = NULL;
+                ps->graph = NULL;
+                cudaStream_t cap;
+                rc = gp_check(cudaStreamCreateWithFlags(
+                    &cap, cudaStreamNonBlocking));
+                if (rc != 0) return rc;
+                rc = gp_check(cudaStreamBeginCapture(
+                    cap, cudaStreamCaptureModeThreadLocal));
+                if (rc == 0) {
+                        for (int k = 0; k < iters; k++)
+                                gp_iteration(c, k & 1, block, cap);
+                        rc = gp_check(cudaStreamEndCapture(cap, &ps->graph));
+                }
+                if (rc == 0)
+                        rc = gp_check(cudaGraphInstantiate(
+                            &ps->exec, ps->graph, 0));
+                cudaStreamDestroy(cap);
+                if (rc != 0) return rc;
+                ps->graph_batch = iters;
+                ps->graph_tables = c->d_tables;
+                ps->graph_geometry = c->d_geometry;
+        }
+        int n_launch = 0;
+        for (long it = 0;; it++) {
+                rc = gp_check(cudaGraphLaunch(ps->exec, s));
+                if (rc != 0) return rc;
+                n_launch += 3 * iters;
+                rc = gp_check(cudaMemcpyAsync(ps->h_counters, ps->d_counters,
+                    sizeof(gp_counters), cudaMemcpyDeviceToHost, s));
+                if (rc == 0) rc = gp_check(cudaStreamSynchronize(s));
+                if (rc != 0) return rc;
+                if ((ps->h_counters->cursor >= n) &&
+                    (ps->h_counters->active == 0))
+                        break;
+                if (it > (1L << 40)) return GPUMAS_RETURN_INTERNAL_ERROR;
+        }
+        if (launches != NULL) *launches = n_launch;
+        return 0;
+}

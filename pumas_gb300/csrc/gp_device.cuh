@@ -49,7 +49,14 @@
 /* Iteration cap of the reference's unbounded rejection loops. */
 #define GP_MAX_REJECTIONS 100000
 
-#define GPD __device__ __forceinline__
+#define GPD static __device__ __forceinline__
+
+/* Products and sums rounded separately, as on the host: used where the
+ * reference's expression cancels and a fused multiply-add would change the
+ * result beyond the parity tolerance. */
+#define GP_MUL(a, b) __dmul_rn((a), (b))
+#define GP_ADD(a, b) __dadd_rn((a), (b))
+#define GP_SUB(a, b) __dsub_rn((a), (b))
 
 /* Transport settings of a launch (the public fields of pumas_context). */
 struct gp_config {
@@ -620,23 +627,23 @@ GPD double gp_coulomb_restricted_cs(double mu, double fspin, int n_parameters,
 
 /* Gauss-Legendre nodes and weights on [0, 1], 9 and 12 points, as in
  * math_gauss_quad_coefficients (pumas.c:12463-12561). */
-__constant__ double gp_gl9_x[9] = {
+static __constant__ double gp_gl9_x[9] = {
         0.0159198802461870, 0.0819844463366821, 0.1933142836497048,
         0.3378732882980955, 0.5000000000000000, 0.6621267117019045,
         0.8066857163502952, 0.9180155536633179, 0.9840801197538130,
 };
-__constant__ double gp_gl9_w[9] = {
+static __constant__ double gp_gl9_w[9] = {
         0.0406371941807872, 0.0903240803474287, 0.1303053482014677,
         0.1561735385200015, 0.1651196775006299, 0.1561735385200015,
         0.1303053482014677, 0.0903240803474287, 0.0406371941807872,
 };
-__constant__ double gp_gl12_x[12] = {
+static __constant__ double gp_gl12_x[12] = {
         0.0092196828766404, 0.0479413718147625, 0.1150486629028477,
         0.2063410228566913, 0.3160842505009099, 0.4373832957442655,
         0.5626167042557344, 0.6839157494990901, 0.7936589771433087,
         0.8849513370971523, 0.9520586281852375, 0.9907803171233596,
 };
-__constant__ double gp_gl12_w[12] = {
+static __constant__ double gp_gl12_w[12] = {
         0.0235876681932559, 0.0534696629976592, 0.0800391642716731,
         0.1015837133615330, 0.1167462682691774, 0.1245735229067014,
         0.1245735229067014, 0.1167462682691774, 0.1015837133615330,
@@ -645,7 +652,7 @@ __constant__ double gp_gl12_w[12] = {
 
 /* Chebyshev coefficients of CERNLIB RDILOG (C332), math_dilog
  * (pumas.c:12609-12673). */
-__constant__ double gp_dilog_c[20] = {
+static __constant__ double gp_dilog_c[20] = {
         0.42996693560813697, 0.40975987533077105, -0.01858843665014592,
         0.00145751084062268, -0.00014304184442340, 0.00001588415541880,
         -0.00000190784959387, 0.00000024195180854, -0.00000003193341274,
@@ -658,7 +665,7 @@ __constant__ double gp_dilog_c[20] = {
 GPD double gp_sq(double x) { return x * x; }
 
 /* math_dilog (pumas.c:12609-12673); pow(y, 2.) is exactly y * y. */
-__device__ double gp_dilog(double x)
+static __device__ double gp_dilog(double x)
 {
         const double PI3 = GP_PI * GP_PI / 3.;
         const double PI6 = GP_PI * GP_PI / 6.;
@@ -714,7 +721,7 @@ __device__ double gp_dilog(double x)
 #define GP_SSR_RE 2.8179403227E-13
 
 /* dcs_bremsstrahlung_SSR (pumas.c:13915-14005), in m^2/GeV. */
-__device__ double gp_dcs_bremsstrahlung(const gp_tables & T,
+static __device__ double gp_dcs_bremsstrahlung(const gp_tables & T,
     const gp_element & el, double K, double q)
 {
         double m = T.mass;
@@ -769,7 +776,7 @@ __device__ double gp_dcs_bremsstrahlung(const gp_tables & T,
 }
 
 /* dcs_pair_production_d2_SSR (pumas.c:14394-14544). */
-__device__ double gp_dcs_pair_d2(const gp_tables & T, const gp_element & el,
+static __device__ double gp_dcs_pair_d2(const gp_tables & T, const gp_element & el,
     double K, double q, double rho)
 {
         double m = T.mass;
@@ -893,7 +900,7 @@ __device__ double gp_dcs_pair_d2(const gp_tables & T, const gp_element & el,
 }
 
 /* dcs_pair_production_SSR (pumas.c:14560-14604). */
-__device__ double gp_dcs_pair_production(const gp_tables & T,
+static __device__ double gp_dcs_pair_production(const gp_tables & T,
     const gp_element & el, double K, double q)
 {
         const double mass = T.mass;
@@ -951,7 +958,7 @@ GPD double gp_f2p_allm97(const gp_tables & T, double x, double Q2)
 
 /* dcs_photonuclear_d2_DRSS (pumas.c:14923-14943) with the shadowing and F2
  * of pumas.c:14688-14721. */
-__device__ double gp_photonuclear_d2(const gp_tables & T,
+static __device__ double gp_photonuclear_d2(const gp_tables & T,
     const gp_element & el, double K, double q, double Q2)
 {
         const double ml = T.mass;
@@ -984,7 +991,7 @@ __device__ double gp_photonuclear_d2(const gp_tables & T,
 }
 
 /* dcs_photonuclear_DRSS (pumas.c:15002-15083, mode 0). */
-__device__ double gp_dcs_photonuclear(const gp_tables & T,
+static __device__ double gp_dcs_photonuclear(const gp_tables & T,
     const gp_element & el, double K, double q)
 {
         const double ml = T.mass;
@@ -1041,7 +1048,7 @@ GPD double gp_electronic_dcs(double Z, double I, double m, double K, double q)
 }
 
 /* Process DCS wrappers (pumas.c:11003-11122), in m^2/kg. */
-__device__ double gp_dcs_process(const gp_tables & T, int process,
+static __device__ double gp_dcs_process(const gp_tables & T, int process,
     const gp_element & el, double K, double q)
 {
         const double m = T.mass;
@@ -1068,7 +1075,7 @@ GPD float gp_logf(float x) { return (float)log((double)x); }
 GPD float gp_expf(float x) { return (float)exp((double)x); }
 
 /* dcs_evaluate (pumas.c:11243-11347). */
-__device__ double gp_dcs_evaluate(const gp_tables & T, int process,
+static __device__ double gp_dcs_evaluate(const gp_tables & T, int process,
     const gp_element & el, double K, double q)
 {
         const double wj = K / (K + T.mass);
@@ -1221,7 +1228,7 @@ GPD double gp_randn(gp_event & e)
 }
 
 /* step_rotate_direction (pumas.c:7042-7095). */
-__device__ void gp_rotate(gp_event & e, double mu)
+static __device__ void gp_rotate(gp_event & e, double mu)
 {
         double * const direction = e.dir;
         const double cos_theta = 1 - 2 * mu;
@@ -1273,7 +1280,7 @@ __device__ void gp_rotate(gp_event & e, double mu)
 /* ------------------------------------------------------------------------ */
 
 /* polar_bremsstrahlung (pumas.c:11759-11830), also for pair production. */
-__device__ double gp_polar_bremsstrahlung(const gp_tables & T, gp_event & e,
+static __device__ double gp_polar_bremsstrahlung(const gp_tables & T, gp_event & e,
     const gp_element & el, double ki, double kf)
 {
         const double m = T.mass;
@@ -1329,7 +1336,7 @@ GPD double gp_polar_objective(const gp_tables & T, const gp_element & el,
 
 /* math_find_minimum_brent (pumas.c:12233-12325); as in the reference the
  * upper bracket of the search is the initial minimiser xb. */
-__device__ int gp_find_minimum_brent(const gp_tables & T,
+static __device__ int gp_find_minimum_brent(const gp_tables & T,
     const gp_element & el, double K, double q, double xa, double xb,
     double xc, double fb, double tol, int max_iter, double & xopt,
     double & fopt)
@@ -1402,7 +1409,7 @@ __device__ int gp_find_minimum_brent(const gp_tables & T,
 }
 
 /* math_find_minimum with Brent refinement (pumas.c:12105-12206). */
-__device__ int gp_find_minimum(const gp_tables & T, const gp_element & el,
+static __device__ int gp_find_minimum(const gp_tables & T, const gp_element & el,
     double K, double q, double xa, double xc, double tol, int max_iter,
     double & xopt, double & fopt)
 {
@@ -1446,7 +1453,7 @@ __device__ int gp_find_minimum(const gp_tables & T, const gp_element & el,
 }
 
 /* polar_photonuclear (pumas.c:11874-11950). */
-__device__ double gp_polar_photonuclear(const gp_tables & T, gp_event & e,
+static __device__ double gp_polar_photonuclear(const gp_tables & T, gp_event & e,
     const gp_element & el, double ki, double kf)
 {
         const double M = 0.5 * (GP_PROTON_MASS + GP_NEUTRON_MASS);
@@ -1494,7 +1501,7 @@ __device__ double gp_polar_photonuclear(const gp_tables & T, gp_event & e,
         const double eps = ml / E1;
         const double p1 = E1 * sqrt((1. + eps) * (1. - eps));
         const double p2 = p * p1;
-        double tmp = p2 + ml * ml - E * E1;
+        double tmp = GP_SUB(GP_ADD(p2, GP_MUL(ml, ml)), GP_MUL(E, E1));
         if (fabs(tmp) <= 3 * GP_DBL_EPSILON * p2) tmp = 0.;
         const double a_mu = 0.5 * tmp / p2;
         const double b_mu = 0.25 / p2;
@@ -1512,12 +1519,13 @@ GPD double gp_polar_ionisation(const gp_tables & T, double ki, double kf)
         const double nu = ki - kf;
         const double p2 = ki * (ki + 2 * T.mass);
         const double E = ki + T.mass;
-        const double c = (p2 - nu * (E + GP_ELECTRON_MASS)) /
-            sqrt(p2 * (p2 + nu * nu - 2 * nu * E));
+        const double c = GP_SUB(p2, GP_MUL(nu, E + GP_ELECTRON_MASS)) /
+            sqrt(p2 * GP_SUB(GP_ADD(p2, GP_MUL(nu, nu)),
+                          GP_MUL(2 * nu, E)));
         return 0.5 * (1. - c);
 }
 
-__device__ double gp_polar(const gp_tables & T, gp_event & e, int process,
+static __device__ double gp_polar(const gp_tables & T, gp_event & e, int process,
     const gp_element & el, double ki, double kf)
 {
         if (process <= 1)
@@ -1533,7 +1541,7 @@ __device__ double gp_polar(const gp_tables & T, gp_event & e, int process,
 /* ------------------------------------------------------------------------ */
 
 /* dcs_ionisation_randomise (pumas.c:11185-11226). */
-__device__ double gp_ionisation_randomise(const gp_tables & T, gp_event & e,
+static __device__ double gp_ionisation_randomise(const gp_tables & T, gp_event & e,
     const gp_element & el, double K, double xlow)
 {
         const double P2 = K * (K + 2. * T.mass);
@@ -1580,7 +1588,7 @@ GPD double gp_envelope_norm(double a, double xmin, double xmax)
 
 /* del_randomise_target (pumas.c:6154-6270). Returns the process and sets the
  * target element; in backward mode also the DCS sum as *weight. */
-__device__ void gp_del_target(const gp_tables & T, const gp_config & cfg,
+static __device__ void gp_del_target(const gp_tables & T, const gp_config & cfg,
     gp_event & e, int material, double Q, int & process, int & element,
     double & weight)
 {
@@ -1677,7 +1685,7 @@ __device__ void gp_del_target(const gp_tables & T, const gp_config & cfg,
 
 /* del_randomise_forward (pumas.c:5912-6017). Returns true if a polar angle
  * is to be sampled. */
-__device__ bool gp_del_forward(const gp_tables & T, const gp_config & cfg,
+static __device__ bool gp_del_forward(const gp_tables & T, const gp_config & cfg,
     gp_event & e, int material, int & process, int & target)
 {
         if (e.energy <= __ldg(T.Kt + material)) return false;
@@ -1761,7 +1769,7 @@ __device__ bool gp_del_forward(const gp_tables & T, const gp_config & cfg,
 
 /* del_randomise_reverse (pumas.c:6036-6093) with the power law sampling
  * of del_randomise_power_law (pumas.c:6109-6138), alpha = 2. */
-__device__ bool gp_del_reverse(const gp_tables & T, const gp_config & cfg,
+static __device__ bool gp_del_reverse(const gp_tables & T, const gp_config & cfg,
     gp_event & e, int material, int & process, int & target)
 {
         const double lnq0 = -log(T.cutoff);
@@ -1827,7 +1835,7 @@ __device__ bool gp_del_reverse(const gp_tables & T, const gp_config & cfg,
 }
 
 /* transport_do_del (pumas.c:5706-5757). */
-__device__ void gp_do_del(const gp_tables & T, const gp_config & cfg,
+static __device__ void gp_do_del(const gp_tables & T, const gp_config & cfg,
     gp_event & e, int material)
 {
         double ki, kf;
@@ -1868,7 +1876,7 @@ __device__ void gp_do_del(const gp_tables & T, const gp_config & cfg,
 /* ------------------------------------------------------------------------ */
 /* Elastic hard scattering (transport_do_ehs, pumas.c:5768-5885).           */
 /* ------------------------------------------------------------------------ */
-__device__ void gp_do_ehs(const gp_tables & T, const gp_config & cfg,
+static __device__ void gp_do_ehs(const gp_tables & T, const gp_config & cfg,
     gp_event & e, int material)
 {
         const double kinetic = e.energy;
@@ -1969,7 +1977,7 @@ __device__ void gp_do_ehs(const gp_tables & T, const gp_config & cfg,
 /* ------------------------------------------------------------------------ */
 
 /* step_fluctuate (pumas.c:6943-7005). */
-__device__ void gp_fluctuate(const gp_tables & T, const gp_config & cfg,
+static __device__ void gp_fluctuate(const gp_tables & T, const gp_config & cfg,
     gp_event & e, int material, double Xtot, double dX, double & kf,
     double & ratio)
 {
@@ -2028,7 +2036,7 @@ __device__ void gp_fluctuate(const gp_tables & T, const gp_config & cfg,
 }
 
 /* transport_limit (pumas.c:5569-5696). */
-__device__ void gp_limit(const gp_tables & T, const gp_config & cfg,
+static __device__ void gp_limit(const gp_tables & T, const gp_config & cfg,
     gp_event & e, int material, double Xi, double Xf, double & grammage_max)
 {
         e.step_event = e.step_foreseen = GPUMAS_EVENT_NONE;
@@ -2124,7 +2132,7 @@ __device__ void gp_limit(const gp_tables & T, const gp_config & cfg,
 
 /* step_transport (pumas.c:6296-6925) for uniform media without magnetic
  * field. Sets e.step_event and returns the end step medium. */
-__device__ int gp_step(const gp_tables & T, const gp_config & cfg,
+static __device__ int gp_step(const gp_tables & T, const gp_config & cfg,
     const gpumas_geometry & g, gp_event & e, int straight, int medium,
     int material, double density, double grammage_max,
     double step_max_medium)
@@ -2437,7 +2445,7 @@ __device__ int gp_step(const gp_tables & T, const gp_config & cfg,
                         const double c =
                             -2. * (time_max - ti) * momentum / T.mass;
                         if (a != 0.) {
-                                double delta = 1. - a * c;
+                                double delta = GP_SUB(1., GP_MUL(a, c));
                                 if (delta < 0.) delta = 0.;
                                 step = 1. / a * (sqrt(delta) - 1.);
                         } else {
@@ -2445,8 +2453,10 @@ __device__ int gp_step(const gp_tables & T, const gp_config & cfg,
                         }
                         if (step < 0.) step = 0.;
                         if (scheme != GPUMAS_MODE_DISABLED) {
-                                const double p1 = momentum / (1 + a * step);
-                                k1 = sqrt(p1 * p1 - T.mass * T.mass) - T.mass;
+                                const double p1 =
+                                    momentum / GP_ADD(1, GP_MUL(a, step));
+                                k1 = sqrt(GP_SUB(GP_MUL(p1, p1),
+                                         GP_MUL(T.mass, T.mass))) - T.mass;
                                 if (k1 < 0.) k1 = 0.;
                         }
                         const double Xf = Xi + dX;
@@ -2494,119 +2504,209 @@ __device__ int gp_step(const gp_tables & T, const gp_config & cfg,
  * none, the engine stops the event with an internal error instead. */
 #define GP_MAX_STEPS 100000000
 
-/* transport_with_stepping (pumas.c:5194-5514), uniform media. */
-__device__ int gp_transport_stepping(const gp_tables & T,
-    const gp_config & cfg, const gpumas_geometry & g, gp_event & e,
-    int & medium, double density, double step_max_medium)
-{
-        int material = gp_medium_material(g, medium);
-        const int scheme = cfg.energy_loss;
-        const int straight = ((cfg.scattering == GPUMAS_MODE_DISABLED) &&
-                                 (scheme <= GPUMAS_MODE_MIXED)) ? 1 : 0;
-        e.step_event = GPUMAS_EVENT_NONE;
-        double ti = e.time, wi = e.weight, Xi = e.grammage;
-        double dei, Xf;
-        if (scheme > GPUMAS_MODE_DISABLED) {
-                Xf = gp_cel_grammage(T, scheme, material, e.energy);
-                dei = 1. / gp_cel_energy_loss(T, scheme, material, e.energy);
-        } else {
-                Xf = dei = 0.;
-        }
-        if ((cfg.event & GPUMAS_EVENT_LIMIT_DISTANCE) &&
-            (e.distance >= cfg.limit_distance))
-                return GPUMAS_EVENT_LIMIT_DISTANCE;
-        if ((cfg.event & GPUMAS_EVENT_LIMIT_GRAMMAGE) &&
-            (e.grammage >= cfg.limit_grammage))
-                return GPUMAS_EVENT_LIMIT_GRAMMAGE;
-        if ((cfg.event & GPUMAS_EVENT_LIMIT_TIME) &&
-            (e.time >= cfg.limit_time))
-                return GPUMAS_EVENT_LIMIT_TIME;
-        if (e.weight <= 0.) return GPUMAS_EVENT_WEIGHT;
+/* Loop carried locals of transport_with_stepping (pumas.c:5194-5514):
+ * together with gp_event they are the whole state of an event between two
+ * steps, which lets the stepping loop be suspended and resumed in another
+ * kernel. */
+struct gp_loop {
+        int medium, material, straight, step_index;
+        int new_medium;
+        double density, ti, wi, Xi, Xf, dei, grammage_max, step_max_medium;
+};
 
-        double grammage_max = 0.;
+/* What an event needs next. */
+enum gp_next {
+        GP_NEXT_STEP = 1, /* another continuous step */
+        GP_NEXT_DEL = 2,  /* a discrete energy loss (transport_do_del) */
+        GP_NEXT_EHS = 3,  /* a hard elastic scatter (transport_do_ehs) */
+        GP_NEXT_DONE = 4  /* the transport call is over */
+};
+
+/* Prologue of transport_with_stepping, up to the first transport_limit
+ * (pumas.c:5201-5271). Returns GP_NEXT_STEP or GP_NEXT_DONE (then *event is
+ * the end event). */
+static __device__ int gp_stepping_begin(const gp_tables & T, const gp_config & cfg,
+    const gpumas_geometry & g, gp_event & e, gp_loop & L, int & event)
+{
+        L.material = gp_medium_material(g, L.medium);
+        const int scheme = cfg.energy_loss;
+        L.straight = ((cfg.scattering == GPUMAS_MODE_DISABLED) &&
+                         (scheme <= GPUMAS_MODE_MIXED)) ? 1 : 0;
+        e.step_event = GPUMAS_EVENT_NONE;
+        L.ti = e.time;
+        L.wi = e.weight;
+        L.Xi = e.grammage;
+        if (scheme > GPUMAS_MODE_DISABLED) {
+                L.Xf = gp_cel_grammage(T, scheme, L.material, e.energy);
+                L.dei = 1. /
+                    gp_cel_energy_loss(T, scheme, L.material, e.energy);
+        } else {
+                L.Xf = L.dei = 0.;
+        }
+        event = GPUMAS_EVENT_NONE;
+        if ((cfg.event & GPUMAS_EVENT_LIMIT_DISTANCE) &&
+            (e.distance >= cfg.limit_distance)) {
+                event = GPUMAS_EVENT_LIMIT_DISTANCE;
+                return GP_NEXT_DONE;
+        }
+        if ((cfg.event & GPUMAS_EVENT_LIMIT_GRAMMAGE) &&
+            (e.grammage >= cfg.limit_grammage)) {
+                event = GPUMAS_EVENT_LIMIT_GRAMMAGE;
+                return GP_NEXT_DONE;
+        }
+        if ((cfg.event & GPUMAS_EVENT_LIMIT_TIME) &&
+            (e.time >= cfg.limit_time)) {
+                event = GPUMAS_EVENT_LIMIT_TIME;
+                return GP_NEXT_DONE;
+        }
+        if (e.weight <= 0.) {
+                event = GPUMAS_EVENT_WEIGHT;
+                return GP_NEXT_DONE;
+        }
+        L.grammage_max = 0.;
         e.step_event = GPUMAS_EVENT_NONE;
         e.step_first = 1;
         e.step_X_limit = (cfg.event & GPUMAS_EVENT_LIMIT_ENERGY) ?
             gp_cel_grammage(T,
                 (scheme > GPUMAS_MODE_DISABLED) ? scheme : GPUMAS_MODE_CSDA,
-                material, cfg.limit_energy) :
+                L.material, cfg.limit_energy) :
             0.;
         e.step_invlb1 = 0;
-        gp_limit(T, cfg, e, material, Xi, Xf, grammage_max);
-        if (e.step_event) return e.step_event;
+        gp_limit(T, cfg, e, L.material, L.Xi, L.Xf, L.grammage_max);
+        if (e.step_event) {
+                event = e.step_event;
+                return GP_NEXT_DONE;
+        }
+        L.step_index = 1;
+        return GP_NEXT_STEP;
+}
 
-        for (int step_index = 1; step_index < GP_MAX_STEPS; step_index++) {
-                if (e.status != GPUMAS_RETURN_SUCCESS) break;
-                if (step_index > 1) {
-                        const int m = gp_locate(g, e);
-                        step_max_medium = gp_step_proposal(cfg, g, e, m);
-                        if (step_max_medium > 0.)
-                                step_max_medium += 0.5 * GP_STEP_MIN;
-                }
-                const int new_medium = gp_step(T, cfg, g, e, straight, medium,
-                    material, density, grammage_max, step_max_medium);
-                if (!e.step_event) continue;
+/* Refresh of the initial conditions and limits after an event
+ * (pumas.c:5479-5488). */
+static __device__ int gp_stepping_relimit(const gp_tables & T, const gp_config & cfg,
+    gp_event & e, gp_loop & L, int & event)
+{
+        L.ti = e.time;
+        L.wi = e.weight;
+        L.Xi = e.grammage;
+        if (cfg.energy_loss >= GPUMAS_MODE_CSDA) {
+                L.Xf = gp_cel_grammage(T, cfg.energy_loss, L.material,
+                    e.energy);
+                L.dei = 1. / gp_cel_energy_loss(T, cfg.energy_loss,
+                                 L.material, e.energy);
+        }
+        gp_limit(T, cfg, e, L.material, L.Xi, L.Xf, L.grammage_max);
+        if (e.step_event) {
+                event = e.step_event;
+                return GP_NEXT_DONE;
+        }
+        return GP_NEXT_STEP;
+}
 
-                if ((cfg.direction == GPUMAS_MODE_BACKWARD) &&
-                    (cfg.energy_loss >= GPUMAS_MODE_CSDA)) {
-                        const double wt = (cfg.decay == GPUMAS_MODE_WEIGHTED) ?
-                            exp(-fabs(e.time - ti) / T.ctau) : 1.;
-                        e.weight = wi * wt * dei *
-                            gp_cel_energy_loss(T, scheme, material, e.energy);
-                } else if (cfg.decay == GPUMAS_MODE_WEIGHTED) {
-                        e.weight = wi * exp(-fabs(e.time - ti) / T.ctau);
-                }
+/* One iteration of the stepping loop up to the dispatch of its event
+ * (pumas.c:5277-5329 and the medium change of 5417-5467). */
+static __device__ int gp_stepping_step(const gp_tables & T, const gp_config & cfg,
+    const gpumas_geometry & g, gp_event & e, gp_loop & L, int & event)
+{
+        if (L.step_index > 1) {
+                const int m = gp_locate(g, e);
+                L.step_max_medium = gp_step_proposal(cfg, g, e, m);
+                if (L.step_max_medium > 0.)
+                        L.step_max_medium += 0.5 * GP_STEP_MIN;
+        }
+        L.new_medium = gp_step(T, cfg, g, e, L.straight, L.medium,
+            L.material, L.density, L.grammage_max, L.step_max_medium);
+        L.step_index++;
+        if (e.status != GPUMAS_RETURN_SUCCESS) {
+                event = e.step_event;
+                return GP_NEXT_DONE;
+        }
+        if (L.step_index >= GP_MAX_STEPS) {
+                e.status = GPUMAS_RETURN_INTERNAL_ERROR;
+                event = e.step_event;
+                return GP_NEXT_DONE;
+        }
+        if (!e.step_event) return GP_NEXT_STEP;
 
-                if (e.step_event & (GPUMAS_EVENT_LIMIT | GPUMAS_EVENT_WEIGHT |
-                                       GPUMAS_EVENT_VERTEX_DECAY)) {
-                        break;
-                } else if (e.step_event & GPUMAS_EVENT_VERTEX_DEL) {
-                        gp_do_del(T, cfg, e, material);
-                        if ((cfg.event & e.step_event) ||
-                            (e.step_event == GPUMAS_EVENT_WEIGHT))
-                                break;
-                        e.step_first = 1;
-                        e.step_invlb1 = 0;
-                } else if (e.step_event & GPUMAS_EVENT_VERTEX_COULOMB) {
-                        gp_do_ehs(T, cfg, e, material);
-                        if (cfg.event & e.step_event) break;
-                } else if (e.step_event & GPUMAS_EVENT_MEDIUM) {
-                        medium = new_medium;
-                        if ((medium < 0) || (cfg.event & GPUMAS_EVENT_MEDIUM))
-                                break;
-                        material = gp_medium_material(g, medium);
-                        density = gp_medium_density(T, g, medium);
-                        if (density <= 0.) {
-                                e.status = GPUMAS_RETURN_DENSITY_ERROR;
-                                break;
-                        }
-                        e.step_X_limit =
-                            (cfg.event & GPUMAS_EVENT_LIMIT_ENERGY) ?
-                            gp_cel_grammage(T,
-                                scheme > GPUMAS_MODE_DISABLED ? scheme :
-                                                                GPUMAS_MODE_CSDA,
-                                material, cfg.limit_energy) :
-                            0.;
-                        e.step_first = 1;
-                        e.step_invlb1 = 0;
-                } else {
-                        e.status = GPUMAS_RETURN_INTERNAL_ERROR;
-                        break;
-                }
-                ti = e.time;
-                wi = e.weight;
-                Xi = e.grammage;
-                if (cfg.energy_loss >= GPUMAS_MODE_CSDA) {
-                        Xf = gp_cel_grammage(T, scheme, material, e.energy);
-                        dei = 1. /
-                            gp_cel_energy_loss(T, scheme, material, e.energy);
-                }
-                gp_limit(T, cfg, e, material, Xi, Xf, grammage_max);
-                if (e.step_event) break;
-                if (step_index == GP_MAX_STEPS - 1)
-                        e.status = GPUMAS_RETURN_INTERNAL_ERROR;
+        const int scheme = cfg.energy_loss;
+        if ((cfg.direction == GPUMAS_MODE_BACKWARD) &&
+            (cfg.energy_loss >= GPUMAS_MODE_CSDA)) {
+                const double wt = (cfg.decay == GPUMAS_MODE_WEIGHTED) ?
+                    exp(-fabs(e.time - L.ti) / T.ctau) : 1.;
+                e.weight = L.wi * wt * L.dei *
+                    gp_cel_energy_loss(T, scheme, L.material, e.energy);
+        } else if (cfg.decay == GPUMAS_MODE_WEIGHTED) {
+                e.weight = L.wi * exp(-fabs(e.time - L.ti) / T.ctau);
         }
 
+        if (e.step_event & (GPUMAS_EVENT_LIMIT | GPUMAS_EVENT_WEIGHT |
+                               GPUMAS_EVENT_VERTEX_DECAY)) {
+                event = e.step_event;
+                return GP_NEXT_DONE;
+        } else if (e.step_event & GPUMAS_EVENT_VERTEX_DEL) {
+                return GP_NEXT_DEL;
+        } else if (e.step_event & GPUMAS_EVENT_VERTEX_COULOMB) {
+                return GP_NEXT_EHS;
+        } else if (e.step_event & GPUMAS_EVENT_MEDIUM) {
+                L.medium = L.new_medium;
+                if ((L.medium < 0) || (cfg.event & GPUMAS_EVENT_MEDIUM)) {
+                        event = e.step_event;
+                        return GP_NEXT_DONE;
+                }
+                L.material = gp_medium_material(g, L.medium);
+                L.density = gp_medium_density(T, g, L.medium);
+                if (L.density <= 0.) {
+                        e.status = GPUMAS_RETURN_DENSITY_ERROR;
+                        event = e.step_event;
+                        return GP_NEXT_DONE;
+                }
+                e.step_X_limit = (cfg.event & GPUMAS_EVENT_LIMIT_ENERGY) ?
+                    gp_cel_grammage(T,
+                        scheme > GPUMAS_MODE_DISABLED ? scheme :
+                                                        GPUMAS_MODE_CSDA,
+                        L.material, cfg.limit_energy) :
+                    0.;
+                e.step_first = 1;
+                e.step_invlb1 = 0;
+                return gp_stepping_relimit(T, cfg, e, L, event);
+        }
+        e.status = GPUMAS_RETURN_INTERNAL_ERROR;
+        event = e.step_event;
+        return GP_NEXT_DONE;
+}
+
+/* DEL of the stepping loop (pumas.c:5336-5374 and 5479-5488). */
+static __device__ int gp_stepping_del(const gp_tables & T, const gp_config & cfg,
+    gp_event & e, gp_loop & L, int & event)
+{
+        gp_do_del(T, cfg, e, L.material);
+        if ((cfg.event & e.step_event) ||
+            (e.step_event == GPUMAS_EVENT_WEIGHT) ||
+            (e.status != GPUMAS_RETURN_SUCCESS)) {
+                event = e.step_event;
+                return GP_NEXT_DONE;
+        }
+        e.step_first = 1;
+        e.step_invlb1 = 0;
+        return gp_stepping_relimit(T, cfg, e, L, event);
+}
+
+/* EHS of the stepping loop (pumas.c:5393-5400 and 5479-5488). */
+static __device__ int gp_stepping_ehs(const gp_tables & T, const gp_config & cfg,
+    gp_event & e, gp_loop & L, int & event)
+{
+        gp_do_ehs(T, cfg, e, L.material);
+        if ((cfg.event & e.step_event) ||
+            (e.status != GPUMAS_RETURN_SUCCESS)) {
+                event = e.step_event;
+                return GP_NEXT_DONE;
+        }
+        return gp_stepping_relimit(T, cfg, e, L, event);
+}
+
+/* Epilogue: protection of the final kinetic energy (pumas.c:5491-5505). */
+GPD void gp_stepping_end(const gp_config & cfg, gp_event & e)
+{
         if (cfg.direction == GPUMAS_MODE_FORWARD) {
                 const double kinetic_min =
                     (cfg.event & GPUMAS_EVENT_LIMIT_ENERGY) ?
@@ -2618,11 +2718,10 @@ __device__ int gp_transport_stepping(const gp_tables & T,
                     (fabs(e.energy - cfg.limit_energy) < GP_FLT_EPSILON))
                         e.energy = cfg.limit_energy;
         }
-        return e.step_event;
 }
 
 /* transport_with_csda (pumas.c:4777-4949), no magnetic field. */
-__device__ int gp_transport_csda(const gp_tables & T, const gp_config & cfg,
+static __device__ int gp_transport_csda(const gp_tables & T, const gp_config & cfg,
     gp_event & e, int material, double density)
 {
         const double ki = e.energy;
@@ -2775,39 +2874,43 @@ GPD void gp_event_init(gp_event & e, uint64_t seed, uint64_t id)
         e.status = GPUMAS_RETURN_SUCCESS;
 }
 
-/* pumas_context_transport (pumas.c:3114-3251) for one event. The context
- * level checks are done on the host before the launch. */
-__device__ void gp_transport(const gp_tables & T, const gp_config & cfg,
-    const gpumas_geometry & g, gp_event & e, int & event, int & medium_in,
-    int & medium_out)
+/* Entry of pumas_context_transport (pumas.c:3114-3251) for one event, up
+ * to the start of the stepping loop. The context level checks are done on
+ * the host before the launch. Returns GP_NEXT_STEP, or GP_NEXT_DONE with
+ * *event set (including the whole deterministic CSDA case). */
+static __device__ int gp_transport_begin(const gp_tables & T, const gp_config & cfg,
+    const gpumas_geometry & g, gp_event & e, gp_loop & L, int & event,
+    int & medium_in)
 {
         event = GPUMAS_EVENT_NONE;
-        medium_in = medium_out = -1;
+        medium_in = -1;
+        L.medium = -1;
         if (e.decayed) {
                 event = GPUMAS_EVENT_VERTEX_DECAY;
-                return;
+                return GP_NEXT_DONE;
         }
         {
                 const double * const u = e.dir;
                 const double norm2 = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
                 if (fabs(norm2 - 1) > GP_FLT_EPSILON) {
                         e.status = GPUMAS_RETURN_DIRECTION_ERROR;
-                        return;
+                        return GP_NEXT_DONE;
                 }
         }
-        int medium = gp_locate(g, e);
+        const int medium = gp_locate(g, e);
         double step_max_medium = gp_step_proposal(cfg, g, e, medium);
         medium_in = medium;
         if (medium < 0) {
                 event = GPUMAS_EVENT_MEDIUM;
-                return;
+                return GP_NEXT_DONE;
         } else if (step_max_medium > 0.)
                 step_max_medium += 0.5 * GP_STEP_MIN;
-        const double density = gp_medium_density(T, g, medium);
-        if (density <= 0.) {
+        L.density = gp_medium_density(T, g, medium);
+        if (L.density <= 0.) {
                 e.status = GPUMAS_RETURN_DENSITY_ERROR;
-                return;
+                return GP_NEXT_DONE;
         }
+        L.medium = medium;
         if (cfg.decay == GPUMAS_MODE_RANDOMISED) {
                 const double u = gp_random(e);
                 e.lifetime = e.time - T.ctau * log(u);
@@ -2818,20 +2921,49 @@ __device__ void gp_transport(const gp_tables & T, const gp_config & cfg,
                 if ((cfg.energy_loss == GPUMAS_MODE_DISABLED) &&
                     ((cfg.event & GPUMAS_EVENT_LIMIT) == 0)) {
                         e.status = GPUMAS_RETURN_MISSING_LIMIT;
-                        return;
+                        return GP_NEXT_DONE;
                 } else if ((cfg.scattering == GPUMAS_MODE_DISABLED) &&
                     (cfg.energy_loss == GPUMAS_MODE_CSDA)) {
                         do_stepping = 0;
                 }
         }
-        if (do_stepping) {
-                event = gp_transport_stepping(
-                    T, cfg, g, e, medium, density, step_max_medium);
-        } else {
-                event = gp_transport_csda(
-                    T, cfg, e, gp_medium_material(g, medium), density);
+        if (!do_stepping) {
+                event = gp_transport_csda(T, cfg, e,
+                    gp_medium_material(g, medium), L.density);
+                return GP_NEXT_DONE;
         }
-        medium_out = medium;
+        L.step_max_medium = step_max_medium;
+        const int next = gp_stepping_begin(T, cfg, g, e, L, event);
+        if (next == GP_NEXT_DONE) gp_stepping_end(cfg, e);
+        return next;
+}
+
+/* Resume the stepping loop of an event at phase `next` and run it to its
+ * end (the one thread per event form). */
+static __device__ void gp_transport_run(const gp_tables & T, const gp_config & cfg,
+    const gpumas_geometry & g, gp_event & e, gp_loop & L, int next,
+    int & event)
+{
+        while (next != GP_NEXT_DONE) {
+                if (next == GP_NEXT_STEP)
+                        next = gp_stepping_step(T, cfg, g, e, L, event);
+                else if (next == GP_NEXT_DEL)
+                        next = gp_stepping_del(T, cfg, e, L, event);
+                else
+                        next = gp_stepping_ehs(T, cfg, e, L, event);
+        }
+        gp_stepping_end(cfg, e);
+}
+
+/* pumas_context_transport for one event, in one thread. */
+static __device__ void gp_transport(const gp_tables & T, const gp_config & cfg,
+    const gpumas_geometry & g, gp_event & e, int & event, int & medium_in,
+    int & medium_out)
+{
+        gp_loop L;
+        const int next = gp_transport_begin(T, cfg, g, e, L, event, medium_in);
+        if (next != GP_NEXT_DONE) gp_transport_run(T, cfg, g, e, L, next, event);
+        medium_out = L.medium;
 }
 
 #endif /* GP_DEVICE_CUH */

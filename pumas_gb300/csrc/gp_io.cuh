@@ -1,0 +1,127 @@
+/*
+ * gp_io.cuh -- event input / output of the transport kernels: an array of
+ * pumas_state records (with per event results) or a structure of arrays.
+ */
+#ifndef GP_IO_CUH
+#define GP_IO_CUH
+
+#include "gp_device.cuh"
+
+/* ------------------------------------------------------------------------ */
+/* Event I/O: array of pumas_state structures or structure of arrays.       */
+/* ------------------------------------------------------------------------ */
+struct gp_io_aos {
+        gpumas_state * states;
+        gpumas_result * results;
+        __device__ void load(size_t i, gp_event & e) const
+        {
+                const gpumas_state & s = states[i];
+                e.charge = s.charge;
+                e.energy = s.energy;
+                e.distance = s.distance;
+                e.grammage = s.grammage;
+                e.time = s.time;
+                e.weight = s.weight;
+                for (int k = 0; k < 3; k++) {
+                        e.pos[k] = s.position[k];
+                        e.dir[k] = s.direction[k];
+                }
+                e.decayed = s.decayed;
+        }
+        __device__ void store(size_t i, const gp_event & e, int event,
+            int m_in, int m_out) const
+        {
+                gpumas_state & s = states[i];
+                s.charge = e.charge;
+                s.energy = e.energy;
+                s.distance = e.distance;
+                s.grammage = e.grammage;
+                s.time = e.time;
+                s.weight = e.weight;
+                for (int k = 0; k < 3; k++) {
+                        s.position[k] = e.pos[k];
+                        s.direction[k] = e.dir[k];
+                }
+                s.decayed = e.decayed;
+                if (results != NULL) {
+                        gpumas_result r;
+                        r.event = event;
+                        r.medium_in = m_in;
+                        r.medium_out = m_out;
+                        r.status = e.status;
+                        r.steps = e.steps;
+                        r.pad = 0;
+                        r.draws = e.n;
+                        results[i] = r;
+                }
+        }
+};
+
+struct gp_io_soa {
+        gpumas_soa a;
+        __device__ void load(size_t i, gp_event & e) const
+        {
+                e.charge = a.charge[i];
+                e.energy = a.energy[i];
+                e.distance = a.distance[i];
+                e.grammage = a.grammage[i];
+                e.time = a.time[i];
+                e.weight = a.weight[i];
+                for (int k = 0; k < 3; k++) {
+                        e.pos[k] = a.position[k][i];
+                        e.dir[k] = a.direction[k][i];
+                }
+                e.decayed = a.decayed[i];
+        }
+        __device__ void store(size_t i, const gp_event & e, int event,
+            int m_in, int m_out) const
+        {
+                a.charge[i] = e.charge;
+                a.energy[i] = e.energy;
+                a.distance[i] = e.distance;
+                a.grammage[i] = e.grammage;
+                a.time[i] = e.time;
+                a.weight[i] = e.weight;
+                for (int k = 0; k < 3; k++) {
+                        a.position[k][i] = e.pos[k];
+                        a.direction[k][i] = e.dir[k];
+                }
+                a.decayed[i] = e.decayed;
+                if (a.result != NULL) {
+                        gpumas_result r;
+                        r.event = event;
+                        r.medium_in = m_in;
+                        r.medium_out = m_out;
+                        r.status = e.status;
+                        r.steps = e.steps;
+                        r.pad = 0;
+                        r.draws = e.n;
+                        a.result[i] = r;
+                }
+        }
+};
+
+
+/* Event I/O of a launch: AoS (pumas_state array) when `aos.states` is set,
+ * SoA otherwise. */
+struct gp_io {
+        gp_io_aos aos;
+        gp_io_soa soa;
+        __device__ void load(size_t i, gp_event & e) const
+        {
+                if (aos.states != NULL)
+                        aos.load(i, e);
+                else
+                        soa.load(i, e);
+        }
+        __device__ void store(size_t i, const gp_event & e, int event,
+            int m_in, int m_out) const
+        {
+                if (aos.states != NULL)
+                        aos.store(i, e, event, m_in, m_out);
+                else
+                        soa.store(i, e, event, m_in, m_out);
+        }
+};
+
+#endif

@@ -15,125 +15,12 @@
 
 #include "gp_device.cuh"
 
-/* ------------------------------------------------------------------------ */
-/* Event I/O: array of pumas_state structures or structure of arrays.       */
-/* ------------------------------------------------------------------------ */
-struct gp_io_aos {
-        gpumas_state * states;
-        gpumas_result * results;
-        __device__ void load(size_t i, gp_event & e) const
-        {
-                const gpumas_state & s = states[i];
-                e.charge = s.charge;
-                e.energy = s.energy;
-                e.distance = s.distance;
-                e.grammage = s.grammage;
-                e.time = s.time;
-                e.weight = s.weight;
-                for (int k = 0; k < 3; k++) {
-                        e.pos[k] = s.position[k];
-                        e.dir[k] = s.direction[k];
-                }
-                e.decayed = s.decayed;
-        }
-        __device__ void store(size_t i, const gp_event & e, int event,
-            int m_in, int m_out) const
-        {
-                gpumas_state & s = states[i];
-                s.charge = e.charge;
-                s.energy = e.energy;
-                s.distance = e.distance;
-                s.grammage = e.grammage;
-                s.time = e.time;
-                s.weight = e.weight;
-                for (int k = 0; k < 3; k++) {
-                        s.position[k] = e.pos[k];
-                        s.direction[k] = e.dir[k];
-                }
-                s.decayed = e.decayed;
-                if (results != NULL) {
-                        gpumas_result r;
-                        r.event = event;
-                        r.medium_in = m_in;
-                        r.medium_out = m_out;
-                        r.status = e.status;
-                        r.steps = e.steps;
-                        r.pad = 0;
-                        r.draws = e.n;
-                        results[i] = r;
-                }
-        }
-};
+#include "gp_io.cuh"
+#include "gp_context.h"
 
-struct gp_io_soa {
-        gpumas_soa a;
-        __device__ void load(size_t i, gp_event & e) const
-        {
-                e.charge = a.charge[i];
-                e.energy = a.energy[i];
-                e.distance = a.distance[i];
-                e.grammage = a.grammage[i];
-                e.time = a.time[i];
-                e.weight = a.weight[i];
-                for (int k = 0; k < 3; k++) {
-                        e.pos[k] = a.position[k][i];
-                        e.dir[k] = a.direction[k][i];
-                }
-                e.decayed = a.decayed[i];
-        }
-        __device__ void store(size_t i, const gp_event & e, int event,
-            int m_in, int m_out) const
-        {
-                a.charge[i] = e.charge;
-                a.energy[i] = e.energy;
-                a.distance[i] = e.distance;
-                a.grammage[i] = e.grammage;
-                a.time[i] = e.time;
-                a.weight[i] = e.weight;
-                for (int k = 0; k < 3; k++) {
-                        a.position[k][i] = e.pos[k];
-                        a.direction[k][i] = e.dir[k];
-                }
-                a.decayed[i] = e.decayed;
-                if (a.result != NULL) {
-                        gpumas_result r;
-                        r.event = event;
-                        r.medium_in = m_in;
-                        r.medium_out = m_out;
-                        r.status = e.status;
-                        r.steps = e.steps;
-                        r.pad = 0;
-                        r.draws = e.n;
-                        a.result[i] = r;
-                }
-        }
-};
-
-/* ------------------------------------------------------------------------ */
-/* Kernels.                                                                 */
-/* ------------------------------------------------------------------------ */
-
-/* Event I/O of a launch: AoS (pumas_state array) when `aos.states` is set,
- * SoA otherwise. */
-struct gp_io {
-        gp_io_aos aos;
-        gp_io_soa soa;
-        __device__ void load(size_t i, gp_event & e) const
-        {
-                if (aos.states != NULL)
-                        aos.load(i, e);
-                else
-                        soa.load(i, e);
-        }
-        __device__ void store(size_t i, const gp_event & e, int event,
-            int m_in, int m_out) const
-        {
-                if (aos.states != NULL)
-                        aos.store(i, e, event, m_in, m_out);
-                else
-                        soa.store(i, e, event, m_in, m_out);
-        }
-};
+extern "C" int gp_pool_transport(gp_context * c, const gp_config * cfg,
+    const gp_io * io, size_t n, uint64_t first, cudaStream_t s,
+    const gp_tuning * tuning, int * launches);
 
 /* One thread per event, the whole transport call in one launch. */
 __global__ void __launch_bounds__(128) gp_kernel_plain(
@@ -171,27 +58,6 @@ __global__ void gp_kernel_random(uint64_t seed, uint32_t domain,
 /* ------------------------------------------------------------------------ */
 /* Contexts.                                                                */
 /* ------------------------------------------------------------------------ */
-struct gp_context {
-        struct gpumas_context api; /* first member: public view */
-        const struct gpumas_physics * physics;
-        gp_tables * d_tables;
-        gpumas_geometry * d_geometry;
-        void * d_geometry_data;
-        int has_geometry;
-        int n_media;
-        void * d_io;
-        size_t io_size;
-        cudaStream_t stream;
-        cudaEvent_t t0, t1;
-        struct gpumas_stats stats;
-        void * extra;
-};
-
-static int gp_check(cudaError_t rc)
-{
-        return (rc == cudaSuccess) ? GPUMAS_RETURN_SUCCESS :
-                                     GPUMAS_RETURN_DEVICE_ERROR;
-}
 
 extern "C" int gpumas_context_create(struct gpumas_context ** context,
     const struct gpumas_physics * physics, int extra_memory)
@@ -210,6 +76,10 @@ extern "C" int gpumas_context_create(struct gpumas_context ** context,
         c->api.event = GPUMAS_EVENT_NONE;
         c->api.accuracy = 1E-02;
         c->api.seed = 0;
+        c->tuning.engine = 0;
+        c->tuning.pool_slots = 262144;
+        c->tuning.max_inner = 2;
+        c->tuning.batch = 16;
         if (extra_memory > 0) {
                 c->extra = calloc(1, extra_memory);
                 c->api.user_data = c->extra;
@@ -247,6 +117,7 @@ extern "C" void gpumas_context_destroy(struct gpumas_context ** context)
         if (c->d_geometry != NULL) cudaFree(c->d_geometry);
         if (c->d_geometry_data != NULL) cudaFree(c->d_geometry_data);
         if (c->d_io != NULL) cudaFree(c->d_io);
+        gp_pool_free(c->pool);
         if (c->stream != NULL) cudaStreamDestroy(c->stream);
         if (c->t0 != NULL) cudaEventDestroy(c->t0);
         if (c->t1 != NULL) cudaEventDestroy(c->t1);
@@ -347,6 +218,7 @@ extern "C" int gpumas_context_geometry_set(
         c->d_geometry_data = data;
         c->has_geometry = 1;
         c->n_media = geometry->n_media;
+        c->geometry_kind = geometry->kind;
         return GPUMAS_RETURN_SUCCESS;
 }
 
@@ -388,6 +260,74 @@ extern "C" int gp_config_check(const struct gpumas_context * context,
 
 static const int gp_block = 128;
 
+/* Whether events of this configuration can ever take a step: CSDA without
+ * scattering in a uniform infinite medium is the closed form of
+ * transport_with_csda (pumas.c:3220-3246). */
+static int gp_needs_stepping(const gp_context * c, const gp_config & cfg)
+{
+        return !((c->geometry_kind == GPUMAS_GEOMETRY_UNIFORM) &&
+            (cfg.energy_loss == GPUMAS_MODE_CSDA) &&
+            (cfg.scattering == GPUMAS_MODE_DISABLED));
+}
+
+/* Run a transport of n events of `io` on stream s with the context's
+ * engine. */
+static int gp_run(gp_context * c, const gp_config & cfg, const gp_io & io,
+    size_t n, uint64_t first_event, cudaStream_t s, int sync)
+{
+        int engine = c->tuning.engine;
+        if (engine == 0) engine = gp_needs_stepping(c, cfg) ? 2 : 1;
+        int rc;
+        cudaEventRecord(c->t0, s);
+        if (engine == 2) {
+                int launches = 0;
+                rc = gp_pool_transport(
+                    c, &cfg, &io, n, first_event, s, &c->tuning, &launches);
+                c->stats.launches = launches;
+        } else {
+                const unsigned int grid =
+                    (unsigned int)((n + gp_block - 1) / gp_block);
+                gp_kernel_plain<<<grid, gp_block, 0, s>>>(
+                    c->d_tables, cfg, c->d_geometry, io, n, first_event);
+                rc = gp_check(cudaGetLastError());
+                c->stats.launches = 1;
+        }
+        cudaEventRecord(c->t1, s);
+        c->stats.kernel_ms = -1.;
+        if ((rc == 0) && sync) rc = gp_check(cudaStreamSynchronize(s));
+        return rc;
+}
+
+extern "C" int gpumas_context_tuning_set(
+    struct gpumas_context * context, const struct gpumas_tuning * tuning)
+{
+        if ((context == NULL) || (tuning == NULL))
+                return GPUMAS_RETURN_VALUE_ERROR;
+        gp_context * c = (gp_context *)context;
+        if ((tuning->engine < 0) || (tuning->engine > 2) ||
+            (tuning->pool_slots < 0) || (tuning->max_inner < 0) ||
+            (tuning->batch < 0))
+                return GPUMAS_RETURN_VALUE_ERROR;
+        if (tuning->engine != 0) c->tuning.engine = tuning->engine;
+        if (tuning->pool_slots > 0) c->tuning.pool_slots = tuning->pool_slots;
+        if (tuning->max_inner > 0) c->tuning.max_inner = tuning->max_inner;
+        if (tuning->batch > 0) c->tuning.batch = tuning->batch;
+        return GPUMAS_RETURN_SUCCESS;
+}
+
+extern "C" int gpumas_context_tuning_get(
+    const struct gpumas_context * context, struct gpumas_tuning * tuning)
+{
+        if ((context == NULL) || (tuning == NULL))
+                return GPUMAS_RETURN_VALUE_ERROR;
+        const gp_context * c = (const gp_context *)context;
+        tuning->engine = c->tuning.engine;
+        tuning->pool_slots = c->tuning.pool_slots;
+        tuning->max_inner = c->tuning.max_inner;
+        tuning->batch = c->tuning.batch;
+        return GPUMAS_RETURN_SUCCESS;
+}
+
 extern "C" int gpumas_context_transport_device(struct gpumas_context * context,
     size_t n, const struct gpumas_soa * events, uint64_t first_event,
     void * stream)
@@ -400,18 +340,10 @@ extern "C" int gpumas_context_transport_device(struct gpumas_context * context,
         int rc = gp_config_check(context, c->physics, &cfg);
         if (rc != GPUMAS_RETURN_SUCCESS) return rc;
         if (n == 0) return GPUMAS_RETURN_SUCCESS;
-        cudaStream_t s = (cudaStream_t)stream;
         gp_io io;
         memset(&io, 0, sizeof(io));
         io.soa.a = *events;
-        const unsigned int grid = (unsigned int)((n + gp_block - 1) / gp_block);
-        cudaEventRecord(c->t0, s);
-        gp_kernel_plain<<<grid, gp_block, 0, s>>>(
-            c->d_tables, cfg, c->d_geometry, io, n, first_event);
-        cudaEventRecord(c->t1, s);
-        c->stats.launches = 1;
-        c->stats.kernel_ms = -1.;
-        return gp_check(cudaGetLastError());
+        return gp_run(c, cfg, io, n, first_event, (cudaStream_t)stream, 0);
 }
 
 extern "C" int gpumas_context_transport(struct gpumas_context * context,
@@ -447,12 +379,7 @@ extern "C" int gpumas_context_transport(struct gpumas_context * context,
         rc = gp_check(cudaMemcpyAsync(
             io.aos.states, states, sz_s, cudaMemcpyHostToDevice, s));
         if (rc != GPUMAS_RETURN_SUCCESS) return rc;
-        const unsigned int grid = (unsigned int)((n + gp_block - 1) / gp_block);
-        cudaEventRecord(c->t0, s);
-        gp_kernel_plain<<<grid, gp_block, 0, s>>>(
-            c->d_tables, cfg, c->d_geometry, io, n, first_event);
-        cudaEventRecord(c->t1, s);
-        rc = gp_check(cudaGetLastError());
+        rc = gp_run(c, cfg, io, n, first_event, s, 0);
         if (rc != GPUMAS_RETURN_SUCCESS) return rc;
         rc = gp_check(cudaMemcpyAsync(
             states, io.aos.states, sz_s, cudaMemcpyDeviceToHost, s));
@@ -470,7 +397,6 @@ extern "C" int gpumas_context_transport(struct gpumas_context * context,
                 rc = gp_check(cudaStreamSynchronize(s));
         float ms = 0.f;
         cudaEventElapsedTime(&ms, c->t0, c->t1);
-        c->stats.launches = 1;
         c->stats.kernel_ms = ms;
         if (rc == GPUMAS_RETURN_SUCCESS) {
                 for (size_t i = 0; i < n; i++) {

@@ -120,3 +120,25 @@ def test_gpu_edge_cases(gpu_physics):
     with pytest.raises(pg.PumasError) as err:
         ctx.transport(s0[:1])
     assert err.value.code == pg.RETURN_ACCURACY_ERROR
+
+
+@pytest.mark.parametrize("name", ["rock_slab", "stack_forward_mixed",
+                                  "stack_backward_straggled",
+                                  "water_time_limit", "plain_csda"])
+@pytest.mark.parametrize("slots,inner", [(256, 1), (1024, 3)])
+def test_pool_engine_matches_plain_engine(gpu_physics, name, slots, inner):
+    """The slot pool engine reproduces the one thread per event engine bit
+    for bit: regrouping by step kind changes the execution order of events,
+    never the draws or arithmetic of any event."""
+    import pumas_gb300 as pg
+    case = CASES[name]
+    s0 = make_states(name, n=3000, first_event=77)
+    geo = gpu_geometry(gpu_physics, case["geometry"])
+    out = []
+    for engine in (pg.ENGINE_PLAIN, pg.ENGINE_POOL):
+        ctx = gpu_context(gpu_physics, case["config"], case["seed"], geo)
+        ctx.tuning(engine=engine, pool_slots=slots, max_inner=inner, batch=4)
+        out.append(ctx.transport(s0, 77))
+    (a, ra), (b, rb) = out
+    assert a.tobytes() == b.tobytes()
+    assert ra.tobytes() == rb.tobytes()
