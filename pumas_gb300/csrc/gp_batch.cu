@@ -39,6 +39,11 @@
 
 namespace cg = cooperative_groups;
 
+/* Minimum resident blocks per SM of the pool kernels (register budget). */
+#ifndef GP_POOL_MIN_BLOCKS
+#define GP_POOL_MIN_BLOCKS 1
+#endif
+
 /* Field layout of a slot: doubles, ints and 64 bit integers, each as an
  * array of P values. */
 enum gp_slot_double {
@@ -234,7 +239,7 @@ __device__ __forceinline__ void gp_route(const gp_pool & pool, int slot,
                 gp_append(&cnt->n_ehs[parity], ehs_list, slot);
 }
 
-__global__ void __launch_bounds__(128) gp_pool_step(
+__global__ void __launch_bounds__(128, GP_POOL_MIN_BLOCKS) gp_pool_step(
     const gp_tables * __restrict__ Tp, const gpumas_geometry * __restrict__ gp,
     const gp_launch * __restrict__ X, const gp_pool pool, gp_counters * cnt,
     int * del_list, int * ehs_list, int parity)
@@ -302,7 +307,7 @@ __global__ void __launch_bounds__(128) gp_pool_step(
             e, L, event);
 }
 
-__global__ void __launch_bounds__(128) gp_pool_del(
+__global__ void __launch_bounds__(128, GP_POOL_MIN_BLOCKS) gp_pool_del(
     const gp_tables * __restrict__ Tp, const gp_launch * __restrict__ X,
     const gp_pool pool, gp_counters * cnt, const int * __restrict__ list,
     int parity)
@@ -329,7 +334,7 @@ __global__ void __launch_bounds__(128) gp_pool_del(
         }
 }
 
-__global__ void __launch_bounds__(128) gp_pool_ehs(
+__global__ void __launch_bounds__(128, GP_POOL_MIN_BLOCKS) gp_pool_ehs(
     const gp_tables * __restrict__ Tp, const gp_launch * __restrict__ X,
     const gp_pool pool, gp_counters * cnt, const int * __restrict__ list,
     int parity)

@@ -1228,7 +1228,7 @@ GPD double gp_randn(gp_event & e)
 }
 
 /* step_rotate_direction (pumas.c:7042-7095). */
-static __device__ void gp_rotate(gp_event & e, double mu)
+static __device__ __forceinline__ void gp_rotate(gp_event & e, double mu)
 {
         double * const direction = e.dir;
         const double cos_theta = 1 - 2 * mu;
@@ -1280,7 +1280,7 @@ static __device__ void gp_rotate(gp_event & e, double mu)
 /* ------------------------------------------------------------------------ */
 
 /* polar_bremsstrahlung (pumas.c:11759-11830), also for pair production. */
-static __device__ double gp_polar_bremsstrahlung(const gp_tables & T, gp_event & e,
+static __device__ __forceinline__ double gp_polar_bremsstrahlung(const gp_tables & T, gp_event & e,
     const gp_element & el, double ki, double kf)
 {
         const double m = T.mass;
@@ -1453,7 +1453,7 @@ static __device__ int gp_find_minimum(const gp_tables & T, const gp_element & el
 }
 
 /* polar_photonuclear (pumas.c:11874-11950). */
-static __device__ double gp_polar_photonuclear(const gp_tables & T, gp_event & e,
+static __device__ __forceinline__ double gp_polar_photonuclear(const gp_tables & T, gp_event & e,
     const gp_element & el, double ki, double kf)
 {
         const double M = 0.5 * (GP_PROTON_MASS + GP_NEUTRON_MASS);
@@ -1525,7 +1525,7 @@ GPD double gp_polar_ionisation(const gp_tables & T, double ki, double kf)
         return 0.5 * (1. - c);
 }
 
-static __device__ double gp_polar(const gp_tables & T, gp_event & e, int process,
+static __device__ __forceinline__ double gp_polar(const gp_tables & T, gp_event & e, int process,
     const gp_element & el, double ki, double kf)
 {
         if (process <= 1)
@@ -1541,7 +1541,7 @@ static __device__ double gp_polar(const gp_tables & T, gp_event & e, int process
 /* ------------------------------------------------------------------------ */
 
 /* dcs_ionisation_randomise (pumas.c:11185-11226). */
-static __device__ double gp_ionisation_randomise(const gp_tables & T, gp_event & e,
+static __device__ __forceinline__ double gp_ionisation_randomise(const gp_tables & T, gp_event & e,
     const gp_element & el, double K, double xlow)
 {
         const double P2 = K * (K + 2. * T.mass);
@@ -1588,7 +1588,7 @@ GPD double gp_envelope_norm(double a, double xmin, double xmax)
 
 /* del_randomise_target (pumas.c:6154-6270). Returns the process and sets the
  * target element; in backward mode also the DCS sum as *weight. */
-static __device__ void gp_del_target(const gp_tables & T, const gp_config & cfg,
+static __device__ __forceinline__ void gp_del_target(const gp_tables & T, const gp_config & cfg,
     gp_event & e, int material, double Q, int & process, int & element,
     double & weight)
 {
@@ -1685,7 +1685,7 @@ static __device__ void gp_del_target(const gp_tables & T, const gp_config & cfg,
 
 /* del_randomise_forward (pumas.c:5912-6017). Returns true if a polar angle
  * is to be sampled. */
-static __device__ bool gp_del_forward(const gp_tables & T, const gp_config & cfg,
+static __device__ __forceinline__ bool gp_del_forward(const gp_tables & T, const gp_config & cfg,
     gp_event & e, int material, int & process, int & target)
 {
         if (e.energy <= __ldg(T.Kt + material)) return false;
@@ -1769,7 +1769,7 @@ static __device__ bool gp_del_forward(const gp_tables & T, const gp_config & cfg
 
 /* del_randomise_reverse (pumas.c:6036-6093) with the power law sampling
  * of del_randomise_power_law (pumas.c:6109-6138), alpha = 2. */
-static __device__ bool gp_del_reverse(const gp_tables & T, const gp_config & cfg,
+static __device__ __forceinline__ bool gp_del_reverse(const gp_tables & T, const gp_config & cfg,
     gp_event & e, int material, int & process, int & target)
 {
         const double lnq0 = -log(T.cutoff);
@@ -1835,7 +1835,7 @@ static __device__ bool gp_del_reverse(const gp_tables & T, const gp_config & cfg
 }
 
 /* transport_do_del (pumas.c:5706-5757). */
-static __device__ void gp_do_del(const gp_tables & T, const gp_config & cfg,
+static __device__ __forceinline__ void gp_do_del(const gp_tables & T, const gp_config & cfg,
     gp_event & e, int material)
 {
         double ki, kf;
@@ -1876,7 +1876,7 @@ static __device__ void gp_do_del(const gp_tables & T, const gp_config & cfg,
 /* ------------------------------------------------------------------------ */
 /* Elastic hard scattering (transport_do_ehs, pumas.c:5768-5885).           */
 /* ------------------------------------------------------------------------ */
-static __device__ void gp_do_ehs(const gp_tables & T, const gp_config & cfg,
+static __device__ __forceinline__ void gp_do_ehs(const gp_tables & T, const gp_config & cfg,
     gp_event & e, int material)
 {
         const double kinetic = e.energy;
@@ -1977,7 +1977,7 @@ static __device__ void gp_do_ehs(const gp_tables & T, const gp_config & cfg,
 /* ------------------------------------------------------------------------ */
 
 /* step_fluctuate (pumas.c:6943-7005). */
-static __device__ void gp_fluctuate(const gp_tables & T, const gp_config & cfg,
+static __device__ __forceinline__ void gp_fluctuate(const gp_tables & T, const gp_config & cfg,
     gp_event & e, int material, double Xtot, double dX, double & kf,
     double & ratio)
 {
@@ -2036,7 +2036,7 @@ static __device__ void gp_fluctuate(const gp_tables & T, const gp_config & cfg,
 }
 
 /* transport_limit (pumas.c:5569-5696). */
-static __device__ void gp_limit(const gp_tables & T, const gp_config & cfg,
+static __device__ __forceinline__ void gp_limit(const gp_tables & T, const gp_config & cfg,
     gp_event & e, int material, double Xi, double Xf, double & grammage_max)
 {
         e.step_event = e.step_foreseen = GPUMAS_EVENT_NONE;
@@ -2132,7 +2132,7 @@ static __device__ void gp_limit(const gp_tables & T, const gp_config & cfg,
 
 /* step_transport (pumas.c:6296-6925) for uniform media without magnetic
  * field. Sets e.step_event and returns the end step medium. */
-static __device__ int gp_step(const gp_tables & T, const gp_config & cfg,
+static __device__ __forceinline__ int gp_step(const gp_tables & T, const gp_config & cfg,
     const gpumas_geometry & g, gp_event & e, int straight, int medium,
     int material, double density, double grammage_max,
     double step_max_medium)
@@ -2525,7 +2525,7 @@ enum gp_next {
 /* Prologue of transport_with_stepping, up to the first transport_limit
  * (pumas.c:5201-5271). Returns GP_NEXT_STEP or GP_NEXT_DONE (then *event is
  * the end event). */
-static __device__ int gp_stepping_begin(const gp_tables & T, const gp_config & cfg,
+static __device__ __forceinline__ int gp_stepping_begin(const gp_tables & T, const gp_config & cfg,
     const gpumas_geometry & g, gp_event & e, gp_loop & L, int & event)
 {
         L.material = gp_medium_material(g, L.medium);
@@ -2583,7 +2583,7 @@ static __device__ int gp_stepping_begin(const gp_tables & T, const gp_config & c
 
 /* Refresh of the initial conditions and limits after an event
  * (pumas.c:5479-5488). */
-static __device__ int gp_stepping_relimit(const gp_tables & T, const gp_config & cfg,
+static __device__ __forceinline__ int gp_stepping_relimit(const gp_tables & T, const gp_config & cfg,
     gp_event & e, gp_loop & L, int & event)
 {
         L.ti = e.time;
@@ -2605,7 +2605,7 @@ static __device__ int gp_stepping_relimit(const gp_tables & T, const gp_config &
 
 /* One iteration of the stepping loop up to the dispatch of its event
  * (pumas.c:5277-5329 and the medium change of 5417-5467). */
-static __device__ int gp_stepping_step(const gp_tables & T, const gp_config & cfg,
+static __device__ __forceinline__ int gp_stepping_step(const gp_tables & T, const gp_config & cfg,
     const gpumas_geometry & g, gp_event & e, gp_loop & L, int & event)
 {
         if (L.step_index > 1) {
@@ -2676,7 +2676,7 @@ static __device__ int gp_stepping_step(const gp_tables & T, const gp_config & cf
 }
 
 /* DEL of the stepping loop (pumas.c:5336-5374 and 5479-5488). */
-static __device__ int gp_stepping_del(const gp_tables & T, const gp_config & cfg,
+static __device__ __forceinline__ int gp_stepping_del(const gp_tables & T, const gp_config & cfg,
     gp_event & e, gp_loop & L, int & event)
 {
         gp_do_del(T, cfg, e, L.material);
@@ -2692,7 +2692,7 @@ static __device__ int gp_stepping_del(const gp_tables & T, const gp_config & cfg
 }
 
 /* EHS of the stepping loop (pumas.c:5393-5400 and 5479-5488). */
-static __device__ int gp_stepping_ehs(const gp_tables & T, const gp_config & cfg,
+static __device__ __forceinline__ int gp_stepping_ehs(const gp_tables & T, const gp_config & cfg,
     gp_event & e, gp_loop & L, int & event)
 {
         gp_do_ehs(T, cfg, e, L.material);
@@ -2721,7 +2721,7 @@ GPD void gp_stepping_end(const gp_config & cfg, gp_event & e)
 }
 
 /* transport_with_csda (pumas.c:4777-4949), no magnetic field. */
-static __device__ int gp_transport_csda(const gp_tables & T, const gp_config & cfg,
+static __device__ __forceinline__ int gp_transport_csda(const gp_tables & T, const gp_config & cfg,
     gp_event & e, int material, double density)
 {
         const double ki = e.energy;
@@ -2878,7 +2878,7 @@ GPD void gp_event_init(gp_event & e, uint64_t seed, uint64_t id)
  * to the start of the stepping loop. The context level checks are done on
  * the host before the launch. Returns GP_NEXT_STEP, or GP_NEXT_DONE with
  * *event set (including the whole deterministic CSDA case). */
-static __device__ int gp_transport_begin(const gp_tables & T, const gp_config & cfg,
+static __device__ __forceinline__ int gp_transport_begin(const gp_tables & T, const gp_config & cfg,
     const gpumas_geometry & g, gp_event & e, gp_loop & L, int & event,
     int & medium_in)
 {
@@ -2940,7 +2940,7 @@ static __device__ int gp_transport_begin(const gp_tables & T, const gp_config & 
 
 /* Resume the stepping loop of an event at phase `next` and run it to its
  * end (the one thread per event form). */
-static __device__ void gp_transport_run(const gp_tables & T, const gp_config & cfg,
+static __device__ __forceinline__ void gp_transport_run(const gp_tables & T, const gp_config & cfg,
     const gpumas_geometry & g, gp_event & e, gp_loop & L, int next,
     int & event)
 {
@@ -2956,7 +2956,7 @@ static __device__ void gp_transport_run(const gp_tables & T, const gp_config & c
 }
 
 /* pumas_context_transport for one event, in one thread. */
-static __device__ void gp_transport(const gp_tables & T, const gp_config & cfg,
+static __device__ __forceinline__ void gp_transport(const gp_tables & T, const gp_config & cfg,
     const gpumas_geometry & g, gp_event & e, int & event, int & medium_in,
     int & medium_out)
 {

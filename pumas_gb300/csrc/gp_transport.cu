@@ -23,7 +23,7 @@ extern "C" int gp_pool_transport(gp_context * c, const gp_config * cfg,
     const gp_tuning * tuning, int * launches);
 
 /* One thread per event, the whole transport call in one launch. */
-__global__ void __launch_bounds__(128) gp_kernel_plain(
+__global__ void __launch_bounds__(128, 1) gp_kernel_plain(
     const gp_tables * __restrict__ Tp, const gp_config cfg,
     const gpumas_geometry * __restrict__ gp, const gp_io io, size_t n,
     uint64_t first_event)
