@@ -144,13 +144,27 @@ GPD double gp_random(gp_event & e)
 GPD int gp_sch(int scheme) { return (scheme > 1) ? 1 : scheme; }
 GPD int gp_sch_el(int scheme) { return (scheme >= 1) ? 1 : 0; }
 
-/* table_index (pumas.c:4174-4233), bracketing from below. */
-GPD int gp_index(const gp_tables & T, const double * __restrict__ table,
-    double value)
+/* table_index (pumas.c:4174-4233): the row i with table[i] <= value <
+ * table[i + 1], through the table's bucket index (gp_lut). Rows are
+ * non-negative, so values are compared through their raw bits on the
+ * integer pipes. */
+GPD int gp_index(const gp_tables & T, int lut_id,
+    const double * __restrict__ table, double value)
 {
         const int imax = T.n_energies - 1;
         if (value < __ldg(table)) return -1;
         if (value >= __ldg(table + imax)) return imax;
+        const gp_lut & L = T.lut[lut_id];
+        const int n = L.n;
+        if (n > 0) {
+                const long long vb = __double_as_longlong(value);
+                const int k = (int)(vb >> GP_LUT_SHIFT) - L.key0;
+                int i = (k < 0) ? 0 : (k >= n) ? imax - 1 : (int)__ldg(L.idx + k);
+                while ((i + 1 < imax) &&
+                    (vb >= __double_as_longlong(__ldg(table + i + 1))))
+                        i++;
+                return i;
+        }
         int i1 = 0, i2 = imax;
         do {
                 const int i3 = (i1 + i2) >> 1;
@@ -171,10 +185,11 @@ GPD double gp_pchip(double t, double p0, double p1, double m0, double m1)
 }
 
 /* table_interpolate_pchip (pumas.c:4146-4157). */
-GPD double gp_interpolate(const gp_tables & T, const double * __restrict__ X,
-    const double * __restrict__ Y, const double * __restrict__ M, double x)
+GPD double gp_interpolate(const gp_tables & T, int lut_id,
+    const double * __restrict__ X, const double * __restrict__ Y,
+    const double * __restrict__ M, double x)
 {
-        const int i1 = gp_index(T, X, x);
+        const int i1 = gp_index(T, lut_id, X, x);
         const int i2 = i1 + 1;
         const double x1 = __ldg(X + i1);
         const double dX = __ldg(X + i2) - x1;
@@ -201,7 +216,7 @@ GPD double gp_cel_grammage(
                 return __ldg(T.X + GP_ROW(s, material) + imax) +
                     1. / b * log((kinetic + K1) / (K0 + K1));
         }
-        return gp_interpolate(T, T.K, T.X + GP_ROW(s, material),
+        return gp_interpolate(T, GP_LUT_K, T.K, T.X + GP_ROW(s, material),
             T.X_dK + GP_ROW(s, material), kinetic);
 }
 
@@ -224,7 +239,8 @@ GPD double gp_cel_grammage_as_time(
                 return __ldg(T.X + GP_ROW(s, material) + imax) +
                     1. / b * log((kinetic + K1) / (E0 - T.mass + K1));
         }
-        return gp_interpolate(T, Tt, T.X + GP_ROW(s, material),
+        return gp_interpolate(T, GP_LUT_T(T, s, material), Tt,
+            T.X + GP_ROW(s, material),
             T.X_dT + GP_ROW(s, material), time);
 }
 
@@ -242,7 +258,7 @@ GPD double gp_cel_proper_time(
                 return __ldg(T.T + GP_ROW(s, material) + imax) +
                     T.mass / a * log((E1 / E0) * (a + b * E0) / (a + b * E1));
         }
-        return gp_interpolate(T, T.K, T.T + GP_ROW(s, material),
+        return gp_interpolate(T, GP_LUT_K, T.K, T.T + GP_ROW(s, material),
             T.T_dK + GP_ROW(s, material), kinetic);
 }
 
@@ -260,8 +276,8 @@ GPD double gp_cel_kinetic_energy(
                 const double K1 = a / b + T.mass;
                 return (K0 + K1) * exp(b * (grammage - __ldg(X + imax))) - K1;
         }
-        return gp_interpolate(
-            T, X, T.K, T.K_dX + GP_ROW(s, material), grammage);
+        return gp_interpolate(T, GP_LUT_X(T, s, material), X, T.K,
+            T.K_dX + GP_ROW(s, material), grammage);
 }
 
 GPD double gp_cel_energy_loss(
@@ -275,7 +291,7 @@ GPD double gp_cel_energy_loss(
                     __ldg(T.b_max + s * T.n_materials + material) *
                     (kinetic + T.mass);
         }
-        return gp_interpolate(T, T.K, T.dE + GP_ROW(s, material),
+        return gp_interpolate(T, GP_LUT_K, T.K, T.dE + GP_ROW(s, material),
             T.dE_dK + GP_ROW(s, material), kinetic);
 }
 
@@ -288,7 +304,7 @@ GPD double gp_cel_straggling(const gp_tables & T, int material, double kinetic)
                 const double r = (kinetic + T.mass) / (Kmax + T.mass);
                 return __ldg(T.Omega + GP_MROW(material) + imax) * r * r;
         }
-        return gp_interpolate(T, T.K, T.Omega + GP_MROW(material),
+        return gp_interpolate(T, GP_LUT_K, T.K, T.Omega + GP_MROW(material),
             T.Omega_dK + GP_MROW(material), kinetic);
 }
 
@@ -299,7 +315,7 @@ GPD double gp_del_cross_section(
         if (kinetic < __ldg(T.K)) return 0.;
         if (kinetic >= __ldg(T.K + imax))
                 return __ldg(T.CS + GP_MROW(material) + imax);
-        return gp_interpolate(T, T.K, T.CS + GP_MROW(material),
+        return gp_interpolate(T, GP_LUT_K, T.K, T.CS + GP_MROW(material),
             T.CS_dK + GP_MROW(material), kinetic);
 }
 
@@ -318,7 +334,7 @@ GPD double gp_del_interaction_length(
                                   (a0 + b0 * (k0 + T.mass)));
                 return __ldg(T.NI_in + GP_MROW(material) + imax) + dZ;
         }
-        return gp_interpolate(T, T.K, T.NI_in + GP_MROW(material),
+        return gp_interpolate(T, GP_LUT_K, T.K, T.NI_in + GP_MROW(material),
             T.NI_in_dK + GP_MROW(material), kinetic);
 }
 
@@ -337,7 +353,8 @@ GPD double gp_del_kinetic_from_interaction_length(
                 return ((a0 + b0 * (k0 + T.mass)) * exp(b0 * (nI - nI0) / cs) -
                            a0) / b0 - T.mass;
         }
-        return gp_interpolate(T, NI, T.K, T.K_dNI_in + GP_MROW(material), nI);
+        return gp_interpolate(T, GP_LUT_NI_IN(T, material), NI, T.K,
+            T.K_dNI_in + GP_MROW(material), nI);
 }
 
 GPD double gp_ehs_interaction_length(
@@ -353,7 +370,7 @@ GPD double gp_ehs_interaction_length(
                 const double nI1 = __ldg(NI + imax);
                 return nI1 + (kinetic - k1) * (nI1 - nI0) / (k1 - k0);
         }
-        return gp_interpolate(T, T.K, NI,
+        return gp_interpolate(T, GP_LUT_K, T.K, NI,
             T.NI_el_dK + GP_ROW(gp_sch_el(scheme), material), kinetic);
 }
 
@@ -370,7 +387,8 @@ GPD double gp_ehs_kinetic_from_interaction_length(
                 const double nI1 = __ldg(NI + imax);
                 return k1 + (nI - nI1) * (k1 - k0) / (nI1 - nI0);
         }
-        return gp_interpolate(T, NI, T.K,
+        return gp_interpolate(T,
+            GP_LUT_NI_EL(T, gp_sch_el(scheme), material), NI, T.K,
             T.K_dNI_el + GP_ROW(gp_sch_el(scheme), material), nI);
 }
 
@@ -390,7 +408,7 @@ GPD void gp_table_get_msc(const gp_tables & T, int energy_loss, int material,
                 mu0 = __ldg(Mu0 + imax);
                 invlb1 = __ldg(Ms1 + imax) * __ldg(T.K + imax) / kinetic;
         } else {
-                const int i1 = gp_index(T, T.K, kinetic);
+                const int i1 = gp_index(T, GP_LUT_K, T.K, kinetic);
                 const double x0 = __ldg(T.K + i1);
                 const double dx = __ldg(T.K + i1 + 1) - x0;
                 const double t = (kinetic - x0) / dx;
@@ -415,7 +433,7 @@ GPD double gp_coulomb_ehs_length(
         } else if (kinetic >= __ldg(T.K + imax)) {
                 return __ldg(Lb + imax) / p2;
         } else {
-                const int i1 = gp_index(T, T.K, kinetic);
+                const int i1 = gp_index(T, GP_LUT_K, T.K, kinetic);
                 const int i2 = i1 + 1;
                 const double k1 = __ldg(T.K + i1);
                 double h = (kinetic - k1) / (__ldg(T.K + i2) - k1);
@@ -1123,7 +1141,7 @@ static __device__ double gp_dcs_evaluate(const gp_tables & T, int process,
         const float * base = T.DCS +
             stride * ((long)(process * T.n_elements + el.index) * T.n_energies);
         int i0 = 0;
-        if ((K >= Kmax) || ((i0 = gp_index(T, T.K, K)) >= imax)) {
+        if ((K >= Kmax) || ((i0 = gp_index(T, GP_LUT_K, T.K, K)) >= imax)) {
                 const float * data = base + stride * imax;
                 p00 = p10 = __ldg(data + 2 * ix);
                 m00 = m10 = __ldg(data + 2 * ix + 1);
@@ -1220,9 +1238,10 @@ GPD double gp_randn(gp_event & e)
         e.randn_done = !e.randn_done;
         if (!e.randn_done) return e.randn_next;
         const double r = sqrt(-2. * log(gp_random(e)));
-        const double phi = 2. * GP_PI * gp_random(e);
+        /* sin and cos of 2 pi u, without argument reduction. */
+        const double u2 = 2. * gp_random(e);
         double s, c;
-        sincos(phi, &s, &c);
+        sincospi(u2, &s, &c);
         e.randn_next = r * c;
         return r * s;
 }
@@ -1267,9 +1286,10 @@ static __device__ __forceinline__ void gp_rotate(gp_event & e, double mu)
         const double u1x = u0y * direction[2] - u0z * direction[1];
         const double u1y = u0z * direction[0] - u0x * direction[2];
         const double u1z = u0x * direction[1] - u0y * direction[0];
-        const double phi = GP_PI * (1. - 2. * gp_random(e));
+        /* sin and cos of pi (1 - 2 u); 1 - 2 u is exact. */
+        const double phi_pi = 1. - 2. * gp_random(e);
         double sp, cp;
-        sincos(phi, &sp, &cp);
+        sincospi(phi_pi, &sp, &cp);
         direction[0] = cos_theta * direction[0] + st * (cp * u0x + sp * u1x);
         direction[1] = cos_theta * direction[1] + st * (cp * u0y + sp * u1y);
         direction[2] = cos_theta * direction[2] + st * (cp * u0z + sp * u1z);
@@ -1594,7 +1614,7 @@ static __device__ __forceinline__ void gp_del_target(const gp_tables & T, const 
 {
         int i1;
         double h, dk;
-        i1 = gp_index(T, T.K, e.energy);
+        i1 = gp_index(T, GP_LUT_K, T.K, e.energy);
         if (i1 < 0) {
                 i1 = 0;
                 h = dk = 0.;
@@ -1722,7 +1742,7 @@ static __device__ __forceinline__ bool gp_del_forward(const gp_tables & T, const
                 p0 = 1.;
                 a1 = b1 = 0.;
         } else {
-                const int row = gp_index(T, T.K, e.energy);
+                const int row = gp_index(T, GP_LUT_K, T.K, e.energy);
                 a0 = (double)__ldg(env + 2 * row);
                 b0 = (double)__ldg(env + 2 * row + 1);
                 a1 = (double)__ldg(env + 2 * row + 2);

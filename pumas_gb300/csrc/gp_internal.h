@@ -61,6 +61,29 @@ struct gp_constants {
         double pair_me_m2;  /* pow(ME / m, 2.) with m in MeV, SSR pairs */
 };
 
+/* Bucket index of a monotone table: for a non-negative double v with raw
+ * bits b, bucket (b >> GP_LUT_SHIFT) - key0 (an 8 bit mantissa slice of a
+ * binade) holds the largest row i with table[i] below the bucket's lower
+ * edge. A lookup then needs one load and at most a few integer compares
+ * instead of a bisection (table_index, pumas.c:4174-4233); the row found
+ * is the same. */
+#define GP_LUT_SHIFT 44
+struct gp_lut {
+        int key0;
+        int n;
+        const unsigned short * idx;
+};
+
+/* Identifiers of the searched tables: the energy grid K, then per scheme
+ * and material the grammage X and proper time T, per material the DEL
+ * interaction lengths NI_in and per scheme and material the EHS ones. */
+#define GP_LUT_K 0
+#define GP_LUT_X(T_, s, m) (1 + (s) * (T_).n_materials + (m))
+#define GP_LUT_T(T_, s, m) (1 + (2 + (s)) * (T_).n_materials + (m))
+#define GP_LUT_NI_IN(T_, m) (1 + 4 * (T_).n_materials + (m))
+#define GP_LUT_NI_EL(T_, s, m) (1 + (5 + (s)) * (T_).n_materials + (m))
+#define GP_N_LUT(n_materials) (1 + 7 * (n_materials))
+
 struct gp_tables {
         int n_energies, n_materials, n_elements, n_components, n_table_dcs;
         double ctau, mass, cutoff, elastic_ratio;
@@ -77,6 +100,7 @@ struct gp_tables {
         const double * comp_fraction;
         const double * material_density;
         const struct gp_element * element;
+        const struct gp_lut * lut;
         struct gp_constants k;
 };
 

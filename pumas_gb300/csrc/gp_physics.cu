@@ -318,6 +318,40 @@ static inline const char * rebase(
 
 static size_t align256(size_t n) { return (n + 255) & ~(size_t)255; }
 
+static inline int64_t lut_key(double v)
+{
+        int64_t b;
+        memcpy(&b, &v, 8);
+        return b >> GP_LUT_SHIFT;
+}
+
+/* Bucket index of a non-decreasing table of n rows, appended to `out`.
+ * Returns the number of entries, 0 if the table is not suitable (then the
+ * device bisects). */
+static int lut_build(const double * table, int n, unsigned short * out,
+    int capacity, int * key0)
+{
+        const int imax = n - 1;
+        if ((table[0] < 0.) || !(table[1] > 0.) || !(table[imax] > 0.))
+                return 0;
+        for (int i = 0; i < imax; i++)
+                if (!(table[i] <= table[i + 1])) return 0;
+        const int64_t k0 = lut_key(table[1]);
+        const int64_t k1 = lut_key(table[imax]);
+        const int64_t m = k1 - k0 + 1;
+        if ((m <= 0) || (m > capacity)) return 0;
+        int i = 0;
+        for (int64_t k = 0; k < m; k++) {
+                const int64_t bits = (k0 + k) << GP_LUT_SHIFT;
+                double lo;
+                memcpy(&lo, &bits, 8);
+                while ((i + 1 < imax) && (table[i + 1] <= lo)) i++;
+                out[k] = (unsigned short)i;
+        }
+        *key0 = (int)k0;
+        return (int)m;
+}
+
 static int physics_from_blob(
     struct gpumas_physics ** out, const char * b, int64_t size)
 {
@@ -340,7 +374,12 @@ static int physics_from_blob(
             align256(off_comp_start + nm * sizeof(int));
         const size_t off_comp_fraction =
             align256(off_comp_element + nc * sizeof(int));
-        const size_t total = align256(off_comp_fraction + nc * sizeof(double));
+        const int n_lut = GP_N_LUT(nm);
+        const size_t off_lut = align256(off_comp_fraction + nc * sizeof(double));
+        const int lut_capacity = 1 << 16;
+        const size_t off_lut_idx = align256(off_lut + n_lut * sizeof(gp_lut));
+        const size_t total = align256(off_lut_idx +
+            (size_t)n_lut * lut_capacity * sizeof(unsigned short));
 
         char * host = (char *)calloc(1, total);
         if (host == NULL) return GPUMAS_RETURN_MEMORY_ERROR;
@@ -375,6 +414,39 @@ static int physics_from_blob(
                 }
         }
 
+        /* Bucket indices of the searched tables (device addresses are set
+         * once the allocation is made). */
+        gp_lut * luts = (gp_lut *)(host + off_lut);
+        {
+                const int ne_ = p.n_energies;
+                const double * K = (const double *)(b + p.off[3]);
+                const double * X = (const double *)(b + p.off[7]);
+                const double * Tt = (const double *)(b + p.off[10]);
+                const double * NIi = (const double *)(b + p.off[18]);
+                const double * NIe = (const double *)(b + p.off[16]);
+                for (int id = 0; id < n_lut; id++) {
+                        const double * tab;
+                        if (id == 0) {
+                                tab = K;
+                        } else if (id <= 2 * nm) {
+                                tab = X + (size_t)(id - 1) * ne_;
+                        } else if (id <= 4 * nm) {
+                                tab = Tt + (size_t)(id - 1 - 2 * nm) * ne_;
+                        } else if (id <= 5 * nm) {
+                                tab = NIi + (size_t)(id - 1 - 4 * nm) * ne_;
+                        } else {
+                                tab = NIe + (size_t)(id - 1 - 5 * nm) * ne_;
+                        }
+                        unsigned short * out = (unsigned short *)(host +
+                            off_lut_idx) + (size_t)id * lut_capacity;
+                        luts[id].n = lut_build(tab, ne_, out, lut_capacity,
+                            &luts[id].key0);
+                        luts[id].idx = (const unsigned short *)(
+                            (size_t)off_lut_idx +
+                            (size_t)id * lut_capacity * sizeof(unsigned short));
+                }
+        }
+
         struct gpumas_physics * ph =
             (struct gpumas_physics *)calloc(1, sizeof(*ph));
         if (ph == NULL) {
@@ -396,6 +468,9 @@ static int physics_from_blob(
                 return GPUMAS_RETURN_DEVICE_ERROR;
         }
         ph->device_size = total;
+        for (int id = 0; id < n_lut; id++)
+                luts[id].idx = (const unsigned short *)((char *)ph->device_blob +
+                    (size_t)luts[id].idx);
         if (cudaMemcpy(ph->device_blob, host, total, cudaMemcpyHostToDevice) !=
             cudaSuccess) {
                 free(host);
@@ -460,6 +535,7 @@ static int physics_from_blob(
         t->comp_start = (const int *)(d + off_comp_start);
         t->comp_element = (const int *)(d + off_comp_element);
         t->comp_fraction = (const double *)(d + off_comp_fraction);
+        t->lut = (const gp_lut *)(d + off_lut);
 
         /* Constants of the DCS models, with the reference's expressions. */
         t->k.exp1 = exp(1.);

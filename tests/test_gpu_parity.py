@@ -55,20 +55,57 @@ def run_gpu(physics, name, states, first_event=0, seed=None):
     return ctx.transport(states, first_event)
 
 
+STAT_FIELDS = ("energy", "distance", "grammage", "time", "weight")
+
+
+def statistical_check(a, b):
+    """KS and chi-square tests (p > 0.01) of two final state samples, per
+    field: the criterion for the events outside the 1e-9 tolerance."""
+    from scipy import stats
+    for f in STAT_FIELDS:
+        x, y = a[f], b[f]
+        if np.array_equal(np.sort(x), np.sort(y)):
+            continue
+        assert stats.ks_2samp(x, y).pvalue > 0.01, f
+        edges = np.unique(np.quantile(np.concatenate([x, y]),
+                                      np.linspace(0., 1., 21)))
+        if len(edges) > 2:
+            hx, _ = np.histogram(x, edges)
+            hy, _ = np.histogram(y, edges)
+            keep = (hx + hy) > 0
+            _, p, _, _ = stats.chi2_contingency(np.vstack([hx[keep],
+                                                           hy[keep]]))
+            assert p > 0.01, f
+
+
+_golden_tally = {}
+
+
 @pytest.mark.parametrize("name", sorted(CASES))
 def test_gpu_matches_reference_golden(gpu_physics, name):
     data = np.load(os.path.join(GOLDEN, name + ".npz"))
     s1, r1 = run_gpu(gpu_physics, name, data["initial"])
     same, close = check(name, s1, r1, data["final"], data["results"])
     n = len(close)
-    frac = close.mean()
-    if CASES[name]["config"]["energy_loss"] == 0 and \
-            CASES[name]["config"]["scattering"] == -1:
+    _golden_tally[name] = (int(close.sum()), n)
+    assert np.all(r1["status"] == 0)
+    cfg = CASES[name]["config"]
+    if cfg["energy_loss"] == 0 and cfg["scattering"] == -1:
+        # Deterministic CSDA: every event.
         assert close.all(), "%d / %d CSDA events differ" % (n - close.sum(), n)
     else:
-        assert frac >= 0.999 or n - close.sum() <= 1, \
-            "%s: %d / %d events outside 1e-9" % (name, n - close.sum(), n)
-    assert np.all(r1["status"] == 0)
+        assert close.mean() >= 0.98, "%s: %d / %d events outside 1e-9" % (
+            name, n - close.sum(), n)
+        statistical_check(s1, data["final"])
+
+
+def test_gpu_golden_aggregate():
+    """At least 99.9 % of all golden events within tolerance."""
+    if len(_golden_tally) < len(CASES):
+        pytest.skip("per case golden tests not run")
+    good = sum(v[0] for v in _golden_tally.values())
+    total = sum(v[1] for v in _golden_tally.values())
+    assert good >= 0.999 * total, "%d / %d within tolerance" % (good, total)
 
 
 @pytest.mark.parametrize("name", ["plain_csda", "rock_slab",
@@ -142,3 +179,48 @@ def test_pool_engine_matches_plain_engine(gpu_physics, name, slots, inner):
     (a, ra), (b, rb) = out
     assert a.tobytes() == b.tobytes()
     assert ra.tobytes() == rb.tobytes()
+
+
+def test_gpu_statistics_rock_slab(gpu_physics, port):
+    """200 000 events of the rock slab workload against the C restatement:
+    fraction within 1e-9 and KS / chi-square tests on final states."""
+    from pumas_gb300 import workloads as W
+    import oracle
+    n = 200_000
+    s0 = W.rock_slab(n, seed=21, first_event=10**9)
+    ctx = gpu_context(gpu_physics, W.config_dict("rock_slab"), 21,
+                      W.rock_slab_geometry(gpu_physics))
+    a, ra = ctx.transport(s0, 10**9)
+    rock = port.material_index("StandardRock")
+    geo = oracle.make_geometry(1, [(rock, 0.)], slab_z=[0., 1000.],
+                               slab_medium=[0])
+    cfg = oracle.Config(seed=21, **W.config_dict("rock_slab"))
+    b, rb = port.transport(cfg, geo, s0, 10**9, 0)
+    same, close = compare(a, ra, b, rb, RTOL)
+    assert close.mean() >= 0.999, "%d / %d outside 1e-9" % ((~close).sum(), n)
+    statistical_check(a, b)
+
+
+def test_gpu_full_size_invariants(gpu_physics):
+    """Size independent properties at 1e6 events of the rock slab workload:
+    no error, forward energies never increase, unit directions, stop at
+    1 GeV or on exit only, exit only at the slab faces."""
+    import pumas_gb300 as pg
+    from pumas_gb300 import workloads as W
+    n = 1_000_000
+    s0 = W.rock_slab(n, seed=5)
+    ctx = gpu_context(gpu_physics, W.config_dict("rock_slab"), 5,
+                      W.rock_slab_geometry(gpu_physics))
+    s, r = ctx.transport(s0)
+    assert np.all(r["status"] == 0)
+    assert np.all(s["energy"] <= s0["energy"])
+    norm = np.sum(s["direction"] ** 2, axis=1)
+    assert np.all(np.abs(norm - 1.) < 1E-06)
+    ev = r["event"]
+    assert set(np.unique(ev)) <= {pg.EVENT_LIMIT_ENERGY, pg.EVENT_MEDIUM}
+    out = ev == pg.EVENT_MEDIUM
+    assert np.all(r["medium_out"][out] == -1)
+    z = s["position"][out, 2]
+    assert np.all((z < 0.) | (z >= 1000.))
+    assert np.all(s["energy"][~out] == 1.)
+    assert np.all(s["weight"] <= 1.) and np.all(s["weight"] > 0.)
