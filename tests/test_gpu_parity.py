@@ -222,5 +222,8 @@ def test_gpu_full_size_invariants(gpu_physics):
     assert np.all(r["medium_out"][out] == -1)
     z = s["position"][out, 2]
     assert np.all((z < 0.) | (z >= 1000.))
-    assert np.all(s["energy"][~out] == 1.)
+    # Stops at the energy limit end at 1 GeV, or below it when a discrete
+    # loss crossed the limit (transport_limit, pumas.c:5586-5592).
+    assert np.all(s["energy"][~out] <= 1.)
+    assert np.mean(s["energy"][~out] == 1.) > 0.9
     assert np.all(s["weight"] <= 1.) and np.all(s["weight"] > 0.)
