@@ -272,6 +272,32 @@ int gpumas_context_tuning_set(
 int gpumas_context_tuning_get(
     const struct gpumas_context * context, struct gpumas_tuning * tuning);
 
+/**
+ * Allocation free form of gpumas_context_transport_device. It has no
+ * counterpart in the reference: it exists for callers that cannot allocate
+ * device memory while they transport (a host whose allocator owns the GPU
+ * memory, a plugin whose framework forbids allocation on its hot path).
+ *
+ * The slot pool lives in one static device array of the library, sized for
+ * GPUMAS_STATIC_SLOTS slots (about 10 MB), which every GPU that loads the
+ * library holds until the process exits. `pool_slots` must be a multiple of
+ * 128 in [128, GPUMAS_STATIC_SLOTS], or 0 for the maximum; other values
+ * return GPUMAS_RETURN_VALUE_ERROR. The call makes no cudaMalloc or
+ * cudaFree; events, of any number n, stream through the slots as in the
+ * pool engine and give the same results.
+ *
+ * The first call on a device looks up the device address of the array
+ * (cudaGetSymbolAddress with that device current): make it before any
+ * stream capture. Every call shares the array and clears it at its start,
+ * so calls that overlap on the GPU (other streams or threads) race and must
+ * be serialised by the caller. The call synchronises `stream` before it
+ * returns.
+ */
+#define GPUMAS_STATIC_SLOTS 32768
+int gpumas_context_transport_device_static(struct gpumas_context * context,
+    size_t n, const struct gpumas_soa * events, uint64_t first_event,
+    int pool_slots, void * stream);
+
 /** Engine statistics of the last transport call on this context. */
 struct gpumas_stats {
         /** Kernel launches of the call. */

@@ -514,3 +514,149 @@ extern "C" int gp_pool_transport(gp_context * c, const gp_config * cfg_,
         if (launches != NULL) *launches = n_launch;
         return 0;
 }
+
+/* ------------------------------------------------------------------------ */
+/* Allocation free transport.                                               */
+/*                                                                          */
+/* Some callers cannot allocate device memory while they transport: a host  */
+/* program whose allocator owns all of the GPU memory and hands out fixed   */
+/* arenas, a plugin embedded in a framework that forbids allocation on its  */
+/* hot path, or code that must not pay (or fail on) a cudaMalloc in the     */
+/* middle of a run. For them the slot pool of the pool engine also exists   */
+/* as one static device array, reserved when the library is loaded on a     */
+/* device and kept until the process exits.                                 */
+/* ------------------------------------------------------------------------ */
+
+/* Largest pool of the allocation free entry point, in event slots
+ * (GPUMAS_STATIC_SLOTS of gpumas.h). */
+#define GP_STATIC_SLOTS GPUMAS_STATIC_SLOTS
+
+/* Bytes of the static pool: slot fields, the DEL / EHS lists of both
+ * parities, the counters and the launch descriptor. */
+#define GP_STATIC_BYTES                                                       \
+        ((size_t)GP_STATIC_SLOTS *                                            \
+                (SD_N * sizeof(double) + SU_N * sizeof(uint64_t) +            \
+                    SI_N * sizeof(int) + 4 * sizeof(int)) +                   \
+            512 + sizeof(gp_launch))
+
+static __device__ __align__(256) unsigned char gp_static_pool[GP_STATIC_BYTES];
+
+/* Device address of gp_static_pool on each device, found once per device
+ * with that device current (a host side use of the symbol itself is not a
+ * device address). */
+#define GP_STATIC_DEVICES 64
+static void * gp_static_address[GP_STATIC_DEVICES];
+
+static int gp_static_setup(int device, void ** address)
+{
+        if ((device < 0) || (device >= GP_STATIC_DEVICES))
+                return GPUMAS_RETURN_DEVICE_ERROR;
+        if (gp_static_address[device] == NULL) {
+                void * ptr = NULL;
+                if (cudaGetSymbolAddress(&ptr, gp_static_pool) != cudaSuccess)
+                        return GPUMAS_RETURN_DEVICE_ERROR;
+                gp_static_address[device] = ptr;
+        }
+        *address = gp_static_address[device];
+        return GPUMAS_RETURN_SUCCESS;
+}
+
+extern "C" int gp_config_check(const struct gpumas_context * context,
+    const struct gpumas_physics * physics, gp_config * cfg);
+
+extern "C" int gpumas_context_transport_device_static(
+    struct gpumas_context * context, size_t n,
+    const struct gpumas_soa * events, uint64_t first_event, int pool_slots,
+    void * stream)
+{
+        if ((context == NULL) || (events == NULL))
+                return GPUMAS_RETURN_VALUE_ERROR;
+        if (pool_slots == 0) pool_slots = GP_STATIC_SLOTS;
+        if ((pool_slots < 128) || (pool_slots > GP_STATIC_SLOTS) ||
+            (pool_slots % 128 != 0))
+                return GPUMAS_RETURN_VALUE_ERROR;
+        gp_context * c = (gp_context *)context;
+        if (!c->has_geometry) return GPUMAS_RETURN_MEDIUM_ERROR;
+        gp_config cfg;
+        int rc = gp_config_check(context, c->physics, &cfg);
+        if (rc != GPUMAS_RETURN_SUCCESS) return rc;
+        if (n == 0) return GPUMAS_RETURN_SUCCESS;
+
+        int device = 0;
+        if (cudaGetDevice(&device) != cudaSuccess)
+                return GPUMAS_RETURN_DEVICE_ERROR;
+        void * base = NULL;
+        rc = gp_static_setup(device, &base);
+        if (rc != GPUMAS_RETURN_SUCCESS) return rc;
+
+        /* Carve the static array: the layout of the pool engine for P
+         * slots, followed by the counters and the launch descriptor. */
+        const int P = pool_slots;
+        char * p = (char *)base;
+        gp_pool pool;
+        pool.d = (double *)p;
+        p += (size_t)SD_N * P * sizeof(double);
+        pool.u = (uint64_t *)p;
+        p += (size_t)SU_N * P * sizeof(uint64_t);
+        pool.i = (int *)p;
+        p += (size_t)SI_N * P * sizeof(int);
+        int * lists = (int *)p;
+        p += (size_t)4 * P * sizeof(int);
+        p = (char *)(((size_t)p + 255) & ~(size_t)255);
+        gp_counters * counters = (gp_counters *)p;
+        gp_launch * launch = (gp_launch *)(p + 256);
+        pool.P = P;
+
+        cudaStream_t s = (cudaStream_t)stream;
+        /* The array keeps the previous call's contents: empty every slot
+         * and zero the counters and list lengths. */
+        rc = gp_check(cudaMemsetAsync(pool.i + (size_t)SI_PHASE * P, 0,
+            (size_t)P * sizeof(int), s));
+        if (rc == GPUMAS_RETURN_SUCCESS)
+                rc = gp_check(cudaMemsetAsync(counters, 0,
+                    sizeof(gp_counters), s));
+        gp_launch h;
+        memset(&h, 0, sizeof(h));
+        h.cfg = cfg;
+        memset(&h.io, 0, sizeof(h.io));
+        h.io.soa.a = *events;
+        h.n = n;
+        h.first_event = first_event;
+        h.max_inner = (c->tuning.max_inner > 0) ? c->tuning.max_inner : 1;
+        if (rc == GPUMAS_RETURN_SUCCESS)
+                rc = gp_check(cudaMemcpyAsync(launch, &h, sizeof(h),
+                    cudaMemcpyHostToDevice, s));
+        if (rc == GPUMAS_RETURN_SUCCESS)
+                rc = gp_check(cudaStreamSynchronize(s));
+        if (rc != GPUMAS_RETURN_SUCCESS) return rc;
+
+        const int block = 128;
+        const unsigned int grid = (P + block - 1) / block;
+        const unsigned int grid2 = (grid + 3) / 4;
+        const int batch = 16;
+        for (long it = 0;; it++) {
+                for (int k = 0; k < batch; k++) {
+                        const int parity = k & 1;
+                        int * del_list = lists + (size_t)parity * P;
+                        int * ehs_list = lists + (size_t)(2 + parity) * P;
+                        gp_pool_step<<<grid, block, 0, s>>>(c->d_tables,
+                            c->d_geometry, launch, pool, counters, del_list,
+                            ehs_list, parity);
+                        gp_pool_del<<<grid2, block, 0, s>>>(c->d_tables,
+                            launch, pool, counters, del_list, parity);
+                        gp_pool_ehs<<<grid2, block, 0, s>>>(c->d_tables,
+                            launch, pool, counters, ehs_list, parity);
+                }
+                rc = gp_check(cudaGetLastError());
+                gp_counters hc;
+                if (rc == GPUMAS_RETURN_SUCCESS)
+                        rc = gp_check(cudaMemcpyAsync(&hc, counters,
+                            sizeof(hc), cudaMemcpyDeviceToHost, s));
+                if (rc == GPUMAS_RETURN_SUCCESS)
+                        rc = gp_check(cudaStreamSynchronize(s));
+                if (rc != GPUMAS_RETURN_SUCCESS) return rc;
+                if ((hc.cursor >= n) && (hc.active == 0)) break;
+                if (it > (1L << 40)) return GPUMAS_RETURN_INTERNAL_ERROR;
+        }
+        return GPUMAS_RETURN_SUCCESS;
+}
