@@ -199,6 +199,26 @@ GPD double gp_interpolate(const gp_tables & T, int lut_id,
         return gp_pchip(t, __ldg(Y + i1), __ldg(Y + i2), m1, m2);
 }
 
+/* Baked cubic Hermite interpolant (gp_coef, gp_node): the same rows and
+ * coefficients as table_interpolate_pchip (pumas.c:4146-4157). */
+GPD double gp_baked_row(const gp_tables & T, int grid, int cid, int i,
+    double x)
+{
+        const size_t ne = (size_t)T.n_energies;
+        const double2 nd = __ldg((const double2 *)(T.node + grid * ne + i));
+        const double t = (x - nd.x) * nd.y;
+        const double2 * c = (const double2 *)(T.coef + cid * ne + i);
+        const double2 c01 = __ldg(c);
+        const double2 c23 = __ldg(c + 1);
+        return c01.x + t * (c01.y + t * (c23.x + t * c23.y));
+}
+
+GPD double gp_baked(const gp_tables & T, int grid,
+    const double * __restrict__ gx, int cid, double x)
+{
+        return gp_baked_row(T, grid, cid, gp_index(T, grid, gx, x), x);
+}
+
 #define GP_ROW(s, m) ((long)((s) * T.n_materials + (m)) * T.n_energies)
 #define GP_MROW(m) ((long)(m) * T.n_energies)
 
@@ -216,8 +236,8 @@ GPD double gp_cel_grammage(
                 return __ldg(T.X + GP_ROW(s, material) + imax) +
                     1. / b * log((kinetic + K1) / (K0 + K1));
         }
-        return gp_interpolate(T, GP_LUT_K, T.K, T.X + GP_ROW(s, material),
-            T.X_dK + GP_ROW(s, material), kinetic);
+        return gp_baked(T, GP_LUT_K, T.K, GP_C_X(T.n_materials, s, material),
+            kinetic);
 }
 
 GPD double gp_cel_grammage_as_time(
@@ -239,9 +259,8 @@ GPD double gp_cel_grammage_as_time(
                 return __ldg(T.X + GP_ROW(s, material) + imax) +
                     1. / b * log((kinetic + K1) / (E0 - T.mass + K1));
         }
-        return gp_interpolate(T, GP_LUT_T(T, s, material), Tt,
-            T.X + GP_ROW(s, material),
-            T.X_dT + GP_ROW(s, material), time);
+        return gp_baked(T, GP_LUT_T(T, s, material), Tt,
+            GP_C_X_OF_T(T.n_materials, s, material), time);
 }
 
 GPD double gp_cel_proper_time(
@@ -258,8 +277,8 @@ GPD double gp_cel_proper_time(
                 return __ldg(T.T + GP_ROW(s, material) + imax) +
                     T.mass / a * log((E1 / E0) * (a + b * E0) / (a + b * E1));
         }
-        return gp_interpolate(T, GP_LUT_K, T.K, T.T + GP_ROW(s, material),
-            T.T_dK + GP_ROW(s, material), kinetic);
+        return gp_baked(T, GP_LUT_K, T.K, GP_C_T(T.n_materials, s, material),
+            kinetic);
 }
 
 GPD double gp_cel_kinetic_energy(
@@ -276,8 +295,8 @@ GPD double gp_cel_kinetic_energy(
                 const double K1 = a / b + T.mass;
                 return (K0 + K1) * exp(b * (grammage - __ldg(X + imax))) - K1;
         }
-        return gp_interpolate(T, GP_LUT_X(T, s, material), X, T.K,
-            T.K_dX + GP_ROW(s, material), grammage);
+        return gp_baked(T, GP_LUT_X(T, s, material), X,
+            GP_C_K_OF_X(T.n_materials, s, material), grammage);
 }
 
 GPD double gp_cel_energy_loss(
@@ -291,8 +310,8 @@ GPD double gp_cel_energy_loss(
                     __ldg(T.b_max + s * T.n_materials + material) *
                     (kinetic + T.mass);
         }
-        return gp_interpolate(T, GP_LUT_K, T.K, T.dE + GP_ROW(s, material),
-            T.dE_dK + GP_ROW(s, material), kinetic);
+        return gp_baked(T, GP_LUT_K, T.K,
+            GP_C_DE(T.n_materials, s, material), kinetic);
 }
 
 GPD double gp_cel_straggling(const gp_tables & T, int material, double kinetic)
@@ -304,8 +323,8 @@ GPD double gp_cel_straggling(const gp_tables & T, int material, double kinetic)
                 const double r = (kinetic + T.mass) / (Kmax + T.mass);
                 return __ldg(T.Omega + GP_MROW(material) + imax) * r * r;
         }
-        return gp_interpolate(T, GP_LUT_K, T.K, T.Omega + GP_MROW(material),
-            T.Omega_dK + GP_MROW(material), kinetic);
+        return gp_baked(T, GP_LUT_K, T.K, GP_C_OMEGA(T.n_materials, material),
+            kinetic);
 }
 
 GPD double gp_del_cross_section(
@@ -315,8 +334,8 @@ GPD double gp_del_cross_section(
         if (kinetic < __ldg(T.K)) return 0.;
         if (kinetic >= __ldg(T.K + imax))
                 return __ldg(T.CS + GP_MROW(material) + imax);
-        return gp_interpolate(T, GP_LUT_K, T.K, T.CS + GP_MROW(material),
-            T.CS_dK + GP_MROW(material), kinetic);
+        return gp_baked(T, GP_LUT_K, T.K, GP_C_CS(T.n_materials, material),
+            kinetic);
 }
 
 GPD double gp_del_interaction_length(
@@ -334,8 +353,8 @@ GPD double gp_del_interaction_length(
                                   (a0 + b0 * (k0 + T.mass)));
                 return __ldg(T.NI_in + GP_MROW(material) + imax) + dZ;
         }
-        return gp_interpolate(T, GP_LUT_K, T.K, T.NI_in + GP_MROW(material),
-            T.NI_in_dK + GP_MROW(material), kinetic);
+        return gp_baked(T, GP_LUT_K, T.K, GP_C_NI_IN(T.n_materials, material),
+            kinetic);
 }
 
 GPD double gp_del_kinetic_from_interaction_length(
@@ -353,8 +372,8 @@ GPD double gp_del_kinetic_from_interaction_length(
                 return ((a0 + b0 * (k0 + T.mass)) * exp(b0 * (nI - nI0) / cs) -
                            a0) / b0 - T.mass;
         }
-        return gp_interpolate(T, GP_LUT_NI_IN(T, material), NI, T.K,
-            T.K_dNI_in + GP_MROW(material), nI);
+        return gp_baked(T, GP_LUT_NI_IN(T, material), NI,
+            GP_C_K_OF_NI_IN(T.n_materials, material), nI);
 }
 
 GPD double gp_ehs_interaction_length(
@@ -370,8 +389,8 @@ GPD double gp_ehs_interaction_length(
                 const double nI1 = __ldg(NI + imax);
                 return nI1 + (kinetic - k1) * (nI1 - nI0) / (k1 - k0);
         }
-        return gp_interpolate(T, GP_LUT_K, T.K, NI,
-            T.NI_el_dK + GP_ROW(gp_sch_el(scheme), material), kinetic);
+        return gp_baked(T, GP_LUT_K, T.K,
+            GP_C_NI_EL(T.n_materials, gp_sch_el(scheme), material), kinetic);
 }
 
 GPD double gp_ehs_kinetic_from_interaction_length(
@@ -387,9 +406,8 @@ GPD double gp_ehs_kinetic_from_interaction_length(
                 const double nI1 = __ldg(NI + imax);
                 return k1 + (nI - nI1) * (k1 - k0) / (nI1 - nI0);
         }
-        return gp_interpolate(T,
-            GP_LUT_NI_EL(T, gp_sch_el(scheme), material), NI, T.K,
-            T.K_dNI_el + GP_ROW(gp_sch_el(scheme), material), nI);
+        return gp_baked(T, GP_LUT_NI_EL(T, gp_sch_el(scheme), material), NI,
+            GP_C_K_OF_NI_EL(T.n_materials, gp_sch_el(scheme), material), nI);
 }
 
 /* table_get_msc (pumas.c:4077-4111). */
@@ -409,15 +427,10 @@ GPD void gp_table_get_msc(const gp_tables & T, int energy_loss, int material,
                 invlb1 = __ldg(Ms1 + imax) * __ldg(T.K + imax) / kinetic;
         } else {
                 const int i1 = gp_index(T, GP_LUT_K, T.K, kinetic);
-                const double x0 = __ldg(T.K + i1);
-                const double dx = __ldg(T.K + i1 + 1) - x0;
-                const double t = (kinetic - x0) / dx;
-                const double * m0 = T.Mu0_dK + GP_MROW(material) + i1;
-                const double * m1 = T.Ms1_dK + GP_ROW(s + 1, material) + i1;
-                mu0 = gp_pchip(t, __ldg(Mu0 + i1), __ldg(Mu0 + i1 + 1),
-                    __ldg(m0) * dx, __ldg(m0 + 1) * dx);
-                invlb1 = gp_pchip(t, __ldg(Ms1 + i1), __ldg(Ms1 + i1 + 1),
-                    __ldg(m1) * dx, __ldg(m1 + 1) * dx);
+                mu0 = gp_baked_row(T, GP_LUT_K, GP_C_MU0(T.n_materials,
+                    material), i1, kinetic);
+                invlb1 = gp_baked_row(T, GP_LUT_K, GP_C_MS1(T.n_materials,
+                    s + 1, material), i1, kinetic);
         }
 }
 

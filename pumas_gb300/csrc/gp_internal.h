@@ -84,6 +84,39 @@ struct gp_lut {
 #define GP_LUT_NI_EL(T_, s, m) (1 + (5 + (s)) * (T_).n_materials + (m))
 #define GP_N_LUT(n_materials) (1 + 7 * (n_materials))
 
+/* Baked cubic Hermite interpolants. For a table (grid x, values y,
+ * derivatives m) the reference computes, at each lookup in row i
+ * (table_interpolate_pchip and math_pchip_interpolate, pumas.c:4118-4157),
+ * dx = x[i+1] - x[i], m0 = m[i] dx, m1 = m[i+1] dx (m0 in row 0), then
+ * c2 = -3 (y[i] - y[i+1]) - 2 m0 - m1 and c3 = 2 (y[i] - y[i+1]) + m0 + m1.
+ * These are evaluated once on the host with the same expressions and
+ * stored per row; a lookup is then p0 + t (m0 + t (c2 + t c3)) with
+ * t = (v - x[i]) / dx, the division being replaced by the stored 1 / dx. */
+struct __align__(32) gp_coef {
+        double p0, m0, c2, c3;
+};
+struct __align__(16) gp_node {
+        double x, inv_dx;
+};
+
+/* Identifiers of the baked interpolants, M materials, s a scheme in {0, 1}
+ * (CSDA, MIXED) and s3 the Ms1 scheme row in {0, 1, 2}. Node grids use the
+ * GP_LUT_* identifiers. */
+#define GP_C_X(M, s, m) ((s) * (M) + (m))
+#define GP_C_T(M, s, m) ((2 + (s)) * (M) + (m))
+#define GP_C_DE(M, s, m) ((4 + (s)) * (M) + (m))
+#define GP_C_OMEGA(M, m) (6 * (M) + (m))
+#define GP_C_CS(M, m) (7 * (M) + (m))
+#define GP_C_NI_IN(M, m) (8 * (M) + (m))
+#define GP_C_NI_EL(M, s, m) ((9 + (s)) * (M) + (m))
+#define GP_C_MU0(M, m) (11 * (M) + (m))
+#define GP_C_MS1(M, s3, m) ((12 + (s3)) * (M) + (m))
+#define GP_C_K_OF_X(M, s, m) ((15 + (s)) * (M) + (m))
+#define GP_C_X_OF_T(M, s, m) ((17 + (s)) * (M) + (m))
+#define GP_C_K_OF_NI_IN(M, m) (19 * (M) + (m))
+#define GP_C_K_OF_NI_EL(M, s, m) ((20 + (s)) * (M) + (m))
+#define GP_N_COEF(M) (22 * (M))
+
 struct gp_tables {
         int n_energies, n_materials, n_elements, n_components, n_table_dcs;
         double ctau, mass, cutoff, elastic_ratio;
@@ -101,6 +134,8 @@ struct gp_tables {
         const double * material_density;
         const struct gp_element * element;
         const struct gp_lut * lut;
+        const struct gp_coef * coef; /* GP_N_COEF tables of n_energies rows */
+        const struct gp_node * node; /* GP_N_LUT grids of n_energies rows */
         struct gp_constants k;
 };
 

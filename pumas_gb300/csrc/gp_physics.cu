@@ -263,6 +263,37 @@ static void element_constants(struct gp_element * e, double mass)
         e->shadow_low = exp(-0.1 * log(A));
 }
 
+/* Bake the cubic Hermite rows of (x, y, m) as in table_interpolate_pchip
+ * (pumas.c:4146-4157), with the row 0 rule of m1 unless `no_row0_rule`
+ * (table_get_msc, pumas.c:4097-4110, never uses row 0). */
+static void bake(const double * x, const double * y, const double * m, int n,
+    struct gp_coef * out, int no_row0_rule)
+{
+        for (int i1 = 0; i1 < n - 1; i1++) {
+                const int i2 = i1 + 1;
+                const double dX = x[i2] - x[i1];
+                const double m1 = m[i1] * dX;
+                const double m2 = ((i2 > 1) || no_row0_rule) ? m[i2] * dX : m1;
+                const double p0 = y[i1], p1 = y[i2];
+                out[i1].p0 = p0;
+                out[i1].m0 = m1;
+                out[i1].c2 = -3 * (p0 - p1) - 2 * m1 - m2;
+                out[i1].c3 = 2 * (p0 - p1) + m1 + m2;
+        }
+        out[n - 1].p0 = y[n - 1];
+        out[n - 1].m0 = out[n - 1].c2 = out[n - 1].c3 = 0.;
+}
+
+static void bake_nodes(const double * x, int n, struct gp_node * out)
+{
+        for (int i = 0; i < n - 1; i++) {
+                out[i].x = x[i];
+                out[i].inv_dx = 1. / (x[i + 1] - x[i]);
+        }
+        out[n - 1].x = x[n - 1];
+        out[n - 1].inv_dx = 0.;
+}
+
 struct parsed {
         int n_energies, n_materials, n_composites, n_elements, n_components;
         int max_components, n_table_dcs, particle;
@@ -378,8 +409,12 @@ static int physics_from_blob(
         const size_t off_lut = align256(off_comp_fraction + nc * sizeof(double));
         const int lut_capacity = 1 << 16;
         const size_t off_lut_idx = align256(off_lut + n_lut * sizeof(gp_lut));
-        const size_t total = align256(off_lut_idx +
+        const size_t off_node = align256(off_lut_idx +
             (size_t)n_lut * lut_capacity * sizeof(unsigned short));
+        const size_t off_coef = align256(off_node +
+            (size_t)n_lut * p.n_energies * sizeof(gp_node));
+        const size_t total = align256(off_coef +
+            (size_t)GP_N_COEF(nm) * p.n_energies * sizeof(gp_coef));
 
         char * host = (char *)calloc(1, total);
         if (host == NULL) return GPUMAS_RETURN_MEMORY_ERROR;
@@ -445,6 +480,68 @@ static int physics_from_blob(
                             (size_t)off_lut_idx +
                             (size_t)id * lut_capacity * sizeof(unsigned short));
                 }
+        }
+
+        /* Baked interpolants and node grids. */
+        {
+                const int ne_ = p.n_energies;
+                const int M = nm;
+#define TAB(k) ((const double *)(b + p.off[k]))
+                const double * K = TAB(3);
+                gp_node * node = (gp_node *)(host + off_node);
+                gp_coef * coef = (gp_coef *)(host + off_coef);
+                bake_nodes(K, ne_, node + (size_t)GP_LUT_K * ne_);
+                for (int m = 0; m < M; m++) {
+                        for (int sc = 0; sc < 2; sc++) {
+                                const size_t r = (size_t)(sc * M + m) * ne_;
+                                const double * X = TAB(7) + r;
+                                const double * Tt = TAB(10) + r;
+                                const double * NIe = TAB(16) + r;
+                                bake_nodes(X, ne_, node +
+                                    (size_t)(1 + sc * M + m) * ne_);
+                                bake_nodes(Tt, ne_, node +
+                                    (size_t)(1 + (2 + sc) * M + m) * ne_);
+                                bake_nodes(NIe, ne_, node +
+                                    (size_t)(1 + (5 + sc) * M + m) * ne_);
+                                bake(K, X, TAB(8) + r, ne_,
+                                    coef + (size_t)GP_C_X(M, sc, m) * ne_, 0);
+                                bake(K, Tt, TAB(11) + r, ne_,
+                                    coef + (size_t)GP_C_T(M, sc, m) * ne_, 0);
+                                bake(K, TAB(12) + r, TAB(13) + r, ne_,
+                                    coef + (size_t)GP_C_DE(M, sc, m) * ne_, 0);
+                                bake(K, NIe, TAB(17) + r, ne_,
+                                    coef + (size_t)GP_C_NI_EL(M, sc, m) * ne_,
+                                    0);
+                                bake(X, K, TAB(4) + r, ne_, coef +
+                                    (size_t)GP_C_K_OF_X(M, sc, m) * ne_, 0);
+                                bake(Tt, X, TAB(9) + r, ne_, coef +
+                                    (size_t)GP_C_X_OF_T(M, sc, m) * ne_, 0);
+                                bake(NIe, K, TAB(6) + r, ne_, coef +
+                                    (size_t)GP_C_K_OF_NI_EL(M, sc, m) * ne_,
+                                    0);
+                        }
+                        const size_t r = (size_t)m * ne_;
+                        const double * NIi = TAB(18) + r;
+                        bake_nodes(NIi, ne_, node +
+                            (size_t)(1 + 4 * M + m) * ne_);
+                        bake(K, TAB(14) + r, TAB(15) + r, ne_,
+                            coef + (size_t)GP_C_OMEGA(M, m) * ne_, 0);
+                        bake(K, TAB(20) + r, TAB(21) + r, ne_,
+                            coef + (size_t)GP_C_CS(M, m) * ne_, 0);
+                        bake(K, NIi, TAB(19) + r, ne_,
+                            coef + (size_t)GP_C_NI_IN(M, m) * ne_, 0);
+                        bake(NIi, K, TAB(5) + r, ne_,
+                            coef + (size_t)GP_C_K_OF_NI_IN(M, m) * ne_, 0);
+                        bake(K, TAB(35) + r, TAB(36) + r, ne_,
+                            coef + (size_t)GP_C_MU0(M, m) * ne_, 1);
+                        for (int s3 = 0; s3 < 3; s3++) {
+                                const size_t r3 = (size_t)(s3 * M + m) * ne_;
+                                bake(K, TAB(39) + r3, TAB(40) + r3, ne_,
+                                    coef + (size_t)GP_C_MS1(M, s3, m) * ne_,
+                                    1);
+                        }
+                }
+#undef TAB
         }
 
         struct gpumas_physics * ph =
@@ -536,6 +633,8 @@ static int physics_from_blob(
         t->comp_element = (const int *)(d + off_comp_element);
         t->comp_fraction = (const double *)(d + off_comp_fraction);
         t->lut = (const gp_lut *)(d + off_lut);
+        t->node = (const gp_node *)(d + off_node);
+        t->coef = (const gp_coef *)(d + off_coef);
 
         /* Constants of the DCS models, with the reference's expressions. */
         t->k.exp1 = exp(1.);
