@@ -77,8 +77,8 @@ extern "C" int gpumas_context_create(struct gpumas_context ** context,
         c->api.accuracy = 1E-02;
         c->api.seed = 0;
         c->tuning.engine = 0;
-        c->tuning.pool_slots = 262144;
-        c->tuning.max_inner = 2;
+        c->tuning.pool_slots = 1048576;
+        c->tuning.max_inner = 4;
         c->tuning.batch = 16;
         if (extra_memory > 0) {
                 c->extra = calloc(1, extra_memory);
