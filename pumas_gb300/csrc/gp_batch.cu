@@ -51,13 +51,13 @@ enum gp_slot_double {
         SD_POS0, SD_POS1, SD_POS2, SD_DIR0, SD_DIR1, SD_DIR2,
         SD_STEP_X_LIMIT, SD_STEP_INVLB1, SD_RANDN_NEXT, SD_LIFETIME, SD_RNEXT,
         SD_DENSITY, SD_TI, SD_WI, SD_XI, SD_XF, SD_DEI, SD_GRAMMAGE_MAX,
-        SD_STEP_MAX_MEDIUM, SD_N
+        SD_STEP_MAX_MEDIUM, SD_POLAR_KI, SD_POLAR_KF, SD_N
 };
 enum gp_slot_int {
         SI_DECAYED, SI_STEP_FIRST, SI_STEP_EVENT, SI_STEP_FORESEEN,
         SI_RANDN_DONE, SI_STEPS, SI_STATUS, SI_MEDIUM, SI_MATERIAL,
         SI_STRAIGHT, SI_STEP_INDEX, SI_NEW_MEDIUM, SI_PHASE, SI_MEDIUM_IN,
-        SI_N_DRAWS, SI_N
+        SI_N_DRAWS, SI_POLAR_PROCESS, SI_POLAR_TARGET, SI_N
 };
 enum gp_slot_u64 { SU_ID, SU_SRC, SU_N };
 
@@ -76,6 +76,7 @@ struct gp_counters {
         int pad;
         int n_del[2];
         int n_ehs[2];
+        int n_polar[2];
 };
 
 /* Per call launch parameters, read by the kernels from device memory so
@@ -94,6 +95,7 @@ struct gp_pool_state {
         gp_counters * h_counters;
         int * del_list[2];
         int * ehs_list[2];
+        int * polar_list[2];
         void * d_mem;
         size_t capacity;
         gp_launch * d_launch;
@@ -255,6 +257,7 @@ __global__ void __launch_bounds__(128, GP_POOL_MIN_BLOCKS) gp_pool_step(
                  * iteration's kernels, which precede this one. */
                 cnt->n_del[parity ^ 1] = 0;
                 cnt->n_ehs[parity ^ 1] = 0;
+                cnt->n_polar[parity ^ 1] = 0;
         }
         if (slot >= pool.P) return;
         const gp_tables & T = *Tp;
@@ -307,10 +310,14 @@ __global__ void __launch_bounds__(128, GP_POOL_MIN_BLOCKS) gp_pool_step(
             e, L, event);
 }
 
+/* DELs: energy loss and, except for photonuclear events, polar angle.
+ * Photonuclear polar angles (a Brent maximisation of the DDCS followed by a
+ * rejection sampling, pumas.c:11874-11950) cost far more than the others
+ * and are deferred to the polar list, so that they run in full warps. */
 __global__ void __launch_bounds__(128, GP_POOL_MIN_BLOCKS) gp_pool_del(
     const gp_tables * __restrict__ Tp, const gp_launch * __restrict__ X,
     const gp_pool pool, gp_counters * cnt, const int * __restrict__ list,
-    int parity)
+    int * polar_list, int parity)
 {
         const gp_config & cfg = X->cfg;
         const gp_io & io = X->io;
@@ -323,7 +330,54 @@ __global__ void __launch_bounds__(128, GP_POOL_MIN_BLOCKS) gp_pool_del(
                 gp_loop L;
                 gp_slot_load(pool, slot, cfg, e, L);
                 int event = GPUMAS_EVENT_NONE;
-                const int next = gp_stepping_del(T, cfg, e, L, event);
+                gp_polar_job job;
+                gp_do_del_energy(T, cfg, e, L.material, job);
+                if (job.process == 2) {
+                        gp_slot_store(pool, slot, e, L);
+                        PD(SD_POLAR_KI) = job.ki;
+                        PD(SD_POLAR_KF) = job.kf;
+                        PI(SI_POLAR_PROCESS) = job.process;
+                        PI(SI_POLAR_TARGET) = job.target;
+                        PI(SI_PHASE) = GP_NEXT_DEL;
+                        gp_append(&cnt->n_polar[parity], polar_list, slot);
+                        continue;
+                }
+                gp_do_del_polar(T, e, job);
+                const int next = gp_stepping_del_end(T, cfg, e, L, event);
+                if (next == GP_NEXT_DONE) {
+                        gp_finish(pool, slot, cfg, io, cnt, e, event,
+                            L.medium);
+                } else {
+                        gp_slot_store(pool, slot, e, L);
+                        PI(SI_PHASE) = GP_NEXT_STEP;
+                }
+        }
+}
+
+/* Deferred photonuclear polar angles. */
+__global__ void __launch_bounds__(128, GP_POOL_MIN_BLOCKS) gp_pool_polar(
+    const gp_tables * __restrict__ Tp, const gp_launch * __restrict__ X,
+    const gp_pool pool, gp_counters * cnt, const int * __restrict__ list,
+    int parity)
+{
+        const gp_config & cfg = X->cfg;
+        const gp_io & io = X->io;
+        const int count = cnt->n_polar[parity];
+        const gp_tables & T = *Tp;
+        for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < count;
+             j += gridDim.x * blockDim.x) {
+                const int slot = list[j];
+                gp_event e;
+                gp_loop L;
+                gp_slot_load(pool, slot, cfg, e, L);
+                gp_polar_job job;
+                job.ki = PD(SD_POLAR_KI);
+                job.kf = PD(SD_POLAR_KF);
+                job.process = PI(SI_POLAR_PROCESS);
+                job.target = PI(SI_POLAR_TARGET);
+                gp_do_del_polar(T, e, job);
+                int event = GPUMAS_EVENT_NONE;
+                const int next = gp_stepping_del_end(T, cfg, e, L, event);
                 if (next == GP_NEXT_DONE) {
                         gp_finish(pool, slot, cfg, io, cnt, e, event,
                             L.medium);
@@ -387,7 +441,7 @@ static int gp_pool_alloc(gp_context * c, int P)
         const size_t si = (size_t)SI_N * P * sizeof(int);
         const size_t su = (size_t)SU_N * P * sizeof(uint64_t);
         const size_t sl = (size_t)P * sizeof(int);
-        const size_t total = sd + si + su + 4 * sl + 256 + sizeof(gp_launch);
+        const size_t total = sd + si + su + 6 * sl + 256 + sizeof(gp_launch);
         int rc = gp_check(cudaMalloc(&ps->d_mem, total));
         if (rc == 0)
                 rc = gp_check(cudaMallocHost(
@@ -407,7 +461,9 @@ static int gp_pool_alloc(gp_context * c, int P)
         ps->del_list[1] = ps->del_list[0] + P;
         ps->ehs_list[0] = ps->del_list[1] + P;
         ps->ehs_list[1] = ps->ehs_list[0] + P;
-        ps->d_counters = (gp_counters *)(ps->ehs_list[1] + P);
+        ps->polar_list[0] = ps->ehs_list[1] + P;
+        ps->polar_list[1] = ps->polar_list[0] + P;
+        ps->d_counters = (gp_counters *)(ps->polar_list[1] + P);
         ps->d_launch = (gp_launch *)((char *)ps->d_counters + 256);
         ps->pool.P = P;
         ps->capacity = P;
@@ -426,7 +482,10 @@ static void gp_iteration(gp_context * c, int parity, int block,
             ps->ehs_list[parity], parity);
         const unsigned int grid2 = (grid + 3) / 4;
         gp_pool_del<<<grid2, block, 0, s>>>(c->d_tables, ps->d_launch,
-            ps->pool, ps->d_counters, ps->del_list[parity], parity);
+            ps->pool, ps->d_counters, ps->del_list[parity],
+            ps->polar_list[parity], parity);
+        gp_pool_polar<<<grid2, block, 0, s>>>(c->d_tables, ps->d_launch,
+            ps->pool, ps->d_counters, ps->polar_list[parity], parity);
         gp_pool_ehs<<<grid2, block, 0, s>>>(c->d_tables, ps->d_launch,
             ps->pool, ps->d_counters, ps->ehs_list[parity], parity);
 }
@@ -501,7 +560,7 @@ extern "C" int gp_pool_transport(gp_context * c, const gp_config * cfg_,
         for (long it = 0;; it++) {
                 rc = gp_check(cudaGraphLaunch(ps->exec, s));
                 if (rc != 0) return rc;
-                n_launch += 3 * iters;
+                n_launch += 4 * iters;
                 rc = gp_check(cudaMemcpyAsync(ps->h_counters, ps->d_counters,
                     sizeof(gp_counters), cudaMemcpyDeviceToHost, s));
                 if (rc == 0) rc = gp_check(cudaStreamSynchronize(s));
@@ -536,7 +595,7 @@ extern "C" int gp_pool_transport(gp_context * c, const gp_config * cfg_,
 #define GP_STATIC_BYTES                                                       \
         ((size_t)GP_STATIC_SLOTS *                                            \
                 (SD_N * sizeof(double) + SU_N * sizeof(uint64_t) +            \
-                    SI_N * sizeof(int) + 4 * sizeof(int)) +                   \
+                    SI_N * sizeof(int) + 6 * sizeof(int)) +                   \
             512 + sizeof(gp_launch))
 
 static __device__ __align__(256) unsigned char gp_static_pool[GP_STATIC_BYTES];
@@ -601,7 +660,7 @@ extern "C" int gpumas_context_transport_device_static(
         pool.i = (int *)p;
         p += (size_t)SI_N * P * sizeof(int);
         int * lists = (int *)p;
-        p += (size_t)4 * P * sizeof(int);
+        p += (size_t)6 * P * sizeof(int);
         p = (char *)(((size_t)p + 255) & ~(size_t)255);
         gp_counters * counters = (gp_counters *)p;
         gp_launch * launch = (gp_launch *)(p + 256);
@@ -639,11 +698,15 @@ extern "C" int gpumas_context_transport_device_static(
                         const int parity = k & 1;
                         int * del_list = lists + (size_t)parity * P;
                         int * ehs_list = lists + (size_t)(2 + parity) * P;
+                        int * polar_list = lists + (size_t)(4 + parity) * P;
                         gp_pool_step<<<grid, block, 0, s>>>(c->d_tables,
                             c->d_geometry, launch, pool, counters, del_list,
                             ehs_list, parity);
                         gp_pool_del<<<grid2, block, 0, s>>>(c->d_tables,
-                            launch, pool, counters, del_list, parity);
+                            launch, pool, counters, del_list, polar_list,
+                            parity);
+                        gp_pool_polar<<<grid2, block, 0, s>>>(c->d_tables,
+                            launch, pool, counters, polar_list, parity);
                         gp_pool_ehs<<<grid2, block, 0, s>>>(c->d_tables,
                             launch, pool, counters, ehs_list, parity);
                 }

@@ -1868,8 +1868,17 @@ static __device__ __forceinline__ bool gp_del_reverse(const gp_tables & T, const
 }
 
 /* transport_do_del (pumas.c:5706-5757). */
-static __device__ __forceinline__ void gp_do_del(const gp_tables & T, const gp_config & cfg,
-    gp_event & e, int material)
+/* A sampled DEL whose polar angle is still to be drawn. */
+struct gp_polar_job {
+        int process;   /* -1 if no polar angle is to be sampled */
+        int target;
+        double ki, kf; /* initial and final energies, ki >= kf */
+};
+
+/* First part of transport_do_del (pumas.c:5706-5745): the energy loss and
+ * the event flag. Returns in *job the pending polar angle, if any. */
+static __device__ __forceinline__ void gp_do_del_energy(const gp_tables & T,
+    const gp_config & cfg, gp_event & e, int material, gp_polar_job & job)
 {
         double ki, kf;
         int process = -1, target = 0;
@@ -1894,16 +1903,38 @@ static __device__ __forceinline__ void gp_do_del(const gp_tables & T, const gp_c
                     (process == 3) ? GPUMAS_EVENT_VERTEX_DELTA_RAY :
                                      GPUMAS_EVENT_VERTEX;
         }
+        job.process = -1;
         if ((cfg.scattering == GPUMAS_MODE_MIXED) && polar) {
                 if (kf > ki) {
                         const double tmp = kf;
                         kf = ki;
                         ki = tmp;
                 }
-                const double mu = gp_polar(T, e, process, T.element[target],
-                    ki, kf);
-                gp_rotate(e, mu);
+                job.process = process;
+                job.target = target;
+                job.ki = ki;
+                job.kf = kf;
         }
+}
+
+/* Second part of transport_do_del (pumas.c:5746-5756): the polar angle and
+ * the rotation of the direction. */
+static __device__ __forceinline__ void gp_do_del_polar(const gp_tables & T,
+    gp_event & e, const gp_polar_job & job)
+{
+        if (job.process < 0) return;
+        const double mu = gp_polar(T, e, job.process, T.element[job.target],
+            job.ki, job.kf);
+        gp_rotate(e, mu);
+}
+
+/* transport_do_del (pumas.c:5706-5757). */
+static __device__ __forceinline__ void gp_do_del(const gp_tables & T,
+    const gp_config & cfg, gp_event & e, int material)
+{
+        gp_polar_job job;
+        gp_do_del_energy(T, cfg, e, material, job);
+        gp_do_del_polar(T, e, job);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -2708,11 +2739,11 @@ static __device__ __forceinline__ int gp_stepping_step(const gp_tables & T, cons
         return GP_NEXT_DONE;
 }
 
-/* DEL of the stepping loop (pumas.c:5336-5374 and 5479-5488). */
-static __device__ __forceinline__ int gp_stepping_del(const gp_tables & T, const gp_config & cfg,
-    gp_event & e, gp_loop & L, int & event)
+/* Tail of a DEL in the stepping loop, once the polar angle is applied
+ * (pumas.c:5361-5374 and 5479-5488). */
+static __device__ __forceinline__ int gp_stepping_del_end(const gp_tables & T,
+    const gp_config & cfg, gp_event & e, gp_loop & L, int & event)
 {
-        gp_do_del(T, cfg, e, L.material);
         if ((cfg.event & e.step_event) ||
             (e.step_event == GPUMAS_EVENT_WEIGHT) ||
             (e.status != GPUMAS_RETURN_SUCCESS)) {
@@ -2722,6 +2753,14 @@ static __device__ __forceinline__ int gp_stepping_del(const gp_tables & T, const
         e.step_first = 1;
         e.step_invlb1 = 0;
         return gp_stepping_relimit(T, cfg, e, L, event);
+}
+
+/* DEL of the stepping loop (pumas.c:5336-5374 and 5479-5488). */
+static __device__ __forceinline__ int gp_stepping_del(const gp_tables & T,
+    const gp_config & cfg, gp_event & e, gp_loop & L, int & event)
+{
+        gp_do_del(T, cfg, e, L.material);
+        return gp_stepping_del_end(T, cfg, e, L, event);
 }
 
 /* EHS of the stepping loop (pumas.c:5393-5400 and 5479-5488). */
