@@ -77,6 +77,7 @@ struct gp_counters {
         int n_del[2];
         int n_ehs[2];
         int n_polar[2];
+        int polar_next[2];
 };
 
 /* Per call launch parameters, read by the kernels from device memory so
@@ -258,6 +259,7 @@ __global__ void __launch_bounds__(128, GP_POOL_MIN_BLOCKS) gp_pool_step(
                 cnt->n_del[parity ^ 1] = 0;
                 cnt->n_ehs[parity ^ 1] = 0;
                 cnt->n_polar[parity ^ 1] = 0;
+                cnt->polar_next[parity ^ 1] = 0;
         }
         if (slot >= pool.P) return;
         const gp_tables & T = *Tp;
@@ -354,7 +356,324 @@ __global__ void __launch_bounds__(128, GP_POOL_MIN_BLOCKS) gp_pool_del(
         }
 }
 
-/* Deferred photonuclear polar angles. */
+/* ------------------------------------------------------------------------ */
+/* Photonuclear polar angles in lockstep.                                   */
+/*                                                                          */
+/* polar_photonuclear (pumas.c:11874-11950) maximises Q2 d2S/dqdQ2 over     */
+/* ln Q2 with math_find_minimum (pumas.c:12105-12206; bisection, then       */
+/* Brent, pumas.c:12233-12325), possibly twice, then samples Q2 by          */
+/* rejection. Every step of it costs one evaluation of the DRSS DDCS, and   */
+/* the number of steps differs from event to event. Here each lane runs     */
+/* its own copy of that procedure as a state machine whose every iteration  */
+/* needs exactly one DDCS evaluation, done by all lanes together; a lane    */
+/* whose event is done takes the next event of the list. The arithmetic and */
+/* the random draws of each event are those of the sequential procedure.    */
+/* ------------------------------------------------------------------------ */
+enum gp_pn_phase {
+        PN_MIN_A, PN_MIN_C, PN_BISECT, PN_BRENT, PN_REJECT, PN_DONE
+};
+
+struct gp_pn {
+        /* Event. */
+        double ki, q, Q2min, lnQ2max, rQ2;
+        int target;
+        /* Search state (math_find_minimum and math_find_minimum_brent). */
+        int phase, second, i, ib, max_b;
+        double xa, xc, fa, fc, xb, fb, atol;
+        double x, w, v, fx, fw, fv, d, e, tolb;
+        double u;
+        /* First search result and the maximum of the objective. */
+        double xopt, fopt;
+        /* Pending evaluation: Q2 and kind (0: objective, 1: rejection). */
+        double Q2;
+        double mu;
+};
+
+#define PN_TOL 1E-06
+#define PN_MAX_ITER 100
+
+/* Start a find_minimum search over [xa, xc]. */
+static __device__ __forceinline__ void gp_pn_search(gp_pn & s, double xa,
+    double xc, int second)
+{
+        s.xa = xa;
+        s.xc = xc;
+        s.second = second;
+        s.phase = PN_MIN_A;
+}
+
+/* End of a search with (xopt, fopt, status): continue as in
+ * polar_photonuclear. */
+static __device__ __forceinline__ void gp_pn_searched(
+    gp_pn & s, gp_event & e, double xo, double fo, int status)
+{
+        const double M = 0.5 * (GP_PROTON_MASS + GP_NEUTRON_MASS);
+        if (!s.second) {
+                s.xopt = xo;
+                s.fopt = -fo;
+                if (status == -2) {
+                        s.mu = 0.;
+                        s.phase = PN_DONE;
+                        return;
+                }
+                const double x = exp(s.xopt) / (2 * s.q * M);
+                const double lne = 0.1;
+                if ((x <= 0.04) && (s.xopt + lne < s.lnQ2max)) {
+                        gp_pn_search(s, s.xopt + lne, s.lnQ2max, 1);
+                        return;
+                }
+        } else if (status >= 0) {
+                const double f2 = -fo;
+                if (f2 > s.fopt) {
+                        s.xopt = xo;
+                        s.fopt = f2;
+                }
+        }
+        s.i = 0;
+        s.phase = PN_REJECT;
+}
+
+/* Advance the state machine up to its next DDCS evaluation (s.Q2), or to
+ * its end (PN_DONE). `f` is the objective value of the last requested
+ * point, if any. */
+static __device__ __forceinline__ void gp_pn_advance(const gp_tables & T,
+    gp_pn & s, gp_event & e, int have_value, double value)
+{
+        const double EPS = 1E-15;
+        const double GOLD = 0.3819660;
+        for (int guard = 0; guard < 64; guard++) {
+                switch (s.phase) {
+                case PN_MIN_A:
+                        if (!have_value) {
+                                s.Q2 = exp(s.xa);
+                                return;
+                        }
+                        s.fa = value;
+                        have_value = 0;
+                        s.phase = PN_MIN_C;
+                        break;
+                case PN_MIN_C:
+                        if (!have_value) {
+                                s.Q2 = exp(s.xc);
+                                return;
+                        }
+                        s.fc = value;
+                        have_value = 0;
+                        s.atol = PN_TOL * fabs(s.xc - s.xa);
+                        s.i = 0;
+                        s.phase = PN_BISECT;
+                        break;
+                case PN_BISECT:
+                        if (!have_value) {
+                                if (s.i == PN_MAX_ITER) {
+                                        if (s.fa < s.fb) {
+                                                s.fb = s.fa;
+                                                s.xb = s.xa;
+                                        } else if (s.fc < s.fb) {
+                                                s.fb = s.fc;
+                                                s.xb = s.xc;
+                                        }
+                                        gp_pn_searched(s, e, s.xb, s.fb, -1);
+                                        break;
+                                }
+                                s.xb = 0.5 * (s.xa + s.xc);
+                                s.Q2 = exp(s.xb);
+                                return;
+                        }
+                        s.fb = value;
+                        have_value = 0;
+                        if ((s.fb < s.fa) && (s.fb < s.fc)) {
+                                /* Brent refinement, math_find_minimum_brent
+                                 * with bracket (xa, xb) as in the reference. */
+                                s.max_b = PN_MAX_ITER - s.i;
+                                s.tolb = PN_TOL * fabs(s.xc - s.xa);
+                                s.x = s.w = s.v = s.xb;
+                                s.fw = s.fv = s.fx = s.fb;
+                                s.d = s.e = 0.;
+                                s.ib = 0;
+                                s.phase = PN_BRENT;
+                                break;
+                        }
+                        if (fabs(s.xc - s.xa) <= s.atol) {
+                                gp_pn_searched(s, e, s.xb, s.fb, s.i);
+                                break;
+                        }
+                        if (s.fb < s.fc) {
+                                s.xc = s.xb;
+                                s.fc = s.fb;
+                        } else {
+                                s.xa = s.xb;
+                                s.fa = s.fb;
+                        }
+                        s.i++;
+                        break;
+                case PN_BRENT:
+                        if (!have_value) {
+                                if (s.ib >= s.max_b) {
+                                        gp_pn_searched(s, e, s.x, s.fx, -2);
+                                        break;
+                                }
+                                const double xm = 0.5 * (s.xa + s.xb);
+                                const double tol1 = s.tolb * fabs(s.x) + EPS;
+                                const double tol2 = 2 * tol1;
+                                if (fabs(s.x - xm) <=
+                                    (tol2 - 0.5 * (s.xb - s.xa))) {
+                                        gp_pn_searched(s, e, s.x, s.fx,
+                                            s.ib + s.i);
+                                        break;
+                                }
+                                if (fabs(s.e) > tol1) {
+                                        const double r = (s.x - s.w) *
+                                            (s.fx - s.fv);
+                                        double qq = (s.x - s.v) * (s.fx - s.fw);
+                                        double p = (s.x - s.v) * qq -
+                                            (s.x - s.w) * r;
+                                        qq = 2. * (qq - r);
+                                        if (qq > 0.) p = -p;
+                                        qq = fabs(qq);
+                                        const double etemp = s.e;
+                                        s.e = s.d;
+                                        if (fabs(p) >= fabs(0.5 * qq * etemp) ||
+                                            (p <= qq * (s.xa - s.x)) ||
+                                            (p >= qq * (s.xb - s.x))) {
+                                                s.e = (s.x >= xm) ? s.xa - s.x :
+                                                                    s.xb - s.x;
+                                                s.d = GOLD * s.e;
+                                        } else {
+                                                s.d = p / qq;
+                                                const double uu = s.x + s.d;
+                                                if ((uu - s.xa < tol2) ||
+                                                    (s.xb - uu < tol2))
+                                                        s.d = ((xm - s.x) >= 0.0) ?
+                                                            fabs(tol1) :
+                                                            -fabs(tol1);
+                                        }
+                                } else {
+                                        s.e = (s.x >= xm) ? s.xa - s.x :
+                                                            s.xb - s.x;
+                                        s.d = GOLD * s.e;
+                                }
+                                s.u = (fabs(s.d) >= tol1) ? s.x + s.d :
+                                    s.x + ((s.d >= 0.0) ? fabs(tol1) :
+                                                          -fabs(tol1));
+                                s.Q2 = exp(s.u);
+                                return;
+                        }
+                        {
+                                const double fu = value;
+                                const double uu = s.u;
+                                have_value = 0;
+                                if (fu <= s.fx) {
+                                        if (uu >= s.x)
+                                                s.xa = s.x;
+                                        else
+                                                s.xb = s.x;
+                                        s.v = s.w, s.w = s.x, s.x = uu;
+                                        s.fv = s.fw, s.fw = s.fx, s.fx = fu;
+                                } else {
+                                        if (uu < s.x)
+                                                s.xa = uu;
+                                        else
+                                                s.xb = uu;
+                                        if ((fu <= s.fw) || (s.w == s.x)) {
+                                                s.v = s.w;
+                                                s.w = uu;
+                                                s.fv = s.fw;
+                                                s.fw = fu;
+                                        } else if ((fu <= s.fv) ||
+                                            (s.v == s.x) || (s.v == s.w)) {
+                                                s.v = uu;
+                                                s.fv = fu;
+                                        }
+                                }
+                                s.ib++;
+                        }
+                        break;
+                case PN_REJECT:
+                        if (!have_value) {
+                                if (s.i == 100) {
+                                        s.mu = 0.;
+                                        s.phase = PN_DONE;
+                                        return;
+                                }
+                                const double uu = gp_random(e);
+                                s.Q2 = s.Q2min * exp(s.rQ2 * uu);
+                                return;
+                        }
+                        if (gp_random(e) * s.fopt <= value) {
+                                /* Accepted: polar parameter of Q2. */
+                                const double ml = T.mass;
+                                const double ki = s.ki, q = s.q;
+                                const double E = ki + ml;
+                                const double p = sqrt(ki * (ki + 2 * ml));
+                                const double E1 = E - q;
+                                const double eps = ml / E1;
+                                const double p1 = E1 * sqrt((1. + eps) *
+                                                         (1. - eps));
+                                const double p2 = p * p1;
+                                double tmp = GP_SUB(GP_ADD(p2, GP_MUL(ml, ml)),
+                                    GP_MUL(E, E1));
+                                if (fabs(tmp) <= 3 * GP_DBL_EPSILON * p2)
+                                        tmp = 0.;
+                                const double a_mu = 0.5 * tmp / p2;
+                                const double b_mu = 0.25 / p2;
+                                double mu = a_mu + b_mu * s.Q2;
+                                if (mu < 0)
+                                        mu = 0.;
+                                else if (mu > 1.)
+                                        mu = 1.;
+                                s.mu = mu;
+                                s.phase = PN_DONE;
+                                return;
+                        }
+                        have_value = 0;
+                        s.i++;
+                        break;
+                default:
+                        return;
+                }
+        }
+}
+
+/* Set up the polar sampling of a photonuclear DEL (ki >= kf). Returns
+ * with PN_DONE when no sampling is needed. */
+static __device__ __forceinline__ void gp_pn_start(const gp_tables & T,
+    gp_pn & s, gp_event & e, double ki, double kf, int target)
+{
+        const double M = 0.5 * (GP_PROTON_MASS + GP_NEUTRON_MASS);
+        s.ki = ki;
+        s.q = ki - kf;
+        s.target = target;
+        const double ml = T.mass;
+        const double E = ki + ml;
+        const double ml2 = ml * ml;
+        const double q = s.q;
+        const double Q2min = ml2 * (q * q - 0.5 * ml2) / (E * (E - q));
+        const double Q2max =
+            2.0 * M * (q - GP_PION_MASS) - GP_PION_MASS * GP_PION_MASS;
+        s.mu = 0.;
+        if ((Q2max < Q2min) | (Q2min < 0)) {
+                s.phase = PN_DONE;
+                return;
+        }
+        s.Q2min = Q2min;
+        const double lnQ2min = log(Q2min);
+        s.lnQ2max = log(Q2max);
+        s.rQ2 = s.lnQ2max - lnQ2min;
+        gp_pn_search(s, lnQ2min, s.lnQ2max, 0);
+        gp_pn_advance(T, s, e, 0, 0.);
+}
+
+/* The objective or rejection value at the pending point. */
+static __device__ __forceinline__ double gp_pn_value(
+    const gp_tables & T, const gp_pn & s)
+{
+        const gp_element & el = T.element[s.target];
+        const double d2 = gp_photonuclear_d2(T, el, s.ki, s.q, s.Q2);
+        return (s.phase == PN_REJECT) ? d2 * s.Q2 : -d2 * s.Q2;
+}
+
+/* Deferred photonuclear polar angles: lanes refill from the list. */
 __global__ void __launch_bounds__(128, GP_POOL_MIN_BLOCKS) gp_pool_polar(
     const gp_tables * __restrict__ Tp, const gp_launch * __restrict__ X,
     const gp_pool pool, gp_counters * cnt, const int * __restrict__ list,
@@ -364,26 +683,54 @@ __global__ void __launch_bounds__(128, GP_POOL_MIN_BLOCKS) gp_pool_polar(
         const gp_io & io = X->io;
         const int count = cnt->n_polar[parity];
         const gp_tables & T = *Tp;
-        for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < count;
-             j += gridDim.x * blockDim.x) {
-                const int slot = list[j];
-                gp_event e;
-                gp_loop L;
-                gp_slot_load(pool, slot, cfg, e, L);
-                gp_polar_job job;
-                job.ki = PD(SD_POLAR_KI);
-                job.kf = PD(SD_POLAR_KF);
-                job.process = PI(SI_POLAR_PROCESS);
-                job.target = PI(SI_POLAR_TARGET);
-                gp_do_del_polar(T, e, job);
-                int event = GPUMAS_EVENT_NONE;
-                const int next = gp_stepping_del_end(T, cfg, e, L, event);
-                if (next == GP_NEXT_DONE) {
-                        gp_finish(pool, slot, cfg, io, cnt, e, event,
-                            L.medium);
-                } else {
-                        gp_slot_store(pool, slot, e, L);
-                        PI(SI_PHASE) = GP_NEXT_STEP;
+        int * cursor = &cnt->polar_next[parity];
+        gp_event e;
+        gp_loop L;
+        gp_pn s;
+        int slot = -1;
+        for (int guard = 0; guard < (1 << 30); guard++) {
+                if (slot < 0) {
+                        /* Take events until one needs a sampling. */
+                        while (true) {
+                                const int j = atomicAdd(cursor, 1);
+                                if (j >= count) break;
+                                slot = list[j];
+                                gp_slot_load(pool, slot, cfg, e, L);
+                                gp_pn_start(T, s, e, PD(SD_POLAR_KI),
+                                    PD(SD_POLAR_KF), PI(SI_POLAR_TARGET));
+                                if (s.phase != PN_DONE) break;
+                                gp_rotate(e, s.mu);
+                                int event = GPUMAS_EVENT_NONE;
+                                const int next = gp_stepping_del_end(
+                                    T, cfg, e, L, event);
+                                if (next == GP_NEXT_DONE) {
+                                        gp_finish(pool, slot, cfg, io, cnt, e,
+                                            event, L.medium);
+                                } else {
+                                        gp_slot_store(pool, slot, e, L);
+                                        PI(SI_PHASE) = GP_NEXT_STEP;
+                                }
+                                slot = -1;
+                        }
+                }
+                if (!__any_sync(0xFFFFFFFFu, slot >= 0)) break;
+                if (slot >= 0) {
+                        const double value = gp_pn_value(T, s);
+                        gp_pn_advance(T, s, e, 1, value);
+                        if (s.phase == PN_DONE) {
+                                gp_rotate(e, s.mu);
+                                int event = GPUMAS_EVENT_NONE;
+                                const int next = gp_stepping_del_end(
+                                    T, cfg, e, L, event);
+                                if (next == GP_NEXT_DONE) {
+                                        gp_finish(pool, slot, cfg, io, cnt, e,
+                                            event, L.medium);
+                                } else {
+                                        gp_slot_store(pool, slot, e, L);
+                                        PI(SI_PHASE) = GP_NEXT_STEP;
+                                }
+                                slot = -1;
+                        }
                 }
         }
 }

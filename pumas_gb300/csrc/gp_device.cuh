@@ -973,14 +973,17 @@ GPD double gp_f2p_allm97(const gp_tables & T, double x, double Q2)
         const double t = log(log((Q2 + Q02) / Lambda2) / T.k.allm_lq0);
         const double xP = (Q2 + mP2) / (Q2 + mP2 + W2 - M2);
         const double xR = (Q2 + mR2) / (Q2 + mR2 + W2 - M2);
-        const double cP =
-            0.28067 + (0.28067 - 0.22291) * (1.0 / (1.0 + pow(t, 2.1979)) - 1.0);
-        const double aP =
-            -0.0808 + (-0.0808 - -0.44812) * (1.0 / (1.0 + pow(t, 1.1709)) - 1.0);
-        const double bP = 0.36292 + 1.8917 * pow(t, 1.8439);
-        const double cR = 0.80107 + 0.97307 * pow(t, 3.4942);
-        const double aR = 0.58400 + 0.37888 * pow(t, 2.6063);
-        const double bR = 0.01147 + 3.7582 * pow(t, 0.49338);
+        /* The six powers of t share one logarithm: t^c = exp(c ln t), exact
+         * to a few ulps (t = 0 gives exp(-inf) = 0 as pow). */
+        const double lt = log(t);
+        const double cP = 0.28067 +
+            (0.28067 - 0.22291) * (1.0 / (1.0 + exp(2.1979 * lt)) - 1.0);
+        const double aP = -0.0808 +
+            (-0.0808 - -0.44812) * (1.0 / (1.0 + exp(1.1709 * lt)) - 1.0);
+        const double bP = 0.36292 + 1.8917 * exp(1.8439 * lt);
+        const double cR = 0.80107 + 0.97307 * exp(3.4942 * lt);
+        const double aR = 0.58400 + 0.37888 * exp(2.6063 * lt);
+        const double bR = 0.01147 + 3.7582 * exp(0.49338 * lt);
         const double l1x = log(1 - x);
         const double F2P = cP * exp(aP * log(xP) + bP * l1x);
         const double F2R = cR * exp(aR * log(xR) + bR * l1x);
