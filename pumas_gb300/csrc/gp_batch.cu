@@ -78,6 +78,7 @@ struct gp_counters {
         int n_ehs[2];
         int n_polar[2];
         int polar_next[2];
+        int step_next[2];
 };
 
 /* Per call launch parameters, read by the kernels from device memory so
@@ -106,6 +107,7 @@ struct gp_pool_state {
         int graph_batch;
         const void * graph_tables;
         const void * graph_geometry;
+        unsigned int step_grid;
 };
 
 #define PD(f) pool.d[(size_t)(f) * pool.P + slot]
@@ -242,6 +244,47 @@ __device__ __forceinline__ void gp_route(const gp_pool & pool, int slot,
                 gp_append(&cnt->n_ehs[parity], ehs_list, slot);
 }
 
+/* Refill slot `slot` from the input queue. Events that end before their
+ * first step are finished here and the next one is taken. Returns 1 if the
+ * slot now holds an event to step (e, L loaded), 0 if the input is empty. */
+static __device__ __forceinline__ int gp_refill(const gp_tables & T,
+    const gp_config & cfg, const gpumas_geometry & g, const gp_io & io,
+    size_t n, uint64_t first_event, const gp_pool & pool, int slot,
+    gp_counters * cnt, gp_event & e, gp_loop & L)
+{
+        for (;;) {
+                if (*(volatile unsigned long long *)&cnt->cursor >= n)
+                        return 0;
+                cg::coalesced_group w = cg::coalesced_threads();
+                unsigned long long base = 0;
+                if (w.thread_rank() == 0)
+                        base = atomicAdd(&cnt->cursor,
+                            (unsigned long long)w.size());
+                base = w.shfl(base, 0);
+                const unsigned long long idx = base + w.thread_rank();
+                if (idx >= n) return 0;
+                io.load((size_t)idx, e);
+                gp_event_init(e, cfg.seed, first_event + idx);
+                int medium_in, event = GPUMAS_EVENT_NONE;
+                const int next = gp_transport_begin(
+                    T, cfg, g, e, L, event, medium_in);
+                if (next == GP_NEXT_DONE) {
+                        io.store((size_t)idx, e, event, medium_in, L.medium);
+                        continue;
+                }
+                PU(SU_SRC) = idx;
+                PI(SI_MEDIUM_IN) = medium_in;
+                atomicAdd(&cnt->active, 1);
+                return 1;
+        }
+}
+
+/* Continuous steps. The kernel is persistent: each lane takes slots from a
+ * cursor over the pool (refilling empty ones from the input), steps its
+ * slot until the step ends on an event or after max_inner steps, routes it
+ * to the next phase and takes the next slot. All lanes thus execute the step
+ * together until the pool is exhausted, whatever the number of steps of
+ * each event. */
 __global__ void __launch_bounds__(128, GP_POOL_MIN_BLOCKS) gp_pool_step(
     const gp_tables * __restrict__ Tp, const gpumas_geometry * __restrict__ gp,
     const gp_launch * __restrict__ X, const gp_pool pool, gp_counters * cnt,
@@ -252,64 +295,62 @@ __global__ void __launch_bounds__(128, GP_POOL_MIN_BLOCKS) gp_pool_step(
         const size_t n = X->n;
         const uint64_t first_event = X->first_event;
         const int max_inner = X->max_inner;
-        const int slot = blockIdx.x * blockDim.x + threadIdx.x;
-        if (slot == 0) {
-                /* The other parity's lists were consumed by the previous
-                 * iteration's kernels, which precede this one. */
-                cnt->n_del[parity ^ 1] = 0;
-                cnt->n_ehs[parity ^ 1] = 0;
-                cnt->n_polar[parity ^ 1] = 0;
-                cnt->polar_next[parity ^ 1] = 0;
-        }
-        if (slot >= pool.P) return;
         const gp_tables & T = *Tp;
         const gpumas_geometry & g = *gp;
+        int * scursor = &cnt->step_next[parity];
         gp_event e;
         gp_loop L;
-        int event = GPUMAS_EVENT_NONE;
-        int next;
-        if (PI(SI_PHASE) == GP_EMPTY) {
-                /* Refill from the input queue. Events that end before their
-                 * first step are finished here and the next one is taken. */
-                next = GP_EMPTY;
-                for (;;) {
-                        if (*(volatile unsigned long long *)&cnt->cursor >= n)
-                                break;
+        int slot = -1, k = 0, exhausted = 0;
+        for (long guard = 0; guard < (1L << 40); guard++) {
+                while ((slot < 0) && !exhausted) {
                         cg::coalesced_group w = cg::coalesced_threads();
-                        unsigned long long base = 0;
+                        int base = 0;
                         if (w.thread_rank() == 0)
-                                base = atomicAdd(&cnt->cursor,
-                                    (unsigned long long)w.size());
+                                base = atomicAdd(scursor, (int)w.size());
                         base = w.shfl(base, 0);
-                        const unsigned long long idx = base + w.thread_rank();
-                        if (idx >= n) break;
-                        io.load((size_t)idx, e);
-                        gp_event_init(e, cfg.seed, first_event + idx);
-                        int medium_in;
-                        next = gp_transport_begin(
-                            T, cfg, g, e, L, event, medium_in);
-                        if (next == GP_NEXT_DONE) {
-                                io.store((size_t)idx, e, event, medium_in,
-                                    L.medium);
-                                next = GP_EMPTY;
-                                continue;
+                        const int j = base + (int)w.thread_rank();
+                        if (j >= pool.P) {
+                                exhausted = 1;
+                                break;
                         }
-                        PU(SU_SRC) = idx;
-                        PI(SI_MEDIUM_IN) = medium_in;
-                        atomicAdd(&cnt->active, 1);
-                        break;
+                        if (j == 0) {
+                                /* The other parity's lists and cursors were
+                                 * consumed by the previous iteration's
+                                 * kernels, which precede this one. */
+                                cnt->n_del[parity ^ 1] = 0;
+                                cnt->n_ehs[parity ^ 1] = 0;
+                                cnt->n_polar[parity ^ 1] = 0;
+                                cnt->polar_next[parity ^ 1] = 0;
+                                cnt->step_next[parity ^ 1] = 0;
+                        }
+                        const int s_ = j;
+                        {
+                                const int slot = s_;
+                                if (PI(SI_PHASE) == GP_EMPTY) {
+                                        if (!gp_refill(T, cfg, g, io, n,
+                                                first_event, pool, slot, cnt,
+                                                e, L))
+                                                continue;
+                                } else {
+                                        gp_slot_load(pool, slot, cfg, e, L);
+                                }
+                        }
+                        slot = s_;
+                        k = 0;
                 }
-                if (next == GP_EMPTY) return;
-        } else {
-                gp_slot_load(pool, slot, cfg, e, L);
+                if (!__any_sync(0xFFFFFFFFu, slot >= 0)) break;
+                if (slot >= 0) {
+                        int event = GPUMAS_EVENT_NONE;
+                        const int next =
+                            gp_stepping_step(T, cfg, g, e, L, event);
+                        k++;
+                        if ((next != GP_NEXT_STEP) || (k >= max_inner)) {
+                                gp_route(pool, slot, cfg, io, cnt, del_list,
+                                    ehs_list, parity, next, e, L, event);
+                                slot = -1;
+                        }
+                }
         }
-        next = GP_NEXT_STEP;
-        for (int k = 0; k < max_inner; k++) {
-                next = gp_stepping_step(T, cfg, g, e, L, event);
-                if (next != GP_NEXT_STEP) break;
-        }
-        gp_route(pool, slot, cfg, io, cnt, del_list, ehs_list, parity, next,
-            e, L, event);
 }
 
 /* DELs: energy loss and, except for photonuclear events, polar angle.
@@ -814,6 +855,16 @@ static int gp_pool_alloc(gp_context * c, int P)
         ps->d_launch = (gp_launch *)((char *)ps->d_counters + 256);
         ps->pool.P = P;
         ps->capacity = P;
+        {
+                /* One wave of persistent step blocks. */
+                int device = 0, sms = 0, per_sm = 0;
+                cudaGetDevice(&device);
+                cudaDeviceGetAttribute(
+                    &sms, cudaDevAttrMultiProcessorCount, device);
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                    &per_sm, gp_pool_step, 128, 0);
+                ps->step_grid = (unsigned int)(sms * (per_sm > 0 ? per_sm : 1));
+        }
         c->pool = ps;
         return 0;
 }
@@ -824,7 +875,10 @@ static void gp_iteration(gp_context * c, int parity, int block,
         gp_pool_state * ps = c->pool;
         const int P = ps->pool.P;
         const unsigned int grid = (P + block - 1) / block;
-        gp_pool_step<<<grid, block, 0, s>>>(c->d_tables, c->d_geometry,
+        const unsigned int grid_step =
+            (ps->step_grid > 0) && (ps->step_grid < grid) ? ps->step_grid :
+                                                             grid;
+        gp_pool_step<<<grid_step, block, 0, s>>>(c->d_tables, c->d_geometry,
             ps->d_launch, ps->pool, ps->d_counters, ps->del_list[parity],
             ps->ehs_list[parity], parity);
         const unsigned int grid2 = (grid + 3) / 4;
@@ -1039,6 +1093,17 @@ extern "C" int gpumas_context_transport_device_static(
         const int block = 128;
         const unsigned int grid = (P + block - 1) / block;
         const unsigned int grid2 = (grid + 3) / 4;
+        unsigned int grid_step = grid;
+        {
+                int sms = 0, per_sm = 0;
+                cudaDeviceGetAttribute(
+                    &sms, cudaDevAttrMultiProcessorCount, device);
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                    &per_sm, gp_pool_step, block, 0);
+                const unsigned int wave =
+                    (unsigned int)(sms * (per_sm > 0 ? per_sm : 1));
+                if (wave < grid_step) grid_step = wave;
+        }
         const int batch = 16;
         for (long it = 0;; it++) {
                 for (int k = 0; k < batch; k++) {
@@ -1046,9 +1111,9 @@ extern "C" int gpumas_context_transport_device_static(
                         int * del_list = lists + (size_t)parity * P;
                         int * ehs_list = lists + (size_t)(2 + parity) * P;
                         int * polar_list = lists + (size_t)(4 + parity) * P;
-                        gp_pool_step<<<grid, block, 0, s>>>(c->d_tables,
-                            c->d_geometry, launch, pool, counters, del_list,
-                            ehs_list, parity);
+                        gp_pool_step<<<grid_step, block, 0, s>>>(
+                            c->d_tables, c->d_geometry, launch, pool,
+                            counters, del_list, ehs_list, parity);
                         gp_pool_del<<<grid2, block, 0, s>>>(c->d_tables,
                             launch, pool, counters, del_list, polar_list,
                             parity);

@@ -447,11 +447,10 @@ GPD double gp_coulomb_ehs_length(
                 return __ldg(Lb + imax) / p2;
         } else {
                 const int i1 = gp_index(T, GP_LUT_K, T.K, kinetic);
-                const int i2 = i1 + 1;
-                const double k1 = __ldg(T.K + i1);
-                double h = (kinetic - k1) / (__ldg(T.K + i2) - k1);
+                const double2 nd = __ldg((const double2 *)(T.node + i1));
+                const double h = (kinetic - nd.x) * nd.y;
                 const double l1 = __ldg(Lb + i1);
-                return (l1 + h * (__ldg(Lb + i2) - l1)) / p2;
+                return (l1 + h * (__ldg(Lb + i1 + 1) - l1)) / p2;
         }
 }
 
@@ -1277,25 +1276,25 @@ static __device__ __forceinline__ void gp_rotate(gp_event & e, double mu)
         if (a0 > a1) {
                 if (a0 > a2) {
                         const double nrm =
-                            1. / sqrt(direction[0] * direction[0] +
-                                     direction[2] * direction[2]);
+                            rsqrt(direction[0] * direction[0] +
+                                direction[2] * direction[2]);
                         u0x = -direction[2] * nrm, u0z = direction[0] * nrm;
                 } else {
                         const double nrm =
-                            1. / sqrt(direction[1] * direction[1] +
-                                     direction[2] * direction[2]);
+                            rsqrt(direction[1] * direction[1] +
+                                direction[2] * direction[2]);
                         u0y = direction[2] * nrm, u0z = -direction[1] * nrm;
                 }
         } else {
                 if (a1 > a2) {
                         const double nrm =
-                            1. / sqrt(direction[0] * direction[0] +
-                                     direction[1] * direction[1]);
+                            rsqrt(direction[0] * direction[0] +
+                                direction[1] * direction[1]);
                         u0x = direction[1] * nrm, u0y = -direction[0] * nrm;
                 } else {
                         const double nrm =
-                            1. / sqrt(direction[1] * direction[1] +
-                                     direction[2] * direction[2]);
+                            rsqrt(direction[1] * direction[1] +
+                                direction[2] * direction[2]);
                         u0y = direction[2] * nrm, u0z = -direction[1] * nrm;
                 }
         }
@@ -2057,8 +2056,7 @@ static __device__ __forceinline__ void gp_fluctuate(const gp_tables & T, const g
                 const double Omega0 = gp_cel_straggling(T, material, e.energy);
                 const double Omega1 = gp_cel_straggling(T, material, k1);
                 double dk12 = 0.5 * dX * (Omega0 + Omega1);
-                const double tmp = dX / Xtot;
-                if (tmp > 5E-02) {
+                if (dX > 5E-02 * Xtot) {
                         const double de1 =
                             gp_cel_energy_loss(T, scheme, material, k1);
                         const double de0 =
@@ -2075,7 +2073,7 @@ static __device__ __forceinline__ void gp_fluctuate(const gp_tables & T, const g
                             (++trials < GP_MAX_REJECTIONS));
                         if (trials == GP_MAX_REJECTIONS)
                                 e.status = GPUMAS_RETURN_INTERNAL_ERROR;
-                        u /= 1.015387;
+                        u *= 1. / 1.015387;
                         k1 += u * dk1;
                 } else if (dk0 >= 1.7320508 * dk1) {
                         const double u = 1.7320508 * (1. - 2. * gp_random(e));
@@ -2503,7 +2501,9 @@ static __device__ __forceinline__ int gp_step(const gp_tables & T, const gp_conf
                 const double p_f =
                     (k1 <= 0) ? momentum : sqrt(k1 * (k1 + 2. * T.mass));
                 const double ti = e.time;
-                e.time += 0.5 * step * T.mass * (1. / momentum + 1. / p_f);
+                /* 1 / momentum + 1 / p_f with one division. */
+                e.time += 0.5 * step * T.mass *
+                    ((momentum + p_f) / (momentum * p_f));
                 if ((time_max > 0.) && (e.time >= time_max)) {
                         event = GPUMAS_EVENT_LIMIT_TIME;
                         e.time = time_max;
