@@ -34,10 +34,19 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-# FP64 operations (DADD, DMUL: 1, DFMA: 2, per thread) per reference step
-# of the rock slab workload, from ncu sass counters of gp_kernel_plain
-# (profiles/gp_kernel_plain_rock_slab.md), frozen.
-F_STEP = None
+# Algorithmic FP64 work of one reference step (one step_transport call,
+# pumas.c:6296-6925, with its share of DEL / EHS work) for the rock slab
+# workload: FP64 flops (DADD, DMUL: 1, DFMA: 2, per thread) counted by ncu
+# on the one thread per event restatement of the algorithm (gp_kernel_plain)
+# over 20 000 rock slab events (5 482 614 steps), frozen here. The pool
+# engine's own executed count over the same events (its four kernels) is
+# reported beside it.
+F_STEP = 680.4
+F_STEP_EXECUTED = 681.7
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum over the four
+# pool kernels) per reference step, from ncu on 200 000 rock slab events;
+# None until captured.
+TRAFFIC_STEP = None
 
 
 def parse():
@@ -324,7 +333,12 @@ def main():
         achieved = F_STEP * steps_total / kernel_s * 1E-12
         roofline = {"bound": "fp64", "achieved": achieved, "peak": peak,
                     "unit": "TFLOP/s", "frac": achieved / peak,
-                    "traffic": None, "f_step": F_STEP,
+                    "traffic": (None if TRAFFIC_STEP is None else
+                                TRAFFIC_STEP * steps_total),
+                    "kernel": "transport of one batch: gp_pool_step, "
+                              "gp_pool_del, gp_pool_polar, gp_pool_ehs",
+                    "f_step": F_STEP,
+                    "f_step_executed": F_STEP_EXECUTED,
                     "peak_source": "measured: DFMA microbenchmark in this "
                                    "process (MEASURED_PEAKS.json has no "
                                    "FP64 figure)"}

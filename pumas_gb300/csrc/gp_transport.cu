@@ -78,7 +78,7 @@ extern "C" int gpumas_context_create(struct gpumas_context ** context,
         c->api.seed = 0;
         c->tuning.engine = 0;
         c->tuning.pool_slots = 1048576;
-        c->tuning.max_inner = 4;
+        c->tuning.max_inner = 8;
         c->tuning.batch = 16;
         if (extra_memory > 0) {
                 c->extra = calloc(1, extra_memory);
