@@ -148,7 +148,7 @@ struct gpumas_physics;
 
 /**
  * Load physics tables from the bytes of a `pumas_physics_dump` stream
- * (pumas.c:2167-2196; replaces pumas_physics_load, pumas.h:948-949) and
+ * (pumas.c:2167-2196; replaces pumas_physics_load, pumas.h:980-981) and
  * upload them to the current CUDA device. The dump must come from an LP64
  * little-endian host (tag 13) with the default DCS models (SSR, SSR, DRSS)
  * for muons; otherwise GPUMAS_RETURN_FORMAT_ERROR or
@@ -159,17 +159,17 @@ int gpumas_physics_load(
 
 /**
  * Upload a live `struct pumas_physics` (returned by the reference's
- * pumas_physics_create or pumas_physics_load, pumas.h:898-949) of this
+ * pumas_physics_create or pumas_physics_load, pumas.h:898-981) of this
  * process. Same checks as gpumas_physics_load.
  */
 int gpumas_physics_upload(
     struct gpumas_physics ** physics, const void * pumas_physics);
 
-/** Release the device image (pumas_physics_destroy, pumas.h:908). */
+/** Release the device image (pumas_physics_destroy, pumas.h:924). */
 void gpumas_physics_destroy(struct gpumas_physics ** physics);
 
 /** Index of a material from its name (pumas_physics_material_index,
- * pumas.h:1468-1469). */
+ * pumas.h:1772-1773). */
 int gpumas_physics_material_index(const struct gpumas_physics * physics,
     const char * name, int * index);
 
@@ -218,7 +218,7 @@ struct gpumas_context {
 int gpumas_context_create(struct gpumas_context ** context,
     const struct gpumas_physics * physics, int extra_memory);
 
-/** Destroy a context and its device buffers (pumas_context_destroy). */
+/** Destroy a context and its device buffers (pumas_context_destroy, pumas.h:1326). */
 void gpumas_context_destroy(struct gpumas_context ** context);
 
 /**
