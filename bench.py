@@ -65,6 +65,22 @@ def parse():
     p.add_argument("--pool-slots", type=int, default=0)
     p.add_argument("--max-inner", type=int, default=0)
     p.add_argument("--batch", type=int, default=0)
+    p.add_argument("--workload", default="rock_slab",
+                   choices=["rock_slab", "slab_jobs", "terrain",
+                            "plain_csda", "serve"])
+    p.add_argument("--jobs", type=int, default=8192)
+    p.add_argument("--job-scale", type=float, default=0.01,
+                   help="slab_jobs: factor on the events per job")
+    p.add_argument("--plain-stride", type=int, default=8,
+                   help="slab_jobs: plain comparison on every n-th job")
+    p.add_argument("--per-direction", type=int, default=10_000,
+                   help="terrain: events per direction")
+    p.add_argument("--rates", default="100,300,1000,3000,10000",
+                   help="serve: Poisson arrival rates (requests/s)")
+    p.add_argument("--serve-seconds", type=float, default=2.0)
+    p.add_argument("--serve-scale", type=float, default=1E-03)
+    p.add_argument("--autotune", action="store_true",
+                   help="slab_jobs: tune the pool on every 8th job first")
     return p.parse_args()
 
 
@@ -206,11 +222,434 @@ def run_reference_arm(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+class DeviceEvents:
+    """Events of several jobs in one device structure of arrays (torch
+    tensors), with a pristine copy to restore them between steps."""
+
+    FIELDS = ("charge", "energy", "distance", "grammage", "time", "weight")
+
+    def __init__(self, states, dev):
+        import numpy as np
+        import torch
+        self.n = len(states)
+        self.cols = {}
+        for f in self.FIELDS:
+            self.cols[f] = torch.from_numpy(
+                np.ascontiguousarray(states[f])).to(dev)
+        for k in range(3):
+            self.cols["position%d" % k] = torch.from_numpy(
+                np.ascontiguousarray(states["position"][:, k])).to(dev)
+            self.cols["direction%d" % k] = torch.from_numpy(
+                np.ascontiguousarray(states["direction"][:, k])).to(dev)
+        self.cols["decayed"] = torch.from_numpy(
+            np.ascontiguousarray(states["decayed"])).to(dev)
+        self.work = {k: v.clone() for k, v in self.cols.items()}
+        self.results = torch.zeros((self.n, 32), dtype=torch.uint8,
+                                   device=dev)
+
+    def restore(self, stream=None):
+        import torch
+        with torch.cuda.stream(stream) if stream is not None else \
+                _nullcontext():
+            for k in self.work:
+                self.work[k].copy_(self.cols[k], non_blocking=True)
+
+    def soa(self, offset=0):
+        w = self.work
+        d = {f: w[f].data_ptr() + 8 * offset for f in self.FIELDS}
+        d["decayed"] = w["decayed"].data_ptr() + 4 * offset
+        d["position"] = [w["position%d" % k].data_ptr() + 8 * offset
+                         for k in range(3)]
+        d["direction"] = [w["direction%d" % k].data_ptr() + 8 * offset
+                          for k in range(3)]
+        d["result"] = self.results.data_ptr() + 32 * offset
+        return d
+
+    def result_records(self):
+        import numpy as np
+        import pumas_gb300 as pg
+        return np.frombuffer(self.results.cpu().numpy().tobytes(),
+                             dtype=pg.RESULT_DTYPE)
+
+    def final_states(self):
+        import numpy as np
+        import pumas_gb300 as pg
+        s = np.zeros(self.n, dtype=pg.STATE_DTYPE)
+        for f in self.FIELDS + ("decayed",):
+            s[f] = self.work[f].cpu().numpy()
+        for k in range(3):
+            s["position"][:, k] = self.work["position%d" % k].cpu().numpy()
+            s["direction"][:, k] = self.work["direction%d" % k].cpu().numpy()
+        return s
+
+
+class _nullcontext:
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        return False
+
+
+def base_line(args, world, metric, value, unit, ms_per_step, config,
+              higher=True):
+    return {"metric": metric, "value": value, "unit": unit,
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms_per_step, "higher_is_better": higher,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": config}
+
+
+def run_slab_jobs(args, rank, world, local):
+    """Batched uneven jobs: every job of the slab-stack workload in one
+    engine run (one pool, CUDA graph batches) against one plain
+    one-thread-per-event launch per job, on the same device-resident
+    events."""
+    import numpy as np
+    import torch
+    import pumas_gb300 as pg
+    from pumas_gb300 import workloads as W
+    dev = torch.device("cuda", local)
+    physics = pg.Physics()
+    jobs = W.slab_jobs(args.jobs, seed=args.seed, event_scale=args.job_scale)
+    t0 = time.perf_counter()
+    ctxs, states, offsets = [], [], []
+    off = 0
+    for k, job in enumerate(jobs):
+        c = pg.Context(physics)
+        W.apply_config(c, W.slab_job_config(job))
+        c.seed = args.seed * 100003 + k
+        c.set_geometry(W.slab_job_geometry(physics, job))
+        ctxs.append(c)
+        states.append(W.slab_job_states(job, seed=args.seed))
+        offsets.append(off)
+        off += job["n"]
+    s0 = np.concatenate(states)
+    ev = DeviceEvents(s0, dev)
+    setup_s = time.perf_counter() - t0
+    spec = [(c, job["n"], None, job["first_event"])
+            for c, job in zip(ctxs, jobs)]
+    tuned = None
+    if args.autotune:
+        from pumas_gb300 import autotune
+
+        def sample_run(eng):
+            ev.restore()
+            eng.run([(c, n, ev.soa(o), fe) for k, ((c, n, _, fe), o) in
+                     enumerate(zip(spec, offsets)) if k % 8 == 0])
+            torch.cuda.synchronize()
+
+        tuned = autotune.tune(physics, sample_run)
+        autotune.save(tuned)
+        args.pool_slots = tuned["pool_slots"]
+        args.max_inner = tuned["max_inner"]
+        args.batch = tuned["batch"]
+    eng = pg.Engine(physics, pool_slots=args.pool_slots,
+                    max_inner=args.max_inner, batch=args.batch,
+                    max_jobs=len(jobs) + 1)
+
+    def batched():
+        ev.restore()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        eng.run([(c, n, ev.soa(o), fe)
+                 for (c, n, _, fe), o in zip(spec, offsets)])
+        torch.cuda.synchronize()
+        return time.perf_counter() - t
+
+    stream = torch.cuda.Stream(device=dev)
+    # The one-launch-per-job comparison runs on every plain_stride-th job
+    # (the plain form takes minutes on the whole set), both ways.
+    sub = list(range(0, len(jobs), args.plain_stride))
+
+    def batched_subset():
+        ev.restore()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        eng.run([(spec[k][0], spec[k][1], ev.soa(offsets[k]), spec[k][3])
+                 for k in sub])
+        torch.cuda.synchronize()
+        return time.perf_counter() - t
+
+    def plain():
+        ev.restore()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for k in sub:
+            c, n, _, fe = spec[k]
+            rc = c.transport_device(n, ev.soa(offsets[k]), fe,
+                                    stream.cuda_stream)
+            if rc != 0:
+                raise RuntimeError("plain transport: %d" % rc)
+        e1.record(stream)
+        stream.synchronize()
+        return e0.elapsed_time(e1) * 1E-03
+
+    for c in ctxs:
+        c.tuning(engine=pg.ENGINE_PLAIN)
+    for _ in range(max(1, args.warmup // 3)):
+        batched()
+    st0 = eng.stats()
+    with ClockSampler(local) as clocks:
+        tb = [batched() for _ in range(args.steps)]
+    st1 = eng.stats()
+    res = ev.result_records()
+    steps_total = float(res["steps"].sum())
+    bad = int(np.count_nonzero(res["status"]))
+    n = len(s0)
+    n_sub = sum(jobs[k]["n"] for k in sub)
+    idx_sub = np.concatenate([np.arange(offsets[k], offsets[k] + jobs[k]["n"])
+                              for k in sub])
+    tbs = batched_subset()
+    tp = plain()
+    res_p = ev.result_records()
+    same = bool(np.array_equal(res_p[idx_sub], res[idx_sub]))
+    tb_m = sum(tb) / len(tb)
+    kernel_ms = (st1["kernel_ms"] - st0["kernel_ms"]) / args.steps
+    peak = fp64_peak_tflops(torch)
+    achieved = F_STEP * steps_total / (kernel_ms * 1E-03) * 1E-12
+    if rank != 0:
+        return
+    line = base_line(args, world, "events/s", world * n / tb_m, "events/s",
+                     tb_m * 1E+03, {
+                         "workload": "slab_jobs: %d uneven jobs, 1-8 slabs "
+                                     "of rock / water / iron, 50/50 "
+                                     "forward / backward, straggled + "
+                                     "mixed" % len(jobs),
+                         "events_per_step": n,
+                         "event_scale": args.job_scale,
+                         "events_per_job": [int(min(j["n"] for j in jobs)),
+                                            int(max(j["n"] for j in jobs))],
+                         "setup_s": setup_s})
+    cpu = None
+    if not args.no_baseline:
+        cpu = slab_jobs_cpu(jobs, ctxs, states, args.seed)
+    line.update({
+        "cpu_baseline": cpu,
+        "impl_detail": "one engine run per step (all jobs in one slot "
+                       "pool, CUDA graph batches)",
+        "steps_per_s": steps_total / tb_m,
+        "steps_per_event": steps_total / n,
+        "event_errors": bad,
+        "plain": {"value": n_sub / tp, "unit": "events/s",
+                  "ms": tp * 1E+03, "jobs": len(sub), "events": n_sub,
+                  "batched_same_jobs": n_sub / tbs,
+                  "detail": "every %d-th job: one gp_kernel_plain launch "
+                            "per job on one stream, against one engine "
+                            "run of the same jobs" % args.plain_stride,
+                  "identical_results": same},
+        "batched_over_plain": tp / tbs,
+        "engine": {"pool_slots": args.pool_slots or 1048576,
+                   "max_inner": args.max_inner or 8,
+                   "batch": args.batch or 16,
+                   "autotuned": None if tuned is None else {
+                       "sample": "every 8th job",
+                       "trials": tuned["trials"]}},
+        "kernel_ms": kernel_ms,
+        "gpu_launches": (st1["launches"] - st0["launches"]) // args.steps,
+        "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak,
+                     "unit": "TFLOP/s", "frac": achieved / peak,
+                     "traffic": None, "f_step": F_STEP},
+        "clocks": clocks.summary()})
+    print(json.dumps(line), flush=True)
+
+
+def slab_jobs_cpu(jobs, ctxs, states, seed, stride=100):
+    """The C restatement with OpenMP over all host cores on every
+    `stride`-th job of the slab-stack workload (a seeded 1 % job subset),
+    scaled to events/s."""
+    import oracle
+    import pumas_gb300 as pg
+    from pumas_gb300 import workloads as W
+    oracle.build_port()
+    port = oracle.Port(pg.default_dump())
+    threads = port.max_threads()
+    n = 0
+    dt = 0.
+    for k in range(0, len(jobs), stride):
+        job = jobs[k]
+        mats = [port.material_index(m) for m in job["materials"]]
+        geo = oracle.make_geometry(
+            1, [(m, 0.) for m in mats], slab_z=job["slab_z"],
+            slab_medium=list(range(len(mats))))
+        cfg = oracle.Config(seed=ctxs[k].seed, **W.slab_job_config(job))
+        t = time.perf_counter()
+        port.transport(cfg, geo, states[k], job["first_event"], threads)
+        dt += time.perf_counter() - t
+        n += job["n"]
+    return {"value": n / dt, "unit": "events/s", "cores": threads,
+            "kind": "port",
+            "sample": "every %d-th job (%d jobs, %d events), %.1f s on %d "
+                      "OpenMP threads, one job after the other"
+                      % (stride, (len(jobs) + stride - 1) // stride, n, dt,
+                         threads)}
+
+
+def run_terrain(args, rank, world, local):
+    """Backward muography over the synthetic terrain: 32 x 64 directions x
+    per-direction events through the context's device entry point."""
+    import numpy as np
+    import torch
+    import pumas_gb300 as pg
+    from pumas_gb300 import workloads as W
+    dev = torch.device("cuda", local)
+    physics = pg.Physics()
+    ctx = pg.Context(physics)
+    W.apply_config(ctx, W.config_dict("terrain"))
+    ctx.seed = args.seed
+    t0 = time.perf_counter()
+    heights = W.terrain_heights()
+    ctx.set_geometry(W.terrain_geometry(physics))
+    dirs = W.terrain_directions()
+    s0, d = W.terrain(args.per_direction, seed=args.seed, heights=heights,
+                      directions=dirs)
+    setup_s = time.perf_counter() - t0
+    ctx.tuning(engine=args.engine, pool_slots=args.pool_slots,
+               max_inner=args.max_inner, batch=args.batch)
+    ev = DeviceEvents(s0, dev)
+    stream = torch.cuda.Stream(device=dev)
+    n = len(s0)
+
+    def step(k):
+        ev.restore(stream)
+        rc = ctx.transport_device(n, ev.soa(), 0, stream.cuda_stream)
+        if rc != 0:
+            raise RuntimeError("transport_device: %d" % rc)
+
+    for k in range(args.warmup):
+        step(k)
+    stream.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clocks:
+        e0.record(stream)
+        for k in range(args.steps):
+            step(k)
+        e1.record(stream)
+        stream.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    res = ev.result_records()
+    fin = ev.final_states()
+    flux = W.terrain_flux(fin, res, d, len(dirs[0]))
+    steps_total = float(res["steps"].sum())
+    st = ctx.stats()
+    peak = fp64_peak_tflops(torch)
+    achieved = F_STEP * steps_total / (st["kernel_ms"] * 1E-03) * 1E-12
+    if rank != 0:
+        return
+    line = base_line(args, world, "events/s", world * n / (ms * 1E-03),
+                     "events/s", ms, {
+                         "workload": "terrain: backward muography, 512 x "
+                                     "512 heightmap (10 m), 32 x 64 "
+                                     "directions x %d events, 1 GeV - "
+                                     "100 TeV, straggled + mixed, "
+                                     "weighted decay, stop at 3 km"
+                                     % args.per_direction,
+                         "events_per_step": n, "setup_s": setup_s})
+    line.update({
+        "steps_per_s": steps_total / (ms * 1E-03),
+        "steps_per_event": steps_total / n,
+        "event_errors": int(np.count_nonzero(res["status"])),
+        "flux_total": float(flux.sum()),
+        "flux_zenith_profile": [float(x) for x in
+                                flux.reshape(32, 64).mean(axis=1)[::4]],
+        "gpu_launches": st["launches"],
+        "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak,
+                     "unit": "TFLOP/s", "frac": achieved / peak,
+                     "traffic": None, "f_step": F_STEP},
+        "clocks": clocks.summary()})
+    print(json.dumps(line), flush=True)
+
+
+def run_plain_csda(args, rank, world, local):
+    """Deterministic CSDA in infinite rock: one thread per event, streaming
+    8 B in and 32 B out per event (HBM roofline)."""
+    import numpy as np
+    import torch
+    import pumas_gb300 as pg
+    from pumas_gb300 import workloads as W
+    dev = torch.device("cuda", local)
+    physics = pg.Physics()
+    ctx = pg.Context(physics)
+    W.plain_csda_config(ctx)
+    ctx.seed = args.seed
+    ctx.set_geometry(pg.Geometry.uniform(
+        physics.material_index("StandardRock")))
+    n = args.events
+    s0 = W.plain_csda(n, seed=args.seed)
+    ev = DeviceEvents(s0, dev)
+    stream = torch.cuda.Stream(device=dev)
+    soa = ev.soa()
+    soa["result"] = None
+
+    def step():
+        with torch.cuda.stream(stream):
+            ev.work["energy"].copy_(ev.cols["energy"], non_blocking=True)
+        rc = ctx.transport_device(n, soa, 0, stream.cuda_stream)
+        if rc != 0:
+            raise RuntimeError("transport_device: %d" % rc)
+
+    for _ in range(args.warmup):
+        step()
+    stream.synchronize()
+    kms = []
+    with ClockSampler(local) as clocks:
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+            kms.append(None)
+        e1.record(stream)
+        stream.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    kernel_ms = ctx.stats()["kernel_ms"]
+    hbm = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))[
+        "hbm_gbs"] if os.path.exists(os.path.join(
+            ROOT, "MEASURED_PEAKS.json")) else 6800.
+    # 8 B in (kinetic energy) + 32 B out (energy, distance, grammage,
+    # time) per event; position z is also written (8 B).
+    algo = 48. * n
+    if rank != 0:
+        return
+    line = base_line(args, world, "events/s", world * n / (ms * 1E-03),
+                     "events/s", ms, {
+                         "workload": "plain_csda: forward CSDA, infinite "
+                                     "StandardRock, mu-, 10 GeV - 10 TeV, "
+                                     "stop at 1 GeV",
+                         "events_per_step": n,
+                         "l2": "state %.1f GB larger than L2"
+                               % (n * 104 / 1E+09)})
+    line.update({
+        "kernel_ms": kernel_ms,
+        "roofline": {"bound": "hbm",
+                     "achieved": algo / (kernel_ms * 1E-03) * 1E-09,
+                     "peak": hbm, "unit": "GB/s",
+                     "frac": algo / (kernel_ms * 1E-03) * 1E-09 / hbm,
+                     "traffic": None,
+                     "algorithmic_bytes_per_event": 48},
+        "gpu_launches": 1, "clocks": clocks.summary()})
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local = dist_info()
     if args.impl == "reference":
         return run_reference_arm(args, rank, world)
+    if args.workload != "rock_slab":
+        import torch
+        import pumas_gb300 as pg
+        torch.cuda.set_device(local)
+        pg.library(build=True)
+        fn = {"slab_jobs": run_slab_jobs, "terrain": run_terrain,
+              "plain_csda": run_plain_csda}.get(args.workload)
+        if fn is None:
+            from pumas_gb300 import serving
+            return serving.bench(args, rank, world, local)
+        return fn(args, rank, world, local)
 
     import numpy as np
     import torch

@@ -298,6 +298,100 @@ int gpumas_context_transport_device_static(struct gpumas_context * context,
     size_t n, const struct gpumas_soa * events, uint64_t first_event,
     int pool_slots, void * stream);
 
+/* ------------------------------------------------------------------------ */
+/* Batched jobs and continuous batching.                                    */
+/* ------------------------------------------------------------------------ */
+
+/*
+ * The reference transports one event per call; a program with many
+ * independent transport jobs (different geometries, modes, limits, seeds
+ * and event counts) calls pumas_context_transport in nested loops over jobs
+ * and events (e.g. examples/pumas/geometry.c:229-313 for one job). An
+ * engine runs all of them in one resident slot pool: the events of every
+ * submitted job share one device event queue, each slot steps the event of
+ * whatever job it took, and a slot freed by a finished event takes the next
+ * queued event, of any job. Jobs can be submitted while others run
+ * (continuous batching): their events join the queue and fill slots as
+ * they free up. Results do not depend on what else runs: event k of a job
+ * always uses the random stream (context seed, first_event + k).
+ */
+
+/** A job whose events are in device memory (structure of arrays). The
+ * context supplies the settings, the geometry and the seed; it must use the
+ * engine's physics and outlive the job, with its geometry unchanged. */
+struct gpumas_job {
+        const struct gpumas_context * context;
+        size_t n;
+        struct gpumas_soa events;
+        uint64_t first_event;
+};
+
+/** A persistent transport engine. */
+struct gpumas_engine;
+
+/**
+ * Create an engine for `physics` with the pool parameters of `tuning` (NULL
+ * or zero fields for defaults: 1 048 576 slots, 8 steps per slot visit, 16
+ * iterations per graph), room for `max_jobs` jobs in flight (0: 65 536) and
+ * a device budget of `state_budget` bytes for the events of jobs submitted
+ * from host memory (0: none). Allocates all of its device memory here.
+ */
+int gpumas_engine_create(struct gpumas_engine ** engine,
+    const struct gpumas_physics * physics,
+    const struct gpumas_tuning * tuning, int max_jobs, size_t state_budget);
+
+/** Wait for the engine's work and release it. */
+void gpumas_engine_destroy(struct gpumas_engine ** engine);
+
+/**
+ * Queue a job whose events are in device memory. Returns its ticket in
+ * *ticket. The job starts running at the next gpumas_engine_step. Returns
+ * GPUMAS_RETURN_MEMORY_ERROR if `max_jobs` jobs are already in flight,
+ * other codes for an invalid context (the checks of pumas.c:3120-3177).
+ */
+int gpumas_engine_submit(struct gpumas_engine * engine,
+    const struct gpumas_job * job, int * ticket);
+
+/**
+ * Queue a job whose events are `pumas_state` records in host memory. The
+ * events are copied into the engine's state budget (136 bytes per event)
+ * and back into `states` (and `results`, if not NULL) when the job
+ * completes, before its ticket is reported. Returns
+ * GPUMAS_RETURN_MEMORY_ERROR, with no side effect, when the budget has no
+ * room for the job now (submit it again after some jobs completed).
+ */
+int gpumas_engine_submit_host(struct gpumas_engine * engine,
+    const struct gpumas_context * context, size_t n,
+    struct gpumas_state * states, struct gpumas_result * results,
+    uint64_t first_event, int * ticket);
+
+/**
+ * Run one batch of pool iterations (one CUDA graph launch) and wait for it.
+ * Tickets of jobs completed since the last call are written to `done` (at
+ * most `max_done`; the rest are reported by the next calls), their number
+ * to *n_done and the number of submitted jobs not yet reported to
+ * *pending. Does nothing on the device when no event is queued or running.
+ */
+int gpumas_engine_step(struct gpumas_engine * engine, int max_done,
+    int * done, int * n_done, int * pending);
+
+/** Submit `n_jobs` device jobs and step until all of them completed (the
+ * batched form: one pool, one event queue, CUDA graph batches). */
+int gpumas_engine_run(struct gpumas_engine * engine, size_t n_jobs,
+    const struct gpumas_job * jobs);
+
+/** Cumulated statistics: kernel launches and device time of the engine's
+ * graph batches since the engine was created. */
+struct gpumas_engine_stats {
+        long long launches;
+        long long batches;
+        double kernel_ms;
+        long long events;
+        size_t budget_used;
+};
+int gpumas_engine_stats(const struct gpumas_engine * engine,
+    struct gpumas_engine_stats * stats);
+
 /** Engine statistics of the last transport call on this context. */
 struct gpumas_stats {
         /** Kernel launches of the call. */

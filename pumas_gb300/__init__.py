@@ -126,6 +126,19 @@ class _Soa(ctypes.Structure):
         ("decayed", ctypes.c_void_p), ("result", ctypes.c_void_p)]
 
 
+class _Job(ctypes.Structure):
+    _fields_ = [("context", ctypes.c_void_p), ("n", ctypes.c_size_t),
+                ("events", _Soa), ("first_event", ctypes.c_uint64)]
+
+
+class _EngineStats(ctypes.Structure):
+    _fields_ = [("launches", ctypes.c_longlong),
+                ("batches", ctypes.c_longlong),
+                ("kernel_ms", ctypes.c_double),
+                ("events", ctypes.c_longlong),
+                ("budget_used", ctypes.c_size_t)]
+
+
 _lib = None
 
 
@@ -169,6 +182,19 @@ def library(build=False):
             ctypes.POINTER(_Context), ctypes.POINTER(_Tuning)]
         lib.gpumas_context_tuning_get.argtypes = [
             ctypes.POINTER(_Context), ctypes.POINTER(_Tuning)]
+        lib.gpumas_engine_create.argtypes = [
+            pp, vp, ctypes.POINTER(_Tuning), i, sz]
+        lib.gpumas_engine_destroy.argtypes = [pp]
+        lib.gpumas_engine_destroy.restype = None
+        lib.gpumas_engine_submit.argtypes = [
+            vp, ctypes.POINTER(_Job), ctypes.POINTER(i)]
+        lib.gpumas_engine_submit_host.argtypes = [
+            vp, ctypes.POINTER(_Context), sz, vp, vp, u64, ctypes.POINTER(i)]
+        lib.gpumas_engine_step.argtypes = [
+            vp, i, ctypes.POINTER(i), ctypes.POINTER(i), ctypes.POINTER(i)]
+        lib.gpumas_engine_run.argtypes = [vp, sz, ctypes.POINTER(_Job)]
+        lib.gpumas_engine_stats.argtypes = [
+            vp, ctypes.POINTER(_EngineStats)]
         lib.gpumas_bench_dfma.argtypes = [ctypes.POINTER(ctypes.c_double)]
         lib.gpumas_random_fill.argtypes = [
             u64, ctypes.c_uint32, u64, u64, sz, vp]
@@ -178,7 +204,10 @@ def library(build=False):
                   "gpumas_context_transport",
                   "gpumas_context_transport_device", "gpumas_context_stats",
                   "gpumas_context_tuning_set", "gpumas_context_tuning_get",
-                  "gpumas_bench_dfma", "gpumas_random_fill"):
+                  "gpumas_bench_dfma", "gpumas_random_fill",
+                  "gpumas_engine_create", "gpumas_engine_submit",
+                  "gpumas_engine_submit_host", "gpumas_engine_step",
+                  "gpumas_engine_run", "gpumas_engine_stats"):
             getattr(lib, f).restype = i
         _lib = lib
     return _lib
@@ -331,14 +360,7 @@ class Context:
 
     def transport_device(self, n, soa, first_event=0, stream=None):
         """Transport n events of a device SoA (dict of device pointers)."""
-        c = _Soa()
-        for k in ("charge", "energy", "distance", "grammage", "time",
-                  "weight", "decayed"):
-            setattr(c, k, soa[k])
-        for k in range(3):
-            c.position[k] = soa["position"][k]
-            c.direction[k] = soa["direction"][k]
-        c.result = soa.get("result", None)
+        c = _soa(soa)
         return self._lib.gpumas_context_transport_device(
             self._ptr, n, ctypes.byref(c), first_event, stream)
 
@@ -361,6 +383,98 @@ class Context:
     def __del__(self):
         if getattr(self, "_ptr", None):
             self._lib.gpumas_context_destroy(ctypes.byref(self._ptr))
+
+
+def _soa(soa):
+    """A gpumas_soa from a dict of device pointers (position and direction
+    as 3-lists, result optional)."""
+    c = _Soa()
+    for k in ("charge", "energy", "distance", "grammage", "time", "weight",
+              "decayed"):
+        setattr(c, k, soa[k])
+    for k in range(3):
+        c.position[k] = soa["position"][k]
+        c.direction[k] = soa["direction"][k]
+    c.result = soa.get("result", None)
+    return c
+
+
+class Engine:
+    """A persistent transport engine (gpumas_engine): many jobs of different
+    contexts in one slot pool, submitted at once (``run``) or while others
+    run (``submit`` / ``submit_host`` then ``step``)."""
+
+    def __init__(self, physics, pool_slots=0, max_inner=0, batch=0,
+                 max_jobs=0, state_budget=0):
+        self.physics = physics
+        self._lib = physics._lib
+        self._ptr = ctypes.c_void_p()
+        t = _Tuning(ENGINE_POOL, pool_slots, max_inner, batch)
+        _check(self._lib.gpumas_engine_create(
+            ctypes.byref(self._ptr), physics._ptr, ctypes.byref(t),
+            max_jobs, state_budget), "gpumas_engine_create")
+        self._host = {}
+
+    @staticmethod
+    def _job(context, n, soa, first_event):
+        return _Job(ctypes.cast(context._ptr, ctypes.c_void_p), n, _soa(soa),
+                    first_event)
+
+    def submit(self, context, n, soa, first_event=0):
+        """Queue a job of n events in device memory; returns its ticket."""
+        job = self._job(context, n, soa, first_event)
+        t = ctypes.c_int()
+        _check(self._lib.gpumas_engine_submit(self._ptr, ctypes.byref(job),
+                                              ctypes.byref(t)),
+               "gpumas_engine_submit")
+        return t.value
+
+    def submit_host(self, context, states, first_event=0):
+        """Queue a job of pumas_state records from host memory (copied into
+        the state budget). Returns its ticket, or None when the budget has
+        no room now. The (states, results) arrays are filled when the
+        ticket is reported done; get them with ``result(ticket)``."""
+        s = np.array(states, dtype=STATE_DTYPE, copy=True, order="C")
+        r = np.zeros(len(s), dtype=RESULT_DTYPE)
+        t = ctypes.c_int()
+        rc = self._lib.gpumas_engine_submit_host(
+            self._ptr, context._ptr, len(s), s.ctypes.data, r.ctypes.data,
+            first_event, ctypes.byref(t))
+        if rc == RETURN_MEMORY_ERROR:
+            return None
+        _check(rc, "gpumas_engine_submit_host")
+        self._host[t.value] = (s, r)
+        return t.value
+
+    def result(self, ticket):
+        """(states, results) of a completed host job (once)."""
+        return self._host.pop(ticket)
+
+    def step(self, max_done=4096):
+        """One graph batch; returns (completed tickets, pending jobs)."""
+        done = (ctypes.c_int * max_done)()
+        nd, pend = ctypes.c_int(), ctypes.c_int()
+        _check(self._lib.gpumas_engine_step(
+            self._ptr, max_done, done, ctypes.byref(nd), ctypes.byref(pend)),
+            "gpumas_engine_step")
+        return list(done[:nd.value]), pend.value
+
+    def run(self, jobs):
+        """Run jobs [(context, n, soa, first_event), ...] to completion."""
+        arr = (_Job * len(jobs))(*[self._job(*j) for j in jobs])
+        _check(self._lib.gpumas_engine_run(self._ptr, len(jobs), arr),
+               "gpumas_engine_run")
+
+    def stats(self):
+        st = _EngineStats()
+        self._lib.gpumas_engine_stats(self._ptr, ctypes.byref(st))
+        return {"launches": st.launches, "batches": st.batches,
+                "kernel_ms": st.kernel_ms, "events": st.events,
+                "budget_used": st.budget_used}
+
+    def __del__(self):
+        if getattr(self, "_ptr", None):
+            self._lib.gpumas_engine_destroy(ctypes.byref(self._ptr))
 
 
 def random_fill(seed, domain, event, first, n):

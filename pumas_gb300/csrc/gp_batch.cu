@@ -43,6 +43,11 @@ namespace cg = cooperative_groups;
 #ifndef GP_POOL_MIN_BLOCKS
 #define GP_POOL_MIN_BLOCKS 1
 #endif
+/* The step kernel runs as one persistent wave: 3 blocks of 128 threads per
+ * SM, i.e. at most 168 registers per thread. */
+#ifndef GP_STEP_MIN_BLOCKS
+#define GP_STEP_MIN_BLOCKS 3
+#endif
 
 /* Field layout of a slot: doubles, ints and 64 bit integers, each as an
  * array of P values. */
@@ -57,7 +62,7 @@ enum gp_slot_int {
         SI_DECAYED, SI_STEP_FIRST, SI_STEP_EVENT, SI_STEP_FORESEEN,
         SI_RANDN_DONE, SI_STEPS, SI_STATUS, SI_MEDIUM, SI_MATERIAL,
         SI_STRAIGHT, SI_STEP_INDEX, SI_NEW_MEDIUM, SI_PHASE, SI_MEDIUM_IN,
-        SI_N_DRAWS, SI_POLAR_PROCESS, SI_POLAR_TARGET, SI_N
+        SI_N_DRAWS, SI_POLAR_PROCESS, SI_POLAR_TARGET, SI_JOB, SI_N
 };
 enum gp_slot_u64 { SU_ID, SU_SRC, SU_N };
 
@@ -73,7 +78,7 @@ struct gp_pool {
 struct gp_counters {
         unsigned long long cursor;
         int active;
-        int pad;
+        int n_done;
         int n_del[2];
         int n_ehs[2];
         int n_polar[2];
@@ -81,34 +86,32 @@ struct gp_counters {
         int step_next[2];
 };
 
-/* Per call launch parameters, read by the kernels from device memory so
- * that one instantiated graph serves every call. */
-struct gp_launch {
+/* A job: events of one context (settings, geometry, random seed), read from
+ * and written back to `io` at their index in the job. The job owns queue
+ * positions [begin, begin + n) of the engine's event queue; event k of the
+ * job uses the random stream of event id first_event + k. */
+struct gp_job {
         gp_config cfg;
+        const gpumas_geometry * geometry;
         gp_io io;
-        size_t n;
+        unsigned long long begin;
+        unsigned long long n;
         uint64_t first_event;
-        int max_inner;
 };
 
-struct gp_pool_state {
-        gp_pool pool;
-        gp_counters * d_counters;
-        gp_counters * h_counters;
-        int * del_list[2];
-        int * ehs_list[2];
-        int * polar_list[2];
-        void * d_mem;
-        size_t capacity;
-        gp_launch * d_launch;
-        gp_launch * h_launch;
-        cudaGraph_t graph;
-        cudaGraphExec_t exec;
-        int graph_batch;
-        const void * graph_tables;
-        const void * graph_geometry;
-        unsigned int step_grid;
+/* Per call launch parameters, read by the kernels from device memory so
+ * that one instantiated graph serves every call: the job table (sorted by
+ * queue position), per job counts of finished events, the list of jobs
+ * completed so far and the end of the queue. */
+struct gp_launch {
+        const gp_job * jobs;
+        unsigned long long * job_done;
+        int * done_list;
+        int n_jobs;
+        int max_inner;
+        unsigned long long total;
 };
+
 
 #define PD(f) pool.d[(size_t)(f) * pool.P + slot]
 #define PI(f) pool.i[(size_t)(f) * pool.P + slot]
@@ -214,26 +217,40 @@ __device__ __forceinline__ void gp_append(int * count, int * list, int slot)
         list[base + g.thread_rank()] = slot;
 }
 
-/* Finish an event: write its state and results back at its input index
- * and free the slot. */
+/* Count a finished event of job `job`; the event that completes the job
+ * appends it to the list of completed jobs. */
+__device__ __forceinline__ void gp_job_event_done(const gp_launch * X,
+    gp_counters * cnt, int job)
+{
+        const unsigned long long k = atomicAdd(&X->job_done[job], 1ull) + 1;
+        if (k == X->jobs[job].n) {
+                const int pos = atomicAdd(&cnt->n_done, 1);
+                X->done_list[pos] = job;
+        }
+}
+
+/* Finish an event: write its state and results back at its index in its
+ * job and free the slot. */
 __device__ __forceinline__ void gp_finish(const gp_pool & pool, int slot,
-    const gp_config & cfg, const gp_io & io, gp_counters * cnt, gp_event & e,
+    const gp_launch * X, const gp_job & J, gp_counters * cnt, gp_event & e,
     int event, int medium_out)
 {
-        gp_stepping_end(cfg, e);
-        io.store((size_t)PU(SU_SRC), e, event, PI(SI_MEDIUM_IN), medium_out);
+        gp_stepping_end(J.cfg, e);
+        J.io.store((size_t)PU(SU_SRC), e, event, PI(SI_MEDIUM_IN),
+            medium_out);
         PI(SI_PHASE) = GP_EMPTY;
         atomicSub(&cnt->active, 1);
+        gp_job_event_done(X, cnt, PI(SI_JOB));
 }
 
 /* Route a slot to its next phase. */
 __device__ __forceinline__ void gp_route(const gp_pool & pool, int slot,
-    const gp_config & cfg, const gp_io & io, gp_counters * cnt,
+    const gp_launch * X, const gp_job & J, gp_counters * cnt,
     int * del_list, int * ehs_list, int parity, int next, gp_event & e,
     gp_loop & L, int event)
 {
         if (next == GP_NEXT_DONE) {
-                gp_finish(pool, slot, cfg, io, cnt, e, event, L.medium);
+                gp_finish(pool, slot, X, J, cnt, e, event, L.medium);
                 return;
         }
         gp_slot_store(pool, slot, e, L);
@@ -244,16 +261,34 @@ __device__ __forceinline__ void gp_route(const gp_pool & pool, int slot,
                 gp_append(&cnt->n_ehs[parity], ehs_list, slot);
 }
 
-/* Refill slot `slot` from the input queue. Events that end before their
- * first step are finished here and the next one is taken. Returns 1 if the
- * slot now holds an event to step (e, L loaded), 0 if the input is empty. */
-static __device__ __forceinline__ int gp_refill(const gp_tables & T,
-    const gp_config & cfg, const gpumas_geometry & g, const gp_io & io,
-    size_t n, uint64_t first_event, const gp_pool & pool, int slot,
-    gp_counters * cnt, gp_event & e, gp_loop & L)
+/* Job owning queue position idx: the last job whose first position is not
+ * above idx (the table is sorted by position and positions between two
+ * jobs are never handed out, see gp_engine_append). */
+__device__ __forceinline__ int gp_job_of(const gp_launch * X,
+    unsigned long long idx)
 {
+        int lo = 0, hi = X->n_jobs;
+        while (hi - lo > 1) {
+                const int mid = (lo + hi) >> 1;
+                if (X->jobs[mid].begin <= idx)
+                        lo = mid;
+                else
+                        hi = mid;
+        }
+        return lo;
+}
+
+/* Refill slot `slot` from the event queue. Events that end before their
+ * first step are finished here and the next one is taken. Returns 1 if the
+ * slot now holds an event to step (e, L loaded, *job set), 0 if the queue
+ * is empty. */
+static __device__ __forceinline__ int gp_refill(const gp_tables & T,
+    const gp_launch * X, const gp_pool & pool, int slot, gp_counters * cnt,
+    gp_event & e, gp_loop & L, int & job)
+{
+        const unsigned long long total = X->total;
         for (;;) {
-                if (*(volatile unsigned long long *)&cnt->cursor >= n)
+                if (*(volatile unsigned long long *)&cnt->cursor >= total)
                         return 0;
                 cg::coalesced_group w = cg::coalesced_threads();
                 unsigned long long base = 0;
@@ -262,18 +297,23 @@ static __device__ __forceinline__ int gp_refill(const gp_tables & T,
                             (unsigned long long)w.size());
                 base = w.shfl(base, 0);
                 const unsigned long long idx = base + w.thread_rank();
-                if (idx >= n) return 0;
-                io.load((size_t)idx, e);
-                gp_event_init(e, cfg.seed, first_event + idx);
+                if (idx >= total) return 0;
+                job = gp_job_of(X, idx);
+                const gp_job & J = X->jobs[job];
+                const unsigned long long k = idx - J.begin;
+                J.io.load((size_t)k, e);
+                gp_event_init(e, J.cfg.seed, J.first_event + k);
                 int medium_in, event = GPUMAS_EVENT_NONE;
                 const int next = gp_transport_begin(
-                    T, cfg, g, e, L, event, medium_in);
+                    T, J.cfg, *J.geometry, e, L, event, medium_in);
                 if (next == GP_NEXT_DONE) {
-                        io.store((size_t)idx, e, event, medium_in, L.medium);
+                        J.io.store((size_t)k, e, event, medium_in, L.medium);
+                        gp_job_event_done(X, cnt, job);
                         continue;
                 }
-                PU(SU_SRC) = idx;
+                PU(SU_SRC) = k;
                 PI(SI_MEDIUM_IN) = medium_in;
+                PI(SI_JOB) = job;
                 atomicAdd(&cnt->active, 1);
                 return 1;
         }
@@ -285,21 +325,17 @@ static __device__ __forceinline__ int gp_refill(const gp_tables & T,
  * to the next phase and takes the next slot. All lanes thus execute the step
  * together until the pool is exhausted, whatever the number of steps of
  * each event. */
-__global__ void __launch_bounds__(128, GP_POOL_MIN_BLOCKS) gp_pool_step(
-    const gp_tables * __restrict__ Tp, const gpumas_geometry * __restrict__ gp,
-    const gp_launch * __restrict__ X, const gp_pool pool, gp_counters * cnt,
-    int * del_list, int * ehs_list, int parity)
+__global__ void __launch_bounds__(128, GP_STEP_MIN_BLOCKS) gp_pool_step(
+    const gp_tables * __restrict__ Tp, const gp_launch * __restrict__ X,
+    const gp_pool pool, gp_counters * cnt, int * del_list, int * ehs_list,
+    int parity)
 {
-        const gp_config & cfg = X->cfg;
-        const gp_io & io = X->io;
-        const size_t n = X->n;
-        const uint64_t first_event = X->first_event;
         const int max_inner = X->max_inner;
         const gp_tables & T = *Tp;
-        const gpumas_geometry & g = *gp;
         int * scursor = &cnt->step_next[parity];
         gp_event e;
         gp_loop L;
+        const gp_job * J = X->jobs;
         int slot = -1, k = 0, exhausted = 0;
         for (long guard = 0; guard < (1L << 40); guard++) {
                 while ((slot < 0) && !exhausted) {
@@ -326,14 +362,17 @@ __global__ void __launch_bounds__(128, GP_POOL_MIN_BLOCKS) gp_pool_step(
                         const int s_ = j;
                         {
                                 const int slot = s_;
+                                int job;
                                 if (PI(SI_PHASE) == GP_EMPTY) {
-                                        if (!gp_refill(T, cfg, g, io, n,
-                                                first_event, pool, slot, cnt,
-                                                e, L))
+                                        if (!gp_refill(T, X, pool, slot, cnt,
+                                                e, L, job))
                                                 continue;
                                 } else {
-                                        gp_slot_load(pool, slot, cfg, e, L);
+                                        job = PI(SI_JOB);
+                                        gp_slot_load(pool, slot,
+                                            X->jobs[job].cfg, e, L);
                                 }
+                                J = X->jobs + job;
                         }
                         slot = s_;
                         k = 0;
@@ -341,11 +380,11 @@ __global__ void __launch_bounds__(128, GP_POOL_MIN_BLOCKS) gp_pool_step(
                 if (!__any_sync(0xFFFFFFFFu, slot >= 0)) break;
                 if (slot >= 0) {
                         int event = GPUMAS_EVENT_NONE;
-                        const int next =
-                            gp_stepping_step(T, cfg, g, e, L, event);
+                        const int next = gp_stepping_step(
+                            T, J->cfg, *J->geometry, e, L, event);
                         k++;
                         if ((next != GP_NEXT_STEP) || (k >= max_inner)) {
-                                gp_route(pool, slot, cfg, io, cnt, del_list,
+                                gp_route(pool, slot, X, *J, cnt, del_list,
                                     ehs_list, parity, next, e, L, event);
                                 slot = -1;
                         }
@@ -362,13 +401,13 @@ __global__ void __launch_bounds__(128, GP_POOL_MIN_BLOCKS) gp_pool_del(
     const gp_pool pool, gp_counters * cnt, const int * __restrict__ list,
     int * polar_list, int parity)
 {
-        const gp_config & cfg = X->cfg;
-        const gp_io & io = X->io;
         const int count = cnt->n_del[parity];
         const gp_tables & T = *Tp;
         for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < count;
              j += gridDim.x * blockDim.x) {
                 const int slot = list[j];
+                const gp_job & J = X->jobs[PI(SI_JOB)];
+                const gp_config & cfg = J.cfg;
                 gp_event e;
                 gp_loop L;
                 gp_slot_load(pool, slot, cfg, e, L);
@@ -388,8 +427,7 @@ __global__ void __launch_bounds__(128, GP_POOL_MIN_BLOCKS) gp_pool_del(
                 gp_do_del_polar(T, e, job);
                 const int next = gp_stepping_del_end(T, cfg, e, L, event);
                 if (next == GP_NEXT_DONE) {
-                        gp_finish(pool, slot, cfg, io, cnt, e, event,
-                            L.medium);
+                        gp_finish(pool, slot, X, J, cnt, e, event, L.medium);
                 } else {
                         gp_slot_store(pool, slot, e, L);
                         PI(SI_PHASE) = GP_NEXT_STEP;
@@ -720,14 +758,13 @@ __global__ void __launch_bounds__(128, GP_POOL_MIN_BLOCKS) gp_pool_polar(
     const gp_pool pool, gp_counters * cnt, const int * __restrict__ list,
     int parity)
 {
-        const gp_config & cfg = X->cfg;
-        const gp_io & io = X->io;
         const int count = cnt->n_polar[parity];
         const gp_tables & T = *Tp;
         int * cursor = &cnt->polar_next[parity];
         gp_event e;
         gp_loop L;
         gp_pn s;
+        const gp_job * J = X->jobs;
         int slot = -1;
         for (int guard = 0; guard < (1 << 30); guard++) {
                 if (slot < 0) {
@@ -736,16 +773,17 @@ __global__ void __launch_bounds__(128, GP_POOL_MIN_BLOCKS) gp_pool_polar(
                                 const int j = atomicAdd(cursor, 1);
                                 if (j >= count) break;
                                 slot = list[j];
-                                gp_slot_load(pool, slot, cfg, e, L);
+                                J = X->jobs + PI(SI_JOB);
+                                gp_slot_load(pool, slot, J->cfg, e, L);
                                 gp_pn_start(T, s, e, PD(SD_POLAR_KI),
                                     PD(SD_POLAR_KF), PI(SI_POLAR_TARGET));
                                 if (s.phase != PN_DONE) break;
                                 gp_rotate(e, s.mu);
                                 int event = GPUMAS_EVENT_NONE;
                                 const int next = gp_stepping_del_end(
-                                    T, cfg, e, L, event);
+                                    T, J->cfg, e, L, event);
                                 if (next == GP_NEXT_DONE) {
-                                        gp_finish(pool, slot, cfg, io, cnt, e,
+                                        gp_finish(pool, slot, X, *J, cnt, e,
                                             event, L.medium);
                                 } else {
                                         gp_slot_store(pool, slot, e, L);
@@ -762,9 +800,9 @@ __global__ void __launch_bounds__(128, GP_POOL_MIN_BLOCKS) gp_pool_polar(
                                 gp_rotate(e, s.mu);
                                 int event = GPUMAS_EVENT_NONE;
                                 const int next = gp_stepping_del_end(
-                                    T, cfg, e, L, event);
+                                    T, J->cfg, e, L, event);
                                 if (next == GP_NEXT_DONE) {
-                                        gp_finish(pool, slot, cfg, io, cnt, e,
+                                        gp_finish(pool, slot, X, *J, cnt, e,
                                             event, L.medium);
                                 } else {
                                         gp_slot_store(pool, slot, e, L);
@@ -781,21 +819,20 @@ __global__ void __launch_bounds__(128, GP_POOL_MIN_BLOCKS) gp_pool_ehs(
     const gp_pool pool, gp_counters * cnt, const int * __restrict__ list,
     int parity)
 {
-        const gp_config & cfg = X->cfg;
-        const gp_io & io = X->io;
         const int count = cnt->n_ehs[parity];
         const gp_tables & T = *Tp;
         for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < count;
              j += gridDim.x * blockDim.x) {
                 const int slot = list[j];
+                const gp_job & J = X->jobs[PI(SI_JOB)];
+                const gp_config & cfg = J.cfg;
                 gp_event e;
                 gp_loop L;
                 gp_slot_load(pool, slot, cfg, e, L);
                 int event = GPUMAS_EVENT_NONE;
                 const int next = gp_stepping_ehs(T, cfg, e, L, event);
                 if (next == GP_NEXT_DONE) {
-                        gp_finish(pool, slot, cfg, io, cnt, e, event,
-                            L.medium);
+                        gp_finish(pool, slot, X, J, cnt, e, event, L.medium);
                 } else {
                         gp_slot_store(pool, slot, e, L);
                         PI(SI_PHASE) = GP_NEXT_STEP;
@@ -804,175 +841,814 @@ __global__ void __launch_bounds__(128, GP_POOL_MIN_BLOCKS) gp_pool_ehs(
 }
 
 /* ------------------------------------------------------------------------ */
-/* Host driver.                                                             */
+/* Pool layout and iterations (host side).                                  */
 /* ------------------------------------------------------------------------ */
-extern "C" void gp_pool_free(struct gp_pool_state * ps)
+
+/* Round a byte count up to 256. */
+static inline size_t gp_align256(size_t n) { return (n + 255) & ~(size_t)255; }
+
+/* Bytes of a pool of P slots: slot fields, the six work lists (DEL, EHS and
+ * photonuclear polar, two parities each), the counters and the launch
+ * descriptor, each 256 byte aligned. */
+static size_t gp_pool_bytes(int P)
 {
-        if (ps == NULL) return;
-        if (ps->exec != NULL) cudaGraphExecDestroy(ps->exec);
-        if (ps->graph != NULL) cudaGraphDestroy(ps->graph);
-        if (ps->d_mem != NULL) cudaFree(ps->d_mem);
-        if (ps->h_counters != NULL) cudaFreeHost(ps->h_counters);
-        if (ps->h_launch != NULL) cudaFreeHost(ps->h_launch);
-        free(ps);
+        return gp_align256((size_t)SD_N * P * sizeof(double)) +
+            gp_align256((size_t)SU_N * P * sizeof(uint64_t)) +
+            gp_align256((size_t)SI_N * P * sizeof(int)) +
+            gp_align256((size_t)6 * P * sizeof(int)) +
+            gp_align256(sizeof(gp_counters)) + gp_align256(sizeof(gp_launch));
 }
 
-static int gp_pool_alloc(gp_context * c, int P)
+/* Device side view of a pool laid out over gp_pool_bytes(P) bytes. */
+struct gp_pool_view {
+        gp_pool pool;
+        int * lists[6];
+        gp_counters * counters;
+        gp_launch * launch;
+};
+
+static void gp_pool_carve(char * base, int P, gp_pool_view * v)
 {
-        gp_pool_state * ps = c->pool;
-        if ((ps != NULL) && (ps->capacity == (size_t)P)) return 0;
-        gp_pool_free(ps);
-        c->pool = NULL;
-        ps = (gp_pool_state *)calloc(1, sizeof(*ps));
-        if (ps == NULL) return GPUMAS_RETURN_MEMORY_ERROR;
-        const size_t sd = (size_t)SD_N * P * sizeof(double);
-        const size_t si = (size_t)SI_N * P * sizeof(int);
-        const size_t su = (size_t)SU_N * P * sizeof(uint64_t);
-        const size_t sl = (size_t)P * sizeof(int);
-        const size_t total = sd + si + su + 6 * sl + 256 + sizeof(gp_launch);
-        int rc = gp_check(cudaMalloc(&ps->d_mem, total));
-        if (rc == 0)
-                rc = gp_check(cudaMallocHost(
-                    (void **)&ps->h_counters, sizeof(gp_counters)));
-        if (rc == 0)
-                rc = gp_check(cudaMallocHost(
-                    (void **)&ps->h_launch, sizeof(gp_launch)));
-        if (rc != 0) {
-                gp_pool_free(ps);
-                return rc;
+        char * p = base;
+        v->pool.P = P;
+        v->pool.d = (double *)p;
+        p += gp_align256((size_t)SD_N * P * sizeof(double));
+        v->pool.u = (uint64_t *)p;
+        p += gp_align256((size_t)SU_N * P * sizeof(uint64_t));
+        v->pool.i = (int *)p;
+        p += gp_align256((size_t)SI_N * P * sizeof(int));
+        for (int k = 0; k < 6; k++) v->lists[k] = (int *)p + (size_t)k * P;
+        p += gp_align256((size_t)6 * P * sizeof(int));
+        v->counters = (gp_counters *)p;
+        p += gp_align256(sizeof(gp_counters));
+        v->launch = (gp_launch *)p;
+}
+
+/* One wave of persistent step blocks on the current device. */
+static unsigned int gp_step_wave(int P, int block)
+{
+        int device = 0, sms = 0, per_sm = 0;
+        cudaGetDevice(&device);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &per_sm, gp_pool_step, block, 0);
+        const unsigned int wave =
+            (unsigned int)(sms * (per_sm > 0 ? per_sm : 1));
+        const unsigned int grid = (P + block - 1) / block;
+        return (wave < grid) ? wave : grid;
+}
+
+/* Launch one pool iteration: continuous steps, DELs, photonuclear polar
+ * angles, hard elastic scatters. Lists 0-1 are the DEL lists, 2-3 the EHS
+ * lists and 4-5 the polar lists of both parities. */
+static void gp_iteration(const gp_tables * d_tables, const gp_pool_view & v,
+    unsigned int grid_step, int parity, cudaStream_t s)
+{
+        const int block = 128;
+        const unsigned int grid = (v.pool.P + block - 1) / block;
+        const unsigned int grid2 = (grid + 3) / 4;
+        int * del_list = v.lists[parity];
+        int * ehs_list = v.lists[2 + parity];
+        int * polar_list = v.lists[4 + parity];
+        gp_pool_step<<<grid_step, block, 0, s>>>(d_tables, v.launch, v.pool,
+            v.counters, del_list, ehs_list, parity);
+        gp_pool_del<<<grid2, block, 0, s>>>(d_tables, v.launch, v.pool,
+            v.counters, del_list, polar_list, parity);
+        gp_pool_polar<<<grid2, block, 0, s>>>(d_tables, v.launch, v.pool,
+            v.counters, polar_list, parity);
+        gp_pool_ehs<<<grid2, block, 0, s>>>(d_tables, v.launch, v.pool,
+            v.counters, ehs_list, parity);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Engine: job table, state budget and graph batches.                       */
+/* ------------------------------------------------------------------------ */
+
+/* First fit allocator of the state budget (host side bookkeeping of one
+ * device allocation), in units of 256 bytes. */
+struct gp_arena {
+        char * base;
+        size_t size;
+        size_t used;
+        /* Free blocks (offset, size), sorted by offset. */
+        size_t * off;
+        size_t * len;
+        int n, cap;
+};
+
+static int gp_arena_alloc(gp_arena * a, size_t size, size_t * offset)
+{
+        size = gp_align256(size);
+        for (int k = 0; k < a->n; k++) {
+                if (a->len[k] >= size) {
+                        *offset = a->off[k];
+                        a->off[k] += size;
+                        a->len[k] -= size;
+                        if (a->len[k] == 0) {
+                                memmove(a->off + k, a->off + k + 1,
+                                    (a->n - k - 1) * sizeof(size_t));
+                                memmove(a->len + k, a->len + k + 1,
+                                    (a->n - k - 1) * sizeof(size_t));
+                                a->n--;
+                        }
+                        a->used += size;
+                        return 1;
+                }
         }
-        char * p = (char *)ps->d_mem;
-        ps->pool.d = (double *)p;
-        ps->pool.u = (uint64_t *)(p + sd);
-        ps->pool.i = (int *)(p + sd + su);
-        ps->del_list[0] = (int *)(p + sd + su + si);
-        ps->del_list[1] = ps->del_list[0] + P;
-        ps->ehs_list[0] = ps->del_list[1] + P;
-        ps->ehs_list[1] = ps->ehs_list[0] + P;
-        ps->polar_list[0] = ps->ehs_list[1] + P;
-        ps->polar_list[1] = ps->polar_list[0] + P;
-        ps->d_counters = (gp_counters *)(ps->polar_list[1] + P);
-        ps->d_launch = (gp_launch *)((char *)ps->d_counters + 256);
-        ps->pool.P = P;
-        ps->capacity = P;
-        {
-                /* One wave of persistent step blocks. */
-                int device = 0, sms = 0, per_sm = 0;
-                cudaGetDevice(&device);
-                cudaDeviceGetAttribute(
-                    &sms, cudaDevAttrMultiProcessorCount, device);
-                cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                    &per_sm, gp_pool_step, 128, 0);
-                ps->step_grid = (unsigned int)(sms * (per_sm > 0 ? per_sm : 1));
-        }
-        c->pool = ps;
         return 0;
 }
 
-static void gp_iteration(gp_context * c, int parity, int block,
-    cudaStream_t s)
+static int gp_arena_free(gp_arena * a, size_t offset, size_t size)
 {
-        gp_pool_state * ps = c->pool;
-        const int P = ps->pool.P;
-        const unsigned int grid = (P + block - 1) / block;
-        const unsigned int grid_step =
-            (ps->step_grid > 0) && (ps->step_grid < grid) ? ps->step_grid :
-                                                             grid;
-        gp_pool_step<<<grid_step, block, 0, s>>>(c->d_tables, c->d_geometry,
-            ps->d_launch, ps->pool, ps->d_counters, ps->del_list[parity],
-            ps->ehs_list[parity], parity);
-        const unsigned int grid2 = (grid + 3) / 4;
-        gp_pool_del<<<grid2, block, 0, s>>>(c->d_tables, ps->d_launch,
-            ps->pool, ps->d_counters, ps->del_list[parity],
-            ps->polar_list[parity], parity);
-        gp_pool_polar<<<grid2, block, 0, s>>>(c->d_tables, ps->d_launch,
-            ps->pool, ps->d_counters, ps->polar_list[parity], parity);
-        gp_pool_ehs<<<grid2, block, 0, s>>>(c->d_tables, ps->d_launch,
-            ps->pool, ps->d_counters, ps->ehs_list[parity], parity);
+        size = gp_align256(size);
+        int k = 0;
+        while ((k < a->n) && (a->off[k] < offset)) k++;
+        const int merge_prev = (k > 0) && (a->off[k - 1] + a->len[k - 1] ==
+                                              offset);
+        const int merge_next = (k < a->n) && (offset + size == a->off[k]);
+        if (merge_prev && merge_next) {
+                a->len[k - 1] += size + a->len[k];
+                memmove(a->off + k, a->off + k + 1,
+                    (a->n - k - 1) * sizeof(size_t));
+                memmove(a->len + k, a->len + k + 1,
+                    (a->n - k - 1) * sizeof(size_t));
+                a->n--;
+        } else if (merge_prev) {
+                a->len[k - 1] += size;
+        } else if (merge_next) {
+                a->off[k] = offset;
+                a->len[k] += size;
+        } else {
+                if (a->n == a->cap) {
+                        const int cap = 2 * a->cap + 16;
+                        size_t * off = (size_t *)realloc(
+                            a->off, cap * sizeof(size_t));
+                        if (off == NULL) return GPUMAS_RETURN_MEMORY_ERROR;
+                        a->off = off;
+                        size_t * len = (size_t *)realloc(
+                            a->len, cap * sizeof(size_t));
+                        if (len == NULL) return GPUMAS_RETURN_MEMORY_ERROR;
+                        a->len = len;
+                        a->cap = cap;
+                }
+                memmove(a->off + k + 1, a->off + k,
+                    (a->n - k) * sizeof(size_t));
+                memmove(a->len + k + 1, a->len + k,
+                    (a->n - k) * sizeof(size_t));
+                a->off[k] = offset;
+                a->len[k] = size;
+                a->n++;
+        }
+        a->used -= size;
+        return GPUMAS_RETURN_SUCCESS;
 }
 
-/* Transport n events of `io` with the slot pool. Returns the number of
- * kernel launches in *launches. */
-extern "C" int gp_pool_transport(gp_context * c, const gp_config * cfg_,
-    const gp_io * io_, size_t n, uint64_t first, cudaStream_t s,
+/* Host side record of a job in flight. */
+struct gp_job_host {
+        int ticket;
+        /* Jobs submitted from host memory: their records in the budget. */
+        gpumas_state * states;
+        gpumas_result * results;
+        size_t offset, bytes;
+        int in_arena;
+};
+
+struct gpumas_engine {
+        const struct gpumas_physics * physics;
+        gp_tables * d_tables;  /* owned unless borrowed from a context */
+        int own_tables;
+        gp_tuning tuning;
+        cudaStream_t stream;
+        int own_stream;
+        /* Pool. */
+        void * d_pool;
+        int P;
+        gp_pool_view view;
+        unsigned int grid_step;
+        cudaGraph_t graph;
+        cudaGraphExec_t exec;
+        int graph_iters;
+        /* Jobs: device table, completion counts and list. */
+        int capacity;
+        gp_job * d_jobs;
+        unsigned long long * d_job_done;
+        int * d_done_list;
+        gp_job * h_jobs;
+        gp_job_host * h_info;
+        int n_jobs;      /* jobs in the table */
+        int n_uploaded;  /* jobs of the table already on the device */
+        int n_reported;  /* entries of the completion list already read */
+        int ticket0;     /* ticket of table entry 0 */
+        int inflight;    /* jobs of the table not yet seen completed */
+        unsigned long long total;  /* end of the event queue */
+        int busy;        /* events queued or in slots */
+        /* Tickets completed and not yet reported. */
+        int * fifo;
+        int fifo_head, fifo_n, fifo_cap;
+        /* Pinned mirrors. */
+        gp_counters * h_counters;
+        gp_launch * h_launch;
+        int * h_done;
+        /* State budget. */
+        gp_arena arena;
+        /* Statistics. */
+        cudaEvent_t t0, t1;
+        struct gpumas_engine_stats stats;
+};
+
+static int gp_fifo_push(gpumas_engine * g, int ticket)
+{
+        if (g->fifo_n == g->fifo_cap) {
+                const int cap = 2 * g->fifo_cap + 64;
+                int * f = (int *)malloc(cap * sizeof(int));
+                if (f == NULL) return GPUMAS_RETURN_MEMORY_ERROR;
+                for (int k = 0; k < g->fifo_n; k++)
+                        f[k] = g->fifo[(g->fifo_head + k) % g->fifo_cap];
+                free(g->fifo);
+                g->fifo = f;
+                g->fifo_head = 0;
+                g->fifo_cap = cap;
+        }
+        g->fifo[(g->fifo_head + g->fifo_n) % g->fifo_cap] = ticket;
+        g->fifo_n++;
+        return GPUMAS_RETURN_SUCCESS;
+}
+
+/* (Re)allocate the pool for P slots; the graph is rebuilt. */
+static int gp_engine_pool(gpumas_engine * g, int P)
+{
+        if ((g->d_pool != NULL) && (g->P == P)) return GPUMAS_RETURN_SUCCESS;
+        if (g->exec != NULL) cudaGraphExecDestroy(g->exec);
+        if (g->graph != NULL) cudaGraphDestroy(g->graph);
+        g->exec = NULL;
+        g->graph = NULL;
+        if (g->d_pool != NULL) cudaFree(g->d_pool);
+        g->d_pool = NULL;
+        g->P = 0;
+        int rc = gp_check(cudaMalloc(&g->d_pool, gp_pool_bytes(P)));
+        if (rc != GPUMAS_RETURN_SUCCESS) return rc;
+        g->P = P;
+        gp_pool_carve((char *)g->d_pool, P, &g->view);
+        if (g->h_counters != NULL) memset(g->h_counters, 0,
+            sizeof(gp_counters));
+        g->grid_step = gp_step_wave(P, 128);
+        rc = gp_check(cudaMemsetAsync(g->view.pool.i + (size_t)SI_PHASE * P,
+            0, (size_t)P * sizeof(int), g->stream));
+        if (rc == GPUMAS_RETURN_SUCCESS)
+                rc = gp_check(cudaMemsetAsync(g->view.counters, 0,
+                    sizeof(gp_counters), g->stream));
+        return rc;
+}
+
+/* Capture `iters` iterations (an even number, for the list parity) as a
+ * CUDA graph, once per pool. */
+static int gp_engine_graph(gpumas_engine * g)
+{
+        const int batch = (g->tuning.batch > 0) ? g->tuning.batch : 16;
+        const int iters = 2 * ((batch + 1) / 2);
+        if ((g->exec != NULL) && (g->graph_iters == iters))
+                return GPUMAS_RETURN_SUCCESS;
+        if (g->exec != NULL) cudaGraphExecDestroy(g->exec);
+        if (g->graph != NULL) cudaGraphDestroy(g->graph);
+        g->exec = NULL;
+        g->graph = NULL;
+        cudaStream_t cap;
+        int rc = gp_check(cudaStreamCreateWithFlags(
+            &cap, cudaStreamNonBlocking));
+        if (rc != GPUMAS_RETURN_SUCCESS) return rc;
+        rc = gp_check(cudaStreamBeginCapture(
+            cap, cudaStreamCaptureModeThreadLocal));
+        if (rc == GPUMAS_RETURN_SUCCESS) {
+                for (int k = 0; k < iters; k++)
+                        gp_iteration(g->d_tables, g->view, g->grid_step,
+                            k & 1, cap);
+                rc = gp_check(cudaStreamEndCapture(cap, &g->graph));
+        }
+        if (rc == GPUMAS_RETURN_SUCCESS)
+                rc = gp_check(cudaGraphInstantiate(&g->exec, g->graph, 0));
+        cudaStreamDestroy(cap);
+        if (rc == GPUMAS_RETURN_SUCCESS) g->graph_iters = iters;
+        return rc;
+}
+
+static void gp_engine_free(gpumas_engine * g)
+{
+        if (g->exec != NULL) cudaGraphExecDestroy(g->exec);
+        if (g->graph != NULL) cudaGraphDestroy(g->graph);
+        if (g->d_pool != NULL) cudaFree(g->d_pool);
+        if (g->d_jobs != NULL) cudaFree(g->d_jobs);
+        if (g->own_tables && (g->d_tables != NULL)) cudaFree(g->d_tables);
+        if (g->arena.base != NULL) cudaFree(g->arena.base);
+        if (g->h_counters != NULL) cudaFreeHost(g->h_counters);
+        if (g->h_launch != NULL) cudaFreeHost(g->h_launch);
+        if (g->h_done != NULL) cudaFreeHost(g->h_done);
+        if (g->own_stream && (g->stream != NULL))
+                cudaStreamDestroy(g->stream);
+        if (g->t0 != NULL) cudaEventDestroy(g->t0);
+        if (g->t1 != NULL) cudaEventDestroy(g->t1);
+        free(g->h_jobs);
+        free(g->h_info);
+        free(g->fifo);
+        free(g->arena.off);
+        free(g->arena.len);
+        free(g);
+}
+
+/* Create an engine. `d_tables` may borrow an existing device copy of the
+ * tables (the context path); `stream` may be NULL for an own stream. */
+static int gp_engine_new(gpumas_engine ** out,
+    const struct gpumas_physics * physics, gp_tables * d_tables,
+    const gp_tuning * tuning, int max_jobs, size_t budget)
+{
+        *out = NULL;
+        gpumas_engine * g = (gpumas_engine *)calloc(1, sizeof(*g));
+        if (g == NULL) return GPUMAS_RETURN_MEMORY_ERROR;
+        g->physics = physics;
+        g->tuning = *tuning;
+        g->capacity = max_jobs;
+        int rc = gp_check(cudaStreamCreateWithFlags(
+            &g->stream, cudaStreamNonBlocking));
+        g->own_stream = 1;
+        if ((rc == GPUMAS_RETURN_SUCCESS) && (d_tables == NULL)) {
+                gp_tables tables;
+                gp_physics_tables(physics, &tables);
+                rc = gp_check(cudaMalloc(&g->d_tables, sizeof(gp_tables)));
+                g->own_tables = 1;
+                if (rc == GPUMAS_RETURN_SUCCESS)
+                        rc = gp_check(cudaMemcpy(g->d_tables, &tables,
+                            sizeof(gp_tables), cudaMemcpyHostToDevice));
+        } else {
+                g->d_tables = d_tables;
+        }
+        /* Job table, completion counts and list in one allocation. */
+        const size_t o_done = gp_align256((size_t)max_jobs * sizeof(gp_job));
+        const size_t o_list = o_done + gp_align256(
+            (size_t)max_jobs * sizeof(unsigned long long));
+        const size_t jbytes = o_list + (size_t)max_jobs * sizeof(int);
+        if (rc == GPUMAS_RETURN_SUCCESS)
+                rc = gp_check(cudaMalloc((void **)&g->d_jobs, jbytes));
+        if (rc == GPUMAS_RETURN_SUCCESS) {
+                g->d_job_done = (unsigned long long *)((char *)g->d_jobs +
+                    o_done);
+                g->d_done_list = (int *)((char *)g->d_jobs + o_list);
+                g->h_jobs = (gp_job *)calloc(max_jobs, sizeof(gp_job));
+                g->h_info = (gp_job_host *)calloc(
+                    max_jobs, sizeof(gp_job_host));
+                if ((g->h_jobs == NULL) || (g->h_info == NULL))
+                        rc = GPUMAS_RETURN_MEMORY_ERROR;
+        }
+        if (rc == GPUMAS_RETURN_SUCCESS)
+                rc = gp_check(cudaMallocHost(
+                    (void **)&g->h_counters, sizeof(gp_counters)));
+        if (rc == GPUMAS_RETURN_SUCCESS)
+                rc = gp_check(cudaMallocHost(
+                    (void **)&g->h_launch, sizeof(gp_launch)));
+        if (rc == GPUMAS_RETURN_SUCCESS)
+                rc = gp_check(cudaMallocHost(
+                    (void **)&g->h_done, (size_t)max_jobs * sizeof(int)));
+        if ((rc == GPUMAS_RETURN_SUCCESS) && (budget > 0)) {
+                budget = budget & ~(size_t)255;
+                rc = gp_check(cudaMalloc((void **)&g->arena.base, budget));
+                if (rc == GPUMAS_RETURN_SUCCESS) {
+                        g->arena.size = budget;
+                        g->arena.cap = 16;
+                        g->arena.off = (size_t *)malloc(16 * sizeof(size_t));
+                        g->arena.len = (size_t *)malloc(16 * sizeof(size_t));
+                        if ((g->arena.off == NULL) || (g->arena.len == NULL))
+                                rc = GPUMAS_RETURN_MEMORY_ERROR;
+                        else {
+                                g->arena.off[0] = 0;
+                                g->arena.len[0] = budget;
+                                g->arena.n = 1;
+                        }
+                }
+        }
+        if (rc == GPUMAS_RETURN_SUCCESS)
+                rc = gp_check(cudaEventCreate(&g->t0));
+        if (rc == GPUMAS_RETURN_SUCCESS)
+                rc = gp_check(cudaEventCreate(&g->t1));
+        if (rc == GPUMAS_RETURN_SUCCESS) {
+                const int P = (tuning->pool_slots > 0) ? tuning->pool_slots :
+                                                         1048576;
+                rc = gp_engine_pool(g, (P + 127) / 128 * 128);
+        }
+        if (rc == GPUMAS_RETURN_SUCCESS)
+                rc = gp_check(cudaStreamSynchronize(g->stream));
+        if (rc != GPUMAS_RETURN_SUCCESS) {
+                gp_engine_free(g);
+                return rc;
+        }
+        *out = g;
+        return GPUMAS_RETURN_SUCCESS;
+}
+
+/* Start a new job table when nothing is in flight (queue positions,
+ * completion counts and list restart at 0). */
+static int gp_engine_restart(gpumas_engine * g)
+{
+        if ((g->inflight > 0) || g->busy || (g->n_jobs == 0))
+                return GPUMAS_RETURN_SUCCESS;
+        g->ticket0 += g->n_jobs;
+        g->n_jobs = 0;
+        g->n_uploaded = 0;
+        g->n_reported = 0;
+        g->total = 0;
+        memset(g->h_counters, 0, sizeof(gp_counters));
+        return gp_check(cudaMemsetAsync(
+            g->view.counters, 0, sizeof(gp_counters), g->stream));
+}
+
+/* Append a job to the table. Queue positions handed out before (and
+ * burned by lanes that found the queue empty) are skipped: the job starts
+ * at the larger of the queue end and the cursor read after the last batch,
+ * so that no lane can ever be given a position between two jobs. */
+static int gp_engine_append(gpumas_engine * g, const gp_config & cfg,
+    const gpumas_geometry * geometry, const gp_io & io, size_t n,
+    uint64_t first_event, const gp_job_host & info, int * ticket)
+{
+        gp_job & J = g->h_jobs[g->n_jobs];
+        memset(&J, 0, sizeof(J));
+        J.cfg = cfg;
+        J.geometry = geometry;
+        J.io = io;
+        unsigned long long begin = g->total;
+        if (g->h_counters->cursor > begin) begin = g->h_counters->cursor;
+        J.begin = begin;
+        J.n = n;
+        J.first_event = first_event;
+        g->total = begin + n;
+        g->h_info[g->n_jobs] = info;
+        g->h_info[g->n_jobs].ticket = g->ticket0 + g->n_jobs;
+        *ticket = g->ticket0 + g->n_jobs;
+        g->n_jobs++;
+        g->stats.events += (long long)n;
+        if (n == 0) {
+                /* Never seen by the device: completed now. */
+                return gp_fifo_push(g, *ticket);
+        }
+        g->inflight++;
+        g->busy = 1;
+        return GPUMAS_RETURN_SUCCESS;
+}
+
+extern "C" int gp_config_check(const struct gpumas_context * context,
+    const struct gpumas_physics * physics, gp_config * cfg);
+
+/* Checks and settings of a job's context. */
+static int gp_engine_context(gpumas_engine * g,
+    const struct gpumas_context * context, gp_config * cfg,
+    const gpumas_geometry ** geometry)
+{
+        if (context == NULL) return GPUMAS_RETURN_VALUE_ERROR;
+        const gp_context * c = (const gp_context *)context;
+        if (c->physics != g->physics) return GPUMAS_RETURN_PHYSICS_ERROR;
+        if (!c->has_geometry) return GPUMAS_RETURN_MEDIUM_ERROR;
+        const int rc = gp_config_check(context, c->physics, cfg);
+        if (rc != GPUMAS_RETURN_SUCCESS) return rc;
+        *geometry = c->d_geometry;
+        return GPUMAS_RETURN_SUCCESS;
+}
+
+/* One graph batch on the engine's stream, then the completions. */
+static int gp_engine_batch(gpumas_engine * g)
+{
+        cudaStream_t s = g->stream;
+        int rc = GPUMAS_RETURN_SUCCESS;
+        if (g->n_uploaded < g->n_jobs) {
+                const int k0 = g->n_uploaded, k = g->n_jobs - g->n_uploaded;
+                rc = gp_check(cudaMemcpyAsync(g->d_jobs + k0, g->h_jobs + k0,
+                    (size_t)k * sizeof(gp_job), cudaMemcpyHostToDevice, s));
+                if (rc == GPUMAS_RETURN_SUCCESS)
+                        rc = gp_check(cudaMemsetAsync(g->d_job_done + k0, 0,
+                            (size_t)k * sizeof(unsigned long long), s));
+                if (rc != GPUMAS_RETURN_SUCCESS) return rc;
+                g->n_uploaded = g->n_jobs;
+        }
+        if (g->busy) {
+                gp_launch * h = g->h_launch;
+                h->jobs = g->d_jobs;
+                h->job_done = g->d_job_done;
+                h->done_list = g->d_done_list;
+                h->n_jobs = g->n_jobs;
+                h->max_inner = (g->tuning.max_inner > 0) ?
+                    g->tuning.max_inner : 8;
+                h->total = g->total;
+                rc = gp_check(cudaMemcpyAsync(g->view.launch, h,
+                    sizeof(gp_launch), cudaMemcpyHostToDevice, s));
+                if (rc == GPUMAS_RETURN_SUCCESS) rc = gp_engine_graph(g);
+                if (rc != GPUMAS_RETURN_SUCCESS) return rc;
+                cudaEventRecord(g->t0, s);
+                rc = gp_check(cudaGraphLaunch(g->exec, s));
+                cudaEventRecord(g->t1, s);
+                if (rc != GPUMAS_RETURN_SUCCESS) return rc;
+                g->stats.launches += 4 * g->graph_iters;
+                g->stats.batches++;
+        }
+        rc = gp_check(cudaMemcpyAsync(g->h_counters, g->view.counters,
+            sizeof(gp_counters), cudaMemcpyDeviceToHost, s));
+        if (rc == GPUMAS_RETURN_SUCCESS)
+                rc = gp_check(cudaStreamSynchronize(s));
+        if (rc != GPUMAS_RETURN_SUCCESS) return rc;
+        if (g->busy) {
+                float ms = 0.f;
+                if (cudaEventElapsedTime(&ms, g->t0, g->t1) == cudaSuccess)
+                        g->stats.kernel_ms += ms;
+        }
+        g->busy = !((g->h_counters->cursor >= g->total) &&
+            (g->h_counters->active == 0));
+
+        /* Jobs completed during the batch, in completion order. */
+        const int nd = g->h_counters->n_done;
+        if (nd > g->n_reported) {
+                const int k0 = g->n_reported, k = nd - g->n_reported;
+                rc = gp_check(cudaMemcpyAsync(g->h_done + k0,
+                    g->d_done_list + k0, (size_t)k * sizeof(int),
+                    cudaMemcpyDeviceToHost, s));
+                if (rc == GPUMAS_RETURN_SUCCESS)
+                        rc = gp_check(cudaStreamSynchronize(s));
+                if (rc != GPUMAS_RETURN_SUCCESS) return rc;
+                int copies = 0;
+                for (int q = k0; q < nd; q++) {
+                        const int j = g->h_done[q];
+                        const gp_job_host & info = g->h_info[j];
+                        if (!info.in_arena) continue;
+                        const gp_job & J = g->h_jobs[j];
+                        rc = gp_check(cudaMemcpyAsync(info.states,
+                            J.io.aos.states, J.n * sizeof(gpumas_state),
+                            cudaMemcpyDeviceToHost, s));
+                        if ((rc == GPUMAS_RETURN_SUCCESS) &&
+                            (info.results != NULL))
+                                rc = gp_check(cudaMemcpyAsync(info.results,
+                                    J.io.aos.results,
+                                    J.n * sizeof(gpumas_result),
+                                    cudaMemcpyDeviceToHost, s));
+                        if (rc != GPUMAS_RETURN_SUCCESS) return rc;
+                        copies++;
+                }
+                if (copies > 0) {
+                        rc = gp_check(cudaStreamSynchronize(s));
+                        if (rc != GPUMAS_RETURN_SUCCESS) return rc;
+                }
+                for (int q = k0; q < nd; q++) {
+                        const int j = g->h_done[q];
+                        gp_job_host & info = g->h_info[j];
+                        if (info.in_arena) {
+                                rc = gp_arena_free(
+                                    &g->arena, info.offset, info.bytes);
+                                if (rc != GPUMAS_RETURN_SUCCESS) return rc;
+                                info.in_arena = 0;
+                        }
+                        rc = gp_fifo_push(g, info.ticket);
+                        if (rc != GPUMAS_RETURN_SUCCESS) return rc;
+                        g->inflight--;
+                }
+                g->n_reported = nd;
+        }
+        return gp_engine_restart(g);
+}
+
+extern "C" void gpumas_engine_destroy(struct gpumas_engine ** engine)
+{
+        if ((engine == NULL) || (*engine == NULL)) return;
+        gpumas_engine * g = *engine;
+        if (g->stream != NULL) cudaStreamSynchronize(g->stream);
+        gp_engine_free(g);
+        *engine = NULL;
+}
+
+extern "C" int gpumas_engine_create(struct gpumas_engine ** engine,
+    const struct gpumas_physics * physics,
+    const struct gpumas_tuning * tuning, int max_jobs, size_t state_budget)
+{
+        if (engine == NULL) return GPUMAS_RETURN_VALUE_ERROR;
+        *engine = NULL;
+        if (physics == NULL) return GPUMAS_RETURN_PHYSICS_ERROR;
+        if (max_jobs < 0) return GPUMAS_RETURN_VALUE_ERROR;
+        gp_tuning t;
+        t.engine = 2;
+        t.pool_slots = 1048576;
+        t.max_inner = 8;
+        t.batch = 16;
+        if (tuning != NULL) {
+                if ((tuning->pool_slots < 0) || (tuning->max_inner < 0) ||
+                    (tuning->batch < 0))
+                        return GPUMAS_RETURN_VALUE_ERROR;
+                if (tuning->pool_slots > 0) t.pool_slots = tuning->pool_slots;
+                if (tuning->max_inner > 0) t.max_inner = tuning->max_inner;
+                if (tuning->batch > 0) t.batch = tuning->batch;
+        }
+        if (t.pool_slots < 128) t.pool_slots = 128;
+        return gp_engine_new(engine, physics, NULL, &t,
+            (max_jobs > 0) ? max_jobs : 65536, state_budget);
+}
+
+/* Room for one more job in the table. */
+static int gp_engine_room(gpumas_engine * g)
+{
+        if (g->n_jobs < g->capacity) return GPUMAS_RETURN_SUCCESS;
+        const int rc = gp_engine_restart(g);
+        if (rc != GPUMAS_RETURN_SUCCESS) return rc;
+        return (g->n_jobs < g->capacity) ? GPUMAS_RETURN_SUCCESS :
+                                           GPUMAS_RETURN_MEMORY_ERROR;
+}
+
+extern "C" int gpumas_engine_submit(struct gpumas_engine * engine,
+    const struct gpumas_job * job, int * ticket)
+{
+        if ((engine == NULL) || (job == NULL) || (ticket == NULL))
+                return GPUMAS_RETURN_VALUE_ERROR;
+        gpumas_engine * g = engine;
+        gp_config cfg;
+        const gpumas_geometry * geometry;
+        int rc = gp_engine_context(g, job->context, &cfg, &geometry);
+        if (rc != GPUMAS_RETURN_SUCCESS) return rc;
+        if (job->n > 0) {
+                const gpumas_soa & a = job->events;
+                if ((a.charge == NULL) || (a.energy == NULL) ||
+                    (a.distance == NULL) || (a.grammage == NULL) ||
+                    (a.time == NULL) || (a.weight == NULL) ||
+                    (a.position[0] == NULL) || (a.position[1] == NULL) ||
+                    (a.position[2] == NULL) || (a.direction[0] == NULL) ||
+                    (a.direction[1] == NULL) || (a.direction[2] == NULL) ||
+                    (a.decayed == NULL))
+                        return GPUMAS_RETURN_VALUE_ERROR;
+        }
+        rc = gp_engine_room(g);
+        if (rc != GPUMAS_RETURN_SUCCESS) return rc;
+        gp_io io;
+        memset(&io, 0, sizeof(io));
+        io.soa.a = job->events;
+        gp_job_host info;
+        memset(&info, 0, sizeof(info));
+        return gp_engine_append(g, cfg, geometry, io, job->n,
+            job->first_event, info, ticket);
+}
+
+extern "C" int gpumas_engine_submit_host(struct gpumas_engine * engine,
+    const struct gpumas_context * context, size_t n,
+    struct gpumas_state * states, struct gpumas_result * results,
+    uint64_t first_event, int * ticket)
+{
+        if ((engine == NULL) || (ticket == NULL) ||
+            ((n > 0) && (states == NULL)))
+                return GPUMAS_RETURN_VALUE_ERROR;
+        gpumas_engine * g = engine;
+        gp_config cfg;
+        const gpumas_geometry * geometry;
+        int rc = gp_engine_context(g, context, &cfg, &geometry);
+        if (rc != GPUMAS_RETURN_SUCCESS) return rc;
+        rc = gp_engine_room(g);
+        if (rc != GPUMAS_RETURN_SUCCESS) return rc;
+        gp_job_host info;
+        memset(&info, 0, sizeof(info));
+        gp_io io;
+        memset(&io, 0, sizeof(io));
+        if (n > 0) {
+                const size_t bs = gp_align256(n * sizeof(gpumas_state));
+                const size_t bytes = bs + n * sizeof(gpumas_result);
+                size_t offset;
+                if ((g->arena.base == NULL) ||
+                    !gp_arena_alloc(&g->arena, bytes, &offset))
+                        return GPUMAS_RETURN_MEMORY_ERROR;
+                io.aos.states = (gpumas_state *)(g->arena.base + offset);
+                io.aos.results = (gpumas_result *)(g->arena.base + offset +
+                    bs);
+                rc = gp_check(cudaMemcpyAsync(io.aos.states, states,
+                    n * sizeof(gpumas_state), cudaMemcpyHostToDevice,
+                    g->stream));
+                if (rc != GPUMAS_RETURN_SUCCESS) {
+                        gp_arena_free(&g->arena, offset, bytes);
+                        return rc;
+                }
+                info.states = states;
+                info.results = results;
+                info.offset = offset;
+                info.bytes = bytes;
+                info.in_arena = 1;
+        }
+        return gp_engine_append(g, cfg, geometry, io, n, first_event, info,
+            ticket);
+}
+
+extern "C" int gpumas_engine_step(struct gpumas_engine * engine,
+    int max_done, int * done, int * n_done, int * pending)
+{
+        if ((engine == NULL) || ((max_done > 0) && (done == NULL)))
+                return GPUMAS_RETURN_VALUE_ERROR;
+        gpumas_engine * g = engine;
+        int rc = GPUMAS_RETURN_SUCCESS;
+        if (g->busy || (g->n_uploaded < g->n_jobs)) rc = gp_engine_batch(g);
+        int k = 0;
+        while ((rc == GPUMAS_RETURN_SUCCESS) && (k < max_done) &&
+            (g->fifo_n > 0)) {
+                done[k++] = g->fifo[g->fifo_head];
+                g->fifo_head = (g->fifo_head + 1) % g->fifo_cap;
+                g->fifo_n--;
+        }
+        if (n_done != NULL) *n_done = k;
+        if (pending != NULL) *pending = g->inflight + g->fifo_n;
+        return rc;
+}
+
+extern "C" int gpumas_engine_run(struct gpumas_engine * engine,
+    size_t n_jobs, const struct gpumas_job * jobs)
+{
+        if ((engine == NULL) || ((n_jobs > 0) && (jobs == NULL)))
+                return GPUMAS_RETURN_VALUE_ERROR;
+        gpumas_engine * g = engine;
+        for (size_t k = 0; k < n_jobs; k++) {
+                int ticket;
+                int rc = gpumas_engine_submit(g, jobs + k, &ticket);
+                if (rc == GPUMAS_RETURN_MEMORY_ERROR) {
+                        /* Table full: drain it, then go on. */
+                        while ((rc == GPUMAS_RETURN_MEMORY_ERROR) &&
+                            (g->inflight > 0)) {
+                                rc = gp_engine_batch(g);
+                                if (rc == GPUMAS_RETURN_SUCCESS)
+                                        rc = gpumas_engine_submit(
+                                            g, jobs + k, &ticket);
+                        }
+                }
+                if (rc != GPUMAS_RETURN_SUCCESS) return rc;
+        }
+        for (long it = 0; g->inflight > 0 || g->busy; it++) {
+                const int rc = gp_engine_batch(g);
+                if (rc != GPUMAS_RETURN_SUCCESS) return rc;
+                if (it > (1L << 40)) return GPUMAS_RETURN_INTERNAL_ERROR;
+        }
+        /* Completions of a run are not reported as tickets. */
+        g->fifo_n = 0;
+        g->fifo_head = 0;
+        return GPUMAS_RETURN_SUCCESS;
+}
+
+extern "C" int gpumas_engine_stats(const struct gpumas_engine * engine,
+    struct gpumas_engine_stats * stats)
+{
+        if ((engine == NULL) || (stats == NULL))
+                return GPUMAS_RETURN_VALUE_ERROR;
+        *stats = engine->stats;
+        stats->budget_used = engine->arena.used;
+        return GPUMAS_RETURN_SUCCESS;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Context path: one job through the context's own engine.                  */
+/* ------------------------------------------------------------------------ */
+extern "C" void gp_pool_free(struct gpumas_engine * g)
+{
+        if (g != NULL) gp_engine_free(g);
+}
+
+/* Transport n events of `io` with the slot pool, on stream s. Returns the
+ * number of kernel launches in *launches. */
+extern "C" int gp_pool_transport(gp_context * c, const gp_config * cfg,
+    const gp_io * io, size_t n, uint64_t first, cudaStream_t s,
     const gp_tuning * tuning, int * launches)
 {
-        const gp_config cfg = *cfg_;
-        const gp_io io = *io_;
         int P = tuning->pool_slots;
         if ((size_t)P > n) P = (int)((n + 127) / 128 * 128);
         if (P < 128) P = 128;
-        int rc = gp_pool_alloc(c, P);
-        if (rc != 0) return rc;
-        gp_pool_state * ps = c->pool;
-        const int block = 128;
-        const int batch = (tuning->batch > 0) ? tuning->batch : 16;
-        const int inner = (tuning->max_inner > 0) ? tuning->max_inner : 1;
-
-        rc = gp_check(cudaMemsetAsync(ps->pool.i + (size_t)SI_PHASE * P, 0,
-            (size_t)P * sizeof(int), s));
-        if (rc == 0)
-                rc = gp_check(cudaMemsetAsync(
-                    ps->d_counters, 0, sizeof(gp_counters), s));
-        if (rc != 0) return rc;
-
-        /* Launch parameters of this call. */
-        ps->h_launch->cfg = cfg;
-        ps->h_launch->io = io;
-        ps->h_launch->n = n;
-        ps->h_launch->first_event = first;
-        ps->h_launch->max_inner = inner;
-        rc = gp_check(cudaMemcpyAsync(ps->d_launch, ps->h_launch,
-            sizeof(gp_launch), cudaMemcpyHostToDevice, s));
-        if (rc != 0) return rc;
-
-        /* A batch of iterations as a CUDA graph (an even number, for the
-         * list parity), rebuilt only when the pool or the context changes. */
-        const int iters = 2 * ((batch + 1) / 2);
-        const int same = (ps->exec != NULL) && (ps->graph_batch == iters) &&
-            (ps->graph_tables == c->d_tables) &&
-            (ps->graph_geometry == c->d_geometry);
-        if (!same) {
-                if (ps->exec != NULL) cudaGraphExecDestroy(ps->exec);
-                if (ps->graph != NULL) cudaGraphDestroy(ps->graph);
-                ps->exec = NULL;
-                ps->graph = NULL;
-                cudaStream_t cap;
-                rc = gp_check(cudaStreamCreateWithFlags(
-                    &cap, cudaStreamNonBlocking));
-                if (rc != 0) return rc;
-                rc = gp_check(cudaStreamBeginCapture(
-                    cap, cudaStreamCaptureModeThreadLocal));
-                if (rc == 0) {
-                        for (int k = 0; k < iters; k++)
-                                gp_iteration(c, k & 1, block, cap);
-                        rc = gp_check(cudaStreamEndCapture(cap, &ps->graph));
-                }
-                if (rc == 0)
-                        rc = gp_check(cudaGraphInstantiate(
-                            &ps->exec, ps->graph, 0));
-                cudaStreamDestroy(cap);
-                if (rc != 0) return rc;
-                ps->graph_batch = iters;
-                ps->graph_tables = c->d_tables;
-                ps->graph_geometry = c->d_geometry;
+        int rc;
+        if (c->pool == NULL) {
+                gp_tuning t = *tuning;
+                t.pool_slots = P;
+                rc = gp_engine_new(&c->pool, c->physics, c->d_tables, &t, 1,
+                    0);
+                if (rc != GPUMAS_RETURN_SUCCESS) return rc;
         }
-        int n_launch = 0;
-        for (long it = 0;; it++) {
-                rc = gp_check(cudaGraphLaunch(ps->exec, s));
-                if (rc != 0) return rc;
-                n_launch += 4 * iters;
-                rc = gp_check(cudaMemcpyAsync(ps->h_counters, ps->d_counters,
-                    sizeof(gp_counters), cudaMemcpyDeviceToHost, s));
-                if (rc == 0) rc = gp_check(cudaStreamSynchronize(s));
-                if (rc != 0) return rc;
-                if ((ps->h_counters->cursor >= n) &&
-                    (ps->h_counters->active == 0))
-                        break;
-                if (it > (1L << 40)) return GPUMAS_RETURN_INTERNAL_ERROR;
+        gpumas_engine * g = c->pool;
+        g->tuning = *tuning;
+        /* Work of this call on the caller's stream. */
+        cudaStream_t own = g->stream;
+        g->stream = s;
+        rc = gp_engine_pool(g, P);
+        const long long l0 = g->stats.launches;
+        int ticket = 0;
+        if (rc == GPUMAS_RETURN_SUCCESS) rc = gp_engine_room(g);
+        if (rc == GPUMAS_RETURN_SUCCESS) {
+                gp_job_host info;
+                memset(&info, 0, sizeof(info));
+                rc = gp_engine_append(g, *cfg, c->d_geometry, *io, n, first,
+                    info, &ticket);
         }
-        if (launches != NULL) *launches = n_launch;
-        return 0;
+        for (long it = 0; (rc == GPUMAS_RETURN_SUCCESS) &&
+             (g->inflight > 0 || g->busy);
+             it++) {
+                rc = gp_engine_batch(g);
+                if (it > (1L << 40)) rc = GPUMAS_RETURN_INTERNAL_ERROR;
+        }
+        g->fifo_n = 0;
+        g->fifo_head = 0;
+        g->stream = own;
+        if (launches != NULL) *launches = (int)(g->stats.launches - l0);
+        if (rc != GPUMAS_RETURN_SUCCESS) {
+                /* Start afresh at the next call. */
+                cudaStreamSynchronize(s);
+                gp_engine_free(g);
+                c->pool = NULL;
+        }
+        return rc;
 }
 
 /* ------------------------------------------------------------------------ */
@@ -991,13 +1667,16 @@ extern "C" int gp_pool_transport(gp_context * c, const gp_config * cfg_,
  * (GPUMAS_STATIC_SLOTS of gpumas.h). */
 #define GP_STATIC_SLOTS GPUMAS_STATIC_SLOTS
 
-/* Bytes of the static pool: slot fields, the DEL / EHS lists of both
- * parities, the counters and the launch descriptor. */
-#define GP_STATIC_BYTES                                                       \
-        ((size_t)GP_STATIC_SLOTS *                                            \
-                (SD_N * sizeof(double) + SU_N * sizeof(uint64_t) +            \
-                    SI_N * sizeof(int) + 6 * sizeof(int)) +                   \
-            512 + sizeof(gp_launch))
+/* Bytes of the static pool: the layout of gp_pool_bytes for the largest
+ * pool, then one job record, its completion count and completion list. */
+#define GP_A256(n) ((((size_t)(n)) + 255) & ~(size_t)255)
+#define GP_STATIC_POOL_BYTES                                                  \
+        (GP_A256((size_t)SD_N * GP_STATIC_SLOTS * sizeof(double)) +           \
+            GP_A256((size_t)SU_N * GP_STATIC_SLOTS * sizeof(uint64_t)) +      \
+            GP_A256((size_t)SI_N * GP_STATIC_SLOTS * sizeof(int)) +           \
+            GP_A256((size_t)6 * GP_STATIC_SLOTS * sizeof(int)) +              \
+            GP_A256(sizeof(gp_counters)) + GP_A256(sizeof(gp_launch)))
+#define GP_STATIC_BYTES (GP_STATIC_POOL_BYTES + GP_A256(sizeof(gp_job)) + 256)
 
 static __device__ __align__(256) unsigned char gp_static_pool[GP_STATIC_BYTES];
 
@@ -1020,9 +1699,6 @@ static int gp_static_setup(int device, void ** address)
         *address = gp_static_address[device];
         return GPUMAS_RETURN_SUCCESS;
 }
-
-extern "C" int gp_config_check(const struct gpumas_context * context,
-    const struct gpumas_physics * physics, gp_config * cfg);
 
 extern "C" int gpumas_context_transport_device_static(
     struct gpumas_context * context, size_t n,
@@ -1049,83 +1725,61 @@ extern "C" int gpumas_context_transport_device_static(
         rc = gp_static_setup(device, &base);
         if (rc != GPUMAS_RETURN_SUCCESS) return rc;
 
-        /* Carve the static array: the layout of the pool engine for P
-         * slots, followed by the counters and the launch descriptor. */
+        /* Carve the static array: the pool of P slots, then the job. */
         const int P = pool_slots;
-        char * p = (char *)base;
-        gp_pool pool;
-        pool.d = (double *)p;
-        p += (size_t)SD_N * P * sizeof(double);
-        pool.u = (uint64_t *)p;
-        p += (size_t)SU_N * P * sizeof(uint64_t);
-        pool.i = (int *)p;
-        p += (size_t)SI_N * P * sizeof(int);
-        int * lists = (int *)p;
-        p += (size_t)6 * P * sizeof(int);
-        p = (char *)(((size_t)p + 255) & ~(size_t)255);
-        gp_counters * counters = (gp_counters *)p;
-        gp_launch * launch = (gp_launch *)(p + 256);
-        pool.P = P;
+        gp_pool_view v;
+        gp_pool_carve((char *)base, P, &v);
+        gp_job * job = (gp_job *)((char *)base + GP_STATIC_POOL_BYTES);
+        unsigned long long * job_done = (unsigned long long *)(
+            (char *)job + GP_A256(sizeof(gp_job)));
+        int * done_list = (int *)(job_done + 1);
 
         cudaStream_t s = (cudaStream_t)stream;
         /* The array keeps the previous call's contents: empty every slot
-         * and zero the counters and list lengths. */
-        rc = gp_check(cudaMemsetAsync(pool.i + (size_t)SI_PHASE * P, 0,
+         * and zero the counters and the completion count. */
+        rc = gp_check(cudaMemsetAsync(v.pool.i + (size_t)SI_PHASE * P, 0,
             (size_t)P * sizeof(int), s));
         if (rc == GPUMAS_RETURN_SUCCESS)
-                rc = gp_check(cudaMemsetAsync(counters, 0,
+                rc = gp_check(cudaMemsetAsync(v.counters, 0,
                     sizeof(gp_counters), s));
+        if (rc == GPUMAS_RETURN_SUCCESS)
+                rc = gp_check(cudaMemsetAsync(job_done, 0,
+                    sizeof(unsigned long long), s));
+        gp_job hj;
+        memset(&hj, 0, sizeof(hj));
+        hj.cfg = cfg;
+        hj.geometry = c->d_geometry;
+        hj.io.soa.a = *events;
+        hj.begin = 0;
+        hj.n = n;
+        hj.first_event = first_event;
         gp_launch h;
         memset(&h, 0, sizeof(h));
-        h.cfg = cfg;
-        memset(&h.io, 0, sizeof(h.io));
-        h.io.soa.a = *events;
-        h.n = n;
-        h.first_event = first_event;
+        h.jobs = job;
+        h.job_done = job_done;
+        h.done_list = done_list;
+        h.n_jobs = 1;
         h.max_inner = (c->tuning.max_inner > 0) ? c->tuning.max_inner : 1;
+        h.total = n;
         if (rc == GPUMAS_RETURN_SUCCESS)
-                rc = gp_check(cudaMemcpyAsync(launch, &h, sizeof(h),
+                rc = gp_check(cudaMemcpyAsync(job, &hj, sizeof(hj),
+                    cudaMemcpyHostToDevice, s));
+        if (rc == GPUMAS_RETURN_SUCCESS)
+                rc = gp_check(cudaMemcpyAsync(v.launch, &h, sizeof(h),
                     cudaMemcpyHostToDevice, s));
         if (rc == GPUMAS_RETURN_SUCCESS)
                 rc = gp_check(cudaStreamSynchronize(s));
         if (rc != GPUMAS_RETURN_SUCCESS) return rc;
 
-        const int block = 128;
-        const unsigned int grid = (P + block - 1) / block;
-        const unsigned int grid2 = (grid + 3) / 4;
-        unsigned int grid_step = grid;
-        {
-                int sms = 0, per_sm = 0;
-                cudaDeviceGetAttribute(
-                    &sms, cudaDevAttrMultiProcessorCount, device);
-                cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                    &per_sm, gp_pool_step, block, 0);
-                const unsigned int wave =
-                    (unsigned int)(sms * (per_sm > 0 ? per_sm : 1));
-                if (wave < grid_step) grid_step = wave;
-        }
+        const unsigned int grid_step = gp_step_wave(P, 128);
         const int batch = 16;
         for (long it = 0;; it++) {
-                for (int k = 0; k < batch; k++) {
-                        const int parity = k & 1;
-                        int * del_list = lists + (size_t)parity * P;
-                        int * ehs_list = lists + (size_t)(2 + parity) * P;
-                        int * polar_list = lists + (size_t)(4 + parity) * P;
-                        gp_pool_step<<<grid_step, block, 0, s>>>(
-                            c->d_tables, c->d_geometry, launch, pool,
-                            counters, del_list, ehs_list, parity);
-                        gp_pool_del<<<grid2, block, 0, s>>>(c->d_tables,
-                            launch, pool, counters, del_list, polar_list,
-                            parity);
-                        gp_pool_polar<<<grid2, block, 0, s>>>(c->d_tables,
-                            launch, pool, counters, polar_list, parity);
-                        gp_pool_ehs<<<grid2, block, 0, s>>>(c->d_tables,
-                            launch, pool, counters, ehs_list, parity);
-                }
+                for (int k = 0; k < batch; k++)
+                        gp_iteration(c->d_tables, v, grid_step, k & 1, s);
                 rc = gp_check(cudaGetLastError());
                 gp_counters hc;
                 if (rc == GPUMAS_RETURN_SUCCESS)
-                        rc = gp_check(cudaMemcpyAsync(&hc, counters,
+                        rc = gp_check(cudaMemcpyAsync(&hc, v.counters,
                             sizeof(hc), cudaMemcpyDeviceToHost, s));
                 if (rc == GPUMAS_RETURN_SUCCESS)
                         rc = gp_check(cudaStreamSynchronize(s));

@@ -9,7 +9,7 @@
 #include "gpumas.h"
 #include "gp_internal.h"
 
-struct gp_pool_state;
+struct gpumas_engine;
 
 /* Engine parameters (gpumas_tuning of gpumas.h). */
 struct gp_tuning {
@@ -34,7 +34,7 @@ struct gp_context {
         cudaEvent_t t0, t1;
         struct gpumas_stats stats;
         void * extra;
-        struct gp_pool_state * pool;
+        struct gpumas_engine * pool; /* slot pool engine of the context */
         struct gp_tuning tuning;
 };
 
@@ -48,7 +48,7 @@ static inline int gp_check(cudaError_t rc)
 #ifdef __cplusplus
 extern "C" {
 #endif
-void gp_pool_free(struct gp_pool_state * ps);
+void gp_pool_free(struct gpumas_engine * engine);
 #ifdef __cplusplus
 }
 #endif

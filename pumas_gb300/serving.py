@@ -1,0 +1,279 @@
+"""Continuous-batching request server over the transport engine.
+
+A request is a transport job whose initial states are in host memory: the
+events of a slab-stack job, or a muography flux query over a set of
+directions through the resident terrain. Physics tables, geometries and
+contexts stay resident on the device. The server runs one engine
+(gpumas_engine) and loops over three things:
+
+* admit: queued requests enter the running engine in arrival order as long
+  as the device state budget has room (gpumas_engine_submit_host refuses a
+  request that does not fit; it waits for running requests to free memory);
+* step: one CUDA graph batch of pool iterations, in which the events of
+  every admitted request share the slot pool;
+* complete: requests whose last event finished have their states and
+  results copied back to host memory and are returned with their latency
+  (arrival to results in host memory).
+
+A request's results do not depend on what else runs: event k of a request
+uses the random stream (context seed, first_event + k).
+
+`plain_serve` is the baseline: one request at a time, each with one plain
+one-thread-per-event launch through its context.
+"""
+import collections
+import time
+
+import numpy as np
+
+from . import (ENGINE_PLAIN, MODE_BACKWARD, Context, Engine, PumasError,
+               STATE_DTYPE, RESULT_DTYPE)
+from . import workloads as W
+
+
+class Request:
+    """A transport request: a context (settings, geometry, seed) and the
+    pumas_state records of its events, with event ids from first_event."""
+
+    __slots__ = ("context", "states", "first_event", "kind", "arrival",
+                 "admitted", "completed", "final", "results", "ticket")
+
+    def __init__(self, context, states, first_event, kind=""):
+        self.context = context
+        self.states = states
+        self.first_event = first_event
+        self.kind = kind
+        self.arrival = self.admitted = self.completed = None
+        self.final = self.results = self.ticket = None
+
+    @property
+    def n(self):
+        return len(self.states)
+
+    @property
+    def latency(self):
+        return self.completed - self.arrival
+
+
+class Server:
+    """Continuous batching of transport requests on one GPU."""
+
+    def __init__(self, physics, state_budget=40 << 30, max_jobs=1 << 20,
+                 pool_slots=65536, max_inner=8, batch=4):
+        self.engine = Engine(physics, pool_slots=pool_slots,
+                             max_inner=max_inner, batch=batch,
+                             max_jobs=max_jobs, state_budget=state_budget)
+        self.queue = collections.deque()
+        self.running = {}
+        self.completed = 0
+
+    def submit(self, request, now=None):
+        """Queue a request (arrival time `now`, default: the clock)."""
+        request.arrival = time.perf_counter() if now is None else now
+        self.queue.append(request)
+
+    def _admit(self):
+        while self.queue:
+            r = self.queue[0]
+            t = self.engine.submit_host(r.context, r.states, r.first_event)
+            if t is None:
+                break
+            r.ticket = t
+            r.admitted = time.perf_counter()
+            self.running[t] = r
+            self.queue.popleft()
+
+    def poll(self):
+        """Admit what fits, run one batch, return the completed requests."""
+        self._admit()
+        done, _ = self.engine.step()
+        now = time.perf_counter()
+        out = []
+        for t in done:
+            r = self.running.pop(t)
+            r.final, r.results = self.engine.result(t)
+            r.completed = now
+            out.append(r)
+        self.completed += len(out)
+        # Memory freed by completions admits queued requests at once.
+        if out:
+            self._admit()
+        return out
+
+    @property
+    def idle(self):
+        return not self.queue and not self.running
+
+
+def serve_open_loop(server, requests, arrivals):
+    """Offer `requests` at times `arrivals` (s from now) and serve them all.
+    Returns the wall time from the first arrival to the last completion."""
+    order = np.argsort(arrivals)
+    t0 = time.perf_counter()
+    k = 0
+    n = len(requests)
+    while k < n or not server.idle:
+        now = time.perf_counter() - t0
+        while k < n and arrivals[order[k]] <= now:
+            server.submit(requests[order[k]], t0 + arrivals[order[k]])
+            k += 1
+        if server.idle:
+            if k < n:
+                time.sleep(max(0., min(1E-04, arrivals[order[k]] - now)))
+            continue
+        server.poll()
+    return time.perf_counter() - t0
+
+
+def plain_serve(requests, arrivals):
+    """Baseline: requests in arrival order, one at a time, each through a
+    plain one-thread-per-event launch of its context (synchronous
+    gpumas_context_transport). Returns the wall time."""
+    order = np.argsort(arrivals)
+    t0 = time.perf_counter()
+    for k in order:
+        r = requests[k]
+        now = time.perf_counter() - t0
+        if arrivals[k] > now:
+            time.sleep(arrivals[k] - now)
+        r.arrival = t0 + arrivals[k]
+        r.context.tuning(engine=ENGINE_PLAIN)
+        r.final, r.results = r.context.transport(r.states, r.first_event)
+        r.completed = time.perf_counter()
+    return time.perf_counter() - t0
+
+
+# ---------------------------------------------------------------------------
+# Request mix of the serving workload.
+# ---------------------------------------------------------------------------
+class RequestMix:
+    """Request generator: with probability 0.7 a slab-stack job drawn from
+    a resident set of job geometries (events log-uniform in [1e2, 1e6]),
+    otherwise a terrain flux query over 1-256 random directions with
+    1e3-1e5 events each (log-uniform); event counts are multiplied by
+    `scale` (at least 1 event). Request i uses event ids from i << 32."""
+
+    def __init__(self, physics, seed=11, n_templates=256, scale=1E-03,
+                 terrain_n=512):
+        self.physics = physics
+        self.seed = seed
+        self.scale = scale
+        self.templates = []
+        for k, job in enumerate(W.slab_jobs(n_templates, seed=seed)):
+            c = Context(physics)
+            W.apply_config(c, W.slab_job_config(job))
+            c.seed = seed * 7919 + k
+            c.set_geometry(W.slab_job_geometry(physics, job))
+            self.templates.append((job, c))
+        self.terrain = Context(physics)
+        W.apply_config(self.terrain, W.config_dict("terrain"))
+        self.terrain.seed = seed
+        self.heights = W.terrain_heights(n=terrain_n)
+        self.terrain.set_geometry(W.terrain_geometry(physics, n=terrain_n))
+
+    def make(self, i):
+        """Request number i (deterministic in (seed, i))."""
+        idx = np.array([i], dtype=np.uint64)
+        u = [float(W.uniform(self.seed, 4, idx, k)[0]) for k in range(5)]
+        first = int(i) << 32
+        if u[0] < 0.7:
+            job, c = self.templates[min(int(u[1] * len(self.templates)),
+                                        len(self.templates) - 1)]
+            n = max(1, int(round(self.scale * 100. * 1E+04 ** u[2])))
+            j = dict(job, n=n, first_event=first)
+            return Request(c, W.slab_job_states(j, seed=self.seed), first,
+                           "job")
+        nd = 1 + min(int(256 * u[1]), 255)
+        per = max(1, int(round(self.scale * 1E+03 * 100. ** u[2])))
+        ev = np.arange(nd, dtype=np.uint64) + np.uint64(first)
+        zen = np.radians(85.) * W.uniform(self.seed, 4, ev, 5)
+        azi = 2. * np.pi * W.uniform(self.seed, 4, ev, 6)
+        s, _ = W.terrain(per, seed=self.seed, first_event=first,
+                         directions=(zen, azi), heights=self.heights)
+        return Request(self.terrain, s, first, "flux")
+
+
+def percentiles(values):
+    v = np.asarray(values, dtype=np.float64)
+    if len(v) == 0:
+        return {"p50": None, "p95": None, "p99": None}
+    return {"p50": float(np.percentile(v, 50)),
+            "p95": float(np.percentile(v, 95)),
+            "p99": float(np.percentile(v, 99))}
+
+
+def bench(args, rank, world, local):
+    """Serving sweep: Poisson arrivals at each rate of args.rates for
+    args.serve_seconds, continuous batching against the plain
+    one-launch-per-request baseline, p50/p95/p99 latency in ms."""
+    import json
+
+    import pumas_gb300 as pg
+    physics = pg.Physics()
+    mix = RequestMix(physics, seed=args.seed, scale=args.serve_scale)
+    server = Server(physics, pool_slots=args.pool_slots or 65536,
+                    max_inner=args.max_inner or 8, batch=args.batch or 4)
+    rates = [float(x) for x in args.rates.split(",")]
+    rng_seed = args.seed
+    # Warm-up: a few requests through both paths.
+    warm = [mix.make(10 ** 9 + i) for i in range(20)]
+    serve_open_loop(server, warm, np.zeros(len(warm)))
+    plain_serve([mix.make(10 ** 9 + i) for i in range(5)], np.zeros(5))
+    sweep = []
+    best = None
+    base = 0
+    for rate in rates:
+        n = max(1, int(round(rate * args.serve_seconds)))
+        gaps = -np.log(W.uniform(rng_seed, 5, np.arange(
+            base, base + n, dtype=np.uint64), 0)) / rate
+        arrivals = np.cumsum(gaps) - gaps[0]
+        reqs = [mix.make(base + i) for i in range(n)]
+        events = sum(r.n for r in reqs)
+        wall = serve_open_loop(server, reqs, arrivals)
+        lat = [1E+03 * r.latency for r in reqs]
+        errors = sum(int(np.count_nonzero(r.results["status"]))
+                     for r in reqs)
+        window = float(arrivals[-1]) if n > 1 else 0.
+        entry = {"rate": rate, "requests": n, "events": events,
+                 "wall_s": wall, "throughput_rps": n / wall,
+                 "events_per_s": events / wall,
+                 "latency_ms": percentiles(lat), "event_errors": errors,
+                 "sustained": bool(wall <= 1.1 * window + 0.05)}
+        # The plain baseline on the same arrivals (bounded: at most 2000
+        # requests, the first ones).
+        m = min(n, 2000)
+        preqs = [mix.make(base + i) for i in range(m)]
+        pwall = plain_serve(preqs, arrivals[:m])
+        same = all(np.array_equal(a.final, b.final) and
+                   np.array_equal(a.results, b.results)
+                   for a, b in zip(reqs[:m], preqs))
+        entry["plain"] = {"requests": m, "wall_s": pwall,
+                          "throughput_rps": m / pwall,
+                          "events_per_s": sum(r.n for r in preqs) / pwall,
+                          "latency_ms": percentiles(
+                              [1E+03 * r.latency for r in preqs]),
+                          "identical_results": bool(same)}
+        sweep.append(entry)
+        if entry["sustained"]:
+            best = entry
+        base += n
+    if rank != 0:
+        return
+    top = best or sweep[0]
+    line = {"metric": "requests/s at p99 latency", "value":
+            top["throughput_rps"], "unit": "requests/s", "n_gpus": world,
+            "steps": len(rates), "warmup": 1,
+            "ms_per_step": 1E+03 * top["wall_s"],
+            "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "serve: Poisson arrivals, 70 %% slab-"
+                                   "stack jobs, 30 %% terrain flux queries "
+                                   "(1-256 directions), events x %g"
+                                   % args.serve_scale,
+                       "state_budget_gb": 40,
+                       "pool_slots": args.pool_slots or 65536},
+            "highest_sustained_rate": best["rate"] if best else None,
+            "p99_ms_at_highest_sustained": (best["latency_ms"]["p99"]
+                                            if best else None),
+            "sweep": sweep, "engine": server.engine.stats()}
+    print(json.dumps(line), flush=True)

@@ -139,3 +139,209 @@ def apply_config(ctx, cfg):
     ctx.limit.grammage = cfg.get("limit_grammage", 0.)
     ctx.limit.time = cfg.get("limit_time", 0.)
     ctx.accuracy = cfg.get("accuracy", 1E-02)
+
+
+# ---------------------------------------------------------------------------
+# Backward muography over a synthetic terrain.
+# ---------------------------------------------------------------------------
+TERRAIN_N = 512          # nodes per side
+TERRAIN_CELL = 10.       # m
+TERRAIN_PEAK = 800.      # m, height of the Gaussian hill
+TERRAIN_SIGMA = 1500.    # m
+TERRAIN_NOISE = 5.       # m, i.i.d. Gaussian noise before smoothing
+TERRAIN_ZTOP = 3000.     # m, end of the transport (no medium above)
+TERRAIN_DEPTH = 20.      # m, detector depth below the surface
+FLUX_NORM = 0.14         # GeV^-1 cm^-2 s^-1 sr^-1 at 1 GeV
+FLUX_INDEX = 2.7
+
+
+def _normal(seed, domain, events, draw):
+    """Standard normal deviates from two uniforms (Box-Muller)."""
+    u1 = uniform(seed, domain, events, 2 * draw)
+    u2 = uniform(seed, domain, events, 2 * draw + 1)
+    return np.sqrt(-2. * np.log(u1)) * np.cos(2. * np.pi * u2)
+
+
+def terrain_heights(seed=3, n=TERRAIN_N, cell=TERRAIN_CELL):
+    """Heightmap of the terrain workload: a Gaussian hill (peak 800 m,
+    sigma 1.5 km) centred on the grid, plus i.i.d. N(0, 5 m) noise from the
+    Philox stream of (seed, domain 3, node index), smoothed by a 3 x 3 box
+    (edge nodes averaged over their in-grid neighbours). Returns (heights
+    [n, n] indexed [y, x], x0, y0)."""
+    x0 = -0.5 * (n - 1) * cell
+    x = x0 + cell * np.arange(n)
+    xx, yy = np.meshgrid(x, x)
+    hill = TERRAIN_PEAK * np.exp(-(xx ** 2 + yy ** 2) /
+                                 (2. * TERRAIN_SIGMA ** 2))
+    nodes = np.arange(n * n, dtype=np.uint64)
+    noise = TERRAIN_NOISE * _normal(seed, 3, nodes, 0).reshape(n, n)
+    z = hill + noise
+    acc = np.zeros_like(z)
+    cnt = np.zeros_like(z)
+    for dy in (-1, 0, 1):
+        for dx in (-1, 0, 1):
+            ys = slice(max(dy, 0), n + min(dy, 0))
+            yd = slice(max(-dy, 0), n + min(-dy, 0))
+            xs = slice(max(dx, 0), n + min(dx, 0))
+            xd = slice(max(-dx, 0), n + min(-dx, 0))
+            acc[yd, xd] += z[ys, xs]
+            cnt[yd, xd] += 1.
+    return acc / cnt, x0, x0
+
+
+def terrain_geometry(physics_or_index, seed=3, n=TERRAIN_N):
+    """Heightmap geometry: StandardRock below the surface, Air above, no
+    medium above 3 km."""
+    h, x0, y0 = terrain_heights(seed, n)
+    rock = _material(physics_or_index, "StandardRock")
+    air = _material(physics_or_index, "Air")
+    return Geometry.heightmap(h, x0, y0, TERRAIN_CELL, TERRAIN_CELL,
+                              (rock, 0.), (air, 0.), TERRAIN_ZTOP)
+
+
+def terrain_spec(seed=3, n=TERRAIN_N):
+    """The terrain geometry as a plain dict (for oracles and tests)."""
+    h, x0, y0 = terrain_heights(seed, n)
+    return dict(kind=2, media=[("StandardRock", 0.), ("Air", 0.)],
+                hm_z=h, hm_x0=x0, hm_y0=y0, hm_dx=TERRAIN_CELL,
+                hm_dy=TERRAIN_CELL, hm_below=0, hm_above=1,
+                hm_ztop=TERRAIN_ZTOP)
+
+
+def surface_height(h, x0, y0, cell, x, y):
+    """Bilinear surface height (the rule of gpumas_geometry.h)."""
+    fx, fy = (x - x0) / cell, (y - y0) / cell
+    i, j = int(fx), int(fy)
+    s, r = fx - i, fy - j
+    a = h[j, i] + s * (h[j, i + 1] - h[j, i])
+    b = h[j + 1, i] + s * (h[j + 1, i + 1] - h[j + 1, i])
+    return a + r * (b - a)
+
+
+def terrain_directions(n_zenith=32, n_azimuth=64, zmax=85.):
+    """Bin centres of the direction grid: (zenith, azimuth) in radians,
+    zenith bins over [0, zmax] deg, azimuth bins over [0, 360] deg."""
+    dz = zmax / n_zenith
+    za = np.radians(dz * (np.arange(n_zenith) + 0.5))
+    az = np.radians(360. / n_azimuth * (np.arange(n_azimuth) + 0.5))
+    zz, aa = np.meshgrid(za, az, indexing="ij")
+    return zz.ravel(), aa.ravel()
+
+
+def terrain(n_per_direction, seed=1, first_event=0, directions=None,
+            heights=None, emin=1., emax=1E+05):
+    """Initial states of the terrain workload: for each direction of the
+    grid, n_per_direction muons at the detector (20 m below the surface at
+    the grid centre) with momentum pointing down along the direction (they
+    come from the sky), kinetic energy log-uniform in [emin, emax], weight
+    1 / pdf(K), mu+ / mu- by event id parity. Event ids run direction by
+    direction from first_event. Returns (states, direction index)."""
+    if heights is None:
+        heights = terrain_heights()
+    h, x0, y0 = heights
+    if directions is None:
+        directions = terrain_directions()
+    zen, azi = directions
+    nd = len(zen)
+    n = nd * n_per_direction
+    ev = np.arange(first_event, first_event + n, dtype=np.uint64)
+    d = np.repeat(np.arange(nd), n_per_direction)
+    s = np.zeros(n, dtype=STATE_DTYPE)
+    s["charge"] = np.where(ev % 2 == 1, 1., -1.)
+    u = uniform(seed, 1, ev, 0)
+    lr = np.log(emax / emin)
+    k = emin * np.exp(lr * u)
+    s["energy"] = k
+    s["weight"] = k * lr
+    zd = surface_height(h, x0, y0, TERRAIN_CELL, 0., 0.) - TERRAIN_DEPTH
+    s["position"][:, 2] = zd
+    st = np.sin(zen[d])
+    s["direction"][:, 0] = -st * np.cos(azi[d])
+    s["direction"][:, 1] = -st * np.sin(azi[d])
+    s["direction"][:, 2] = -np.cos(zen[d])
+    return s, d
+
+
+def terrain_flux(final, results, direction_index, n_directions):
+    """Muon flux per direction (per cm^2 s sr) from backward transported
+    events: mean over events of weight x 0.14 E^-2.7 cos(theta), with E the
+    total energy and theta the zenith angle at the end point, for events
+    that reached the top of the geometry."""
+    from . import EVENT_MEDIUM
+    e_total = final["energy"] + 0.10565839
+    cos_t = np.clip(-final["direction"][:, 2], 0., 1.)
+    ok = (results["event"] == EVENT_MEDIUM) & (results["medium_out"] == -1)
+    w = np.where(ok, final["weight"] * FLUX_NORM *
+                 e_total ** -FLUX_INDEX * cos_t, 0.)
+    tot = np.bincount(direction_index, weights=w, minlength=n_directions)
+    cnt = np.bincount(direction_index, minlength=n_directions)
+    return tot / np.maximum(cnt, 1)
+
+
+# ---------------------------------------------------------------------------
+# Batched uneven jobs: slab stacks of rock, water and iron.
+# ---------------------------------------------------------------------------
+JOB_MATERIALS = ("StandardRock", "Water", "Iron")
+
+
+def slab_jobs(n_jobs=8192, seed=5, event_scale=1.):
+    """Job descriptions of the batched workload, drawn from the Philox
+    stream of (seed, domain 2, job index):
+
+    * 1 to 8 slabs stacked from z = 0 up, each of StandardRock, Water or
+      Iron (uniform) with a thickness log-uniform in [1 m, 2 km];
+    * events log-uniform in [1e2, 1e6] (times event_scale, at least 1);
+    * Emin log-uniform in [1, 100] GeV, Emax = 1000 Emin;
+    * forward or backward with probability 1/2. Forward muons start at
+      z = 0 going up and stop on exit or at 1 GeV; backward ones are
+      detected at z = 0 coming down and are transported back up to the
+      exit or to 1e7 GeV.
+
+    Straggled energy loss, mixed scattering, weighted decay. Returns a list
+    of dicts (slab boundaries, material names, n, emin, emax, direction,
+    first_event = job index x 2^32)."""
+    jobs = []
+    idx = np.arange(n_jobs, dtype=np.uint64)
+    u = [uniform(seed, 2, idx, k) for k in range(6 + 16)]
+    for j in range(n_jobs):
+        ns = 1 + min(int(8 * u[0][j]), 7)
+        mats = [JOB_MATERIALS[min(int(3 * u[6 + 2 * k][j]), 2)]
+                for k in range(ns)]
+        thick = [2000. ** u[7 + 2 * k][j] for k in range(ns)]
+        z = np.concatenate([[0.], np.cumsum(thick)])
+        n = max(1, int(round(event_scale * 100. * 1E+04 ** u[1][j])))
+        emin = 100. ** u[2][j]
+        jobs.append(dict(slab_z=z, materials=mats, n=n, emin=emin,
+                         emax=1E+03 * emin,
+                         direction=MODE_FORWARD if u[3][j] < 0.5 else
+                         MODE_BACKWARD,
+                         first_event=int(j) << 32))
+    return jobs
+
+
+def slab_job_config(job):
+    c = dict(energy_loss=MODE_STRAGGLED, decay=MODE_WEIGHTED,
+             direction=job["direction"], scattering=MODE_MIXED,
+             event=EVENT_LIMIT_ENERGY, accuracy=1E-02)
+    c["limit_energy"] = 1. if job["direction"] == MODE_FORWARD else 1E+07
+    return c
+
+
+def slab_job_geometry(physics, job):
+    mats = [physics.material_index(m) for m in job["materials"]]
+    return Geometry.slabs(list(job["slab_z"]), mats)
+
+
+def slab_job_states(job, seed=5):
+    """Initial states of a job: kinetic energy log-uniform in
+    [emin, emax] (Philox domain 1 of the event ids), at z = 0, going up
+    (forward) or coming down (backward), mu+ / mu- by event id parity."""
+    n = job["n"]
+    ev = np.arange(job["first_event"], job["first_event"] + n,
+                   dtype=np.uint64)
+    s = np.zeros(n, dtype=STATE_DTYPE)
+    s["charge"] = np.where(ev % 2 == 1, 1., -1.)
+    s["energy"] = _log_uniform(seed, ev, 0, job["emin"], job["emax"])
+    s["weight"] = 1.
+    s["direction"][:, 2] = 1. if job["direction"] == MODE_FORWARD else -1.
+    return s

@@ -114,6 +114,39 @@ CASES = {
 }
 
 
+def _terrain_states(n, seed, first):
+    """Muons at a detector 20 m under the centre of the small terrain, from
+    directions drawn uniformly in zenith [0, 85] deg and azimuth, kinetic
+    energy log-uniform in [1 GeV, 100 TeV], weight 1 / pdf."""
+    h = TERRAIN["hm_z"]
+    ev = np.arange(first, first + n, dtype=np.uint64)
+    s = np.zeros(n, dtype=STATE_DTYPE)
+    s["charge"] = np.where(ev % 2 == 1, 1., -1.)
+    lr = np.log(1E+05)
+    k = np.exp(lr * W.uniform(seed, 1, ev, 0))
+    s["energy"] = k
+    s["weight"] = k * lr
+    zen = np.radians(85.) * W.uniform(seed, 1, ev, 1)
+    azi = 2. * np.pi * W.uniform(seed, 1, ev, 2)
+    z0 = W.surface_height(h, TERRAIN["hm_x0"], TERRAIN["hm_y0"],
+                          TERRAIN["hm_dx"], 0., 0.) - 20.
+    s["position"][:, 2] = z0
+    st = np.sin(zen)
+    s["direction"][:, 0] = -st * np.cos(azi)
+    s["direction"][:, 1] = -st * np.sin(azi)
+    s["direction"][:, 2] = -np.cos(zen)
+    return s
+
+
+# A 64 x 64 node cut of the terrain workload's construction (10 m cells).
+TERRAIN = W.terrain_spec(seed=3, n=64)
+
+CASES["terrain_backward"] = dict(
+    config=_cfg(STRAGGLED, MIXED, BWD),
+    geometry=TERRAIN, n=200, seed=21,
+    states=lambda n, s, f: _terrain_states(n, s, f))
+
+
 def make_states(name, n=None, first_event=0):
     c = CASES[name]
     return c["states"](c["n"] if n is None else n, c["seed"], first_event)

@@ -6,7 +6,7 @@ the initial and final states and per event results as tests/golden/<case>.npz.
 These fixtures let machines without the reference sources check the engine
 against the reference's own outputs.
 
-usage: python tests/golden/make_golden.py
+usage: python tests/golden/make_golden.py [case ...]   (default: all cases)
 """
 import os
 import sys
@@ -32,7 +32,9 @@ def main():
     with open(path, "wb") as f:
         f.write(dump)
     ref = oracle.Reference(path)
-    for name, case in CASES.items():
+    names = sys.argv[1:] or list(CASES)
+    for name in names:
+        case = CASES[name]
         s0 = make_states(name)
         geo = oracle_geometry(ref, case["geometry"])
         cfg = oracle_config(case["config"], case["seed"])
