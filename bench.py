@@ -43,10 +43,11 @@ sys.path.insert(0, ROOT)
 # reported beside it.
 F_STEP = 680.4
 F_STEP_EXECUTED = 681.7
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum over the four
-# pool kernels) per reference step, from ncu on 200 000 rock slab events;
-# None until captured.
-TRAFFIC_STEP = None
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum over every pool
+# kernel launch of one batch) per reference step, from one ncu launch list
+# of a 2e6-event rock slab batch (314.2 GB over 547 988 323 steps); the
+# traffic of a batch is this times its steps.
+TRAFFIC_STEP = 573.3
 
 
 def parse():
@@ -65,6 +66,8 @@ def parse():
     p.add_argument("--pool-slots", type=int, default=0)
     p.add_argument("--max-inner", type=int, default=0)
     p.add_argument("--batch", type=int, default=0)
+    p.add_argument("--tail", type=int, default=0,
+                   help="drain threshold in slots (0: automatic, <0: off)")
     p.add_argument("--workload", default="rock_slab",
                    choices=["rock_slab", "slab_jobs", "terrain",
                             "plain_csda", "serve"])
@@ -82,6 +85,24 @@ def parse():
     p.add_argument("--autotune", action="store_true",
                    help="slab_jobs: tune the pool on every 8th job first")
     return p.parse_args()
+
+
+def rank_first_event(rank):
+    """First event id of a rank: replicas transport disjoint event ranges
+    (events are independent; there is no exchange on the data path)."""
+    return rank * 10 ** 12
+
+
+def max_over_ranks(value, device, world):
+    """The maximum of a per rank value (the step time of the slowest
+    replica), through the default process group when world > 1."""
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
 
 
 def dist_info():
@@ -344,9 +365,10 @@ def run_slab_jobs(args, rank, world, local):
         args.pool_slots = tuned["pool_slots"]
         args.max_inner = tuned["max_inner"]
         args.batch = tuned["batch"]
+        args.tail = tuned["tail"]
     eng = pg.Engine(physics, pool_slots=args.pool_slots,
                     max_inner=args.max_inner, batch=args.batch,
-                    max_jobs=len(jobs) + 1)
+                    max_jobs=len(jobs) + 1, tail=args.tail)
 
     def batched():
         ev.restore()
@@ -443,7 +465,7 @@ def run_slab_jobs(args, rank, world, local):
         "batched_over_plain": tp / tbs,
         "engine": {"pool_slots": args.pool_slots or 1048576,
                    "max_inner": args.max_inner or 8,
-                   "batch": args.batch or 16,
+                   "batch": args.batch or 16, "tail": args.tail,
                    "autotuned": None if tuned is None else {
                        "sample": "every 8th job",
                        "trials": tuned["trials"]}},
@@ -487,6 +509,30 @@ def slab_jobs_cpu(jobs, ctxs, states, seed, stride=100):
                          threads)}
 
 
+def port_baseline(name, states, cfg_dict, geometry_spec, seed, first_event,
+                  sample):
+    """The C restatement with OpenMP over all host cores on `states` (a
+    bounded sample of a workload), in events/s."""
+    import oracle
+    import pumas_gb300 as pg
+    oracle.build_port()
+    port = oracle.Port(pg.default_dump())
+    media = [(port.material_index(m), d) for m, d in geometry_spec["media"]]
+    kw = {k: v for k, v in geometry_spec.items()
+          if k not in ("kind", "media")}
+    geo = oracle.make_geometry(geometry_spec["kind"], media, **kw)
+    cfg = oracle.Config(seed=seed, **cfg_dict)
+    threads = port.max_threads()
+    t0 = time.perf_counter()
+    _, r = port.transport(cfg, geo, states, first_event, threads)
+    dt = time.perf_counter() - t0
+    return {"value": len(states) / dt, "unit": "events/s",
+            "cores": threads, "kind": "port",
+            "steps_per_s": float(r["steps"].sum()) / dt,
+            "sample": "%s: %s, %.1f s wall on %d OpenMP threads"
+                      % (name, sample, dt, threads)}
+
+
 def run_terrain(args, rank, world, local):
     """Backward muography over the synthetic terrain: 32 x 64 directions x
     per-direction events through the context's device entry point."""
@@ -507,7 +553,7 @@ def run_terrain(args, rank, world, local):
                       directions=dirs)
     setup_s = time.perf_counter() - t0
     ctx.tuning(engine=args.engine, pool_slots=args.pool_slots,
-               max_inner=args.max_inner, batch=args.batch)
+               max_inner=args.max_inner, batch=args.batch, tail=args.tail)
     ev = DeviceEvents(s0, dev)
     stream = torch.cuda.Stream(device=dev)
     n = len(s0)
@@ -545,10 +591,21 @@ def run_terrain(args, rank, world, local):
                                      "512 heightmap (10 m), 32 x 64 "
                                      "directions x %d events, 1 GeV - "
                                      "100 TeV, straggled + mixed, "
-                                     "weighted decay, stop at 3 km"
+                                     "weighted decay, stop at 3 km or "
+                                     "1e8 GeV"
                                      % args.per_direction,
                          "events_per_step": n, "setup_s": setup_s})
+    cpu = None
+    if not args.no_baseline:
+        # Every 100th initial state, over all directions, transported with
+        # event ids 0 .. n/100 - 1 (a sample of the same distribution).
+        sub = np.arange(0, n, 100)
+        cpu = port_baseline("terrain", s0[sub], W.config_dict("terrain"),
+                            W.terrain_spec(), args.seed, 0,
+                            "every 100th initial state (%d events)"
+                            % len(sub))
     line.update({
+        "cpu_baseline": cpu,
         "steps_per_s": steps_total / (ms * 1E-03),
         "steps_per_event": steps_total / n,
         "event_errors": int(np.count_nonzero(res["status"])),
@@ -622,7 +679,15 @@ def run_plain_csda(args, rank, world, local):
                          "events_per_step": n,
                          "l2": "state %.1f GB larger than L2"
                                % (n * 104 / 1E+09)})
+    cpu = None
+    if not args.no_baseline:
+        m = min(n, 2_000_000)
+        cpu = port_baseline("plain_csda", s0[:m],
+                            W.config_dict("plain_csda"),
+                            dict(kind=0, media=[("StandardRock", 0.)]),
+                            args.seed, 0, "first %d events" % m)
     line.update({
+        "cpu_baseline": cpu,
         "kernel_ms": kernel_ms,
         "roofline": {"bound": "hbm",
                      "achieved": algo / (kernel_ms * 1E-03) * 1E-09,
@@ -667,10 +732,11 @@ def main():
     ctx.seed = args.seed
     ctx.set_geometry(W.rock_slab_geometry(physics))
     tuning = ctx.tuning(engine=args.engine, pool_slots=args.pool_slots,
-                        max_inner=args.max_inner, batch=args.batch)
+                        max_inner=args.max_inner, batch=args.batch,
+                        tail=args.tail)
 
     n = args.events
-    first = rank * 10 ** 12
+    first = rank_first_event(rank)
     s0 = W.rock_slab(n, seed=args.seed, first_event=first)
     dev = torch.device("cuda", local)
     cols = {}
@@ -730,11 +796,7 @@ def main():
                         dtype=pg.RESULT_DTYPE)
     steps_per_event = float(res["steps"].mean())
     bad = int(np.count_nonzero(res["status"]))
-    ms_per_step = total_ms / args.steps
-    if world > 1:
-        t = torch.tensor([ms_per_step], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_per_step = float(t.item())
+    ms_per_step = max_over_ranks(total_ms / args.steps, dev, world)
     value = world * n / (ms_per_step * 1E-03)
 
     # End to end through the C ABI with pinned host buffers.

@@ -257,14 +257,18 @@ int gpumas_context_transport_device(struct gpumas_context * context,
  * 2 the slot pool, where events are refilled into `pool_slots` resident
  * slots and stepped by kernels regrouped by step kind (continuous step,
  * DEL, hard elastic scatter), with `max_inner` continuous steps per slot and
- * iteration and `batch` iterations per captured CUDA graph. Results do not
- * depend on these parameters. Zero fields keep the current value.
+ * iteration and `batch` iterations per captured CUDA graph. Once every
+ * event is in a slot and at most `tail` slots are active, the remaining
+ * events run to their end in one launch (0: one slot per resident thread,
+ * negative: never). Results do not depend on these parameters. Zero fields
+ * keep the current value (for `tail`: automatic).
  */
 struct gpumas_tuning {
         int engine;
         int pool_slots;
         int max_inner;
         int batch;
+        int tail;
 };
 
 int gpumas_context_tuning_set(
@@ -410,6 +414,11 @@ int gpumas_context_stats(
  * TFLOP/s (2 flops per DFMA), from a register-resident microbenchmark. It
  * is the denominator of the engine's FP64 roofline. */
 int gpumas_bench_dfma(double * tflops);
+
+/** Evaluate the engine's double precision logarithm (fn = 0) or
+ * exponential (fn = 1) on the device for n arguments (for checking; they
+ * replace the CUDA library functions in the transport, see gp_math.cuh). */
+int gpumas_math_eval(int fn, size_t n, const double * x, double * y);
 
 /* ------------------------------------------------------------------------ */
 /* Random stream.                                                           */

@@ -110,7 +110,8 @@ class _Stats(ctypes.Structure):
 
 class _Tuning(ctypes.Structure):
     _fields_ = [("engine", ctypes.c_int), ("pool_slots", ctypes.c_int),
-                ("max_inner", ctypes.c_int), ("batch", ctypes.c_int)]
+                ("max_inner", ctypes.c_int), ("batch", ctypes.c_int),
+                ("tail", ctypes.c_int)]
 
 
 ENGINE_AUTO, ENGINE_PLAIN, ENGINE_POOL = 0, 1, 2
@@ -364,16 +365,16 @@ class Context:
         return self._lib.gpumas_context_transport_device(
             self._ptr, n, ctypes.byref(c), first_event, stream)
 
-    def tuning(self, engine=0, pool_slots=0, max_inner=0, batch=0):
+    def tuning(self, engine=0, pool_slots=0, max_inner=0, batch=0, tail=0):
         """Set engine parameters (zero keeps a value); returns the current
         ones as a dict."""
-        t = _Tuning(engine, pool_slots, max_inner, batch)
+        t = _Tuning(engine, pool_slots, max_inner, batch, tail)
         _check(self._lib.gpumas_context_tuning_set(self._ptr,
                                                    ctypes.byref(t)),
                "gpumas_context_tuning_set")
         self._lib.gpumas_context_tuning_get(self._ptr, ctypes.byref(t))
         return {"engine": t.engine, "pool_slots": t.pool_slots,
-                "max_inner": t.max_inner, "batch": t.batch}
+                "max_inner": t.max_inner, "batch": t.batch, "tail": t.tail}
 
     def stats(self):
         st = _Stats()
@@ -405,11 +406,11 @@ class Engine:
     run (``submit`` / ``submit_host`` then ``step``)."""
 
     def __init__(self, physics, pool_slots=0, max_inner=0, batch=0,
-                 max_jobs=0, state_budget=0):
+                 max_jobs=0, state_budget=0, tail=0):
         self.physics = physics
         self._lib = physics._lib
         self._ptr = ctypes.c_void_p()
-        t = _Tuning(ENGINE_POOL, pool_slots, max_inner, batch)
+        t = _Tuning(ENGINE_POOL, pool_slots, max_inner, batch, tail)
         _check(self._lib.gpumas_engine_create(
             ctypes.byref(self._ptr), physics._ptr, ctypes.byref(t),
             max_jobs, state_budget), "gpumas_engine_create")

@@ -10,7 +10,10 @@ event id):
   its lane (events per lane and visit);
 * ``batch``: pool iterations per CUDA graph launch, i.e. how often the host
   checks for completed jobs and admits new ones (the refill / compaction
-  period seen from the host).
+  period seen from the host);
+* ``tail``: the drain threshold, in active slots, below which the last
+  events run to their end in one launch instead of being regrouped by step
+  kind (0: one slot per resident thread, -1: never).
 
 ``tune`` times an engine run of a sample workload for each point of a grid
 and keeps the fastest; the result is stored as JSON and read back by
@@ -23,9 +26,10 @@ import os
 import time
 
 DEFAULT_GRID = {
-    "pool_slots": [262144, 524288, 1048576, 2097152],
-    "max_inner": [2, 4, 8, 16],
-    "batch": [8, 16, 32],
+    "pool_slots": [524288, 1048576, 2097152],
+    "max_inner": [4, 8, 16],
+    "batch": [8, 16],
+    "tail": [-1, 0],
 }
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -39,7 +43,7 @@ def tune(physics, make_run, grid=None, repeats=1, log=None):
     all points under ``"trials"``."""
     from . import Engine
     grid = dict(DEFAULT_GRID, **(grid or {}))
-    keys = ("pool_slots", "max_inner", "batch")
+    keys = ("pool_slots", "max_inner", "batch", "tail")
     trials = []
     for values in itertools.product(*(grid[k] for k in keys)):
         point = dict(zip(keys, values))
@@ -69,12 +73,12 @@ def save(result, path=DEFAULT_PATH):
 
 
 def load(path=DEFAULT_PATH):
-    """Tuned engine parameters (pool_slots, max_inner, batch), or an empty
-    dict when no tuning was stored."""
+    """Tuned engine parameters (pool_slots, max_inner, batch, tail), or an
+    empty dict when no tuning was stored."""
     try:
         with open(path) as f:
             r = json.load(f)
     except (OSError, ValueError):
         return {}
-    return {k: int(r[k]) for k in ("pool_slots", "max_inner", "batch")
-            if k in r}
+    return {k: int(r[k]) for k in ("pool_slots", "max_inner", "batch",
+                                   "tail") if k in r}

@@ -12,13 +12,18 @@
  * arrays, sized to stay resident in L2) and advances all of them one
  * iteration at a time with one kernel per step kind:
  *
+ *   0. gp_pool_drain: clears the previous iteration's lists and, once the
+ *      queue is empty and few slots remain active, runs their events to
+ *      the end in one launch (otherwise it returns at once).
  *   1. gp_pool_step: every slot makes its continuous step(s). Empty slots are
  *      first refilled from the input (a device work queue: an atomic cursor
- *      over the events). Slots whose step ended on a DEL or an EHS are
- *      appended to the DEL or EHS list with warp aggregated atomics (a
- *      ballot and prefix count per warp), so that the lists are compact.
- *   2. gp_pool_del: one thread per listed DEL, full warps.
- *   3. gp_pool_ehs: one thread per listed EHS, full warps.
+ *      over the events of every job). Slots whose step ended on a DEL or an
+ *      EHS are appended to the DEL or EHS list with warp aggregated atomics
+ *      (a ballot and prefix count per warp), so that the lists are compact.
+ *   2. gp_pool_del: one thread per listed DEL, full warps; photonuclear
+ *      polar angles are deferred to
+ *   3. gp_pool_polar: Brent search and rejection in lockstep, with refill;
+ *   4. gp_pool_ehs: one thread per listed EHS, full warps.
  *
  * Finished events are written back to the caller's arrays at their input
  * index and their slot is refilled at the next iteration. Per event results
@@ -84,6 +89,7 @@ struct gp_counters {
         int n_polar[2];
         int polar_next[2];
         int step_next[2];
+        int drain_next[2];
 };
 
 /* A job: events of one context (settings, geometry, random seed), read from
@@ -110,6 +116,10 @@ struct gp_launch {
         int n_jobs;
         int max_inner;
         unsigned long long total;
+        /* Drain threshold: once the queue is exhausted and at most this many
+         * slots are active, the step kernel runs each remaining event to its
+         * end, DELs and EHSs included (0: never). */
+        int tail_slots;
 };
 
 
@@ -319,6 +329,64 @@ static __device__ __forceinline__ int gp_refill(const gp_tables & T,
         }
 }
 
+/* First kernel of a pool iteration. Block 0 clears the other parity's
+ * lists and cursors, which the previous iteration's kernels (before this
+ * one in stream order) have consumed.
+ *
+ * It also drains the pool: once no event is left in the queue and at most
+ * tail_slots slots are active, regrouping by step kind would leave most
+ * lanes idle for hundreds of short iterations. Each lane then takes active
+ * slots and carries their events to the end, DELs and EHSs included (the
+ * one thread per event scheme); an event's operations and draws are the
+ * same either way. Otherwise the kernel returns at once. At the start of
+ * an iteration every active slot is in the continuous step phase: the DEL,
+ * polar and EHS kernels of the previous iteration set it back. */
+__global__ void __launch_bounds__(128, 1) gp_pool_drain(
+    const gp_tables * __restrict__ Tp, const gp_launch * __restrict__ X,
+    const gp_pool pool, gp_counters * cnt, int parity)
+{
+        if ((blockIdx.x == 0) && (threadIdx.x == 0)) {
+                cnt->n_del[parity ^ 1] = 0;
+                cnt->n_ehs[parity ^ 1] = 0;
+                cnt->n_polar[parity ^ 1] = 0;
+                cnt->polar_next[parity ^ 1] = 0;
+                cnt->step_next[parity ^ 1] = 0;
+                cnt->drain_next[parity ^ 1] = 0;
+        }
+        const int tail = (X->tail_slots > 0) && (cnt->cursor >= X->total) &&
+            (cnt->active <= X->tail_slots);
+        if (!tail) return;
+        const gp_tables & T = *Tp;
+        int * dcursor = &cnt->drain_next[parity];
+        for (long guard = 0; guard < (1L << 40); guard++) {
+                cg::coalesced_group w = cg::coalesced_threads();
+                int base = 0;
+                if (w.thread_rank() == 0)
+                        base = atomicAdd(dcursor, (int)w.size());
+                base = w.shfl(base, 0);
+                const int slot = base + (int)w.thread_rank();
+                if (slot >= pool.P) return;
+                if (PI(SI_PHASE) != GP_NEXT_STEP) continue;
+                const gp_job & J = X->jobs[PI(SI_JOB)];
+                gp_event e;
+                gp_loop L;
+                gp_slot_load(pool, slot, J.cfg, e, L);
+                int event = GPUMAS_EVENT_NONE;
+                int next = GP_NEXT_STEP;
+                for (long s_ = 0; (s_ < (1L << 40)) && (next != GP_NEXT_DONE);
+                     s_++) {
+                        if (next == GP_NEXT_STEP)
+                                next = gp_stepping_step(
+                                    T, J.cfg, *J.geometry, e, L, event);
+                        else if (next == GP_NEXT_DEL)
+                                next = gp_stepping_del(T, J.cfg, e, L, event);
+                        else
+                                next = gp_stepping_ehs(T, J.cfg, e, L, event);
+                }
+                gp_finish(pool, slot, X, J, cnt, e, event, L.medium);
+        }
+}
+
 /* Continuous steps. The kernel is persistent: each lane takes slots from a
  * cursor over the pool (refilling empty ones from the input), steps its
  * slot until the step ends on an event or after max_inner steps, routes it
@@ -330,8 +398,8 @@ __global__ void __launch_bounds__(128, GP_STEP_MIN_BLOCKS) gp_pool_step(
     const gp_pool pool, gp_counters * cnt, int * del_list, int * ehs_list,
     int parity)
 {
-        const int max_inner = X->max_inner;
         const gp_tables & T = *Tp;
+        const int max_inner = X->max_inner;
         int * scursor = &cnt->step_next[parity];
         gp_event e;
         gp_loop L;
@@ -348,16 +416,6 @@ __global__ void __launch_bounds__(128, GP_STEP_MIN_BLOCKS) gp_pool_step(
                         if (j >= pool.P) {
                                 exhausted = 1;
                                 break;
-                        }
-                        if (j == 0) {
-                                /* The other parity's lists and cursors were
-                                 * consumed by the previous iteration's
-                                 * kernels, which precede this one. */
-                                cnt->n_del[parity ^ 1] = 0;
-                                cnt->n_ehs[parity ^ 1] = 0;
-                                cnt->n_polar[parity ^ 1] = 0;
-                                cnt->polar_next[parity ^ 1] = 0;
-                                cnt->step_next[parity ^ 1] = 0;
                         }
                         const int s_ = j;
                         {
@@ -495,7 +553,7 @@ static __device__ __forceinline__ void gp_pn_searched(
                         s.phase = PN_DONE;
                         return;
                 }
-                const double x = exp(s.xopt) / (2 * s.q * M);
+                const double x = gp_exp(s.xopt) / (2 * s.q * M);
                 const double lne = 0.1;
                 if ((x <= 0.04) && (s.xopt + lne < s.lnQ2max)) {
                         gp_pn_search(s, s.xopt + lne, s.lnQ2max, 1);
@@ -524,7 +582,7 @@ static __device__ __forceinline__ void gp_pn_advance(const gp_tables & T,
                 switch (s.phase) {
                 case PN_MIN_A:
                         if (!have_value) {
-                                s.Q2 = exp(s.xa);
+                                s.Q2 = gp_exp(s.xa);
                                 return;
                         }
                         s.fa = value;
@@ -533,7 +591,7 @@ static __device__ __forceinline__ void gp_pn_advance(const gp_tables & T,
                         break;
                 case PN_MIN_C:
                         if (!have_value) {
-                                s.Q2 = exp(s.xc);
+                                s.Q2 = gp_exp(s.xc);
                                 return;
                         }
                         s.fc = value;
@@ -556,7 +614,7 @@ static __device__ __forceinline__ void gp_pn_advance(const gp_tables & T,
                                         break;
                                 }
                                 s.xb = 0.5 * (s.xa + s.xc);
-                                s.Q2 = exp(s.xb);
+                                s.Q2 = gp_exp(s.xb);
                                 return;
                         }
                         s.fb = value;
@@ -635,7 +693,7 @@ static __device__ __forceinline__ void gp_pn_advance(const gp_tables & T,
                                 s.u = (fabs(s.d) >= tol1) ? s.x + s.d :
                                     s.x + ((s.d >= 0.0) ? fabs(tol1) :
                                                           -fabs(tol1));
-                                s.Q2 = exp(s.u);
+                                s.Q2 = gp_exp(s.u);
                                 return;
                         }
                         {
@@ -676,7 +734,7 @@ static __device__ __forceinline__ void gp_pn_advance(const gp_tables & T,
                                         return;
                                 }
                                 const double uu = gp_random(e);
-                                s.Q2 = s.Q2min * exp(s.rQ2 * uu);
+                                s.Q2 = s.Q2min * gp_exp(s.rQ2 * uu);
                                 return;
                         }
                         if (gp_random(e) * s.fopt <= value) {
@@ -736,8 +794,8 @@ static __device__ __forceinline__ void gp_pn_start(const gp_tables & T,
                 return;
         }
         s.Q2min = Q2min;
-        const double lnQ2min = log(Q2min);
-        s.lnQ2max = log(Q2max);
+        const double lnQ2min = gp_log(Q2min);
+        s.lnQ2max = gp_log(Q2max);
         s.rQ2 = s.lnQ2max - lnQ2min;
         gp_pn_search(s, lnQ2min, s.lnQ2max, 0);
         gp_pn_advance(T, s, e, 0, 0.);
@@ -898,11 +956,22 @@ static unsigned int gp_step_wave(int P, int block)
         return (wave < grid) ? wave : grid;
 }
 
-/* Launch one pool iteration: continuous steps, DELs, photonuclear polar
- * angles, hard elastic scatters. Lists 0-1 are the DEL lists, 2-3 the EHS
- * lists and 4-5 the polar lists of both parities. */
+/* Launch one pool iteration: list reset and drain, continuous steps, DELs,
+ * photonuclear polar angles, hard elastic scatters. Lists 0-1 are the DEL
+ * lists, 2-3 the EHS lists and 4-5 the polar lists of both parities. */
+/* A second stream and two events let the photonuclear polar kernel run
+ * beside the EHS kernel: they work on disjoint slots (a DEL or an EHS per
+ * slot and iteration), and the polar kernel's long per-lane chains of DDCS
+ * evaluations keep few warps per SM busy. With fork == NULL the kernels run
+ * one after the other on s. */
+struct gp_fork {
+        cudaStream_t s2;
+        cudaEvent_t fork, join;
+};
+
 static void gp_iteration(const gp_tables * d_tables, const gp_pool_view & v,
-    unsigned int grid_step, int parity, cudaStream_t s)
+    unsigned int grid_step, int parity, cudaStream_t s,
+    const gp_fork * fork = NULL)
 {
         const int block = 128;
         const unsigned int grid = (v.pool.P + block - 1) / block;
@@ -910,14 +979,26 @@ static void gp_iteration(const gp_tables * d_tables, const gp_pool_view & v,
         int * del_list = v.lists[parity];
         int * ehs_list = v.lists[2 + parity];
         int * polar_list = v.lists[4 + parity];
+        gp_pool_drain<<<grid_step, block, 0, s>>>(d_tables, v.launch, v.pool,
+            v.counters, parity);
         gp_pool_step<<<grid_step, block, 0, s>>>(d_tables, v.launch, v.pool,
             v.counters, del_list, ehs_list, parity);
         gp_pool_del<<<grid2, block, 0, s>>>(d_tables, v.launch, v.pool,
             v.counters, del_list, polar_list, parity);
-        gp_pool_polar<<<grid2, block, 0, s>>>(d_tables, v.launch, v.pool,
+        cudaStream_t sp = s;
+        if (fork != NULL) {
+                cudaEventRecord(fork->fork, s);
+                cudaStreamWaitEvent(fork->s2, fork->fork, 0);
+                sp = fork->s2;
+        }
+        gp_pool_polar<<<grid2, block, 0, sp>>>(d_tables, v.launch, v.pool,
             v.counters, polar_list, parity);
         gp_pool_ehs<<<grid2, block, 0, s>>>(d_tables, v.launch, v.pool,
             v.counters, ehs_list, parity);
+        if (fork != NULL) {
+                cudaEventRecord(fork->join, fork->s2);
+                cudaStreamWaitEvent(s, fork->join, 0);
+        }
 }
 
 /* ------------------------------------------------------------------------ */
@@ -1116,16 +1197,30 @@ static int gp_engine_graph(gpumas_engine * g)
         int rc = gp_check(cudaStreamCreateWithFlags(
             &cap, cudaStreamNonBlocking));
         if (rc != GPUMAS_RETURN_SUCCESS) return rc;
-        rc = gp_check(cudaStreamBeginCapture(
-            cap, cudaStreamCaptureModeThreadLocal));
+        gp_fork fork;
+        memset(&fork, 0, sizeof(fork));
+        rc = gp_check(cudaStreamCreateWithFlags(
+            &fork.s2, cudaStreamNonBlocking));
+        if (rc == GPUMAS_RETURN_SUCCESS)
+                rc = gp_check(cudaEventCreateWithFlags(
+                    &fork.fork, cudaEventDisableTiming));
+        if (rc == GPUMAS_RETURN_SUCCESS)
+                rc = gp_check(cudaEventCreateWithFlags(
+                    &fork.join, cudaEventDisableTiming));
+        if (rc == GPUMAS_RETURN_SUCCESS)
+                rc = gp_check(cudaStreamBeginCapture(
+                    cap, cudaStreamCaptureModeThreadLocal));
         if (rc == GPUMAS_RETURN_SUCCESS) {
                 for (int k = 0; k < iters; k++)
                         gp_iteration(g->d_tables, g->view, g->grid_step,
-                            k & 1, cap);
+                            k & 1, cap, &fork);
                 rc = gp_check(cudaStreamEndCapture(cap, &g->graph));
         }
         if (rc == GPUMAS_RETURN_SUCCESS)
                 rc = gp_check(cudaGraphInstantiate(&g->exec, g->graph, 0));
+        if (fork.join != NULL) cudaEventDestroy(fork.join);
+        if (fork.fork != NULL) cudaEventDestroy(fork.fork);
+        if (fork.s2 != NULL) cudaStreamDestroy(fork.s2);
         cudaStreamDestroy(cap);
         if (rc == GPUMAS_RETURN_SUCCESS) g->graph_iters = iters;
         return rc;
@@ -1333,6 +1428,9 @@ static int gp_engine_batch(gpumas_engine * g)
                 h->max_inner = (g->tuning.max_inner > 0) ?
                     g->tuning.max_inner : 8;
                 h->total = g->total;
+                h->tail_slots = (g->tuning.tail < 0) ? 0 :
+                    (g->tuning.tail > 0) ? g->tuning.tail :
+                                           (int)(g->grid_step * 128);
                 rc = gp_check(cudaMemcpyAsync(g->view.launch, h,
                     sizeof(gp_launch), cudaMemcpyHostToDevice, s));
                 if (rc == GPUMAS_RETURN_SUCCESS) rc = gp_engine_graph(g);
@@ -1341,7 +1439,7 @@ static int gp_engine_batch(gpumas_engine * g)
                 rc = gp_check(cudaGraphLaunch(g->exec, s));
                 cudaEventRecord(g->t1, s);
                 if (rc != GPUMAS_RETURN_SUCCESS) return rc;
-                g->stats.launches += 4 * g->graph_iters;
+                g->stats.launches += 5 * g->graph_iters;
                 g->stats.batches++;
         }
         rc = gp_check(cudaMemcpyAsync(g->h_counters, g->view.counters,
@@ -1429,6 +1527,7 @@ extern "C" int gpumas_engine_create(struct gpumas_engine ** engine,
         t.pool_slots = 1048576;
         t.max_inner = 8;
         t.batch = 16;
+        t.tail = 0;
         if (tuning != NULL) {
                 if ((tuning->pool_slots < 0) || (tuning->max_inner < 0) ||
                     (tuning->batch < 0))
@@ -1436,6 +1535,7 @@ extern "C" int gpumas_engine_create(struct gpumas_engine ** engine,
                 if (tuning->pool_slots > 0) t.pool_slots = tuning->pool_slots;
                 if (tuning->max_inner > 0) t.max_inner = tuning->max_inner;
                 if (tuning->batch > 0) t.batch = tuning->batch;
+                t.tail = tuning->tail;
         }
         if (t.pool_slots < 128) t.pool_slots = 128;
         return gp_engine_new(engine, physics, NULL, &t,
@@ -1761,6 +1861,7 @@ extern "C" int gpumas_context_transport_device_static(
         h.n_jobs = 1;
         h.max_inner = (c->tuning.max_inner > 0) ? c->tuning.max_inner : 1;
         h.total = n;
+        h.tail_slots = 0;
         if (rc == GPUMAS_RETURN_SUCCESS)
                 rc = gp_check(cudaMemcpyAsync(job, &hj, sizeof(hj),
                     cudaMemcpyHostToDevice, s));

@@ -4,9 +4,12 @@
  * A GPU restatement of the reference transport (PUMAS 1.2.3, src/pumas.c):
  * table interpolants, CEL / DEL / EHS samplers, Coulomb scattering, the
  * default DCS models and the polar angle samplers. Floating point
- * expressions keep the reference's evaluation order; the CUDA double
- * precision libm differs from glibc by at most an ulp or two, which the
- * parity tests bound. Differences in structure, all result preserving:
+ * expressions keep the reference's evaluation order. Logarithms and
+ * exponentials are the engine's table-driven ones (gp_math.cuh, below one
+ * ulp, equal to glibc's in about 98 % of arguments); the other CUDA double
+ * precision functions differ from glibc by at most an ulp or two. The
+ * parity tests bound the effect. Differences in structure, all result
+ * preserving:
  *
  *   - no per context index cache in table lookups (pumas.c:4174-4210): the
  *     cache never changes the bracketing index;
@@ -27,6 +30,8 @@
 #define GP_DEVICE_CUH
 
 #include <stdint.h>
+
+#include "gp_math.cuh"
 
 #include "gpumas.h"
 #include "gp_internal.h"
@@ -234,7 +239,7 @@ GPD double gp_cel_grammage(
                 const double K0 = __ldg(T.K + imax);
                 const double K1 = a / b + T.mass;
                 return __ldg(T.X + GP_ROW(s, material) + imax) +
-                    1. / b * log((kinetic + K1) / (K0 + K1));
+                    1. / b * gp_log((kinetic + K1) / (K0 + K1));
         }
         return gp_baked(T, GP_LUT_K, T.K, GP_C_X(T.n_materials, s, material),
             kinetic);
@@ -253,11 +258,11 @@ GPD double gp_cel_grammage_as_time(
                 const double E0 = __ldg(T.K + imax) + T.mass;
                 const double tmax = __ldg(Tt + imax);
                 const double r =
-                    E0 / (a + b * E0) * exp(a * (time - tmax) / T.mass);
+                    E0 / (a + b * E0) * gp_exp(a * (time - tmax) / T.mass);
                 const double kinetic = a * r / (1. - b * r) - T.mass;
                 const double K1 = a / b + T.mass;
                 return __ldg(T.X + GP_ROW(s, material) + imax) +
-                    1. / b * log((kinetic + K1) / (E0 - T.mass + K1));
+                    1. / b * gp_log((kinetic + K1) / (E0 - T.mass + K1));
         }
         return gp_baked(T, GP_LUT_T(T, s, material), Tt,
             GP_C_X_OF_T(T.n_materials, s, material), time);
@@ -275,7 +280,7 @@ GPD double gp_cel_proper_time(
                 const double E0 = __ldg(T.K + imax) + T.mass;
                 const double E1 = kinetic + T.mass;
                 return __ldg(T.T + GP_ROW(s, material) + imax) +
-                    T.mass / a * log((E1 / E0) * (a + b * E0) / (a + b * E1));
+                    T.mass / a * gp_log((E1 / E0) * (a + b * E0) / (a + b * E1));
         }
         return gp_baked(T, GP_LUT_K, T.K, GP_C_T(T.n_materials, s, material),
             kinetic);
@@ -293,7 +298,7 @@ GPD double gp_cel_kinetic_energy(
                 const double b = __ldg(T.b_max + s * T.n_materials + material);
                 const double K0 = __ldg(T.K + imax);
                 const double K1 = a / b + T.mass;
-                return (K0 + K1) * exp(b * (grammage - __ldg(X + imax))) - K1;
+                return (K0 + K1) * gp_exp(b * (grammage - __ldg(X + imax))) - K1;
         }
         return gp_baked(T, GP_LUT_X(T, s, material), X,
             GP_C_K_OF_X(T.n_materials, s, material), grammage);
@@ -349,7 +354,7 @@ GPD double gp_del_interaction_length(
                 const double b0 = __ldg(T.b_max + T.n_materials + material);
                 const double cs = __ldg(T.CS + GP_MROW(material) + imax);
                 const double dZ =
-                    cs / b0 * log((a0 + b0 * (kinetic + T.mass)) /
+                    cs / b0 * gp_log((a0 + b0 * (kinetic + T.mass)) /
                                   (a0 + b0 * (k0 + T.mass)));
                 return __ldg(T.NI_in + GP_MROW(material) + imax) + dZ;
         }
@@ -369,7 +374,7 @@ GPD double gp_del_kinetic_from_interaction_length(
                 const double b0 = __ldg(T.b_max + T.n_materials + material);
                 const double cs = __ldg(T.CS + GP_MROW(material) + imax);
                 const double nI0 = __ldg(NI + imax);
-                return ((a0 + b0 * (k0 + T.mass)) * exp(b0 * (nI - nI0) / cs) -
+                return ((a0 + b0 * (k0 + T.mass)) * gp_exp(b0 * (nI - nI0) / cs) -
                            a0) / b0 - T.mass;
         }
         return gp_baked(T, GP_LUT_NI_IN(T, material), NI,
@@ -476,12 +481,12 @@ GPD int gp_coulomb_screening(const gp_element & el, double mass,
         } else {
                 const double r2i = 1. / (1. + zeta2);
                 const double phi = -atan(sqrt(zeta2));
-                f = -0.5 * log(r2i) + 0.5 * (1. - r2i) +
+                f = -0.5 * gp_log(r2i) + 0.5 * (1. - r2i) +
                     1. / 12. * (1. - cos(2 * phi) * r2i) -
                     1. / 120. * (1. - cos(4 * phi) * r2i * r2i) +
                     1. / 252. * (1. - cos(6 * phi) * r2i * r2i * r2i);
         }
-        const double ktv = exp(2 * f);
+        const double ktv = gp_exp(2 * f);
         const double p02 = kinetic0 * (kinetic0 + 2. * mass);
         const double d = 0.25 * GP_HBAR_C * GP_HBAR_C / p02 * ktv;
         const int n = el.n_screen;
@@ -609,7 +614,7 @@ GPD double gp_coulomb_cs0(double mu, double S, int n_parameters,
                 if (i >= n) break;
                 const double alp = screening[i];
                 const double r = mu / (mu + alp);
-                const double L = log(1. + mu / alp);
+                const double L = gp_log(1. + mu / alp);
                 const double I0 = r / alp;
                 const double J0 = L;
                 const double I1 = L - r;
@@ -618,7 +623,7 @@ GPD double gp_coulomb_cs0(double mu, double S, int n_parameters,
         }
         const double N = screening[n];
         const double r = mu / (mu + N);
-        const double L = log(1. + mu / N);
+        const double L = gp_log(1. + mu / N);
         const double I0 = r / N;
         const double J0 = L;
         const double I1 = L - r;
@@ -710,21 +715,21 @@ static __device__ double gp_dilog(double x)
         if (T <= -2) {
                 Y = -1. / (1. + T);
                 S = 1.;
-                A = -PI3 + 0.5 * (gp_sq(log(-T)) - gp_sq(log(1. + 1. / T)));
+                A = -PI3 + 0.5 * (gp_sq(gp_log(-T)) - gp_sq(gp_log(1. + 1. / T)));
         } else if (T < -1.) {
                 Y = -1. - T;
                 S = -1.;
-                A = log(-T);
-                A = -PI6 + A * (A + log(1. + 1. / T));
+                A = gp_log(-T);
+                A = -PI6 + A * (A + gp_log(1. + 1. / T));
         } else if (T <= -0.5) {
                 Y = -(1. + T) / T;
                 S = 1.;
-                A = log(-T);
-                A = -PI6 + A * (-0.5 * A + log(1. + T));
+                A = gp_log(-T);
+                A = -PI6 + A * (-0.5 * A + gp_log(1. + T));
         } else if (T < 0.) {
                 Y = -T / (1. + T);
                 S = -1.;
-                A = 0.5 * gp_sq(log(1 + T));
+                A = 0.5 * gp_sq(gp_log(1 + T));
         } else if (T <= 1.) {
                 Y = T;
                 S = 1.;
@@ -732,7 +737,7 @@ static __device__ double gp_dilog(double x)
         } else {
                 Y = 1. / T;
                 S = -1.;
-                A = PI6 + 0.5 * gp_sq(log(T));
+                A = PI6 + 0.5 * gp_sq(gp_log(T));
         }
         const double H = Y + Y - 1;
         const double ALFA = H + H;
@@ -766,15 +771,15 @@ static __device__ double gp_dcs_bremsstrahlung(const gp_tables & T,
         const double rad_log = el.rad_log;
         const double rad_log_inel = (Z == 1.) ? 446. : 1429.;
         const double delta = m * m * v / (2. * energy * (1. - v));
-        double phi1 = log(rad_log * Z13 * (m / GP_SSR_ME) /
+        double phi1 = gp_log(rad_log * Z13 * (m / GP_SSR_ME) /
             (1. + rad_log * Z13 * T.k.exp_half * delta / GP_SSR_ME));
-        double phi2 = log(rad_log * Z13 * T.k.exp_m16 * (m / GP_SSR_ME) /
+        double phi2 = gp_log(rad_log * Z13 * T.k.exp_m16 * (m / GP_SSR_ME) /
             (1. + rad_log * Z13 * T.k.exp_13 * delta / GP_SSR_ME));
         phi1 -= el.ssr_delta1 * (1. - 1. / Z);
         phi2 -= el.ssr_delta2 * (1. - 1. / Z);
-        const double s_atomic_1 = log(
+        const double s_atomic_1 = gp_log(
             m / delta / (m * delta / (GP_SSR_ME * GP_SSR_ME) + GP_SSR_SQRTE));
-        const double s_atomic_2 = log(1. + GP_SSR_ME /
+        const double s_atomic_2 = gp_log(1. + GP_SSR_ME /
             (delta * rad_log_inel * Z13 * Z13 * GP_SSR_SQRTE));
         const double s_atomic =
             (4. / 3. * (1. - v) + v * v) * (s_atomic_1 - s_atomic_2);
@@ -788,13 +793,13 @@ static __device__ double gp_dcs_bremsstrahlung(const gp_tables & T,
                     1407.77 * v * v * v;
         } else if (v >= 0.01 && v < 0.9) {
                 s_rad = -2.8922 + -19.0156 * v + 57.698 * v * v;
-                const double tmp = log(1. - v);
-                s_rad += -63.418 * v * log(v) + 14.1166 * tmp +
+                const double tmp = gp_log(1. - v);
+                s_rad += -63.418 * v * gp_log(v) + 14.1166 * tmp +
                     1.84206 * tmp * tmp;
         } else {
                 s_rad = 2134.19 + 581.823 * v + -2708.85 * v * v;
-                const double tmp = log(1. - v);
-                s_rad += 4767.05 * v * log(v) + 1.52918 * tmp +
+                const double tmp = gp_log(1. - v);
+                s_rad += 4767.05 * v * gp_log(v) + 1.52918 * tmp +
                     0.361933 * tmp * tmp;
         }
         const double result =
@@ -834,9 +839,9 @@ static __device__ double gp_dcs_pair_d2(const gp_tables & T, const gp_element & 
                 g2 = 5.3E-05;
         }
         const double zeta1 =
-            (0.073 * log(energy / m / (1. + g1 * el.z23 * energy / m)) - 0.26);
+            (0.073 * gp_log(energy / m / (1. + g1 * el.z23 * energy / m)) - 0.26);
         const double zeta2 =
-            (0.058 * log(energy / m / (1 + g2 / Z13 * energy / m)) - 0.14);
+            (0.058 * gp_log(energy / m / (1 + g2 / Z13 * energy / m)) - 0.14);
         double zeta;
         if ((zeta1 > 0.) && (zeta2 > 0.))
                 zeta = zeta1 / zeta2;
@@ -845,7 +850,7 @@ static __device__ double gp_dcs_pair_d2(const gp_tables & T, const gp_element & 
         const double beta = v * v / (2. * (1. - v));
         const double xi =
             gp_sq(m * v / (2. * GP_SSR_ME)) * (1. - rho2) / (1. - v);
-        const double lxi = log(1. + 1. / xi);
+        const double lxi = gp_log(1. + 1. / xi);
         const double Be = ((2. + rho2) * (1. + beta) + xi * (3. + rho2)) * lxi +
             (1. - rho2 - beta) / (1. + xi) - (3. + rho2);
         const double Ce2 = ((1. - rho2) * (1. + beta) + xi * (3. - rho2)) * lxi +
@@ -859,35 +864,35 @@ static __device__ double gp_dcs_pair_d2(const gp_tables & T, const gp_element & 
         double Le1, Le2;
         if (De / Be > 0.) {
                 const double tmp = De / Be;
-                const double Xe = (tmp < 100) ? exp(-tmp) : 0.;
-                Le1 = log(rad_log * Z13 * sxi /
+                const double Xe = (tmp < 100) ? gp_exp(-tmp) : 0.;
+                Le1 = gp_log(rad_log * Z13 * sxi /
                           (Xe + 2. * GP_SSR_ME * T.k.exp_half * rad_log * Z13 *
                                   (1. + xi) / ev)) - tmp -
-                    0.5 * log(Xe + el.pair_medn2 * (1. + xi));
-                Le2 = log(rad_log * Z13 * T.k.exp_m16 * sxi /
+                    0.5 * gp_log(Xe + el.pair_medn2 * (1. + xi));
+                Le2 = gp_log(rad_log * Z13 * T.k.exp_m16 * sxi /
                           (Xe + 2. * GP_SSR_ME * T.k.exp_13 * rad_log * Z13 *
                                   (1. + xi) / ev)) - tmp -
-                    0.5 * log(Xe + el.pair_medn2 * T.k.exp_m13 * (1. + xi));
+                    0.5 * gp_log(Xe + el.pair_medn2 * T.k.exp_m13 * (1. + xi));
         } else {
                 const double tmp = De / Be;
-                const double Xe_inv = (tmp > -100) ? exp(De / Be) : 0;
-                Le1 = log(rad_log * Z13 * sxi /
+                const double Xe_inv = (tmp > -100) ? gp_exp(De / Be) : 0;
+                Le1 = gp_log(rad_log * Z13 * sxi /
                           (1. + Xe_inv * 2. * GP_SSR_ME * T.k.exp_half *
                                     rad_log * Z13 * (1. + xi) / ev)) -
                     0.5 * De / Be -
-                    0.5 * log(1. + Xe_inv * el.pair_medn2 * (1. + xi));
-                Le2 = log(rad_log * Z13 * T.k.exp_m16 * sxi /
+                    0.5 * gp_log(1. + Xe_inv * el.pair_medn2 * (1. + xi));
+                Le2 = gp_log(rad_log * Z13 * T.k.exp_m16 * sxi /
                           (1. + Xe_inv * 2. * GP_SSR_ME * T.k.exp_13 *
                                     rad_log * Z13 * (1. + xi) / ev)) -
                     0.5 * De / Be -
-                    0.5 * log(1. + Xe_inv * el.pair_medn2 * T.k.exp_m13 *
+                    0.5 * gp_log(1. + Xe_inv * el.pair_medn2 * T.k.exp_m13 *
                                        (1. + xi));
         }
         double diagram_e = const_prefactor * (Z + zeta) * (1. - v) / v *
             (Ce1 * Le1 + Ce2 * Le2);
         if (diagram_e < 0.) diagram_e = 0.;
 
-        const double lxi1 = log(1. + xi);
+        const double lxi1 = gp_log(1. + xi);
         const double Bm = ((1. + rho2) * (1. + (3. * beta) / 2) -
                               1. / xi * (1. + 2. * beta) * (1. - rho2)) * lxi1 +
             xi * (1. - rho2 - beta) / (1. + xi) +
@@ -906,20 +911,20 @@ static __device__ double gp_dcs_pair_d2(const gp_tables & T, const gp_element & 
         double Lm1, Lm2;
         if (Dm / Bm > 0.) {
                 const double tmp = Dm / Bm;
-                const double Xm = (tmp < 100) ? exp(-tmp) : 0.;
-                Lm1 = log(m / GP_SSR_ME * rad_log * Z13 / d_n /
+                const double Xm = (tmp < 100) ? gp_exp(-tmp) : 0.;
+                Lm1 = gp_log(m / GP_SSR_ME * rad_log * Z13 / d_n /
                           (Xm + 2. * GP_SSR_ME * T.k.exp_half * rad_log * Z13 *
                                   (1. + xi) / ev)) - tmp;
-                Lm2 = log(m / GP_SSR_ME * rad_log * Z13 / d_n /
+                Lm2 = gp_log(m / GP_SSR_ME * rad_log * Z13 / d_n /
                           (Xm + 2. * GP_SSR_ME * T.k.exp_13 * rad_log * Z13 *
                                   (1. + xi) / ev)) - tmp;
         } else {
                 const double tmp = Dm / Bm;
-                const double Xmv = (tmp > -100) ? exp(tmp) : 0.;
-                Lm1 = log(m / GP_SSR_ME * rad_log * Z13 / d_n /
+                const double Xmv = (tmp > -100) ? gp_exp(tmp) : 0.;
+                Lm1 = gp_log(m / GP_SSR_ME * rad_log * Z13 / d_n /
                     (1. + 2. * GP_SSR_ME * T.k.exp_half * rad_log * Z13 *
                             (1. + xi) / ev * Xmv));
-                Lm2 = log(m / GP_SSR_ME * rad_log * Z13 / d_n /
+                Lm2 = gp_log(m / GP_SSR_ME * rad_log * Z13 / d_n /
                     (1. + 2. * GP_SSR_ME * T.k.exp_13 * rad_log * Z13 *
                             (1. + xi) / ev * Xmv));
         }
@@ -948,10 +953,10 @@ static __device__ double gp_dcs_pair_production(const gp_tables & T,
                 return 0.;
         const double ri = 1. - rmax;
         if ((ri <= 0.) || (ri >= 1.)) return 0.;
-        const double tmin = log(ri);
+        const double tmin = gp_log(ri);
         double I = 0.;
         for (int i = 0; i < 12; i++) {
-                const double rho = exp(gp_gl12_x[i] * tmin);
+                const double rho = gp_exp(gp_gl12_x[i] * tmin);
                 I -= gp_dcs_pair_d2(T, el, K, q, rho) * rho * gp_gl12_w[i] *
                     tmin;
         }
@@ -969,23 +974,23 @@ GPD double gp_f2p_allm97(const gp_tables & T, double x, double Q2)
         const double M = 0.5 * (GP_PROTON_MASS + GP_NEUTRON_MASS);
         const double M2 = M * M;
         const double W2 = M2 + Q2 * (1.0 / x - 1.0);
-        const double t = log(log((Q2 + Q02) / Lambda2) / T.k.allm_lq0);
+        const double t = gp_log(gp_log((Q2 + Q02) / Lambda2) / T.k.allm_lq0);
         const double xP = (Q2 + mP2) / (Q2 + mP2 + W2 - M2);
         const double xR = (Q2 + mR2) / (Q2 + mR2 + W2 - M2);
         /* The six powers of t share one logarithm: t^c = exp(c ln t), exact
          * to a few ulps (t = 0 gives exp(-inf) = 0 as pow). */
-        const double lt = log(t);
+        const double lt = gp_log(t);
         const double cP = 0.28067 +
-            (0.28067 - 0.22291) * (1.0 / (1.0 + exp(2.1979 * lt)) - 1.0);
+            (0.28067 - 0.22291) * (1.0 / (1.0 + gp_exp(2.1979 * lt)) - 1.0);
         const double aP = -0.0808 +
-            (-0.0808 - -0.44812) * (1.0 / (1.0 + exp(1.1709 * lt)) - 1.0);
-        const double bP = 0.36292 + 1.8917 * exp(1.8439 * lt);
-        const double cR = 0.80107 + 0.97307 * exp(3.4942 * lt);
-        const double aR = 0.58400 + 0.37888 * exp(2.6063 * lt);
-        const double bR = 0.01147 + 3.7582 * exp(0.49338 * lt);
-        const double l1x = log(1 - x);
-        const double F2P = cP * exp(aP * log(xP) + bP * l1x);
-        const double F2R = cR * exp(aR * log(xR) + bR * l1x);
+            (-0.0808 - -0.44812) * (1.0 / (1.0 + gp_exp(1.1709 * lt)) - 1.0);
+        const double bP = 0.36292 + 1.8917 * gp_exp(1.8439 * lt);
+        const double cR = 0.80107 + 0.97307 * gp_exp(3.4942 * lt);
+        const double aR = 0.58400 + 0.37888 * gp_exp(2.6063 * lt);
+        const double bR = 0.01147 + 3.7582 * gp_exp(0.49338 * lt);
+        const double l1x = gp_log(1 - x);
+        const double F2P = cP * gp_exp(aP * gp_log(xP) + bP * l1x);
+        const double F2R = cR * gp_exp(aR * gp_log(xR) + bR * l1x);
         return Q2 / (Q2 + m02) * (F2P + F2R);
 }
 
@@ -1009,7 +1014,7 @@ static __device__ double gp_photonuclear_d2(const gp_tables & T,
         else if (x < 0.0014)
                 shadowing = el.shadow_low;
         else if (x < 0.04)
-                shadowing = exp((0.069 * log10(x) + 0.097) * el.log_A);
+                shadowing = gp_exp((0.069 * log10(x) + 0.097) * el.log_A);
         else
                 shadowing = 1.;
         const double F2A = F2p * shadowing *
@@ -1039,12 +1044,12 @@ static __device__ double gp_dcs_photonuclear(const gp_tables & T,
         const double Q2min = ml2 * (q * q - 0.5 * ml2) / (E * (E - q));
         const double Q2max = 2.0 * M * (q - mpi) - mpi * mpi;
         if ((Q2max < Q2min) | (Q2min < 0)) return 0.;
-        const double xmin = log(Q2min);
-        const double xmax = log(Q2max);
+        const double xmin = gp_log(Q2min);
+        const double xmax = gp_log(Q2max);
         const double dx = xmax - xmin;
         double ds = 0.;
         for (int i = 0; i < 9; i++) {
-                const double Q2 = exp(xmin + dx * gp_gl9_x[i]);
+                const double Q2 = gp_exp(xmin + dx * gp_gl9_x[i]);
                 const double w = gp_gl9_w[i] * (dx * Q2);
                 const double tmp = gp_photonuclear_d2(T, el, K, q, Q2);
                 if (tmp <= 0.) continue;
@@ -1104,8 +1109,8 @@ static __device__ double gp_dcs_process(const gp_tables & T, int process,
 }
 
 /* Single precision log and exp, rounded from double precision. */
-GPD float gp_logf(float x) { return (float)log((double)x); }
-GPD float gp_expf(float x) { return (float)exp((double)x); }
+GPD float gp_logf(float x) { return (float)gp_log((double)x); }
+GPD float gp_expf(float x) { return (float)gp_exp((double)x); }
 
 /* dcs_evaluate (pumas.c:11243-11347). */
 static __device__ double gp_dcs_evaluate(const gp_tables & T, int process,
@@ -1252,7 +1257,7 @@ GPD double gp_randn(gp_event & e)
 {
         e.randn_done = !e.randn_done;
         if (!e.randn_done) return e.randn_next;
-        const double r = sqrt(-2. * log(gp_random(e)));
+        const double r = sqrt(-2. * gp_log(gp_random(e)));
         /* sin and cos of 2 pi u, without argument reduction. */
         const double u2 = 2. * gp_random(e);
         double s, c;
@@ -1334,7 +1339,7 @@ static __device__ __forceinline__ double gp_polar_bremsstrahlung(const gp_tables
                 const double q = muni;
                 const double r = mu0;
                 const double qr = q * r;
-                x0 = (1. + 2 * qr) * log((1. + qr) / (r + qr)) -
+                x0 = (1. + 2 * qr) * gp_log((1. + qr) / (r + qr)) -
                     (1. - r) * (1 + 2 * q) / (1 + q);
         }
         for (int i = 0; i < 100; i++) {
@@ -1353,7 +1358,7 @@ static __device__ __forceinline__ double gp_polar_bremsstrahlung(const gp_tables
                 const double r = mu0 * l2;
                 const double qr = q * r;
                 if (qr > 1E+05) continue;
-                const double x = (1. + 2 * qr) * log((1. + qr) / (r + qr)) -
+                const double x = (1. + 2 * qr) * gp_log((1. + qr) / (r + qr)) -
                     (1. - r) * (1 + 2 * q) / (1 + q);
                 pdf *= x / x0;
                 if (score <= pdf) return mu;
@@ -1365,7 +1370,7 @@ static __device__ __forceinline__ double gp_polar_bremsstrahlung(const gp_tables
 GPD double gp_polar_objective(const gp_tables & T, const gp_element & el,
     double K, double q, double lnQ2)
 {
-        const double Q2 = exp(lnQ2);
+        const double Q2 = gp_exp(lnQ2);
         return -gp_photonuclear_d2(T, el, K, q, Q2) * Q2;
 }
 
@@ -1501,13 +1506,13 @@ static __device__ __forceinline__ double gp_polar_photonuclear(const gp_tables &
             2.0 * M * (q - GP_PION_MASS) - GP_PION_MASS * GP_PION_MASS;
         if ((Q2max < Q2min) | (Q2min < 0)) return 0.;
         double fopt = 0., xopt = 0.;
-        const double lnQ2min = log(Q2min);
-        const double lnQ2max = log(Q2max);
+        const double lnQ2min = gp_log(Q2min);
+        const double lnQ2max = gp_log(Q2max);
         const int status = gp_find_minimum(
             T, el, ki, q, lnQ2min, lnQ2max, 1E-06, 100, xopt, fopt);
         fopt = -fopt;
         if (status == -2) return 0.;
-        const double x = exp(xopt) / (2 * q * M);
+        const double x = gp_exp(xopt) / (2 * q * M);
         const double lne = 0.1;
         if ((x <= 0.04) && (xopt + lne < lnQ2max)) {
                 double f2, x2;
@@ -1526,7 +1531,7 @@ static __device__ __forceinline__ double gp_polar_photonuclear(const gp_tables &
         int i;
         for (i = 0; i < 100; i++) {
                 const double u = gp_random(e);
-                Q2 = Q2min * exp(rQ2 * u);
+                Q2 = Q2min * gp_exp(rQ2 * u);
                 const double r = gp_photonuclear_d2(T, el, ki, q, Q2) * Q2;
                 if (gp_random(e) * fopt <= r) break;
         }
@@ -1616,7 +1621,7 @@ static __device__ __forceinline__ double gp_ionisation_randomise(const gp_tables
 GPD double gp_envelope_norm(double a, double xmin, double xmax)
 {
         if (a == 1)
-                return log(xmax / xmin);
+                return gp_log(xmax / xmin);
         else
                 return (pow(xmin, 1. - a) - pow(xmax, 1. - a)) / (a - 1.);
 }
@@ -1785,7 +1790,7 @@ static __device__ __forceinline__ bool gp_del_forward(const gp_tables & T, const
                         u = (u - p0) / (1. - p0);
                 }
                 if (a == 1) {
-                        x = xmin * exp(u * log(xmax / xmin));
+                        x = xmin * gp_exp(u * gp_log(xmax / xmin));
                 } else {
                         const double am = a - 1.;
                         const double pmin = pow(xmin, -am);
@@ -1807,11 +1812,11 @@ static __device__ __forceinline__ bool gp_del_forward(const gp_tables & T, const
 static __device__ __forceinline__ bool gp_del_reverse(const gp_tables & T, const gp_config & cfg,
     gp_event & e, int material, int & process, int & target)
 {
-        const double lnq0 = -log(T.cutoff);
+        const double lnq0 = -gp_log(T.cutoff);
         const double kt = __ldg(T.Kt + material);
         const double kf = e.energy;
         const double pCEL =
-            (kf >= kt) ? 0. : lnq0 / (lnq0 + log(kt / (kt - kf)));
+            (kf >= kt) ? 0. : lnq0 / (lnq0 + gp_log(kt / (kt - kf)));
         if (pCEL && (gp_random(e) < pCEL)) {
                 e.weight /= pCEL;
                 return false;
@@ -2133,7 +2138,7 @@ static __device__ __forceinline__ void gp_limit(const gp_tables & T, const gp_co
                 if (cfg.scattering == GPUMAS_MODE_MIXED) {
                         const double X = Xi -
                             gp_coulomb_ehs_length(T, material, e.energy) *
-                                log(gp_random(e));
+                                gp_log(gp_random(e));
                         if ((grammage_max == 0.) || (X < grammage_max)) {
                                 grammage_max = X;
                                 e.step_foreseen = GPUMAS_EVENT_VERTEX_COULOMB;
@@ -2151,7 +2156,7 @@ static __device__ __forceinline__ void gp_limit(const gp_tables & T, const gp_co
                         if ((zeta <= 0.) || (zeta >= 1.)) continue;
                         const double nI =
                             gp_del_interaction_length(T, material, e.energy) +
-                            sgn * log(zeta);
+                            sgn * gp_log(zeta);
                         if (nI <= 0.) break;
                         const double k = gp_del_kinetic_from_interaction_length(
                             T, material, nI);
@@ -2172,7 +2177,7 @@ static __device__ __forceinline__ void gp_limit(const gp_tables & T, const gp_co
             (cfg.scattering == GPUMAS_MODE_MIXED)) {
                 const double nI = gp_ehs_interaction_length(
                                       T, scheme, material, e.energy) +
-                    sgn * log(gp_random(e));
+                    sgn * gp_log(gp_random(e));
                 if (nI > 0.) {
                         const double k = gp_ehs_kinetic_from_interaction_length(
                             T, scheme, material, nI);
@@ -2383,7 +2388,7 @@ static __device__ __forceinline__ int gp_step(const gp_tables & T, const gp_conf
                             gp_del_cross_section(T, material, k1);
                         if (tmp_del > xs_del) xs_del = tmp_del;
                         if (xs_del <= 0.) break;
-                        const double X_del = -log(gp_random(e)) / xs_del;
+                        const double X_del = -gp_log(gp_random(e)) / xs_del;
                         if (X_del >= Xmax) break;
                         const double k_h = gp_cel_kinetic_energy(
                             T, scheme, material, Xtot - sgn * X_del);
@@ -2411,7 +2416,7 @@ static __device__ __forceinline__ int gp_step(const gp_tables & T, const gp_conf
                         const double lb_ehs =
                             gp_coulomb_ehs_length(T, material, kmin);
                         if (lb_ehs <= 0.) break;
-                        const double X_ehs = -log(gp_random(e)) * lb_ehs;
+                        const double X_ehs = -gp_log(gp_random(e)) * lb_ehs;
                         if (X_ehs >= Xmax) break;
                         const double k_h = gp_cel_kinetic_energy(
                             T, scheme, material, Xtot - sgn * X_ehs);
@@ -2558,7 +2563,7 @@ static __device__ __forceinline__ int gp_step(const gp_tables & T, const gp_conf
                 double mu;
                 int trials = 0;
                 do {
-                        mu = -ilb1 * log(gp_random(e));
+                        mu = -ilb1 * gp_log(gp_random(e));
                 } while ((mu > 1.) && (++trials < GP_MAX_REJECTIONS));
                 if (trials == GP_MAX_REJECTIONS)
                         e.status = GPUMAS_RETURN_INTERNAL_ERROR;
@@ -2699,11 +2704,11 @@ static __device__ __forceinline__ int gp_stepping_step(const gp_tables & T, cons
         if ((cfg.direction == GPUMAS_MODE_BACKWARD) &&
             (cfg.energy_loss >= GPUMAS_MODE_CSDA)) {
                 const double wt = (cfg.decay == GPUMAS_MODE_WEIGHTED) ?
-                    exp(-fabs(e.time - L.ti) / T.ctau) : 1.;
+                    gp_exp(-fabs(e.time - L.ti) / T.ctau) : 1.;
                 e.weight = L.wi * wt * L.dei *
                     gp_cel_energy_loss(T, scheme, L.material, e.energy);
         } else if (cfg.decay == GPUMAS_MODE_WEIGHTED) {
-                e.weight = L.wi * exp(-fabs(e.time - L.ti) / T.ctau);
+                e.weight = L.wi * gp_exp(-fabs(e.time - L.ti) / T.ctau);
         }
 
         if (e.step_event & (GPUMAS_EVENT_LIMIT | GPUMAS_EVENT_WEIGHT |
@@ -2922,7 +2927,7 @@ static __device__ __forceinline__ int gp_transport_csda(const gp_tables & T, con
                     gp_cel_energy_loss(T, GPUMAS_MODE_CSDA, material, kf) /
                     gp_cel_energy_loss(T, GPUMAS_MODE_CSDA, material, ki);
         if (cfg.decay == GPUMAS_MODE_WEIGHTED)
-                e.weight *= exp(-fabs(ti - e.time) / T.ctau);
+                e.weight *= gp_exp(-fabs(ti - e.time) / T.ctau);
         const double path =
             (cfg.direction == GPUMAS_MODE_FORWARD) ? distance : -distance;
         e.pos[0] += path * e.dir[0];
@@ -2988,7 +2993,7 @@ static __device__ __forceinline__ int gp_transport_begin(const gp_tables & T, co
         L.medium = medium;
         if (cfg.decay == GPUMAS_MODE_RANDOMISED) {
                 const double u = gp_random(e);
-                e.lifetime = e.time - T.ctau * log(u);
+                e.lifetime = e.time - T.ctau * gp_log(u);
         }
         int do_stepping = 1;
         if ((step_max_medium <= 0.) &&

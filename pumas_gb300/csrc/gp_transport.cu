@@ -80,6 +80,7 @@ extern "C" int gpumas_context_create(struct gpumas_context ** context,
         c->tuning.pool_slots = 1048576;
         c->tuning.max_inner = 8;
         c->tuning.batch = 16;
+        c->tuning.tail = 0;
         if (extra_memory > 0) {
                 c->extra = calloc(1, extra_memory);
                 c->api.user_data = c->extra;
@@ -312,6 +313,7 @@ extern "C" int gpumas_context_tuning_set(
         if (tuning->pool_slots > 0) c->tuning.pool_slots = tuning->pool_slots;
         if (tuning->max_inner > 0) c->tuning.max_inner = tuning->max_inner;
         if (tuning->batch > 0) c->tuning.batch = tuning->batch;
+        if (tuning->tail != 0) c->tuning.tail = tuning->tail;
         return GPUMAS_RETURN_SUCCESS;
 }
 
@@ -325,6 +327,7 @@ extern "C" int gpumas_context_tuning_get(
         tuning->pool_slots = c->tuning.pool_slots;
         tuning->max_inner = c->tuning.max_inner;
         tuning->batch = c->tuning.batch;
+        tuning->tail = c->tuning.tail;
         return GPUMAS_RETURN_SUCCESS;
 }
 
@@ -466,6 +469,36 @@ extern "C" int gpumas_bench_dfma(double * tflops)
         cudaFree(d);
         const double flops = 2. * 8. * iters * (double)threads * blocks;
         *tflops = (ms > 0.f) ? flops / (ms * 1E-03) * 1E-12 : 0.;
+        return rc;
+}
+
+/* The engine's elementary functions on the device, for checking. */
+__global__ void gp_kernel_math(int fn, size_t n, const double * x, double * y)
+{
+        const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+        if (i >= n) return;
+        y[i] = (fn == 0) ? gp_log(x[i]) : gp_exp(x[i]);
+}
+
+extern "C" int gpumas_math_eval(int fn, size_t n, const double * x,
+    double * y)
+{
+        if ((x == NULL) || (y == NULL) || (n == 0) || (fn < 0) || (fn > 1))
+                return GPUMAS_RETURN_VALUE_ERROR;
+        double * d = NULL;
+        int rc = gp_check(cudaMalloc(&d, 2 * n * sizeof(double)));
+        if (rc != GPUMAS_RETURN_SUCCESS) return rc;
+        rc = gp_check(cudaMemcpy(d, x, n * sizeof(double),
+            cudaMemcpyHostToDevice));
+        if (rc == GPUMAS_RETURN_SUCCESS) {
+                gp_kernel_math<<<(unsigned int)((n + 255) / 256), 256>>>(
+                    fn, n, d, d + n);
+                rc = gp_check(cudaGetLastError());
+        }
+        if (rc == GPUMAS_RETURN_SUCCESS)
+                rc = gp_check(cudaMemcpy(y, d + n, n * sizeof(double),
+                    cudaMemcpyDeviceToHost));
+        cudaFree(d);
         return rc;
 }
 

@@ -239,9 +239,9 @@ def bench(args, rank, world, local):
                  "events_per_s": events / wall,
                  "latency_ms": percentiles(lat), "event_errors": errors,
                  "sustained": bool(wall <= 1.1 * window + 0.05)}
-        # The plain baseline on the same arrivals (bounded: at most 2000
+        # The plain baseline on the same arrivals (bounded: at most 300
         # requests, the first ones).
-        m = min(n, 2000)
+        m = min(n, 300)
         preqs = [mix.make(base + i) for i in range(m)]
         pwall = plain_serve(preqs, arrivals[:m])
         same = all(np.array_equal(a.final, b.final) and

@@ -122,9 +122,15 @@ def config_dict(kind):
                     event=EVENT_LIMIT_ENERGY, limit_energy=1.,
                     accuracy=1E-02)
     if kind == "terrain":
+        # Backward transport stops on leaving the geometry (z = 3 km) or,
+        # for near horizontal tracks through kilometres of rock, when the
+        # energy reaches the top of the tables (1e8 GeV): beyond it the
+        # muon flux weight is negligible and the reference's hard elastic
+        # scatter sampling (pumas.c:5839-5864) practically never accepts.
         return dict(energy_loss=MODE_STRAGGLED, decay=MODE_WEIGHTED,
                     direction=MODE_BACKWARD, scattering=MODE_MIXED,
-                    event=EVENT_NONE, limit_energy=0., accuracy=1E-02)
+                    event=EVENT_LIMIT_ENERGY, limit_energy=TERRAIN_EMAX,
+                    accuracy=1E-02)
     raise KeyError(kind)
 
 
@@ -151,6 +157,7 @@ TERRAIN_SIGMA = 1500.    # m
 TERRAIN_NOISE = 5.       # m, i.i.d. Gaussian noise before smoothing
 TERRAIN_ZTOP = 3000.     # m, end of the transport (no medium above)
 TERRAIN_DEPTH = 20.      # m, detector depth below the surface
+TERRAIN_EMAX = 1E+08     # GeV, backward energy limit (top of the tables)
 FLUX_NORM = 0.14         # GeV^-1 cm^-2 s^-1 sr^-1 at 1 GeV
 FLUX_INDEX = 2.7
 

@@ -162,11 +162,14 @@ def test_gpu_edge_cases(gpu_physics):
 @pytest.mark.parametrize("name", ["rock_slab", "stack_forward_mixed",
                                   "stack_backward_straggled",
                                   "water_time_limit", "plain_csda"])
-@pytest.mark.parametrize("slots,inner", [(256, 1), (1024, 3)])
-def test_pool_engine_matches_plain_engine(gpu_physics, name, slots, inner):
+@pytest.mark.parametrize("slots,inner,tail", [(256, 1, -1), (1024, 3, 0),
+                                               (2048, 8, 700)])
+def test_pool_engine_matches_plain_engine(gpu_physics, name, slots, inner,
+                                          tail):
     """The slot pool engine reproduces the one thread per event engine bit
-    for bit: regrouping by step kind changes the execution order of events,
-    never the draws or arithmetic of any event."""
+    for bit: regrouping by step kind, and the inline drain of the last
+    events (tail), change the execution order of events, never the draws or
+    arithmetic of any event."""
     import pumas_gb300 as pg
     case = CASES[name]
     s0 = make_states(name, n=3000, first_event=77)
@@ -174,7 +177,8 @@ def test_pool_engine_matches_plain_engine(gpu_physics, name, slots, inner):
     out = []
     for engine in (pg.ENGINE_PLAIN, pg.ENGINE_POOL):
         ctx = gpu_context(gpu_physics, case["config"], case["seed"], geo)
-        ctx.tuning(engine=engine, pool_slots=slots, max_inner=inner, batch=4)
+        ctx.tuning(engine=engine, pool_slots=slots, max_inner=inner, batch=4,
+                   tail=tail)
         out.append(ctx.transport(s0, 77))
     (a, ra), (b, rb) = out
     assert a.tobytes() == b.tobytes()
