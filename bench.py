@@ -44,10 +44,10 @@ sys.path.insert(0, ROOT)
 F_STEP = 680.4
 F_STEP_EXECUTED = 681.7
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum over every pool
-# kernel launch of one batch) per reference step, from one ncu launch list
-# of a 2e6-event rock slab batch (314.2 GB over 547 988 323 steps); the
-# traffic of a batch is this times its steps.
-TRAFFIC_STEP = 573.3
+# kernel launch) per reference step, from one ncu launch list of two
+# 2e6-event rock slab batches (612.4 GB over 1.0957e9 steps); the traffic
+# of a batch is this times its steps.
+TRAFFIC_STEP = 559.0
 
 
 def parse():
@@ -836,8 +836,9 @@ def main():
                     "unit": "TFLOP/s", "frac": achieved / peak,
                     "traffic": (None if TRAFFIC_STEP is None else
                                 TRAFFIC_STEP * steps_total),
-                    "kernel": "transport of one batch: gp_pool_step, "
-                              "gp_pool_del, gp_pool_polar, gp_pool_ehs",
+                    "kernel": "transport of one batch: gp_pool_drain, "
+                              "gp_pool_step, gp_pool_del, gp_pool_polar, "
+                              "gp_pool_ehs",
                     "f_step": F_STEP,
                     "f_step_executed": F_STEP_EXECUTED,
                     "peak_source": "measured: DFMA microbenchmark in this "
