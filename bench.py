@@ -681,7 +681,7 @@ def run_plain_csda(args, rank, world, local):
                                % (n * 104 / 1E+09)})
     cpu = None
     if not args.no_baseline:
-        m = min(n, 2_000_000)
+        m = min(n, 20_000_000)
         cpu = port_baseline("plain_csda", s0[:m],
                             W.config_dict("plain_csda"),
                             dict(kind=0, media=[("StandardRock", 0.)]),

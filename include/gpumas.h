@@ -251,6 +251,44 @@ int gpumas_context_transport_device(struct gpumas_context * context,
     size_t n, const struct gpumas_soa * events, uint64_t first_event,
     void * stream);
 
+/** A recorded frame (struct pumas_frame, pumas.h:378-395): the state, the
+ * medium index in the geometry (-1 for none) and the event flags, with the
+ * reference's PUMAS_EVENT_START (4096) and PUMAS_EVENT_STOP (8192). */
+struct gpumas_frame {
+        struct gpumas_state state;
+        int medium;
+        int event;
+};
+
+#define GPUMAS_EVENT_START 4096
+#define GPUMAS_EVENT_STOP 8192
+
+/**
+ * A device frame recorder (struct pumas_recorder, pumas.h:432-458). Event k
+ * of a transport call writes its frames to frames[k * max_frames ...] and
+ * the number of frames the reference's recorder would hold to length[k];
+ * frames beyond max_frames are not written (length still counts them). As
+ * in the reference, `period` = 1 records every step, n every n-th step and
+ * a period <= 0 only the start, the stop, the DELs and the medium changes
+ * (pumas.c:5227-5231, 5296-5374, 5464-5467, 5507-5510, 4793-4798,
+ * 4944-4946). Both arrays are in device memory.
+ */
+struct gpumas_recorder {
+        int period;
+        int max_frames;
+        struct gpumas_frame * frames;
+        int * length;
+};
+
+/**
+ * Record the next transport calls of this context (the `recorder` field of
+ * pumas_context, pumas.h:636-672), or stop recording with NULL. A
+ * recording context runs the one thread per event engine; the transported
+ * states are the same as without recording.
+ */
+int gpumas_context_recorder_set(struct gpumas_context * context,
+    const struct gpumas_recorder * recorder);
+
 /**
  * Engine parameters of a context. `engine` selects the execution scheme:
  * 0 automatic, 1 one GPU thread per event for the whole transport call,

@@ -36,6 +36,11 @@ RESULT_DTYPE = np.dtype([
     ("status", "i4"), ("steps", "i4"), ("pad", "i4"), ("draws", "u8")])
 
 
+# struct oracle_frame (oracle.h): a state, the medium index and the event.
+FRAME_DTYPE = np.dtype([("state", STATE_DTYPE), ("medium", "i4"),
+                        ("event", "i4")])
+
+
 class Medium(ctypes.Structure):
     _fields_ = [("material", ctypes.c_int), ("density", ctypes.c_double)]
 
@@ -204,6 +209,31 @@ class Reference(_Oracle):
         rc = self.lib.oracle_ref_load(dump_path.encode())
         if rc != 0:
             raise RuntimeError("reference load error %d" % rc)
+
+
+def _reference_record(self, config, geometry, states, first_event, period,
+                      max_frames):
+    """Transport with the reference's frame recorder; returns (states,
+    results, frames [n, max_frames], frame counts)."""
+    f = self.lib.oracle_ref_transport_record
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.POINTER(Config), ctypes.POINTER(Geometry),
+                  ctypes.c_int64, ctypes.c_uint64, ctypes.c_void_p,
+                  ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                  ctypes.c_void_p, ctypes.c_void_p]
+    s = np.array(states, dtype=STATE_DTYPE, copy=True, order="C")
+    r = np.zeros(len(s), dtype=RESULT_DTYPE)
+    frames = np.zeros((len(s), max_frames), dtype=FRAME_DTYPE)
+    length = np.zeros(len(s), dtype=np.int32)
+    rc = f(ctypes.byref(config), ctypes.byref(geometry), len(s), first_event,
+           s.ctypes.data, r.ctypes.data, period, max_frames,
+           frames.ctypes.data, length.ctypes.data)
+    if rc != 0:
+        raise RuntimeError("oracle record error %d" % rc)
+    return s, r, frames, length
+
+
+Reference.transport_record = _reference_record
 
 
 def reference_available():

@@ -60,4 +60,12 @@ struct oracle_result {
         uint64_t draws; /* number of random draws */
 };
 
+/* A recorded frame (struct pumas_frame, pumas.h:378-395) with the medium
+ * as an index, -1 for none. Same layout as struct gpumas_frame. */
+struct oracle_frame {
+        struct oracle_state state;
+        int medium;
+        int event;
+};
+
 #endif

@@ -251,3 +251,99 @@ int oracle_ref_transport(const struct oracle_config * cfg,
         free(media);
         return rc_all;
 }
+
+/* Transport a batch of events with the reference's frame recorder
+ * (pumas_recorder_create, default in-memory recording, pumas.c:2797-2852,
+ * 7738-7780), one event after the other: event k's frames are copied to
+ * frames[k * max_frames ...] (at most max_frames) and the recorder's frame
+ * count to length[k]. */
+int oracle_ref_transport_record(const struct oracle_config * cfg,
+    const struct gpumas_geometry * geometry, int64_t n, uint64_t first_event,
+    struct oracle_state * states, struct oracle_result * results,
+    int period, int max_frames, struct oracle_frame * frames, int * length)
+{
+        if (ref_physics == NULL) return PUMAS_RETURN_PHYSICS_ERROR;
+        pumas_error_handler_set(NULL);
+        struct ref_medium * media =
+            calloc(geometry->n_media > 0 ? geometry->n_media : 1,
+                sizeof(*media));
+        if (media == NULL) return PUMAS_RETURN_MEMORY_ERROR;
+        int i;
+        for (i = 0; i < geometry->n_media; i++) {
+                media[i].api.material = geometry->media[i].material;
+                media[i].density = geometry->media[i].density;
+                media[i].api.locals =
+                    (media[i].density > 0.) ? &ref_locals : NULL;
+        }
+        struct pumas_context * context = NULL;
+        struct pumas_recorder * recorder = NULL;
+        enum pumas_return rc = pumas_context_create(
+            &context, ref_physics, sizeof(struct ref_event));
+        if (rc == PUMAS_RETURN_SUCCESS)
+                rc = pumas_recorder_create(&recorder, 0);
+        if (rc != PUMAS_RETURN_SUCCESS) {
+                if (context != NULL) pumas_context_destroy(&context);
+                free(media);
+                return rc;
+        }
+        recorder->period = period;
+        context->recorder = recorder;
+        context->medium = &ref_medium_cb;
+        context->random = &ref_random;
+        context->mode.energy_loss = cfg->energy_loss;
+        context->mode.decay = cfg->decay;
+        context->mode.direction = cfg->direction;
+        context->mode.scattering = cfg->scattering;
+        context->event = cfg->event;
+        context->limit.energy = cfg->limit_energy;
+        context->limit.distance = cfg->limit_distance;
+        context->limit.grammage = cfg->limit_grammage;
+        context->limit.time = cfg->limit_time;
+        context->accuracy = cfg->accuracy;
+        struct ref_event * data = context->user_data;
+        data->geometry = geometry;
+        data->media = media;
+        struct simulation_context * context_ =
+            (struct simulation_context *)context;
+        int64_t k;
+        for (k = 0; k < n; k++) {
+                data->stream.seed = cfg->seed;
+                data->stream.event = first_event + k;
+                data->stream.n = 0;
+                data->stream.next = 0.;
+                data->steps = 0;
+                context_->randn_done = 0;
+                context_->randn_next = 0.;
+                pumas_recorder_clear(recorder);
+                enum pumas_event event = PUMAS_EVENT_NONE;
+                struct pumas_medium * m[2] = { NULL, NULL };
+                const enum pumas_return rck = pumas_context_transport(
+                    context, (struct pumas_state *)(states + k), &event, m);
+                struct oracle_result * r = results + k;
+                r->event = event;
+                r->medium_in = (m[0] == NULL) ? -1 :
+                    (int)((struct ref_medium *)m[0] - media);
+                r->medium_out = (m[1] == NULL) ? -1 :
+                    (int)((struct ref_medium *)m[1] - media);
+                r->status = rck;
+                r->steps = data->steps;
+                r->pad = 0;
+                r->draws = data->stream.n;
+                length[k] = recorder->length;
+                const struct pumas_frame * f = recorder->first;
+                int j;
+                for (j = 0; (j < max_frames) && (f != NULL);
+                     j++, f = f->next) {
+                        struct oracle_frame * o =
+                            frames + k * (int64_t)max_frames + j;
+                        memcpy(&o->state, &f->state, sizeof(o->state));
+                        o->medium = (f->medium == NULL) ? -1 :
+                            (int)((struct ref_medium *)f->medium - media);
+                        o->event = f->event;
+                }
+        }
+        pumas_recorder_destroy(&recorder);
+        pumas_context_destroy(&context);
+        free(media);
+        return PUMAS_RETURN_SUCCESS;
+}

@@ -58,6 +58,10 @@ STATE_DTYPE = np.dtype([
 RESULT_DTYPE = np.dtype([
     ("event", "i4"), ("medium_in", "i4"), ("medium_out", "i4"),
     ("status", "i4"), ("steps", "i4"), ("pad", "i4"), ("draws", "u8")])
+# struct gpumas_frame: a recorded state, its medium index and event flags.
+FRAME_DTYPE = np.dtype([("state", STATE_DTYPE), ("medium", "i4"),
+                        ("event", "i4")])
+EVENT_START, EVENT_STOP = 4096, 8192
 
 
 class PumasError(RuntimeError):
@@ -102,6 +106,11 @@ class _Context(ctypes.Structure):
     _fields_ = [("mode", _Mode), ("event", ctypes.c_int), ("limit", _Limit),
                 ("accuracy", ctypes.c_double), ("seed", ctypes.c_uint64),
                 ("user_data", ctypes.c_void_p)]
+
+
+class _Recorder(ctypes.Structure):
+    _fields_ = [("period", ctypes.c_int), ("max_frames", ctypes.c_int),
+                ("frames", ctypes.c_void_p), ("length", ctypes.c_void_p)]
 
 
 class _Stats(ctypes.Structure):
@@ -196,6 +205,8 @@ def library(build=False):
         lib.gpumas_engine_run.argtypes = [vp, sz, ctypes.POINTER(_Job)]
         lib.gpumas_engine_stats.argtypes = [
             vp, ctypes.POINTER(_EngineStats)]
+        lib.gpumas_context_recorder_set.argtypes = [
+            ctypes.POINTER(_Context), ctypes.POINTER(_Recorder)]
         lib.gpumas_bench_dfma.argtypes = [ctypes.POINTER(ctypes.c_double)]
         lib.gpumas_random_fill.argtypes = [
             u64, ctypes.c_uint32, u64, u64, sz, vp]
@@ -208,7 +219,8 @@ def library(build=False):
                   "gpumas_bench_dfma", "gpumas_random_fill",
                   "gpumas_engine_create", "gpumas_engine_submit",
                   "gpumas_engine_submit_host", "gpumas_engine_step",
-                  "gpumas_engine_run", "gpumas_engine_stats"):
+                  "gpumas_engine_run", "gpumas_engine_stats",
+                  "gpumas_context_recorder_set"):
             getattr(lib, f).restype = i
         _lib = lib
     return _lib
@@ -353,6 +365,32 @@ class Context:
                                      not np.any(r["status"] == rc)):
             raise PumasError(rc, "gpumas_context_transport")
         return s, r
+
+    def transport_record(self, states, first_event=0, period=1,
+                         max_frames=64):
+        """Transport a copy of `states` with the device frame recorder
+        (pumas_recorder: `period` 1 records every step, <= 0 only starts,
+        stops, DELs and medium changes). Returns (states, results, frames
+        [n, max_frames] of FRAME_DTYPE, frame counts); an event with more
+        than max_frames frames keeps its first max_frames ones."""
+        import torch
+        n = len(states)
+        dev = torch.device("cuda", torch.cuda.current_device())
+        frames = torch.zeros((max(n, 1), max_frames * FRAME_DTYPE.itemsize),
+                             dtype=torch.uint8, device=dev)
+        length = torch.zeros(max(n, 1), dtype=torch.int32, device=dev)
+        rec = _Recorder(period, max_frames, frames.data_ptr(),
+                        length.data_ptr())
+        _check(self._lib.gpumas_context_recorder_set(self._ptr,
+                                                     ctypes.byref(rec)),
+               "gpumas_context_recorder_set")
+        try:
+            s, r = self.transport(states, first_event)
+        finally:
+            self._lib.gpumas_context_recorder_set(self._ptr, None)
+        f = np.frombuffer(frames.cpu().numpy().tobytes(),
+                          dtype=FRAME_DTYPE).reshape(max(n, 1), max_frames)
+        return s, r, f[:n], length.cpu().numpy()[:n]
 
     def transport_raw(self, n, states_ptr, results_ptr, first_event=0):
         """Transport n states at a host address (in place)."""

@@ -37,6 +37,8 @@ struct gp_context {
         void * extra;
         struct gpumas_engine * pool; /* slot pool engine of the context */
         struct gp_tuning tuning;
+        struct gpumas_recorder recorder; /* frames, if recording */
+        int recording;
 };
 
 

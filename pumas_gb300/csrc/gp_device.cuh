@@ -127,6 +127,40 @@ struct gp_event {
         int status;
 };
 
+/* Recorder of one event (struct pumas_recorder, pumas.h:432-458): the
+ * event's frame array of a gpumas_recorder and the count of frames the
+ * reference would have recorded so far. Transport functions take a
+ * pointer to it that is NULL when not recording; they are inlined, so the
+ * recording code vanishes from kernels that never record. */
+struct gp_rec {
+        gpumas_frame * frames;
+        int max_frames;
+        int period;
+        int count;
+};
+
+/* record_state (pumas.c:7738-7780) into the event's frame array. */
+GPD void gp_rec_frame(gp_rec * r, const gp_event & e, int medium, int event)
+{
+        if (r->count < r->max_frames) {
+                gpumas_frame & f = r->frames[r->count];
+                f.state.charge = e.charge;
+                f.state.energy = e.energy;
+                f.state.distance = e.distance;
+                f.state.grammage = e.grammage;
+                f.state.time = e.time;
+                f.state.weight = e.weight;
+                for (int k = 0; k < 3; k++) {
+                        f.state.position[k] = e.pos[k];
+                        f.state.direction[k] = e.dir[k];
+                }
+                f.state.decayed = e.decayed;
+                f.medium = medium;
+                f.event = event;
+        }
+        r->count++;
+}
+
 GPD double gp_random(gp_event & e)
 {
         double u;
@@ -2598,13 +2632,16 @@ enum gp_next {
  * (pumas.c:5201-5271). Returns GP_NEXT_STEP or GP_NEXT_DONE (then *event is
  * the end event). */
 static __device__ __forceinline__ int gp_stepping_begin(const gp_tables & T, const gp_config & cfg,
-    const gpumas_geometry & g, gp_event & e, gp_loop & L, int & event)
+    const gpumas_geometry & g, gp_event & e, gp_loop & L, int & event,
+    gp_rec * rec = NULL)
 {
         L.material = gp_medium_material(g, L.medium);
         const int scheme = cfg.energy_loss;
         L.straight = ((cfg.scattering == GPUMAS_MODE_DISABLED) &&
                          (scheme <= GPUMAS_MODE_MIXED)) ? 1 : 0;
         e.step_event = GPUMAS_EVENT_NONE;
+        if (rec != NULL)
+                gp_rec_frame(rec, e, L.medium, GPUMAS_EVENT_START);
         L.ti = e.time;
         L.wi = e.weight;
         L.Xi = e.grammage;
@@ -2678,7 +2715,8 @@ static __device__ __forceinline__ int gp_stepping_relimit(const gp_tables & T, c
 /* One iteration of the stepping loop up to the dispatch of its event
  * (pumas.c:5277-5329 and the medium change of 5417-5467). */
 static __device__ __forceinline__ int gp_stepping_step(const gp_tables & T, const gp_config & cfg,
-    const gpumas_geometry & g, gp_event & e, gp_loop & L, int & event)
+    const gpumas_geometry & g, gp_event & e, gp_loop & L, int & event,
+    gp_rec * rec = NULL)
 {
         if (L.step_index > 1) {
                 const int m = gp_locate(g, e);
@@ -2698,7 +2736,11 @@ static __device__ __forceinline__ int gp_stepping_step(const gp_tables & T, cons
                 event = e.step_event;
                 return GP_NEXT_DONE;
         }
-        if (!e.step_event) return GP_NEXT_STEP;
+        /* A recorded step (every period-th, pumas.c:5296-5303) also updates
+         * the weight; the update is idempotent until the next event. */
+        const int record_step = (rec != NULL) && (rec->period > 0) &&
+            (L.step_index != 1) && ((L.step_index % rec->period) == 0);
+        if (!e.step_event && !record_step) return GP_NEXT_STEP;
 
         const int scheme = cfg.energy_loss;
         if ((cfg.direction == GPUMAS_MODE_BACKWARD) &&
@@ -2711,6 +2753,10 @@ static __device__ __forceinline__ int gp_stepping_step(const gp_tables & T, cons
                 e.weight = L.wi * gp_exp(-fabs(e.time - L.ti) / T.ctau);
         }
 
+        if (!e.step_event) {
+                gp_rec_frame(rec, e, L.medium, GPUMAS_EVENT_NONE);
+                return GP_NEXT_STEP;
+        }
         if (e.step_event & (GPUMAS_EVENT_LIMIT | GPUMAS_EVENT_WEIGHT |
                                GPUMAS_EVENT_VERTEX_DECAY)) {
                 event = e.step_event;
@@ -2740,6 +2786,8 @@ static __device__ __forceinline__ int gp_stepping_step(const gp_tables & T, cons
                     0.;
                 e.step_first = 1;
                 e.step_invlb1 = 0;
+                if ((rec != NULL) && !(cfg.event & GPUMAS_EVENT_MEDIUM))
+                        gp_rec_frame(rec, e, L.medium, e.step_event);
                 return gp_stepping_relimit(T, cfg, e, L, event);
         }
         e.status = GPUMAS_RETURN_INTERNAL_ERROR;
@@ -2763,12 +2811,40 @@ static __device__ __forceinline__ int gp_stepping_del_end(const gp_tables & T,
         return gp_stepping_relimit(T, cfg, e, L, event);
 }
 
-/* DEL of the stepping loop (pumas.c:5336-5374 and 5479-5488). */
+/* DEL of the stepping loop (pumas.c:5336-5374 and 5479-5488). When
+ * recording with a positive period, the pre step point (energy and
+ * direction before the DEL, with the DEL flag) and, unless the transport
+ * stops, the post step point are recorded. */
 static __device__ __forceinline__ int gp_stepping_del(const gp_tables & T,
-    const gp_config & cfg, gp_event & e, gp_loop & L, int & event)
+    const gp_config & cfg, gp_event & e, gp_loop & L, int & event,
+    gp_rec * rec = NULL)
 {
+        if ((rec == NULL) || (rec->period <= 0)) {
+                gp_do_del(T, cfg, e, L.material);
+                return gp_stepping_del_end(T, cfg, e, L, event);
+        }
+        const double ki = e.energy;
+        const double ui[3] = { e.dir[0], e.dir[1], e.dir[2] };
         gp_do_del(T, cfg, e, L.material);
-        return gp_stepping_del_end(T, cfg, e, L, event);
+        {
+                const double kf = e.energy;
+                const double uf[3] = { e.dir[0], e.dir[1], e.dir[2] };
+                e.energy = ki;
+                e.dir[0] = ui[0], e.dir[1] = ui[1], e.dir[2] = ui[2];
+                gp_rec_frame(rec, e, L.medium, e.step_event);
+                e.energy = kf;
+                e.dir[0] = uf[0], e.dir[1] = uf[1], e.dir[2] = uf[2];
+        }
+        if ((cfg.event & e.step_event) ||
+            (e.step_event == GPUMAS_EVENT_WEIGHT) ||
+            (e.status != GPUMAS_RETURN_SUCCESS)) {
+                event = e.step_event;
+                return GP_NEXT_DONE;
+        }
+        gp_rec_frame(rec, e, L.medium, GPUMAS_EVENT_NONE);
+        e.step_first = 1;
+        e.step_invlb1 = 0;
+        return gp_stepping_relimit(T, cfg, e, L, event);
 }
 
 /* EHS of the stepping loop (pumas.c:5393-5400 and 5479-5488). */
@@ -2802,7 +2878,8 @@ GPD void gp_stepping_end(const gp_config & cfg, gp_event & e)
 
 /* transport_with_csda (pumas.c:4777-4949), no magnetic field. */
 static __device__ __forceinline__ int gp_transport_csda(const gp_tables & T, const gp_config & cfg,
-    gp_event & e, int material, double density)
+    gp_event & e, int material, double density, int medium = -1,
+    gp_rec * rec = NULL)
 {
         const double ki = e.energy;
         const double di = e.distance;
@@ -2810,6 +2887,8 @@ static __device__ __forceinline__ int gp_transport_csda(const gp_tables & T, con
         const double xi = gp_cel_grammage(T, GPUMAS_MODE_CSDA, material, ki);
         const double Ti = gp_cel_proper_time(T, GPUMAS_MODE_CSDA, material, ki);
         int event = GPUMAS_EVENT_NONE;
+        if (rec != NULL)
+                gp_rec_frame(rec, e, medium, GPUMAS_EVENT_START);
         double xB;
         if (cfg.event & GPUMAS_EVENT_LIMIT_GRAMMAGE) {
                 xB = cfg.limit_grammage - e.grammage;
@@ -2933,6 +3012,8 @@ static __device__ __forceinline__ int gp_transport_csda(const gp_tables & T, con
         e.pos[0] += path * e.dir[0];
         e.pos[1] += path * e.dir[1];
         e.pos[2] += path * e.dir[2];
+        if (rec != NULL)
+                gp_rec_frame(rec, e, medium, event | GPUMAS_EVENT_STOP);
         return event;
 }
 
@@ -2960,7 +3041,7 @@ GPD void gp_event_init(gp_event & e, uint64_t seed, uint64_t id)
  * *event set (including the whole deterministic CSDA case). */
 static __device__ __forceinline__ int gp_transport_begin(const gp_tables & T, const gp_config & cfg,
     const gpumas_geometry & g, gp_event & e, gp_loop & L, int & event,
-    int & medium_in)
+    int & medium_in, gp_rec * rec = NULL)
 {
         event = GPUMAS_EVENT_NONE;
         medium_in = -1;
@@ -2982,6 +3063,9 @@ static __device__ __forceinline__ int gp_transport_begin(const gp_tables & T, co
         medium_in = medium;
         if (medium < 0) {
                 event = GPUMAS_EVENT_MEDIUM;
+                if (rec != NULL)
+                        gp_rec_frame(rec, e, -1, GPUMAS_EVENT_MEDIUM |
+                            GPUMAS_EVENT_START | GPUMAS_EVENT_STOP);
                 return GP_NEXT_DONE;
         } else if (step_max_medium > 0.)
                 step_max_medium += 0.5 * GP_STEP_MIN;
@@ -3009,40 +3093,47 @@ static __device__ __forceinline__ int gp_transport_begin(const gp_tables & T, co
         }
         if (!do_stepping) {
                 event = gp_transport_csda(T, cfg, e,
-                    gp_medium_material(g, medium), L.density);
+                    gp_medium_material(g, medium), L.density, medium, rec);
                 return GP_NEXT_DONE;
         }
         L.step_max_medium = step_max_medium;
-        const int next = gp_stepping_begin(T, cfg, g, e, L, event);
-        if (next == GP_NEXT_DONE) gp_stepping_end(cfg, e);
-        return next;
+        /* The early stops of the stepping prologue return as they are,
+         * without the final energy protection (pumas.c:5250-5271). */
+        return gp_stepping_begin(T, cfg, g, e, L, event, rec);
 }
 
 /* Resume the stepping loop of an event at phase `next` and run it to its
  * end (the one thread per event form). */
 static __device__ __forceinline__ void gp_transport_run(const gp_tables & T, const gp_config & cfg,
     const gpumas_geometry & g, gp_event & e, gp_loop & L, int next,
-    int & event)
+    int & event, gp_rec * rec = NULL)
 {
         while (next != GP_NEXT_DONE) {
                 if (next == GP_NEXT_STEP)
-                        next = gp_stepping_step(T, cfg, g, e, L, event);
+                        next = gp_stepping_step(T, cfg, g, e, L, event, rec);
                 else if (next == GP_NEXT_DEL)
-                        next = gp_stepping_del(T, cfg, e, L, event);
+                        next = gp_stepping_del(T, cfg, e, L, event, rec);
                 else
                         next = gp_stepping_ehs(T, cfg, e, L, event);
         }
         gp_stepping_end(cfg, e);
+        /* End of the track (pumas.c:5507-5510); a failed step returns
+         * before it in the reference. */
+        if ((rec != NULL) && (e.status == GPUMAS_RETURN_SUCCESS))
+                gp_rec_frame(rec, e, L.medium,
+                    e.step_event | GPUMAS_EVENT_STOP);
 }
 
 /* pumas_context_transport for one event, in one thread. */
 static __device__ __forceinline__ void gp_transport(const gp_tables & T, const gp_config & cfg,
     const gpumas_geometry & g, gp_event & e, int & event, int & medium_in,
-    int & medium_out)
+    int & medium_out, gp_rec * rec = NULL)
 {
         gp_loop L;
-        const int next = gp_transport_begin(T, cfg, g, e, L, event, medium_in);
-        if (next != GP_NEXT_DONE) gp_transport_run(T, cfg, g, e, L, next, event);
+        const int next = gp_transport_begin(
+            T, cfg, g, e, L, event, medium_in, rec);
+        if (next != GP_NEXT_DONE)
+                gp_transport_run(T, cfg, g, e, L, next, event, rec);
         medium_out = L.medium;
 }
 

@@ -40,6 +40,32 @@ __global__ void __launch_bounds__(128, 1) gp_kernel_plain(
         io.store(i, e, event, m_in, m_out);
 }
 
+/* One thread per event with the frame recorder (struct pumas_recorder,
+ * pumas.h:432-458): event i writes its frames after those of events
+ * 0 .. i - 1, max_frames each. */
+__global__ void __launch_bounds__(128, 1) gp_kernel_plain_rec(
+    const gp_tables * __restrict__ Tp, const gp_config cfg,
+    const gpumas_geometry * __restrict__ gp, const gp_io io, size_t n,
+    uint64_t first_event, const gpumas_recorder recorder)
+{
+        const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+        if (i >= n) return;
+        const gp_tables & T = *Tp;
+        const gpumas_geometry & g = *gp;
+        gp_event e;
+        io.load(i, e);
+        gp_event_init(e, cfg.seed, first_event + i);
+        gp_rec r;
+        r.frames = recorder.frames + i * (size_t)recorder.max_frames;
+        r.max_frames = recorder.max_frames;
+        r.period = recorder.period;
+        r.count = 0;
+        int event, m_in, m_out;
+        gp_transport(T, cfg, g, e, event, m_in, m_out, &r);
+        io.store(i, e, event, m_in, m_out);
+        recorder.length[i] = r.count;
+}
+
 /* Draws of the Philox stream, for checking against other implementations. */
 __global__ void gp_kernel_random(uint64_t seed, uint32_t domain,
     uint64_t event, uint64_t first, size_t n, double * out)
@@ -280,7 +306,14 @@ static int gp_run(gp_context * c, const gp_config & cfg, const gp_io & io,
         if (engine == 0) engine = gp_needs_stepping(c, cfg) ? 2 : 1;
         int rc;
         cudaEventRecord(c->t0, s);
-        if (engine == 2) {
+        if (c->recording) {
+                const unsigned int grid =
+                    (unsigned int)((n + gp_block - 1) / gp_block);
+                gp_kernel_plain_rec<<<grid, gp_block, 0, s>>>(c->d_tables,
+                    cfg, c->d_geometry, io, n, first_event, c->recorder);
+                rc = gp_check(cudaGetLastError());
+                c->stats.launches = 1;
+        } else if (engine == 2) {
                 int launches = 0;
                 rc = gp_pool_transport(
                     c, &cfg, &io, n, first_event, s, &c->tuning, &launches);
@@ -297,6 +330,24 @@ static int gp_run(gp_context * c, const gp_config & cfg, const gp_io & io,
         c->stats.kernel_ms = -1.;
         if ((rc == 0) && sync) rc = gp_check(cudaStreamSynchronize(s));
         return rc;
+}
+
+extern "C" int gpumas_context_recorder_set(
+    struct gpumas_context * context, const struct gpumas_recorder * recorder)
+{
+        if (context == NULL) return GPUMAS_RETURN_VALUE_ERROR;
+        gp_context * c = (gp_context *)context;
+        if (recorder == NULL) {
+                c->recording = 0;
+                memset(&c->recorder, 0, sizeof(c->recorder));
+                return GPUMAS_RETURN_SUCCESS;
+        }
+        if ((recorder->max_frames < 0) || (recorder->length == NULL) ||
+            ((recorder->max_frames > 0) && (recorder->frames == NULL)))
+                return GPUMAS_RETURN_VALUE_ERROR;
+        c->recorder = *recorder;
+        c->recording = 1;
+        return GPUMAS_RETURN_SUCCESS;
 }
 
 extern "C" int gpumas_context_tuning_set(

@@ -255,12 +255,11 @@ def bench(args, rank, world, local):
         lat = [1E+03 * r.latency for r in reqs]
         errors = sum(int(np.count_nonzero(r.results["status"]))
                      for r in reqs)
-        window = float(arrivals[-1]) if n > 1 else 0.
         entry = {"rate": rate, "requests": n, "events": events,
                  "wall_s": wall, "throughput_rps": n / wall,
                  "events_per_s": events / wall,
                  "latency_ms": percentiles(lat), "event_errors": errors,
-                 "sustained": bool(wall <= 1.1 * window + 0.05)}
+                 "sustained": bool(n / wall >= 0.9 * rate)}
         # The plain baseline on the same arrivals (bounded: at most 300
         # requests, the first ones).
         m = min(n, 300)

@@ -7,6 +7,8 @@ These fixtures let machines without the reference sources check the engine
 against the reference's own outputs.
 
 usage: python tests/golden/make_golden.py [case ...]   (default: all cases)
+       python tests/golden/make_golden.py frames [case ...]   (recorder
+       frames of the cases of RECORD_CASES)
 """
 import os
 import sys
@@ -24,6 +26,38 @@ from cases import CASES, make_states  # noqa: E402
 from conftest import oracle_config, oracle_geometry  # noqa: E402
 
 
+# Recorder cases: (case, recorder period, events, frames kept per event).
+RECORD_CASES = [
+    ("plain_csda", 1, 20, 4),
+    ("rock_slab", 10, 24, 96),
+    ("stack_forward_mixed", 5, 24, 96),
+    ("stack_backward_straggled", 0, 24, 32),
+    ("terrain_backward", 25, 16, 64),
+]
+
+
+def record_file(name, period):
+    return os.path.join(HERE, "frames_%s_p%d.npz" % (name, period))
+
+
+def make_frames(ref, names=None):
+    """Frames of the reference's recorder for RECORD_CASES."""
+    for name, period, n, max_frames in RECORD_CASES:
+        if names and name not in names:
+            continue
+        case = CASES[name]
+        s0 = make_states(name, n=n)
+        geo = oracle_geometry(ref, case["geometry"])
+        cfg = oracle_config(case["config"], case["seed"])
+        s1, r1, frames, length = ref.transport_record(
+            cfg, geo, s0, 0, period, max_frames)
+        np.savez_compressed(record_file(name, period), initial=s0, final=s1,
+                            results=r1, frames=frames, length=length,
+                            period=period)
+        print("%-28s period %d: %5.1f frames/event (max %d)" % (
+            name, period, length.mean(), length.max()))
+
+
 def main():
     oracle.build_reference()
     dump = pumas_gb300.default_dump()
@@ -32,7 +66,11 @@ def main():
     with open(path, "wb") as f:
         f.write(dump)
     ref = oracle.Reference(path)
-    names = sys.argv[1:] or list(CASES)
+    args = sys.argv[1:]
+    if args and args[0] == "frames":
+        make_frames(ref, args[1:])
+        return
+    names = args or list(CASES)
     for name in names:
         case = CASES[name]
         s0 = make_states(name)
