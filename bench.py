@@ -67,7 +67,7 @@ def parse():
     p.add_argument("--max-inner", type=int, default=0)
     p.add_argument("--batch", type=int, default=0)
     p.add_argument("--tail", type=int, default=0,
-                   help="drain threshold in slots (0: automatic, <0: off)")
+                   help="drain threshold in slots (0: off, <0: automatic)")
     p.add_argument("--workload", default="rock_slab",
                    choices=["rock_slab", "slab_jobs", "terrain",
                             "plain_csda", "serve"])

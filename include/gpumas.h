@@ -295,11 +295,11 @@ int gpumas_context_recorder_set(struct gpumas_context * context,
  * 2 the slot pool, where events are refilled into `pool_slots` resident
  * slots and stepped by kernels regrouped by step kind (continuous step,
  * DEL, hard elastic scatter), with `max_inner` continuous steps per slot and
- * iteration and `batch` iterations per captured CUDA graph. Once every
- * event is in a slot and at most `tail` slots are active, the remaining
- * events run to their end in one launch (0: one slot per resident thread,
- * negative: never). Results do not depend on these parameters. Zero fields
- * keep the current value (for `tail`: automatic).
+ * iteration and `batch` iterations per captured CUDA graph. With `tail`
+ * > 0, once every event is in a slot and at most `tail` slots are active,
+ * the remaining events run to their end in one launch (negative: one slot
+ * per resident thread; 0, the default: never). Results do not depend on
+ * these parameters. Zero fields keep the current value.
  */
 struct gpumas_tuning {
         int engine;

@@ -13,7 +13,7 @@ event id):
   period seen from the host);
 * ``tail``: the drain threshold, in active slots, below which the last
   events run to their end in one launch instead of being regrouped by step
-  kind (0: one slot per resident thread, -1: never).
+  kind (-1: one slot per resident thread, 0: never).
 
 ``tune`` times an engine run of a sample workload for each point of a grid
 and keeps the fastest; the result is stored as JSON and read back by
@@ -29,7 +29,7 @@ DEFAULT_GRID = {
     "pool_slots": [524288, 1048576, 2097152],
     "max_inner": [4, 8, 16],
     "batch": [8, 16],
-    "tail": [-1, 0],
+    "tail": [0, -1],
 }
 
 HERE = os.path.dirname(os.path.abspath(__file__))

@@ -471,6 +471,7 @@ __global__ void __launch_bounds__(128, GP_POOL_MIN_BLOCKS) gp_pool_del(
                 gp_slot_load(pool, slot, cfg, e, L);
                 int event = GPUMAS_EVENT_NONE;
                 gp_polar_job job;
+                gp_stepping_weight(T, cfg, e, L);
                 gp_do_del_energy(T, cfg, e, L.material, job);
                 if (job.process == 2) {
                         gp_slot_store(pool, slot, e, L);
@@ -1428,9 +1429,8 @@ static int gp_engine_batch(gpumas_engine * g)
                 h->max_inner = (g->tuning.max_inner > 0) ?
                     g->tuning.max_inner : 8;
                 h->total = g->total;
-                h->tail_slots = (g->tuning.tail < 0) ? 0 :
-                    (g->tuning.tail > 0) ? g->tuning.tail :
-                                           (int)(g->grid_step * 128);
+                h->tail_slots = (g->tuning.tail > 0) ? g->tuning.tail :
+                    (g->tuning.tail < 0) ? (int)(g->grid_step * 128) : 0;
                 rc = gp_check(cudaMemcpyAsync(g->view.launch, h,
                     sizeof(gp_launch), cudaMemcpyHostToDevice, s));
                 if (rc == GPUMAS_RETURN_SUCCESS) rc = gp_engine_graph(g);

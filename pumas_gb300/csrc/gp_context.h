@@ -17,7 +17,7 @@ struct gp_tuning {
         int pool_slots;  /* number of event slots of the pool engine */
         int max_inner;   /* continuous steps per slot and iteration */
         int batch;       /* iterations per captured graph */
-        int tail;        /* drain threshold in slots (0: automatic, <0: off) */
+        int tail;        /* drain threshold in slots (0: off, <0: automatic) */
 };
 
 struct gp_context {

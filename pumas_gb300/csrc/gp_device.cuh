@@ -2712,6 +2712,23 @@ static __device__ __forceinline__ int gp_stepping_relimit(const gp_tables & T, c
         return GP_NEXT_STEP;
 }
 
+/* Weight update at a stepping event (pumas.c:5309-5321): backward
+ * Jacobian and decay weight since the last event. */
+GPD void gp_stepping_weight(const gp_tables & T, const gp_config & cfg,
+    gp_event & e, const gp_loop & L)
+{
+        if ((cfg.direction == GPUMAS_MODE_BACKWARD) &&
+            (cfg.energy_loss >= GPUMAS_MODE_CSDA)) {
+                const double wt = (cfg.decay == GPUMAS_MODE_WEIGHTED) ?
+                    gp_exp(-fabs(e.time - L.ti) / T.ctau) : 1.;
+                e.weight = L.wi * wt * L.dei *
+                    gp_cel_energy_loss(T, cfg.energy_loss, L.material,
+                        e.energy);
+        } else if (cfg.decay == GPUMAS_MODE_WEIGHTED) {
+                e.weight = L.wi * gp_exp(-fabs(e.time - L.ti) / T.ctau);
+        }
+}
+
 /* One iteration of the stepping loop up to the dispatch of its event
  * (pumas.c:5277-5329 and the medium change of 5417-5467). */
 static __device__ __forceinline__ int gp_stepping_step(const gp_tables & T, const gp_config & cfg,
@@ -2742,16 +2759,18 @@ static __device__ __forceinline__ int gp_stepping_step(const gp_tables & T, cons
             (L.step_index != 1) && ((L.step_index % rec->period) == 0);
         if (!e.step_event && !record_step) return GP_NEXT_STEP;
 
-        const int scheme = cfg.energy_loss;
-        if ((cfg.direction == GPUMAS_MODE_BACKWARD) &&
-            (cfg.energy_loss >= GPUMAS_MODE_CSDA)) {
-                const double wt = (cfg.decay == GPUMAS_MODE_WEIGHTED) ?
-                    gp_exp(-fabs(e.time - L.ti) / T.ctau) : 1.;
-                e.weight = L.wi * wt * L.dei *
-                    gp_cel_energy_loss(T, scheme, L.material, e.energy);
-        } else if (cfg.decay == GPUMAS_MODE_WEIGHTED) {
-                e.weight = L.wi * gp_exp(-fabs(e.time - L.ti) / T.ctau);
+        /* A DEL or an EHS leaves with its weight update still to be made
+         * (gp_stepping_weight, first thing of the DEL and EHS phases): in
+         * the pool engine it then runs in the compact DEL and EHS kernels
+         * instead of a few lanes of each step warp. */
+        if (!(e.step_event & (GPUMAS_EVENT_LIMIT | GPUMAS_EVENT_WEIGHT |
+                                GPUMAS_EVENT_VERTEX_DECAY))) {
+                if (e.step_event & GPUMAS_EVENT_VERTEX_DEL) return GP_NEXT_DEL;
+                if (e.step_event & GPUMAS_EVENT_VERTEX_COULOMB)
+                        return GP_NEXT_EHS;
         }
+        const int scheme = cfg.energy_loss;
+        gp_stepping_weight(T, cfg, e, L);
 
         if (!e.step_event) {
                 gp_rec_frame(rec, e, L.medium, GPUMAS_EVENT_NONE);
@@ -2761,10 +2780,6 @@ static __device__ __forceinline__ int gp_stepping_step(const gp_tables & T, cons
                                GPUMAS_EVENT_VERTEX_DECAY)) {
                 event = e.step_event;
                 return GP_NEXT_DONE;
-        } else if (e.step_event & GPUMAS_EVENT_VERTEX_DEL) {
-                return GP_NEXT_DEL;
-        } else if (e.step_event & GPUMAS_EVENT_VERTEX_COULOMB) {
-                return GP_NEXT_EHS;
         } else if (e.step_event & GPUMAS_EVENT_MEDIUM) {
                 L.medium = L.new_medium;
                 if ((L.medium < 0) || (cfg.event & GPUMAS_EVENT_MEDIUM)) {
@@ -2819,6 +2834,7 @@ static __device__ __forceinline__ int gp_stepping_del(const gp_tables & T,
     const gp_config & cfg, gp_event & e, gp_loop & L, int & event,
     gp_rec * rec = NULL)
 {
+        gp_stepping_weight(T, cfg, e, L);
         if ((rec == NULL) || (rec->period <= 0)) {
                 gp_do_del(T, cfg, e, L.material);
                 return gp_stepping_del_end(T, cfg, e, L, event);
@@ -2851,6 +2867,7 @@ static __device__ __forceinline__ int gp_stepping_del(const gp_tables & T,
 static __device__ __forceinline__ int gp_stepping_ehs(const gp_tables & T, const gp_config & cfg,
     gp_event & e, gp_loop & L, int & event)
 {
+        gp_stepping_weight(T, cfg, e, L);
         gp_do_ehs(T, cfg, e, L.material);
         if ((cfg.event & e.step_event) ||
             (e.status != GPUMAS_RETURN_SUCCESS)) {

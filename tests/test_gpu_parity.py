@@ -162,7 +162,7 @@ def test_gpu_edge_cases(gpu_physics):
 @pytest.mark.parametrize("name", ["rock_slab", "stack_forward_mixed",
                                   "stack_backward_straggled",
                                   "water_time_limit", "plain_csda"])
-@pytest.mark.parametrize("slots,inner,tail", [(256, 1, -1), (1024, 3, 0),
+@pytest.mark.parametrize("slots,inner,tail", [(256, 1, 0), (1024, 3, -1),
                                                (2048, 8, 700)])
 def test_pool_engine_matches_plain_engine(gpu_physics, name, slots, inner,
                                           tail):
