@@ -455,7 +455,10 @@ int gpumas_bench_dfma(double * tflops);
 
 /** Evaluate the engine's double precision logarithm (fn = 0) or
  * exponential (fn = 1) on the device for n arguments (for checking; they
- * replace the CUDA library functions in the transport, see gp_math.cuh). */
+ * replace the CUDA library functions in the transport, see gp_math.cuh).
+ * fn = 2 evaluates the single precision screen of thinned candidates,
+ * gp_neglog_beyond(u, p, q, r), for n quadruples x[4 i] .. x[4 i + 3]:
+ * y[i] is 1 when it rules the candidate out, else 0. */
 int gpumas_math_eval(int fn, size_t n, const double * x, double * y);
 
 /* ------------------------------------------------------------------------ */

@@ -2422,7 +2422,12 @@ static __device__ __forceinline__ int gp_step(const gp_tables & T, const gp_conf
                             gp_del_cross_section(T, material, k1);
                         if (tmp_del > xs_del) xs_del = tmp_del;
                         if (xs_del <= 0.) break;
-                        const double X_del = -gp_log(gp_random(e)) / xs_del;
+                        /* Candidates beyond the step, most of them, are
+                         * ruled out in single precision (gp_math.cuh) with
+                         * the same decision as below. */
+                        const double u_del = gp_random(e);
+                        if (gp_neglog_beyond(u_del, 1., Xmax, xs_del)) break;
+                        const double X_del = -gp_log(u_del) / xs_del;
                         if (X_del >= Xmax) break;
                         const double k_h = gp_cel_kinetic_energy(
                             T, scheme, material, Xtot - sgn * X_del);
@@ -2450,7 +2455,9 @@ static __device__ __forceinline__ int gp_step(const gp_tables & T, const gp_conf
                         const double lb_ehs =
                             gp_coulomb_ehs_length(T, material, kmin);
                         if (lb_ehs <= 0.) break;
-                        const double X_ehs = -gp_log(gp_random(e)) * lb_ehs;
+                        const double u_ehs = gp_random(e);
+                        if (gp_neglog_beyond(u_ehs, lb_ehs, Xmax, 1.)) break;
+                        const double X_ehs = -gp_log(u_ehs) * lb_ehs;
                         if (X_ehs >= Xmax) break;
                         const double k_h = gp_cel_kinetic_energy(
                             T, scheme, material, Xtot - sgn * X_ehs);

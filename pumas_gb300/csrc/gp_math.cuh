@@ -156,4 +156,55 @@ GP_MATH_HD double gp_exp(double x)
         return GP_MM(GP_MM(v, f1), f2);
 }
 
+/* x rounded toward zero to single precision by integer operations on its
+ * bits, for 2^-100 <= x <= 2^100; 0 (no value) outside that range, for
+ * negative x and for non finite x. The conversion instructions of the
+ * GPU run on its double precision pipe; these shifts do not. */
+GP_MATH_HD int gp_math_trunc_float(double x, float * f)
+{
+        const unsigned long long b = (unsigned long long)gp_math_bits(x);
+        /* Biased exponents 923 to 1123, sign bit clear. */
+        if ((b >> 52) - 923ull > 200ull) return 0;
+        const uint32_t fb = (uint32_t)((b >> 29) - (896ull << 23));
+#if defined(__CUDA_ARCH__)
+        *f = __uint_as_float(fb);
+#else
+        memcpy(f, &fb, sizeof(*f));
+#endif
+        return 1;
+}
+
+/* Single precision screen of a thinned interaction candidate: returns 1
+ * only when -ln(u) p >= q r (1 + 9.9e-4) holds for the exact values, so
+ * that a candidate grammage computed in double precision, -gp_log(u) p or
+ * -gp_log(u) / (1 / p), with its errors below 2^-51 relative, is certainly
+ * at or beyond q r. Returns 0 when that is not sure, or when an argument
+ * is outside [2^-100, 2^100]: the caller then computes the candidate in
+ * double precision. The decision is the same as the double precision one
+ * whenever it returns 1, so that results do not change.
+ *
+ * Bounds: each argument truncated to single precision is low by less than
+ * 2^-23 relative; the single precision logarithm of u (u in (0, 1]) has an
+ * error below 1.3e-5 absolute for u < 0.5 (3 ulp of at most 36.8) and
+ * below 4e-7 absolute above; the truncation of u raises -ln by less than
+ * 1.2e-7. The lower bound Lf (1 - 1e-4) - 1e-4 covers all three; the
+ * factor 1.001 covers the truncation of q and r and four single precision
+ * roundings. */
+GP_MATH_HD int gp_neglog_beyond(double u, double p, double q, double r)
+{
+        float uf, pf, qf, rf;
+        if (!gp_math_trunc_float(u, &uf) || !gp_math_trunc_float(p, &pf) ||
+            !gp_math_trunc_float(q, &qf) || !gp_math_trunc_float(r, &rf))
+                return 0;
+        if (uf > 1.f) return 0;
+#if defined(__CUDA_ARCH__)
+        const float L = -__logf(uf);
+#else
+        const float L = -logf(uf);
+#endif
+        const float low = L * 0.9999f - 1e-4f;
+        if (!(low > 0.f)) return 0;
+        return (low * pf >= (qf * rf) * 1.001f) ? 1 : 0;
+}
+
 #endif

@@ -528,26 +528,32 @@ __global__ void gp_kernel_math(int fn, size_t n, const double * x, double * y)
 {
         const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
         if (i >= n) return;
-        y[i] = (fn == 0) ? gp_log(x[i]) : gp_exp(x[i]);
+        if (fn == 2) {
+                const double * a = x + 4 * i;
+                y[i] = gp_neglog_beyond(a[0], a[1], a[2], a[3]);
+        } else {
+                y[i] = (fn == 0) ? gp_log(x[i]) : gp_exp(x[i]);
+        }
 }
 
 extern "C" int gpumas_math_eval(int fn, size_t n, const double * x,
     double * y)
 {
-        if ((x == NULL) || (y == NULL) || (n == 0) || (fn < 0) || (fn > 1))
+        if ((x == NULL) || (y == NULL) || (n == 0) || (fn < 0) || (fn > 2))
                 return GPUMAS_RETURN_VALUE_ERROR;
+        const size_t nx = (fn == 2) ? 4 * n : n;
         double * d = NULL;
-        int rc = gp_check(cudaMalloc(&d, 2 * n * sizeof(double)));
+        int rc = gp_check(cudaMalloc(&d, (nx + n) * sizeof(double)));
         if (rc != GPUMAS_RETURN_SUCCESS) return rc;
-        rc = gp_check(cudaMemcpy(d, x, n * sizeof(double),
+        rc = gp_check(cudaMemcpy(d, x, nx * sizeof(double),
             cudaMemcpyHostToDevice));
         if (rc == GPUMAS_RETURN_SUCCESS) {
                 gp_kernel_math<<<(unsigned int)((n + 255) / 256), 256>>>(
-                    fn, n, d, d + n);
+                    fn, n, d, d + nx);
                 rc = gp_check(cudaGetLastError());
         }
         if (rc == GPUMAS_RETURN_SUCCESS)
-                rc = gp_check(cudaMemcpy(y, d + n, n * sizeof(double),
+                rc = gp_check(cudaMemcpy(y, d + nx, n * sizeof(double),
                     cudaMemcpyDeviceToHost));
         cudaFree(d);
         return rc;

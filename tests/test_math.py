@@ -1,4 +1,5 @@
-"""The engine's table-driven logarithm and exponential (gp_math.cuh).
+"""The engine's table-driven logarithm and exponential, and its single
+precision screen of thinned candidates (gp_math.cuh).
 
 They replace the CUDA library functions in the transport (fewer double
 precision instructions on a GPU whose FP64 rate is 1/64 of its FP32 rate).
@@ -31,7 +32,7 @@ def host(tmp_path_factory):
 
     def run(fn, x):
         x = np.ascontiguousarray(x, dtype=np.float64)
-        y = np.empty_like(x)
+        y = np.empty(len(x))
         h.math_host_eval(fn, len(x), x.ctypes.data, y.ctypes.data)
         return y
     return run
@@ -91,3 +92,67 @@ def test_device_equals_host(host, gpu_physics, fn):
     y = np.empty_like(x)
     assert lib.gpumas_math_eval(fn, len(x), x.ctypes.data, y.ctypes.data) == 0
     assert np.array_equal(y, host(fn, x))
+
+
+def screen_cases(n=20000, seed=5):
+    """Quadruples (u, p, q, r) of the thinning screen in its two forms, DEL
+    (p = 1: grammage -ln(u) / r against q) and EHS (r = 1: grammage -ln(u) p
+    against q), with q placed within 1 % of the boundary -ln(u) p / r, plus
+    far cases and arguments outside the screen's range."""
+    rng = np.random.default_rng(seed)
+    u = np.concatenate([rng.random(n) + 2. ** -53,
+                        1. - rng.random(n // 4) * 1E-04,
+                        np.full(8, 2. ** -53), np.full(8, 1. - 2. ** -53)])
+    m = len(u)
+    scale = np.exp(rng.uniform(-30., 30., m))
+    delta = np.where(rng.random(m) < 0.8, rng.uniform(-1E-02, 1E-02, m),
+                     rng.uniform(-0.9, 5., m))
+    L = -np.log(u)
+    del_form = rng.random(m) < 0.5
+    p = np.where(del_form, 1., scale)
+    r = np.where(del_form, scale, 1.)
+    q = L * p / r / (1. + delta)
+    x = np.stack([u, p, q, r], axis=1)
+    bad = np.array([[0.5, 1., 0., 1.], [0.5, 1., -1., 1.],
+                    [0.5, 1., 1E-200, 1.], [0.5, 1E+200, 1., 1.],
+                    [0.5, 1., np.inf, 1.], [0.5, 1., np.nan, 1.],
+                    [1.5, 1., 1E-03, 1.], [1E-300, 1., 1., 1.]])
+    return np.ascontiguousarray(np.concatenate([x, bad]))
+
+
+def screen_exact(host, x):
+    """Whether the double precision candidate, computed as the transport
+    does with gp_log, is at or beyond q."""
+    L = -host(0, x[:, 0])
+    dbl = np.where(x[:, 1] == 1., L / x[:, 3], L * x[:, 1])
+    return dbl >= x[:, 2]
+
+
+def test_screen_is_conservative(host):
+    """The screen never rules out a candidate that the double precision
+    comparison keeps, and rules out nearly every in-range candidate that is
+    more than 1 % beyond."""
+    x = screen_cases()
+    s = host(2, x) == 1.
+    exact = screen_exact(host, x)
+    assert not np.any(s & ~exact)
+    n = len(x) - 8
+    L = -np.log(x[:n, 0])
+    far = (L * x[:n, 1] >= 1.01 * x[:n, 2] * x[:n, 3]) & (L > 1E-02)
+    assert np.mean(s[:n][far]) > 0.999
+    assert not np.any(s[n:])
+
+
+@pytest.mark.gpu
+def test_device_screen(host, gpu_physics):
+    import pumas_gb300 as pg
+    lib = pg.library()
+    lib.gpumas_math_eval.argtypes = [ctypes.c_int, ctypes.c_size_t,
+                                     ctypes.c_void_p, ctypes.c_void_p]
+    lib.gpumas_math_eval.restype = ctypes.c_int
+    x = screen_cases(n=200000, seed=11)
+    y = np.empty(len(x))
+    assert lib.gpumas_math_eval(2, len(x), x.ctypes.data, y.ctypes.data) == 0
+    s = y == 1.
+    assert not np.any(s & ~screen_exact(host, x))
+    assert np.mean(s == (host(2, x) == 1.)) > 0.999
