@@ -73,6 +73,43 @@ struct gpumas_medium {
         double density;
 };
 
+/** Density models of struct gpumas_locals. */
+enum gpumas_density_model {
+        /** The medium's density (struct gpumas_medium), uniform. */
+        GPUMAS_DENSITY_UNIFORM = 0,
+        /** rho0 exp(-(axis . r - h0) / lambda), e.g. an isothermal
+         * atmosphere with axis the local vertical. */
+        GPUMAS_DENSITY_EXPONENTIAL = 1
+};
+
+/**
+ * Local properties of a medium that vary in space or carry a magnetic
+ * field: the device form of a `pumas_locals_cb` (pumas.h:324-349) that
+ * fills `struct pumas_locals` (density and magnet, pumas.h:314-321).
+ *
+ * - GPUMAS_DENSITY_UNIFORM: the density of the medium entry, and a
+ *   returned inhomogeneity size of 0 (a uniform medium).
+ * - GPUMAS_DENSITY_EXPONENTIAL: density rho0 exp(-(axis . r - h0) /
+ *   lambda) in kg/m^3 at position r, and a returned inhomogeneity size of
+ *   lambda / max(|axis . u|, eps) for the direction u of the state, the
+ *   projected attenuation length (the exponential atmosphere of the
+ *   reference's examples/pumas/geometry.c:76-97).
+ *
+ * `magnet` is a uniform magnetic field in T (zero: no field). The
+ * transport limits its steps to the inhomogeneity size times the context
+ * accuracy (transport_set_locals, pumas.c:5528-5552). As in the reference,
+ * the density and the field must be continuous inside a medium.
+ */
+struct gpumas_locals {
+        int model;
+        double rho0;
+        double axis[3];
+        double h0;
+        double lambda;
+        double eps;
+        double magnet[3];
+};
+
 /** Minimum geometric step, in m (the reference's STEP_MIN, pumas.c:101). */
 #define GPUMAS_STEP_MIN 1E-07
 
@@ -105,6 +142,10 @@ struct gpumas_geometry {
         const double * hm_z;
         int hm_below, hm_above;
         double hm_ztop;
+
+        /* Local properties, NULL or one entry per medium. With NULL every
+         * medium is uniform, at its density, without magnetic field. */
+        const struct gpumas_locals * locals;
 };
 
 /* Slabs: index of the layer containing z, or -1 outside of the stack. */
@@ -171,6 +212,27 @@ GPUMAS_HD int gpumas_geometry_locate(
                 const double zs = gpumas_hm_height(g, i, j, s, t);
                 return (r[2] < zs) ? g->hm_below : g->hm_above;
         }
+}
+
+/* Exponent of an exponential density model at position r,
+ * -(axis . r - h0) / lambda. */
+GPUMAS_HD double gpumas_locals_exponent(
+    const struct gpumas_locals * l, const double * r)
+{
+        const double s = GPUMAS_ADD(GPUMAS_ADD(GPUMAS_MUL(l->axis[0], r[0]),
+            GPUMAS_MUL(l->axis[1], r[1])), GPUMAS_MUL(l->axis[2], r[2]));
+        return -GPUMAS_SUB(s, l->h0) / l->lambda;
+}
+
+/* Inhomogeneity size of an exponential density model for the state
+ * direction u, lambda / max(|axis . u|, eps). */
+GPUMAS_HD double gpumas_locals_size(
+    const struct gpumas_locals * l, const double * u)
+{
+        double c = fabs(GPUMAS_ADD(GPUMAS_ADD(GPUMAS_MUL(l->axis[0], u[0]),
+            GPUMAS_MUL(l->axis[1], u[1])), GPUMAS_MUL(l->axis[2], u[2])));
+        if (c <= l->eps) c = l->eps;
+        return l->lambda / c;
 }
 
 /* Smallest root in ]0, tmax] of c0 + c1 t + c2 t^2, or -1 if none. */

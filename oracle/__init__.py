@@ -45,6 +45,14 @@ class Medium(ctypes.Structure):
     _fields_ = [("material", ctypes.c_int), ("density", ctypes.c_double)]
 
 
+class Locals(ctypes.Structure):
+    """struct gpumas_locals (include/gpumas_geometry.h)."""
+    _fields_ = [("model", ctypes.c_int), ("rho0", ctypes.c_double),
+                ("axis", ctypes.c_double * 3), ("h0", ctypes.c_double),
+                ("lambda_", ctypes.c_double), ("eps", ctypes.c_double),
+                ("magnet", ctypes.c_double * 3)]
+
+
 class Geometry(ctypes.Structure):
     """struct gpumas_geometry (include/gpumas_geometry.h)."""
     _fields_ = [
@@ -59,7 +67,8 @@ class Geometry(ctypes.Structure):
         ("hm_dx", ctypes.c_double), ("hm_dy", ctypes.c_double),
         ("hm_z", ctypes.POINTER(ctypes.c_double)),
         ("hm_below", ctypes.c_int), ("hm_above", ctypes.c_int),
-        ("hm_ztop", ctypes.c_double)]
+        ("hm_ztop", ctypes.c_double),
+        ("locals", ctypes.POINTER(Locals))]
 
 
 class Config(ctypes.Structure):
@@ -100,6 +109,18 @@ def make_geometry(kind, media, **kw):
         g.hm_z = hz.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
         g.hm_below, g.hm_above = kw["hm_below"], kw["hm_above"]
         g.hm_ztop = kw["hm_ztop"]
+    if kw.get("locals") is not None:
+        arr = (Locals * len(media))()
+        for a, d in zip(arr, kw["locals"]):
+            a.model = int(d.get("model", 0))
+            a.rho0 = float(d.get("rho0", 0.))
+            a.axis[:] = [float(v) for v in d.get("axis", (0., 0., 1.))]
+            a.h0 = float(d.get("h0", 0.))
+            a.lambda_ = float(d.get("lambda_", 0.))
+            a.eps = float(d.get("eps", 0.))
+            a.magnet[:] = [float(v) for v in d.get("magnet", (0., 0., 0.))]
+        keep.append(arr)
+        g.locals = arr
     g._keep = keep
     return g
 

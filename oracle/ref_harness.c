@@ -21,16 +21,19 @@
 #include <omp.h>
 #endif
 
+#include "gp_math.cuh"
 #include "oracle.h"
 #include "philox.h"
 
 /* The loaded physics shared by all calls. */
 static struct pumas_physics * ref_physics = NULL;
 
-/* A medium with an optional uniform density override. */
+/* A medium with an optional uniform density override and optional local
+ * properties (struct gpumas_locals). */
 struct ref_medium {
         struct pumas_medium api;
         double density;
+        const struct gpumas_locals * loc;
 };
 
 /* Per event data stored in the context's user memory. */
@@ -41,13 +44,21 @@ struct ref_event {
         int steps;
 };
 
+/* The locals callback of a medium: a uniform density override, or the
+ * density profile and field of its gpumas_locals, evaluated with the same
+ * arithmetic as the device (gp_exp of gp_math.cuh). */
 static double ref_locals(struct pumas_medium * medium,
     struct pumas_state * state, struct pumas_locals * locals)
 {
-        (void)state;
         const struct ref_medium * m = (const struct ref_medium *)medium;
+        const struct gpumas_locals * l = m->loc;
         locals->density = m->density;
-        return 0.;
+        if (l == NULL) return 0.;
+        memcpy(locals->magnet, l->magnet, sizeof(locals->magnet));
+        if (l->model != GPUMAS_DENSITY_EXPONENTIAL) return 0.;
+        locals->density =
+            l->rho0 * gp_exp(gpumas_locals_exponent(l, state->position));
+        return gpumas_locals_size(l, state->direction);
 }
 
 static enum pumas_step ref_medium_cb(struct pumas_context * context,
@@ -178,8 +189,11 @@ int oracle_ref_transport(const struct oracle_config * cfg,
         for (i = 0; i < geometry->n_media; i++) {
                 media[i].api.material = geometry->media[i].material;
                 media[i].density = geometry->media[i].density;
+                media[i].loc = (geometry->locals != NULL) ?
+                    geometry->locals + i : NULL;
                 media[i].api.locals =
-                    (media[i].density > 0.) ? &ref_locals : NULL;
+                    ((media[i].density > 0.) || (media[i].loc != NULL)) ?
+                    &ref_locals : NULL;
         }
 
         int rc_all = PUMAS_RETURN_SUCCESS;
@@ -272,8 +286,11 @@ int oracle_ref_transport_record(const struct oracle_config * cfg,
         for (i = 0; i < geometry->n_media; i++) {
                 media[i].api.material = geometry->media[i].material;
                 media[i].density = geometry->media[i].density;
+                media[i].loc = (geometry->locals != NULL) ?
+                    geometry->locals + i : NULL;
                 media[i].api.locals =
-                    (media[i].density > 0.) ? &ref_locals : NULL;
+                    ((media[i].density > 0.) || (media[i].loc != NULL)) ?
+                    &ref_locals : NULL;
         }
         struct pumas_context * context = NULL;
         struct pumas_recorder * recorder = NULL;

@@ -48,6 +48,7 @@ RETURN_UNKNOWN_MATERIAL, RETURN_VALUE_ERROR = 22, 24
 RETURN_DEVICE_ERROR = 64
 
 GEOMETRY_UNIFORM, GEOMETRY_SLABS, GEOMETRY_HEIGHTMAP = 0, 1, 2
+DENSITY_UNIFORM, DENSITY_EXPONENTIAL = 0, 1
 
 # struct pumas_state (pumas.h:289-309), padded to 8 bytes.
 STATE_DTYPE = np.dtype([
@@ -76,6 +77,13 @@ class _Medium(ctypes.Structure):
     _fields_ = [("material", ctypes.c_int), ("density", ctypes.c_double)]
 
 
+class _Locals(ctypes.Structure):
+    _fields_ = [("model", ctypes.c_int), ("rho0", ctypes.c_double),
+                ("axis", ctypes.c_double * 3), ("h0", ctypes.c_double),
+                ("lambda_", ctypes.c_double), ("eps", ctypes.c_double),
+                ("magnet", ctypes.c_double * 3)]
+
+
 class _Geometry(ctypes.Structure):
     _fields_ = [
         ("kind", ctypes.c_int), ("n_media", ctypes.c_int),
@@ -89,7 +97,8 @@ class _Geometry(ctypes.Structure):
         ("hm_dx", ctypes.c_double), ("hm_dy", ctypes.c_double),
         ("hm_z", ctypes.POINTER(ctypes.c_double)),
         ("hm_below", ctypes.c_int), ("hm_above", ctypes.c_int),
-        ("hm_ztop", ctypes.c_double)]
+        ("hm_ztop", ctypes.c_double),
+        ("locals", ctypes.POINTER(_Locals))]
 
 
 class _Mode(ctypes.Structure):
@@ -271,9 +280,13 @@ class Geometry:
     """A geometry descriptor (include/gpumas_geometry.h).
 
     `media` is a list of (material index, density in kg/m^3 or 0 for the
-    material's default)."""
+    material's default). `locals`, if given, holds one dict per medium
+    (struct gpumas_locals): ``model`` (DENSITY_UNIFORM or
+    DENSITY_EXPONENTIAL), ``rho0``, ``axis``, ``h0``, ``lambda_``, ``eps``
+    for the density profile rho0 exp(-(axis . r - h0) / lambda_), and
+    ``magnet``, a uniform field in T."""
 
-    def __init__(self, kind, media, **kw):
+    def __init__(self, kind, media, locals=None, **kw):
         self._keep = []
         g = _Geometry()
         g.kind = kind
@@ -298,6 +311,20 @@ class Geometry:
             g.hm_z = hz.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
             g.hm_below, g.hm_above = kw["below"], kw["above"]
             g.hm_ztop = kw["ztop"]
+        if locals is not None:
+            if len(locals) != len(media):
+                raise ValueError("one locals entry per medium")
+            arr = (_Locals * len(media))()
+            for a, d in zip(arr, locals):
+                a.model = int(d.get("model", DENSITY_UNIFORM))
+                a.rho0 = float(d.get("rho0", 0.))
+                a.axis[:] = [float(v) for v in d.get("axis", (0., 0., 1.))]
+                a.h0 = float(d.get("h0", 0.))
+                a.lambda_ = float(d.get("lambda_", 0.))
+                a.eps = float(d.get("eps", 0.))
+                a.magnet[:] = [float(v) for v in d.get("magnet", (0., 0., 0.))]
+            self._keep.append(arr)
+            g.locals = arr
         self.c = g
 
     @classmethod
@@ -305,10 +332,10 @@ class Geometry:
         return cls(GEOMETRY_UNIFORM, [(material, density)], medium=0)
 
     @classmethod
-    def slabs(cls, z, materials, densities=None):
+    def slabs(cls, z, materials, densities=None, locals=None):
         densities = densities or [0.] * len(materials)
         media = list(zip(materials, densities))
-        return cls(GEOMETRY_SLABS, media, z=z,
+        return cls(GEOMETRY_SLABS, media, locals=locals, z=z,
                    slab_media=list(range(len(materials))))
 
     @classmethod

@@ -1399,6 +1399,9 @@ static int gp_engine_context(gpumas_engine * g,
         const gp_context * c = (const gp_context *)context;
         if (c->physics != g->physics) return GPUMAS_RETURN_PHYSICS_ERROR;
         if (!c->has_geometry) return GPUMAS_RETURN_MEDIUM_ERROR;
+        /* Media with local properties run on the one thread per event
+         * kernel only (gpumas_context_transport). */
+        if (c->has_locals) return GPUMAS_RETURN_VALUE_ERROR;
         const int rc = gp_config_check(context, c->physics, cfg);
         if (rc != GPUMAS_RETURN_SUCCESS) return rc;
         *geometry = c->d_geometry;
@@ -1813,6 +1816,7 @@ extern "C" int gpumas_context_transport_device_static(
                 return GPUMAS_RETURN_VALUE_ERROR;
         gp_context * c = (gp_context *)context;
         if (!c->has_geometry) return GPUMAS_RETURN_MEDIUM_ERROR;
+        if (c->has_locals) return GPUMAS_RETURN_VALUE_ERROR;
         gp_config cfg;
         int rc = gp_config_check(context, c->physics, &cfg);
         if (rc != GPUMAS_RETURN_SUCCESS) return rc;

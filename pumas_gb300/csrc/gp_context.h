@@ -29,6 +29,7 @@ struct gp_context {
         int has_geometry;
         int n_media;
         int geometry_kind;
+        int has_locals; /* media with local properties: ext kernel only */
         void * d_io;
         size_t io_size;
         cudaStream_t stream;

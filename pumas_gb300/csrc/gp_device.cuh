@@ -47,7 +47,10 @@
 #define GP_PION_MASS 0.13957018
 #define GP_AVOGADRO 6.02214076E+23
 #define GP_PI 3.14159265358979323846
-#define GP_FLT_EPSILON 1.19209290E-07
+/* FLT_EPSILON of the reference, a float literal: exactly 2^-23. */
+#define GP_FLT_EPSILON 0x1p-23
+/* Larmor factor in m^-1 GeV/c T^-1 (pumas.c:145-150). */
+#define GP_LARMOR_FACTOR 0.299792458
 #define GP_DBL_EPSILON 2.2204460492503131E-16
 #define GP_DBL_MAX 1.7976931348623157E+308
 
@@ -1272,6 +1275,68 @@ GPD double gp_medium_density(
                                   __ldg(&g.media[medium].material));
 }
 
+/* Local properties of the current medium on a geometry with locals
+ * (struct medium_locals, pumas.c:396-403): its field, density and step
+ * limit. Without locals the transport functions get a NULL gp_loc and
+ * compile without this code. */
+struct gp_loc {
+        const gpumas_geometry * g;
+        double magnet[3];
+        double density;  /* density at the end of the last step */
+        double step_max; /* step_max_locals: size x accuracy, 0: uniform */
+        int magnetized;
+};
+
+/* transport_set_locals (pumas.c:5528-5552) for medium `medium` of a
+ * geometry with locals, at the event's position and direction: sets the
+ * density and the field and returns the step limit (0: uniform). */
+GPD double gp_set_locals(const gp_tables & T, const gp_config & cfg,
+    const gp_event & e, int medium, double & density, gp_loc & loc)
+{
+        const gpumas_geometry & g = *loc.g;
+        const gpumas_locals * l = g.locals + medium;
+        double size = 0.;
+        if (__ldg(&l->model) == GPUMAS_DENSITY_EXPONENTIAL) {
+                gpumas_locals lc;
+                lc.axis[0] = __ldg(l->axis), lc.axis[1] = __ldg(l->axis + 1);
+                lc.axis[2] = __ldg(l->axis + 2);
+                lc.h0 = __ldg(&l->h0), lc.lambda = __ldg(&l->lambda);
+                lc.eps = __ldg(&l->eps);
+                density = GP_MUL(__ldg(&l->rho0),
+                    gp_exp(gpumas_locals_exponent(&lc, e.pos)));
+                size = gpumas_locals_size(&lc, e.dir);
+        } else {
+                density = __ldg(&g.media[medium].density);
+        }
+        if (density <= 0.)
+                density = __ldg(T.material_density +
+                    __ldg(&g.media[medium].material));
+        loc.magnet[0] = __ldg(l->magnet);
+        loc.magnet[1] = __ldg(l->magnet + 1);
+        loc.magnet[2] = __ldg(l->magnet + 2);
+        loc.magnetized = ((loc.magnet[0] != 0.) || (loc.magnet[1] != 0.) ||
+                             (loc.magnet[2] != 0.)) ? 1 : 0;
+        return GP_MUL(size, cfg.accuracy);
+}
+
+/* Larmor radius and deflection direction (u x B) / p of a step end point
+ * (pumas.c:6352-6378, 6850-6872): returns 0 without transverse field. */
+GPD double gp_larmor(const double * u, const double * B, double p,
+    double * uT)
+{
+        uT[0] = GP_SUB(GP_MUL(u[1], B[2]), GP_MUL(u[2], B[1]));
+        uT[1] = GP_SUB(GP_MUL(u[2], B[0]), GP_MUL(u[0], B[2]));
+        uT[2] = GP_SUB(GP_MUL(u[0], B[1]), GP_MUL(u[1], B[0]));
+        const double BT = sqrt(GP_ADD(GP_ADD(GP_MUL(uT[0], uT[0]),
+            GP_MUL(uT[1], uT[1])), GP_MUL(uT[2], uT[2])));
+        if (BT == 0.) return 0.;
+        const double pinv = 1. / p;
+        uT[0] = GP_MUL(uT[0], pinv);
+        uT[1] = GP_MUL(uT[1], pinv);
+        uT[2] = GP_MUL(uT[2], pinv);
+        return p / GP_MUL(BT, GP_LARMOR_FACTOR);
+}
+
 GPD int gp_locate(const gpumas_geometry & g, const gp_event & e)
 {
         return gpumas_geometry_locate(&g, e.pos);
@@ -2234,12 +2299,67 @@ static __device__ __forceinline__ void gp_limit(const gp_tables & T, const gp_co
         }
 }
 
-/* step_transport (pumas.c:6296-6925) for uniform media without magnetic
- * field. Sets e.step_event and returns the end step medium. */
+/* Magnetic deflection at the end of a step (pumas.c:6833-6911): the
+ * direction turns by the mean of the Larmor angles of the step's two end
+ * points, about the mean of their deflection directions. */
+GPD void gp_step_deflect(const gp_tables & T, const gp_config & cfg,
+    gp_event & e, const gp_loc & loc, const double * Bi, double h_int,
+    double momentum, double step, double rLarmor0, const double * uT0)
+{
+        double rLarmor1 = 0., uT1[3] = { 0., 0., 0. };
+        if (loc.magnetized) {
+                double B[3] = { loc.magnet[0], loc.magnet[1], loc.magnet[2] };
+                int magnetized = loc.magnetized;
+                if (h_int > 0.) {
+                        B[0] = GP_ADD(Bi[0], GP_MUL(h_int, GP_SUB(B[0], Bi[0])));
+                        B[1] = GP_ADD(Bi[1], GP_MUL(h_int, GP_SUB(B[1], Bi[1])));
+                        B[2] = GP_ADD(Bi[2], GP_MUL(h_int, GP_SUB(B[2], Bi[2])));
+                        /* The reference's test, kept as it is: a truncated
+                         * step (h_int > 0) takes no end point deflection
+                         * (pumas.c:6843-6844). */
+                        magnetized = (GP_ADD(GP_ADD(GP_MUL(B[0], B[0]),
+                            GP_MUL(B[1], B[1])), GP_MUL(B[2], B[2])) == 0.);
+                }
+                if (magnetized != 0) {
+                        const double p = (e.energy <= 0) ? momentum :
+                            sqrt(e.energy * (e.energy + 2. * T.mass));
+                        rLarmor1 = gp_larmor(e.dir, B, p, uT1);
+                }
+        }
+        if ((rLarmor0 <= 0.) && (rLarmor1 <= 0.)) return;
+        const double u[3] = { e.dir[0], e.dir[1], e.dir[2] };
+        const double cs = GP_MUL(e.charge, step);
+        const double theta0 = (rLarmor0 > 0.) ? cs / rLarmor0 : 0.;
+        const double theta1 = (rLarmor1 > 0.) ? cs / rLarmor1 : 0.;
+        double theta = GP_MUL(0.5, GP_ADD(theta0, theta1));
+        if (cfg.direction == GPUMAS_MODE_BACKWARD) theta = -theta;
+        double c = cos(theta);
+        double sn = sin(theta);
+        double v[3];
+        for (int i = 0; i < 3; i++) v[i] = GP_MUL(0.5, GP_ADD(uT0[i], uT1[i]));
+        double nrmv = GP_ADD(GP_ADD(GP_MUL(v[0], v[0]), GP_MUL(v[1], v[1])),
+            GP_MUL(v[2], v[2]));
+        if (nrmv > 0.) {
+                nrmv = 1. / sqrt(nrmv);
+                for (int i = 0; i < 3; i++) v[i] = GP_MUL(v[i], nrmv);
+        } else {
+                c = 1.;
+                sn = 0.;
+        }
+        for (int i = 0; i < 3; i++)
+                e.dir[i] = GP_ADD(GP_MUL(c, u[i]), GP_MUL(sn, v[i]));
+        const double norm = 1. / sqrt(GP_ADD(GP_ADD(GP_MUL(e.dir[0], e.dir[0]),
+            GP_MUL(e.dir[1], e.dir[1])), GP_MUL(e.dir[2], e.dir[2])));
+        for (int i = 0; i < 3; i++) e.dir[i] = GP_MUL(e.dir[i], norm);
+}
+
+/* step_transport (pumas.c:6296-6925). Sets e.step_event and returns the
+ * end step medium. With locals (loc not NULL) the density at the end of the
+ * step goes to loc->density, and a magnetic field bends the step. */
 static __device__ __forceinline__ int gp_step(const gp_tables & T, const gp_config & cfg,
     const gpumas_geometry & g, gp_event & e, int straight, int medium,
     int material, double density, double grammage_max,
-    double step_max_medium)
+    double step_max_medium, gp_loc * loc = NULL)
 {
         const int scheme = cfg.energy_loss;
         const double density_i = 1. / density;
@@ -2250,6 +2370,7 @@ static __device__ __forceinline__ int gp_step(const gp_tables & T, const gp_conf
 
         double step_loc;
         double invlb1 = 0.;
+        double rLarmor0 = 0., uT0[3] = { 0., 0., 0. };
         if (!straight) {
                 double r = cfg.accuracy;
                 const double k_threshold = 1E+09;
@@ -2271,6 +2392,13 @@ static __device__ __forceinline__ int gp_step(const gp_tables & T, const gp_conf
                         const double stepT = cfg.accuracy / invlb1;
                         if (stepT < step_loc) step_loc = stepT;
                 }
+                if ((loc != NULL) && loc->magnetized) {
+                        rLarmor0 = gp_larmor(e.dir, loc->magnet, momentum, uT0);
+                        if (rLarmor0 > 0.) {
+                                const double stepM = cfg.accuracy * rLarmor0;
+                                if (stepM < step_loc) step_loc = stepM;
+                        }
+                }
         } else {
                 if (grammage_max <= 0.)
                         step_loc = 1E+09 * density_i;
@@ -2282,6 +2410,8 @@ static __device__ __forceinline__ int gp_step(const gp_tables & T, const gp_conf
         double step = (step_max_medium <= 0) ?
             step_loc :
             (step_max_medium < step_loc ? step_max_medium : step_loc);
+        if ((loc != NULL) && (loc->step_max > 0.) && (step > loc->step_max))
+                step = loc->step_max;
 
         int out_medium = medium;
         int event = GPUMAS_EVENT_NONE;
@@ -2300,6 +2430,9 @@ static __device__ __forceinline__ int gp_step(const gp_tables & T, const gp_conf
         e.pos[2] += step * sd2;
 
         int end_medium = gp_locate(g, e);
+        /* Where the end step locals are evaluated when the step crosses a
+         * boundary: the last point inside the medium (pumas.c:6440-6492). */
+        double pl[3];
         if (end_medium != medium) {
                 /* Boundary check of a PUMAS_STEP_CHECK geometry
                  * (pumas.c:6425-6485). */
@@ -2329,10 +2462,20 @@ static __device__ __forceinline__ int gp_step(const gp_tables & T, const gp_conf
                                 }
                         }
                         step += s1;
+                        if (loc != NULL) {
+                                pl[0] = pi0 + s2 * sd0;
+                                pl[1] = pi1 + s2 * sd1;
+                                pl[2] = pi2 + s2 * sd2;
+                        }
                         e.pos[0] = pi0 + s1 * sd0;
                         e.pos[1] = pi1 + s1 * sd1;
                         e.pos[2] = pi2 + s1 * sd2;
                 } else {
+                        if (loc != NULL) {
+                                pl[0] = e.pos[0];
+                                pl[1] = e.pos[1];
+                                pl[2] = e.pos[2];
+                        }
                         e.pos[0] = pi0;
                         e.pos[1] = pi1;
                         e.pos[2] = pi2;
@@ -2341,7 +2484,34 @@ static __device__ __forceinline__ int gp_step(const gp_tables & T, const gp_conf
                 out_medium = end_medium;
         }
 
-        const double density1 = density;
+        /* End step locals (pumas.c:6488-6503). */
+        double density1 = density;
+        double Bi[3] = { 0., 0., 0. };
+        if (loc != NULL) {
+                if (loc->magnetized) {
+                        Bi[0] = loc->magnet[0];
+                        Bi[1] = loc->magnet[1];
+                        Bi[2] = loc->magnet[2];
+                }
+                if (loc->step_max > 0.) {
+                        double pe[3] = { e.pos[0], e.pos[1], e.pos[2] };
+                        if (event & GPUMAS_EVENT_MEDIUM) {
+                                e.pos[0] = pl[0];
+                                e.pos[1] = pl[1];
+                                e.pos[2] = pl[2];
+                        }
+                        loc->step_max = gp_set_locals(
+                            T, cfg, e, medium, density1, *loc);
+                        e.pos[0] = pe[0];
+                        e.pos[1] = pe[1];
+                        e.pos[2] = pe[2];
+                        if (density1 <= 0.) {
+                                e.status = GPUMAS_RETURN_DENSITY_ERROR;
+                                return out_medium;
+                        }
+                }
+                loc->density = density1;
+        }
         double k1 = e.energy, dk = 0.;
         const double dX = 0.5 * step * (density + density1);
         if ((scheme >= GPUMAS_MODE_CSDA) && (scheme <= GPUMAS_MODE_MIXED)) {
@@ -2480,9 +2650,25 @@ static __device__ __forceinline__ int gp_step(const gp_tables & T, const gp_conf
         const double Xi = e.grammage;
         e.grammage += dX;
         const double sf0 = step;
+        double h_int = 0.;
         if ((grammage_max > 0.) && (e.grammage >= grammage_max)) {
                 const double dX_ = grammage_max - Xi;
-                step = dX_ * density_i;
+                if (loc == NULL) {
+                        step = dX_ * density_i;
+                } else if ((fabs(density - density1) <= GP_FLT_EPSILON) ||
+                    (sf0 <= GP_FLT_EPSILON)) {
+                        step = dX_ * density_i;
+                        h_int = dX_ / (e.grammage - Xi);
+                } else {
+                        /* Step length of a linear density profile
+                         * (pumas.c:6676-6683). */
+                        const double drho = density1 - density;
+                        double tmp = GP_ADD(GP_MUL(density, density),
+                            GP_MUL(GP_MUL(2., dX_), drho) / sf0);
+                        tmp = (tmp > GP_FLT_EPSILON) ? sqrt(tmp) : 0;
+                        h_int = GP_SUB(tmp, density) / drho;
+                        step = GP_MUL(step, h_int);
+                }
                 e.grammage = grammage_max;
                 if (!(event & GPUMAS_EVENT_LIMIT_ENERGY)) {
                         if (scheme <= GPUMAS_MODE_MIXED) {
@@ -2573,7 +2759,13 @@ static __device__ __forceinline__ int gp_step(const gp_tables & T, const gp_conf
                                 if (k1 < 0.) k1 = 0.;
                         }
                         const double Xf = Xi + dX;
-                        e.grammage = Xi + step * density;
+                        if ((loc == NULL) || (density == density1))
+                                e.grammage = Xi + step * density;
+                        else
+                                e.grammage = GP_ADD(Xi, GP_MUL(step,
+                                    GP_ADD(density, GP_MUL(GP_MUL(0.5,
+                                        step) / sf0, GP_SUB(density1,
+                                        density)))));
                         if (e.grammage > Xf) e.grammage = Xf;
                 }
         }
@@ -2598,6 +2790,9 @@ static __device__ __forceinline__ int gp_step(const gp_tables & T, const gp_conf
                         e.step_invlb1 = density1 * invlb1_;
                 }
         }
+        if ((loc != NULL) && (rLarmor0 > 0. || loc->magnetized))
+                gp_step_deflect(T, cfg, e, *loc, Bi, h_int, momentum, step,
+                    rLarmor0, uT0);
         if ((invlb1 > 0.) || (e.step_invlb1 > 0.)) {
                 double ilb1 = 0.25 * step * (invlb1 + e.step_invlb1);
                 if (ilb1 > 1.) ilb1 = 1.;
@@ -2640,12 +2835,14 @@ enum gp_next {
  * the end event). */
 static __device__ __forceinline__ int gp_stepping_begin(const gp_tables & T, const gp_config & cfg,
     const gpumas_geometry & g, gp_event & e, gp_loop & L, int & event,
-    gp_rec * rec = NULL)
+    gp_rec * rec = NULL, const gp_loc * loc = NULL)
 {
         L.material = gp_medium_material(g, L.medium);
         const int scheme = cfg.energy_loss;
         L.straight = ((cfg.scattering == GPUMAS_MODE_DISABLED) &&
-                         (scheme <= GPUMAS_MODE_MIXED)) ? 1 : 0;
+                         (scheme <= GPUMAS_MODE_MIXED) &&
+                         ((loc == NULL) || ((loc->step_max <= 0.) &&
+                                               !loc->magnetized))) ? 1 : 0;
         e.step_event = GPUMAS_EVENT_NONE;
         if (rec != NULL)
                 gp_rec_frame(rec, e, L.medium, GPUMAS_EVENT_START);
@@ -2719,6 +2916,22 @@ static __device__ __forceinline__ int gp_stepping_relimit(const gp_tables & T, c
         return GP_NEXT_STEP;
 }
 
+/* Update of non-uniform locals after a DEL or an EHS (pumas.c:5403-5414).
+ * Returns GP_NEXT_DONE on a density error, else GP_NEXT_STEP. */
+GPD int gp_stepping_locals(const gp_tables & T, const gp_config & cfg,
+    gp_event & e, gp_loop & L, gp_loc * loc, int & event)
+{
+        if ((loc == NULL) || (loc->step_max <= 0.)) return GP_NEXT_STEP;
+        loc->step_max = gp_set_locals(T, cfg, e, L.medium, L.density, *loc);
+        loc->density = L.density;
+        if (L.density <= 0.) {
+                e.status = GPUMAS_RETURN_DENSITY_ERROR;
+                event = e.step_event;
+                return GP_NEXT_DONE;
+        }
+        return GP_NEXT_STEP;
+}
+
 /* Weight update at a stepping event (pumas.c:5309-5321): backward
  * Jacobian and decay weight since the last event. */
 GPD void gp_stepping_weight(const gp_tables & T, const gp_config & cfg,
@@ -2740,7 +2953,7 @@ GPD void gp_stepping_weight(const gp_tables & T, const gp_config & cfg,
  * (pumas.c:5277-5329 and the medium change of 5417-5467). */
 static __device__ __forceinline__ int gp_stepping_step(const gp_tables & T, const gp_config & cfg,
     const gpumas_geometry & g, gp_event & e, gp_loop & L, int & event,
-    gp_rec * rec = NULL)
+    gp_rec * rec = NULL, gp_loc * loc = NULL)
 {
         if (L.step_index > 1) {
                 const int m = gp_locate(g, e);
@@ -2749,7 +2962,8 @@ static __device__ __forceinline__ int gp_stepping_step(const gp_tables & T, cons
                         L.step_max_medium += 0.5 * GP_STEP_MIN;
         }
         L.new_medium = gp_step(T, cfg, g, e, L.straight, L.medium,
-            L.material, L.density, L.grammage_max, L.step_max_medium);
+            L.material, L.density, L.grammage_max, L.step_max_medium, loc);
+        if (loc != NULL) L.density = loc->density;
         L.step_index++;
         if (e.status != GPUMAS_RETURN_SUCCESS) {
                 event = e.step_event;
@@ -2794,7 +3008,18 @@ static __device__ __forceinline__ int gp_stepping_step(const gp_tables & T, cons
                         return GP_NEXT_DONE;
                 }
                 L.material = gp_medium_material(g, L.medium);
-                L.density = gp_medium_density(T, g, L.medium);
+                if (loc != NULL) {
+                        loc->step_max = gp_set_locals(
+                            T, cfg, e, L.medium, L.density, *loc);
+                        loc->density = L.density;
+                        L.straight =
+                            ((cfg.scattering == GPUMAS_MODE_DISABLED) &&
+                                (scheme <= GPUMAS_MODE_MIXED) &&
+                                (loc->step_max <= 0.) && !loc->magnetized) ?
+                            1 : 0;
+                } else {
+                        L.density = gp_medium_density(T, g, L.medium);
+                }
                 if (L.density <= 0.) {
                         e.status = GPUMAS_RETURN_DENSITY_ERROR;
                         event = e.step_event;
@@ -2820,7 +3045,8 @@ static __device__ __forceinline__ int gp_stepping_step(const gp_tables & T, cons
 /* Tail of a DEL in the stepping loop, once the polar angle is applied
  * (pumas.c:5361-5374 and 5479-5488). */
 static __device__ __forceinline__ int gp_stepping_del_end(const gp_tables & T,
-    const gp_config & cfg, gp_event & e, gp_loop & L, int & event)
+    const gp_config & cfg, gp_event & e, gp_loop & L, int & event,
+    gp_loc * loc = NULL)
 {
         if ((cfg.event & e.step_event) ||
             (e.step_event == GPUMAS_EVENT_WEIGHT) ||
@@ -2830,6 +3056,8 @@ static __device__ __forceinline__ int gp_stepping_del_end(const gp_tables & T,
         }
         e.step_first = 1;
         e.step_invlb1 = 0;
+        if (gp_stepping_locals(T, cfg, e, L, loc, event) == GP_NEXT_DONE)
+                return GP_NEXT_DONE;
         return gp_stepping_relimit(T, cfg, e, L, event);
 }
 
@@ -2839,12 +3067,12 @@ static __device__ __forceinline__ int gp_stepping_del_end(const gp_tables & T,
  * stops, the post step point are recorded. */
 static __device__ __forceinline__ int gp_stepping_del(const gp_tables & T,
     const gp_config & cfg, gp_event & e, gp_loop & L, int & event,
-    gp_rec * rec = NULL)
+    gp_rec * rec = NULL, gp_loc * loc = NULL)
 {
         gp_stepping_weight(T, cfg, e, L);
         if ((rec == NULL) || (rec->period <= 0)) {
                 gp_do_del(T, cfg, e, L.material);
-                return gp_stepping_del_end(T, cfg, e, L, event);
+                return gp_stepping_del_end(T, cfg, e, L, event, loc);
         }
         const double ki = e.energy;
         const double ui[3] = { e.dir[0], e.dir[1], e.dir[2] };
@@ -2867,12 +3095,14 @@ static __device__ __forceinline__ int gp_stepping_del(const gp_tables & T,
         gp_rec_frame(rec, e, L.medium, GPUMAS_EVENT_NONE);
         e.step_first = 1;
         e.step_invlb1 = 0;
+        if (gp_stepping_locals(T, cfg, e, L, loc, event) == GP_NEXT_DONE)
+                return GP_NEXT_DONE;
         return gp_stepping_relimit(T, cfg, e, L, event);
 }
 
 /* EHS of the stepping loop (pumas.c:5393-5400 and 5479-5488). */
 static __device__ __forceinline__ int gp_stepping_ehs(const gp_tables & T, const gp_config & cfg,
-    gp_event & e, gp_loop & L, int & event)
+    gp_event & e, gp_loop & L, int & event, gp_loc * loc = NULL)
 {
         gp_stepping_weight(T, cfg, e, L);
         gp_do_ehs(T, cfg, e, L.material);
@@ -2881,6 +3111,8 @@ static __device__ __forceinline__ int gp_stepping_ehs(const gp_tables & T, const
                 event = e.step_event;
                 return GP_NEXT_DONE;
         }
+        if (gp_stepping_locals(T, cfg, e, L, loc, event) == GP_NEXT_DONE)
+                return GP_NEXT_DONE;
         return gp_stepping_relimit(T, cfg, e, L, event);
 }
 
@@ -3065,7 +3297,7 @@ GPD void gp_event_init(gp_event & e, uint64_t seed, uint64_t id)
  * *event set (including the whole deterministic CSDA case). */
 static __device__ __forceinline__ int gp_transport_begin(const gp_tables & T, const gp_config & cfg,
     const gpumas_geometry & g, gp_event & e, gp_loop & L, int & event,
-    int & medium_in, gp_rec * rec = NULL)
+    int & medium_in, gp_rec * rec = NULL, gp_loc * loc = NULL)
 {
         event = GPUMAS_EVENT_NONE;
         medium_in = -1;
@@ -3093,7 +3325,16 @@ static __device__ __forceinline__ int gp_transport_begin(const gp_tables & T, co
                 return GP_NEXT_DONE;
         } else if (step_max_medium > 0.)
                 step_max_medium += 0.5 * GP_STEP_MIN;
-        L.density = gp_medium_density(T, g, medium);
+        if (loc != NULL) {
+                loc->g = &g;
+                loc->step_max = gp_set_locals(T, cfg, e, medium, L.density,
+                    *loc);
+                loc->density = L.density;
+                if ((loc->step_max > 0.) && (loc->step_max < step_max_medium))
+                        step_max_medium = loc->step_max;
+        } else {
+                L.density = gp_medium_density(T, g, medium);
+        }
         if (L.density <= 0.) {
                 e.status = GPUMAS_RETURN_DENSITY_ERROR;
                 return GP_NEXT_DONE;
@@ -3105,6 +3346,7 @@ static __device__ __forceinline__ int gp_transport_begin(const gp_tables & T, co
         }
         int do_stepping = 1;
         if ((step_max_medium <= 0.) &&
+            ((loc == NULL) || (loc->step_max <= 0.)) &&
             (cfg.energy_loss <= GPUMAS_MODE_CSDA)) {
                 if ((cfg.energy_loss == GPUMAS_MODE_DISABLED) &&
                     ((cfg.event & GPUMAS_EVENT_LIMIT) == 0)) {
@@ -3116,6 +3358,13 @@ static __device__ __forceinline__ int gp_transport_begin(const gp_tables & T, co
                 }
         }
         if (!do_stepping) {
+                if ((loc != NULL) && loc->magnetized) {
+                        /* The closed form CSDA deflection in a uniform
+                         * field (transport_csda_deflect, pumas.c:4968-5075)
+                         * has no device form. */
+                        e.status = GPUMAS_RETURN_VALUE_ERROR;
+                        return GP_NEXT_DONE;
+                }
                 event = gp_transport_csda(T, cfg, e,
                     gp_medium_material(g, medium), L.density, medium, rec);
                 return GP_NEXT_DONE;
@@ -3123,22 +3372,23 @@ static __device__ __forceinline__ int gp_transport_begin(const gp_tables & T, co
         L.step_max_medium = step_max_medium;
         /* The early stops of the stepping prologue return as they are,
          * without the final energy protection (pumas.c:5250-5271). */
-        return gp_stepping_begin(T, cfg, g, e, L, event, rec);
+        return gp_stepping_begin(T, cfg, g, e, L, event, rec, loc);
 }
 
 /* Resume the stepping loop of an event at phase `next` and run it to its
  * end (the one thread per event form). */
 static __device__ __forceinline__ void gp_transport_run(const gp_tables & T, const gp_config & cfg,
     const gpumas_geometry & g, gp_event & e, gp_loop & L, int next,
-    int & event, gp_rec * rec = NULL)
+    int & event, gp_rec * rec = NULL, gp_loc * loc = NULL)
 {
         while (next != GP_NEXT_DONE) {
                 if (next == GP_NEXT_STEP)
-                        next = gp_stepping_step(T, cfg, g, e, L, event, rec);
+                        next = gp_stepping_step(
+                            T, cfg, g, e, L, event, rec, loc);
                 else if (next == GP_NEXT_DEL)
-                        next = gp_stepping_del(T, cfg, e, L, event, rec);
+                        next = gp_stepping_del(T, cfg, e, L, event, rec, loc);
                 else
-                        next = gp_stepping_ehs(T, cfg, e, L, event);
+                        next = gp_stepping_ehs(T, cfg, e, L, event, loc);
         }
         gp_stepping_end(cfg, e);
         /* End of the track (pumas.c:5507-5510); a failed step returns
@@ -3151,13 +3401,13 @@ static __device__ __forceinline__ void gp_transport_run(const gp_tables & T, con
 /* pumas_context_transport for one event, in one thread. */
 static __device__ __forceinline__ void gp_transport(const gp_tables & T, const gp_config & cfg,
     const gpumas_geometry & g, gp_event & e, int & event, int & medium_in,
-    int & medium_out, gp_rec * rec = NULL)
+    int & medium_out, gp_rec * rec = NULL, gp_loc * loc = NULL)
 {
         gp_loop L;
         const int next = gp_transport_begin(
-            T, cfg, g, e, L, event, medium_in, rec);
+            T, cfg, g, e, L, event, medium_in, rec, loc);
         if (next != GP_NEXT_DONE)
-                gp_transport_run(T, cfg, g, e, L, next, event, rec);
+                gp_transport_run(T, cfg, g, e, L, next, event, rec, loc);
         medium_out = L.medium;
 }
 

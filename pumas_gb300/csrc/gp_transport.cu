@@ -41,12 +41,14 @@ __global__ void __launch_bounds__(128, 1) gp_kernel_plain(
 }
 
 /* One thread per event with the frame recorder (struct pumas_recorder,
- * pumas.h:432-458): event i writes its frames after those of events
- * 0 .. i - 1, max_frames each. */
-__global__ void __launch_bounds__(128, 1) gp_kernel_plain_rec(
+ * pumas.h:432-458) and / or the media's local properties (density profiles
+ * and magnetic fields, struct gpumas_locals). With the recorder, event i
+ * writes its frames after those of events 0 .. i - 1, max_frames each. */
+__global__ void __launch_bounds__(128, 1) gp_kernel_plain_ext(
     const gp_tables * __restrict__ Tp, const gp_config cfg,
     const gpumas_geometry * __restrict__ gp, const gp_io io, size_t n,
-    uint64_t first_event, const gpumas_recorder recorder)
+    uint64_t first_event, const gpumas_recorder recorder, int recording,
+    int locals)
 {
         const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
         if (i >= n) return;
@@ -56,14 +58,17 @@ __global__ void __launch_bounds__(128, 1) gp_kernel_plain_rec(
         io.load(i, e);
         gp_event_init(e, cfg.seed, first_event + i);
         gp_rec r;
-        r.frames = recorder.frames + i * (size_t)recorder.max_frames;
+        r.frames = recording ?
+            recorder.frames + i * (size_t)recorder.max_frames : NULL;
         r.max_frames = recorder.max_frames;
         r.period = recorder.period;
         r.count = 0;
+        gp_loc l;
         int event, m_in, m_out;
-        gp_transport(T, cfg, g, e, event, m_in, m_out, &r);
+        gp_transport(T, cfg, g, e, event, m_in, m_out,
+            recording ? &r : NULL, locals ? &l : NULL);
         io.store(i, e, event, m_in, m_out);
-        recorder.length[i] = r.count;
+        if (recording) recorder.length[i] = r.count;
 }
 
 /* Draws of the Philox stream, for checking against other implementations. */
@@ -168,7 +173,26 @@ extern "C" int gp_geometry_upload(const struct gpumas_physics * physics,
                         return GPUMAS_RETURN_INDEX_ERROR;
         }
         size_t sz_media = g.n_media * sizeof(gpumas_medium);
-        size_t sz_z = 0, sz_m = 0, sz_h = 0;
+        size_t sz_z = 0, sz_m = 0, sz_h = 0, sz_l = 0;
+        if (g.locals != NULL) {
+                for (int i = 0; i < g.n_media; i++) {
+                        const gpumas_locals & l = g.locals[i];
+                        for (int k = 0; k < 3; k++)
+                                if (!isfinite(l.magnet[k]))
+                                        return GPUMAS_RETURN_VALUE_ERROR;
+                        if (l.model == GPUMAS_DENSITY_UNIFORM) continue;
+                        if (l.model != GPUMAS_DENSITY_EXPONENTIAL)
+                                return GPUMAS_RETURN_VALUE_ERROR;
+                        if (!(l.rho0 > 0.) || !(l.lambda > 0.) ||
+                            !(l.eps > 0.) || !isfinite(l.h0) ||
+                            !isfinite(l.rho0) || !isfinite(l.lambda))
+                                return GPUMAS_RETURN_VALUE_ERROR;
+                        for (int k = 0; k < 3; k++)
+                                if (!isfinite(l.axis[k]))
+                                        return GPUMAS_RETURN_VALUE_ERROR;
+                }
+                sz_l = g.n_media * sizeof(gpumas_locals);
+        }
         if (g.kind == GPUMAS_GEOMETRY_UNIFORM) {
                 if ((g.uniform_medium < 0) || (g.uniform_medium >= g.n_media))
                         return GPUMAS_RETURN_INDEX_ERROR;
@@ -200,13 +224,15 @@ extern "C" int gp_geometry_upload(const struct gpumas_physics * physics,
         const size_t o_z = (o_media + sz_media + 255) & ~(size_t)255;
         const size_t o_m = (o_z + sz_z + 255) & ~(size_t)255;
         const size_t o_h = (o_m + sz_m + 255) & ~(size_t)255;
-        const size_t total = o_h + sz_h;
+        const size_t o_l = (o_h + sz_h + 255) & ~(size_t)255;
+        const size_t total = o_l + sz_l;
         char * host = (char *)calloc(1, total);
         if (host == NULL) return GPUMAS_RETURN_MEMORY_ERROR;
         memcpy(host + o_media, g.media, sz_media);
         if (sz_z) memcpy(host + o_z, g.slab_z, sz_z);
         if (sz_m) memcpy(host + o_m, g.slab_medium, sz_m);
         if (sz_h) memcpy(host + o_h, g.hm_z, sz_h);
+        if (sz_l) memcpy(host + o_l, g.locals, sz_l);
         char * d = NULL;
         int rc = gp_check(cudaMalloc(&d, total));
         if (rc == GPUMAS_RETURN_SUCCESS)
@@ -222,6 +248,7 @@ extern "C" int gp_geometry_upload(const struct gpumas_physics * physics,
         dg.slab_z = sz_z ? (const double *)(d + o_z) : NULL;
         dg.slab_medium = sz_m ? (const int *)(d + o_m) : NULL;
         dg.hm_z = sz_h ? (const double *)(d + o_h) : NULL;
+        dg.locals = sz_l ? (const gpumas_locals *)(d + o_l) : NULL;
         rc = gp_check(cudaMemcpy(
             d_geometry, &dg, sizeof(dg), cudaMemcpyHostToDevice));
         if (rc != GPUMAS_RETURN_SUCCESS) {
@@ -246,6 +273,7 @@ extern "C" int gpumas_context_geometry_set(
         c->has_geometry = 1;
         c->n_media = geometry->n_media;
         c->geometry_kind = geometry->kind;
+        c->has_locals = (geometry->locals != NULL);
         return GPUMAS_RETURN_SUCCESS;
 }
 
@@ -306,11 +334,12 @@ static int gp_run(gp_context * c, const gp_config & cfg, const gp_io & io,
         if (engine == 0) engine = gp_needs_stepping(c, cfg) ? 2 : 1;
         int rc;
         cudaEventRecord(c->t0, s);
-        if (c->recording) {
+        if (c->recording || c->has_locals) {
                 const unsigned int grid =
                     (unsigned int)((n + gp_block - 1) / gp_block);
-                gp_kernel_plain_rec<<<grid, gp_block, 0, s>>>(c->d_tables,
-                    cfg, c->d_geometry, io, n, first_event, c->recorder);
+                gp_kernel_plain_ext<<<grid, gp_block, 0, s>>>(c->d_tables,
+                    cfg, c->d_geometry, io, n, first_event, c->recorder,
+                    c->recording, c->has_locals);
                 rc = gp_check(cudaGetLastError());
                 c->stats.launches = 1;
         } else if (engine == 2) {

@@ -147,6 +147,59 @@ CASES["terrain_backward"] = dict(
     states=lambda n, s, f: _terrain_states(n, s, f))
 
 
+# Media with local properties (struct gpumas_locals): the reference's
+# exponential atmosphere with the geomagnetic field of
+# examples/pumas/geometry.c:76-97, over 200 m of rock, and a magnetised iron
+# slab (1.5 T, a muon spectrometer's magnet).
+AIR_LOCALS = dict(model=1, rho0=1.205, axis=(0., 0., 1.), h0=0.,
+                  lambda_=12E+03, eps=5E-02, magnet=(0., 2E-05, -4E-05))
+ATMOSPHERE = dict(kind=1, media=[("StandardRock", 0.), ("Air", 0.)],
+                  slab_z=[-200., 0., 20000.], slab_media=[0, 1],
+                  locals=[dict(), AIR_LOCALS])
+IRON_FIELD = dict(kind=1, media=[("Iron", 0.)], slab_z=[0., 20.],
+                  slab_media=[0], locals=[dict(magnet=(1.5, 0., 0.))])
+
+
+def _sky_states(n, seed, first, emin, emax, z0, cos_min=0.2):
+    """Muons with momenta pointing down, at zenith angles of cosine in
+    [cos_min, 1] and uniform azimuth."""
+    s = _states(n, seed, first, emin, emax, z0=z0)
+    ev = np.arange(first, first + n, dtype=np.uint64)
+    c = cos_min + (1. - cos_min) * W.uniform(seed, 1, ev, 1)
+    phi = 2. * np.pi * W.uniform(seed, 1, ev, 2)
+    st = np.sqrt(1. - c * c)
+    s["direction"][:, 0] = st * np.cos(phi)
+    s["direction"][:, 1] = st * np.sin(phi)
+    s["direction"][:, 2] = -c
+    return s
+
+
+CASES["atmosphere_forward"] = dict(
+    config=_cfg(STRAGGLED, MIXED, FWD, event=LIMIT_ENERGY, limit_energy=1.),
+    geometry=ATMOSPHERE, n=100, seed=31,
+    states=lambda n, s, f: _sky_states(n, s, f, 1., 1E+03, 15000.))
+CASES["atmosphere_backward"] = dict(
+    config=_cfg(STRAGGLED, MIXED, BWD, event=LIMIT_ENERGY,
+                limit_energy=1E+05),
+    geometry=ATMOSPHERE, n=100, seed=32,
+    states=lambda n, s, f: _sky_states(n, s, f, 1., 1E+02, -199.))
+CASES["atmosphere_csda"] = dict(
+    config=_cfg(CSDA, DISABLED, FWD, decay=DISABLED, event=LIMIT_ENERGY,
+                limit_energy=1.),
+    geometry=ATMOSPHERE, n=100, seed=33,
+    states=lambda n, s, f: _sky_states(n, s, f, 1., 1E+03, 15000.))
+CASES["iron_field"] = dict(
+    config=_cfg(STRAGGLED, MIXED, FWD),
+    geometry=IRON_FIELD, n=200, seed=34,
+    states=lambda n, s, f: _states(n, s, f, 1., 1E+02))
+
+
+def has_locals(name):
+    """Whether a case's media have local properties, which the C
+    restatement does not cover (its oracle is the reference itself)."""
+    return CASES[name]["geometry"].get("locals") is not None
+
+
 def make_states(name, n=None, first_event=0):
     c = CASES[name]
     return c["states"](c["n"] if n is None else n, c["seed"], first_event)

@@ -61,11 +61,12 @@ def oracle_geometry(orc, spec):
 def gpu_geometry(physics, spec):
     import pumas_gb300 as pg
     media = [(physics.material_index(m), d) for m, d in spec["media"]]
+    loc = spec.get("locals")
     if spec["kind"] == pg.GEOMETRY_UNIFORM:
-        return pg.Geometry(pg.GEOMETRY_UNIFORM, media, medium=0)
+        return pg.Geometry(pg.GEOMETRY_UNIFORM, media, locals=loc, medium=0)
     if spec["kind"] == pg.GEOMETRY_SLABS:
-        return pg.Geometry(pg.GEOMETRY_SLABS, media, z=spec["slab_z"],
-                           slab_media=spec["slab_media"])
+        return pg.Geometry(pg.GEOMETRY_SLABS, media, locals=loc,
+                           z=spec["slab_z"], slab_media=spec["slab_media"])
     return pg.Geometry(pg.GEOMETRY_HEIGHTMAP, media,
                        heights=spec["hm_z"], x0=spec["hm_x0"],
                        y0=spec["hm_y0"], dx=spec["hm_dx"], dy=spec["hm_dy"],
