@@ -3132,10 +3132,149 @@ GPD void gp_stepping_end(const gp_config & cfg, gp_event & e)
         }
 }
 
-/* transport_with_csda (pumas.c:4777-4949), no magnetic field. */
+/* Normalised magnetic rotation angle of the deterministic CEL, in
+ * kg/m^2/T (cel_magnetic_rotation, pumas.c:3849-3883): the proper time
+ * integral from the kinetic energy down to the table's bottom. */
+GPD double gp_cel_magnetic_rotation(
+    const gp_tables & T, int material, double kinetic)
+{
+        const int imax = T.n_energies - 1;
+        const double factor = GP_LARMOR_FACTOR / T.mass;
+        const double Tmax = __ldg(T.T + GP_ROW(0, material) + imax);
+        if (kinetic <= __ldg(T.K)) return GP_MUL(Tmax, factor);
+        if (kinetic >= __ldg(T.K + imax)) return 0.;
+        const double t = gp_baked(T, GP_LUT_K, T.K,
+            GP_C_T(T.n_materials, 0, material), kinetic);
+        return GP_MUL(GP_SUB(Tmax, t), factor);
+}
+
+/* Magnetic transport moments x, y, z of the CSDA down from `kinetic` in a
+ * uniform medium and transverse field (csda_magnetic_transport,
+ * pumas.c:5095-5171): the tabulated moments of the 8 orders, combined with
+ * the reference's polynomial fits of cos and sin over [0, 2 pi] (data of
+ * the algorithm, kept as they are). Returns a pumas return code. */
+GPD int gp_csda_magnetic_transport(const gp_tables & T, int material,
+    double density, double magnet, double charge, double kinetic,
+    double phase, double & x, double & y, double & z)
+{
+        const int imax = T.n_energies - 1;
+        double k0 = kinetic;
+        int i1, i2;
+        if (kinetic <= __ldg(T.K)) {
+                k0 = __ldg(T.K);
+                i1 = 0;
+                i2 = 1;
+        } else if (kinetic >= __ldg(T.K + imax)) {
+                y = 0.;
+                x = z = -GP_SUB(gp_cel_grammage(T, GPUMAS_MODE_CSDA, material,
+                                    kinetic),
+                            __ldg(T.X + GP_ROW(0, material) + imax));
+                return GPUMAS_RETURN_SUCCESS;
+        } else {
+                i1 = gp_index(T, GP_LUT_K, T.K, k0);
+                i2 = i1 + 1;
+        }
+        if (fabs(phase) > 2.0 * GP_PI) return GPUMAS_RETURN_VALUE_ERROR;
+        const double poly_x[8] = { 1.000000000e+000, 0.000000000e+000,
+                -5.000000000e-001, -1.048969541e-002, 5.597396438e-002,
+                -6.401353612e-003, -4.495849930e-004, 6.583532135e-005 };
+        const double poly_y[8] = { 0.000000000e+000, 1.000000000e+000,
+                -1.400755143e-002, -1.350173383e-001, -2.838778336e-002,
+                2.123237056e-002, -3.094290091e-003, 1.409012754e-004 };
+        const double a = GP_MUL(-magnet, charge) / density;
+        const double * L = T.Li + (long)material * 8 * T.n_energies;
+        double x1 = 0., x2 = 0., y1 = 0., y2 = 0., u = 1.;
+        for (int j = 0; j < 8; j++) {
+                const double l1 = __ldg(L + j * T.n_energies + i1);
+                const double l2 = __ldg(L + j * T.n_energies + i2);
+                const double ux = GP_MUL(u, poly_x[j]);
+                const double uy = GP_MUL(u, poly_y[j]);
+                x1 = GP_ADD(x1, GP_MUL(ux, l1));
+                y1 = GP_ADD(y1, GP_MUL(uy, l1));
+                x2 = GP_ADD(x2, GP_MUL(ux, l2));
+                y2 = GP_ADD(y2, GP_MUL(uy, l2));
+                u = GP_MUL(u, a);
+        }
+        const double z1 = __ldg(L + i1), z2 = __ldg(L + i2);
+        const double K1 = __ldg(T.K + i1);
+        const double h = GP_SUB(k0, K1) / GP_SUB(__ldg(T.K + i2), K1);
+        x = GP_ADD(x1, GP_MUL(h, GP_SUB(x2, x1))) / density;
+        y = GP_ADD(y1, GP_MUL(h, GP_SUB(y2, y1))) / density;
+        z = GP_ADD(z1, GP_MUL(h, GP_SUB(z2, z1))) / density;
+        return GPUMAS_RETURN_SUCCESS;
+}
+
+/* End point of a CSDA track of length `distance` from kinetic energy ki to
+ * e.energy in a uniform medium and field (transport_csda_deflect,
+ * pumas.c:4968-5075), in the field's frame: ez along the field, ex and ey
+ * across it. Returns a pumas return code; as in the reference, the
+ * position and direction stay as they are when the track has no rotation
+ * at all or on an error. */
+GPD int gp_csda_deflect(const gp_tables & T, gp_event & e, int material,
+    double density, const double * m, double ki, double distance)
+{
+        const double charge = e.charge;
+        const double kf = e.energy;
+        const double * u = e.dir;
+        const double b0 = sqrt(GP_ADD(GP_ADD(GP_MUL(m[0], m[0]),
+            GP_MUL(m[1], m[1])), GP_MUL(m[2], m[2])));
+        const double b0_i = 1.0 / b0;
+        double ex[3], ey[3], ez[3];
+        ey[0] = GP_MUL(GP_SUB(GP_MUL(u[2], m[1]), GP_MUL(u[1], m[2])), b0_i);
+        ey[1] = GP_MUL(GP_SUB(GP_MUL(u[0], m[2]), GP_MUL(u[2], m[0])), b0_i);
+        ey[2] = GP_MUL(GP_SUB(GP_MUL(u[1], m[0]), GP_MUL(u[0], m[1])), b0_i);
+        const double d = GP_MUL(GP_MUL(b0_i, b0_i), GP_ADD(GP_ADD(
+            GP_MUL(m[0], u[0]), GP_MUL(m[1], u[1])), GP_MUL(m[2], u[2])));
+        for (int k = 0; k < 3; k++) {
+                ez[k] = GP_MUL(m[k], d);
+                ex[k] = GP_SUB(u[k], ez[k]);
+        }
+        const double a = GP_MUL(-b0, charge) / density;
+        const double pi = GP_MUL(a, gp_cel_magnetic_rotation(T, material, ki));
+        const double pf = GP_MUL(a, gp_cel_magnetic_rotation(T, material, kf));
+        const double dp = GP_SUB(pf, pi);
+        const double ps = fabs(GP_ADD(pi, pf));
+        if (ps == 0.) return GPUMAS_RETURN_SUCCESS;
+        const double dp0 = fabs(dp);
+        double dx, dy, dz;
+        if ((dp0 < 1E-02) && (dp0 / ps < 1E-02)) {
+                /* Small rotation, linear in the distance. */
+                dz = (ki >= kf) ? distance : -distance;
+                const double sixth = 1 / 6.0;
+                dx = GP_MUL(dz, GP_SUB(1.0, GP_MUL(GP_MUL(sixth, dp), dp)));
+                dy = GP_MUL(GP_MUL(0.5, dz), dp);
+        } else {
+                double xi, yi, zi, xf, yf, zf;
+                int rc = gp_csda_magnetic_transport(T, material, density, b0,
+                    charge, ki, pi, xi, yi, zi);
+                if (rc != GPUMAS_RETURN_SUCCESS) return rc;
+                rc = gp_csda_magnetic_transport(T, material, density, b0,
+                    charge, kf, pf, xf, yf, zf);
+                if (rc != GPUMAS_RETURN_SUCCESS) return rc;
+                const double si = sin(pi);
+                const double ci = cos(pi);
+                xf = GP_SUB(xf, xi);
+                yf = GP_SUB(yf, yi);
+                dx = GP_ADD(GP_MUL(ci, xf), GP_MUL(si, yf));
+                dy = GP_ADD(GP_MUL(-si, xf), GP_MUL(ci, yf));
+                dz = GP_SUB(zf, zi);
+        }
+        for (int k = 0; k < 3; k++)
+                e.pos[k] = GP_ADD(e.pos[k], GP_ADD(GP_ADD(GP_MUL(dx, ex[k]),
+                    GP_MUL(dy, ey[k])), GP_MUL(dz, ez[k])));
+        const double s = sin(dp);
+        const double c = cos(dp);
+        for (int k = 0; k < 3; k++)
+                e.dir[k] = GP_ADD(GP_ADD(GP_MUL(c, ex[k]), GP_MUL(s, ey[k])),
+                    ez[k]);
+        return GPUMAS_RETURN_SUCCESS;
+}
+
+/* transport_with_csda (pumas.c:4777-4949), with the deflection of a
+ * uniform magnetic field when `magnet` is given. */
 static __device__ __forceinline__ int gp_transport_csda(const gp_tables & T, const gp_config & cfg,
     gp_event & e, int material, double density, int medium = -1,
-    gp_rec * rec = NULL)
+    gp_rec * rec = NULL, const double * magnet = NULL)
 {
         const double ki = e.energy;
         const double di = e.distance;
@@ -3263,11 +3402,20 @@ static __device__ __forceinline__ int gp_transport_csda(const gp_tables & T, con
                     gp_cel_energy_loss(T, GPUMAS_MODE_CSDA, material, ki);
         if (cfg.decay == GPUMAS_MODE_WEIGHTED)
                 e.weight *= gp_exp(-fabs(ti - e.time) / T.ctau);
-        const double path =
-            (cfg.direction == GPUMAS_MODE_FORWARD) ? distance : -distance;
-        e.pos[0] += path * e.dir[0];
-        e.pos[1] += path * e.dir[1];
-        e.pos[2] += path * e.dir[2];
+        if (magnet != NULL) {
+                const int rc = gp_csda_deflect(
+                    T, e, material, density, magnet, ki, distance);
+                if (rc != GPUMAS_RETURN_SUCCESS) {
+                        e.status = rc;
+                        return event;
+                }
+        } else {
+                const double path = (cfg.direction == GPUMAS_MODE_FORWARD) ?
+                    distance : -distance;
+                e.pos[0] += path * e.dir[0];
+                e.pos[1] += path * e.dir[1];
+                e.pos[2] += path * e.dir[2];
+        }
         if (rec != NULL)
                 gp_rec_frame(rec, e, medium, event | GPUMAS_EVENT_STOP);
         return event;
@@ -3358,15 +3506,9 @@ static __device__ __forceinline__ int gp_transport_begin(const gp_tables & T, co
                 }
         }
         if (!do_stepping) {
-                if ((loc != NULL) && loc->magnetized) {
-                        /* The closed form CSDA deflection in a uniform
-                         * field (transport_csda_deflect, pumas.c:4968-5075)
-                         * has no device form. */
-                        e.status = GPUMAS_RETURN_VALUE_ERROR;
-                        return GP_NEXT_DONE;
-                }
                 event = gp_transport_csda(T, cfg, e,
-                    gp_medium_material(g, medium), L.density, medium, rec);
+                    gp_medium_material(g, medium), L.density, medium, rec,
+                    ((loc != NULL) && loc->magnetized) ? loc->magnet : NULL);
                 return GP_NEXT_DONE;
         }
         L.step_max_medium = step_max_medium;

@@ -127,6 +127,7 @@ struct gp_tables {
         const float *DCS, *DCS_x, *DCS_env;
         const double *Kt, *a_max, *b_max, *Mu0, *Mu0_dK, *Lb, *Lb_dK;
         const double *Ms1, *Ms1_dK;
+        const double * Li; /* CSDA magnetic moments, 8 orders per material */
         const int * elements_in;
         const int * comp_start;
         const int * comp_element;

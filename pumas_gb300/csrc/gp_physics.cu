@@ -616,6 +616,7 @@ static int physics_from_blob(
         t->DCS_x = DF(27);
         t->DCS_env = DF(28);
         t->Kt = DD(30);
+        t->Li = DD(31);
         t->a_max = DD(33);
         t->b_max = DD(34);
         t->Mu0 = DD(35);

@@ -194,6 +194,30 @@ CASES["iron_field"] = dict(
     states=lambda n, s, f: _states(n, s, f, 1., 1E+02))
 
 
+# Deterministic CSDA in uniform media with a field: the reference's closed
+# form deflection (transport_csda_deflect, pumas.c:4968-5075).
+CASES["rock_csda_field"] = dict(
+    config=_cfg(CSDA, DISABLED, FWD, decay=DISABLED, event=LIMIT_ENERGY,
+                limit_energy=1.),
+    geometry=dict(kind=0, media=[("StandardRock", 0.)],
+                  locals=[dict(magnet=(0., 5E-03, 0.))]),
+    n=200, seed=35,
+    states=lambda n, s, f: _states(n, s, f, 1., 1E+04))
+# Short tracks: the small rotation branch of the closed form.
+CASES["rock_csda_field_distance"] = dict(
+    config=_cfg(CSDA, DISABLED, FWD, decay=DISABLED, event=LIMIT_DISTANCE,
+                limit_distance=20.),
+    geometry=CASES["rock_csda_field"]["geometry"], n=200, seed=37,
+    states=lambda n, s, f: _states(n, s, f, 10., 1E+04))
+CASES["water_csda_field_backward"] = dict(
+    config=_cfg(CSDA, DISABLED, BWD, decay=DISABLED, event=LIMIT_ENERGY,
+                limit_energy=1E+04),
+    geometry=dict(kind=0, media=[("Water", 0.)],
+                  locals=[dict(magnet=(2E-04, 0., 1E-04))]),
+    n=200, seed=36,
+    states=lambda n, s, f: _states(n, s, f, 1., 1E+02))
+
+
 def has_locals(name):
     """Whether a case's media have local properties, which the C
     restatement does not cover (its oracle is the reference itself)."""

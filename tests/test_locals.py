@@ -4,9 +4,11 @@ magnetic fields, the device form of the reference's `pumas_locals_cb`
 steps of pumas.c:6352-6382, 6833-6911).
 
 Parity with the reference runs through the golden cases with locals of
-tests/cases.py (atmosphere_*, iron_field) in test_gpu_parity.py. This file
-covers the descriptor's layout, its checks and the entry points that do not
-take locals.
+tests/cases.py in test_gpu_parity.py: the stepping cases atmosphere_* and
+iron_field, and the closed form CSDA deflection (transport_csda_deflect,
+pumas.c:4968-5171) of rock_csda_field*, water_csda_field_backward. This
+file covers the descriptor's layout, its checks and the entry points that
+do not take locals.
 """
 import ctypes
 import os
@@ -105,22 +107,3 @@ def test_pool_entry_points_refuse_locals(gpu_physics):
     b, rb = ctx.transport(s0)
     assert ctx.stats()["launches"] == 1
     assert np.array_equal(a, b) and np.array_equal(ra, rb)
-
-
-@pytest.mark.gpu
-def test_csda_closed_form_with_field_is_refused(gpu_physics):
-    """Deterministic CSDA in a uniform infinite medium with a field is the
-    reference's closed form deflection (transport_csda_deflect), which has
-    no device form: such events end with a value error."""
-    import pumas_gb300 as pg
-    spec = dict(kind=0, media=[("StandardRock", 0.)],
-                locals=[dict(magnet=(0., 0., 1.))])
-    geo = gpu_geometry(gpu_physics, spec)
-    ctx = gpu_context(gpu_physics, CASES["atmosphere_csda"]["config"], 1,
-                      geo)
-    s0 = pg.new_states(4)
-    s0["energy"] = 10.
-    s0["charge"] = -1.
-    s0["direction"][:, 2] = 1.
-    _, r = ctx.transport(s0)
-    assert np.all(r["status"] == pg.RETURN_VALUE_ERROR)
