@@ -75,6 +75,10 @@ extern "C" {
 #define GPUMAS_MODE_FORWARD 0
 #define GPUMAS_MODE_BACKWARD 1
 
+/* Particles: same values as enum pumas_particle. */
+#define GPUMAS_PARTICLE_MUON 0
+#define GPUMAS_PARTICLE_TAU 1
+
 #define GPUMAS_EVENT_NONE 0
 #define GPUMAS_EVENT_LIMIT_ENERGY 1
 #define GPUMAS_EVENT_LIMIT_DISTANCE 2
@@ -176,6 +180,13 @@ int gpumas_physics_material_index(const struct gpumas_physics * physics,
 /** Number of materials and elements, the cutoff and the particle mass. */
 int gpumas_physics_info(const struct gpumas_physics * physics,
     int * n_materials, int * n_elements, double * cutoff, double * mass);
+
+/** Transported particle (GPUMAS_PARTICLE_MUON or GPUMAS_PARTICLE_TAU), its
+ * proper lifetime c tau in m and its mass in GeV/c^2. Replaces
+ * `pumas_physics_particle` (pumas.h:1106-1108). The particle comes from
+ * the physics dump: both are tabulated with the default models. */
+int gpumas_physics_particle(const struct gpumas_physics * physics,
+    int * particle, double * lifetime, double * mass);
 
 /* ------------------------------------------------------------------------ */
 /* Contexts.                                                                */

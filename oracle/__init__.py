@@ -15,7 +15,9 @@ does.
 """
 import ctypes
 import os
+import shutil
 import subprocess
+import tempfile
 
 import numpy as np
 
@@ -144,10 +146,18 @@ class _Oracle:
     prefix = None
     path = None
 
-    def __init__(self):
+    def __init__(self, private=False):
+        """Load the oracle library. Its physics is a global of the library:
+        with `private`, a copy of the library is loaded instead, so that
+        another physics (taus) can live beside the first one."""
         if not os.path.exists(self.path):
             raise FileNotFoundError(self.path)
-        self.lib = ctypes.CDLL(self.path)
+        path = self.path
+        if private:
+            path = os.path.join(tempfile.mkdtemp(prefix="oracle"),
+                                os.path.basename(self.path))
+            shutil.copy(self.path, path)
+        self.lib = ctypes.CDLL(path)
         p = self.prefix
         self._transport = getattr(self.lib, p + "_transport")
         self._transport.restype = ctypes.c_int
@@ -201,8 +211,8 @@ class Port(_Oracle):
     prefix = "oracle_port"
     path = PORT_LIB
 
-    def __init__(self, dump_bytes):
-        super().__init__()
+    def __init__(self, dump_bytes, private=False):
+        super().__init__(private)
         self.lib.oracle_port_load.restype = ctypes.c_int
         self.lib.oracle_port_load.argtypes = [ctypes.c_char_p,
                                               ctypes.c_int64]
@@ -223,8 +233,8 @@ class Reference(_Oracle):
     prefix = "oracle_ref"
     path = REF_LIB
 
-    def __init__(self, dump_path):
-        super().__init__()
+    def __init__(self, dump_path, private=False):
+        super().__init__(private)
         self.lib.oracle_ref_load.restype = ctypes.c_int
         self.lib.oracle_ref_load.argtypes = [ctypes.c_char_p]
         rc = self.lib.oracle_ref_load(dump_path.encode())

@@ -270,7 +270,8 @@ int oracle_port_load(const void * dump, int64_t size)
         /* Only the default DCS models are restated. */
         if ((strcmp(b + off[50], "SSR") != 0) ||
             (strcmp(b + off[51], "SSR") != 0) ||
-            (strcmp(b + off[52], "DRSS") != 0) || (p->particle != 0)) {
+            (strcmp(b + off[52], "DRSS") != 0) ||
+            ((p->particle != 0) && (p->particle != 1))) {
                 port_free(p);
                 return RC_MODEL_ERROR;
         }

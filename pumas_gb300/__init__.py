@@ -27,6 +27,8 @@ from . import build as _build
 HERE = os.path.dirname(os.path.abspath(__file__))
 DATA = os.path.join(HERE, "data")
 DEFAULT_DUMP = os.path.join(DATA, "muon.pumas.gz")
+TAU_DUMP = os.path.join(DATA, "tau.pumas.gz")
+PARTICLE_MUON, PARTICLE_TAU = 0, 1
 
 # enum pumas_mode / pumas_event / pumas_return values (pumas.h:90-196).
 MODE_DISABLED, MODE_CSDA, MODE_MIXED, MODE_STRAGGLED = -1, 0, 1, 2
@@ -184,6 +186,8 @@ def library(build=False):
         lib.gpumas_physics_info.argtypes = [
             vp, ctypes.POINTER(i), ctypes.POINTER(i), ctypes.POINTER(d),
             ctypes.POINTER(d)]
+        lib.gpumas_physics_particle.argtypes = [
+            vp, ctypes.POINTER(i), ctypes.POINTER(d), ctypes.POINTER(d)]
         lib.gpumas_context_create.argtypes = [
             ctypes.POINTER(ctypes.POINTER(_Context)), vp, i]
         lib.gpumas_context_destroy.argtypes = [
@@ -221,6 +225,7 @@ def library(build=False):
             u64, ctypes.c_uint32, u64, u64, sz, vp]
         for f in ("gpumas_physics_load", "gpumas_physics_upload",
                   "gpumas_physics_material_index", "gpumas_physics_info",
+                  "gpumas_physics_particle",
                   "gpumas_context_create", "gpumas_context_geometry_set",
                   "gpumas_context_transport",
                   "gpumas_context_transport_device", "gpumas_context_stats",
@@ -240,9 +245,11 @@ def _check(rc, where):
         raise PumasError(rc, where)
 
 
-def default_dump():
-    """Bytes of the shipped physics dump (StandardRock, Water, Air, Iron)."""
-    with gzip.open(DEFAULT_DUMP, "rb") as f:
+def default_dump(particle="muon"):
+    """Bytes of a shipped physics dump (StandardRock, Water, Air, Iron) for
+    muons or taus, made by the reference's pumas_physics_create."""
+    path = {"muon": DEFAULT_DUMP, "tau": TAU_DUMP}[particle]
+    with gzip.open(path, "rb") as f:
         return f.read()
 
 
@@ -263,6 +270,11 @@ class Physics:
                                 ctypes.byref(cut), ctypes.byref(mass))
         self.n_materials, self.n_elements = nm.value, ne.value
         self.cutoff, self.mass = cut.value, mass.value
+        part, ctau = ctypes.c_int(), ctypes.c_double()
+        _check(lib.gpumas_physics_particle(self._ptr, ctypes.byref(part),
+                                           ctypes.byref(ctau), None),
+               "gpumas_physics_particle")
+        self.particle, self.ctau = part.value, ctau.value
 
     def material_index(self, name):
         idx = ctypes.c_int(-1)

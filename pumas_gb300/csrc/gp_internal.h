@@ -147,6 +147,7 @@ struct gpumas_physics {
         size_t device_size;
         int n_materials;
         int n_elements;
+        int particle; /* enum pumas_particle: 0 muon, 1 tau */
         char ** material_name;
         int device;
 };

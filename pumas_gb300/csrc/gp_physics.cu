@@ -334,8 +334,12 @@ static int parse_blob(const char * b, int64_t size, struct parsed * p)
                 return GPUMAS_RETURN_FORMAT_ERROR;
         if ((strcmp(b + p->off[50], "SSR") != 0) ||
             (strcmp(b + p->off[51], "SSR") != 0) ||
-            (strcmp(b + p->off[52], "DRSS") != 0) || (p->particle != 0))
+            (strcmp(b + p->off[52], "DRSS") != 0))
                 return GPUMAS_RETURN_MODEL_ERROR;
+        /* Muons or taus (enum pumas_particle, pumas.h:45-50). */
+        if ((p->particle != GPUMAS_PARTICLE_MUON) &&
+            (p->particle != GPUMAS_PARTICLE_TAU))
+                return GPUMAS_RETURN_UNKNOWN_PARTICLE;
         return GPUMAS_RETURN_SUCCESS;
 }
 
@@ -557,6 +561,7 @@ static int physics_from_blob(
         }
         ph->n_materials = nm;
         ph->n_elements = ne;
+        ph->particle = p.particle;
         cudaGetDevice(&ph->device);
 
         if (cudaMalloc(&ph->device_blob, total) != cudaSuccess) {
@@ -712,6 +717,16 @@ extern "C" int gpumas_physics_info(const struct gpumas_physics * physics,
         if (n_materials != NULL) *n_materials = physics->n_materials;
         if (n_elements != NULL) *n_elements = physics->n_elements;
         if (cutoff != NULL) *cutoff = physics->tables.cutoff;
+        if (mass != NULL) *mass = physics->tables.mass;
+        return GPUMAS_RETURN_SUCCESS;
+}
+
+extern "C" int gpumas_physics_particle(const struct gpumas_physics * physics,
+    int * particle, double * lifetime, double * mass)
+{
+        if (physics == NULL) return GPUMAS_RETURN_PHYSICS_ERROR;
+        if (particle != NULL) *particle = physics->particle;
+        if (lifetime != NULL) *lifetime = physics->tables.ctau;
         if (mass != NULL) *mass = physics->tables.mass;
         return GPUMAS_RETURN_SUCCESS;
 }

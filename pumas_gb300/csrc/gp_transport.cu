@@ -101,7 +101,8 @@ extern "C" int gpumas_context_create(struct gpumas_context ** context,
         c->physics = physics;
         /* Defaults of pumas_context_create (pumas.c:2592-2612). */
         c->api.mode.energy_loss = GPUMAS_MODE_STRAGGLED;
-        c->api.mode.decay = GPUMAS_MODE_WEIGHTED;
+        c->api.mode.decay = (physics->particle == GPUMAS_PARTICLE_MUON) ?
+            GPUMAS_MODE_WEIGHTED : GPUMAS_MODE_RANDOMISED;
         c->api.mode.direction = GPUMAS_MODE_FORWARD;
         c->api.mode.scattering = GPUMAS_MODE_MIXED;
         c->api.event = GPUMAS_EVENT_NONE;
@@ -292,6 +293,11 @@ extern "C" int gp_config_check(const struct gpumas_context * context,
                 return GPUMAS_RETURN_VALUE_ERROR;
         if ((context->mode.decay < GPUMAS_MODE_DISABLED) ||
             (context->mode.decay > GPUMAS_MODE_RANDOMISED))
+                return GPUMAS_RETURN_DECAY_ERROR;
+        /* Weighted decay is invalid for forward taus (pumas.c:3157-3161). */
+        if ((physics->particle == GPUMAS_PARTICLE_TAU) &&
+            (context->mode.direction == GPUMAS_MODE_FORWARD) &&
+            (context->mode.decay == GPUMAS_MODE_WEIGHTED))
                 return GPUMAS_RETURN_DECAY_ERROR;
         if ((context->accuracy <= 0) || (context->accuracy > 1))
                 return GPUMAS_RETURN_ACCURACY_ERROR;

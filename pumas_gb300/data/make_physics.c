@@ -9,10 +9,11 @@
  * dump that is shipped as package data, so that machines without the
  * reference can still load the tables.
  *
- * usage: make_physics <materials.xml> <dedx directory> <output dump>
+ * usage: make_physics <materials.xml> <dedx directory> <output dump> [tau]
  */
 #include <stdio.h>
 #include <stdlib.h>
+#include <string.h>
 
 #include "pumas.h"
 
@@ -23,8 +24,11 @@ int main(int argc, char * argv[])
                 return EXIT_FAILURE;
         }
         struct pumas_physics * physics = NULL;
-        if (pumas_physics_create(&physics, PUMAS_PARTICLE_MUON, argv[1],
-                argv[2], NULL) != PUMAS_RETURN_SUCCESS)
+        const enum pumas_particle particle =
+            ((argc > 4) && (strcmp(argv[4], "tau") == 0)) ?
+            PUMAS_PARTICLE_TAU : PUMAS_PARTICLE_MUON;
+        if (pumas_physics_create(&physics, particle, argv[1], argv[2], NULL) !=
+            PUMAS_RETURN_SUCCESS)
                 return EXIT_FAILURE;
         FILE * stream = fopen(argv[3], "wb");
         if (stream == NULL) return EXIT_FAILURE;

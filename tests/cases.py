@@ -218,6 +218,33 @@ CASES["water_csda_field_backward"] = dict(
     states=lambda n, s, f: _states(n, s, f, 1., 1E+02))
 
 
+# Taus (physics made by pumas_physics_create for PUMAS_PARTICLE_TAU): the
+# randomised decay of forward taus through the multi-material stack, with
+# straggling, and in rock in closed form CSDA; weighted backward transport
+# over 20 m of rock.
+CASES["tau_stack_forward"] = dict(
+    physics="tau",
+    config=_cfg(STRAGGLED, MIXED, FWD, decay=RANDOMISED),
+    geometry=STACK, n=200, seed=41,
+    states=lambda n, s, f: _states(n, s, f, 1E+05, 1E+08))
+CASES["tau_rock_csda_randomised"] = dict(
+    physics="tau",
+    config=_cfg(CSDA, DISABLED, FWD, decay=RANDOMISED),
+    geometry=ROCK, n=200, seed=42,
+    states=lambda n, s, f: _states(n, s, f, 1E+02, 1E+06))
+CASES["tau_rock_backward"] = dict(
+    physics="tau",
+    config=_cfg(STRAGGLED, MIXED, BWD, event=LIMIT_DISTANCE,
+                limit_distance=20.),
+    geometry=ROCK_SLAB, n=200, seed=43,
+    states=lambda n, s, f: _states(n, s, f, 1E+04, 1E+06, z0=999.999))
+
+
+def particle(name):
+    """Physics of a case: "muon" (default) or "tau"."""
+    return CASES[name].get("physics", "muon")
+
+
 def has_locals(name):
     """Whether a case's media have local properties, which the C
     restatement does not cover (its oracle is the reference itself)."""

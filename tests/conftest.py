@@ -51,6 +51,50 @@ def gpu_physics(dump):
     return pumas_gb300.Physics(dump)
 
 
+@pytest.fixture(scope="session")
+def tau_dump():
+    import pumas_gb300
+    return pumas_gb300.default_dump("tau")
+
+
+@pytest.fixture(scope="session")
+def tau_port(tau_dump):
+    """The C restatement with the tau physics, in its own copy of the
+    library (the physics is a global of the library)."""
+    import oracle
+    oracle.build_port()
+    return oracle.Port(tau_dump, private=True)
+
+
+@pytest.fixture(scope="session")
+def tau_reference(reference, tau_dump, tmp_path_factory):
+    import oracle
+    path = tmp_path_factory.mktemp("phys") / "tau.pumas"
+    path.write_bytes(tau_dump)
+    return oracle.Reference(str(path), private=True)
+
+
+@pytest.fixture(scope="session")
+def gpu_tau_physics(gpu_physics, tau_dump):
+    import pumas_gb300
+    return pumas_gb300.Physics(tau_dump)
+
+
+def case_oracle(request, name, kind):
+    """The oracle fixture (`port` or `reference`) with a case's physics."""
+    from cases import particle
+    p = particle(name)
+    return request.getfixturevalue(kind if p == "muon" else p + "_" + kind)
+
+
+def case_physics(request, name):
+    """The GPU physics fixture of a case."""
+    from cases import particle
+    p = particle(name)
+    return request.getfixturevalue(
+        "gpu_physics" if p == "muon" else "gpu_%s_physics" % p)
+
+
 def oracle_geometry(orc, spec):
     import oracle
     media = [(orc.material_index(m), d) for m, d in spec["media"]]

@@ -71,12 +71,22 @@ def main():
         make_frames(ref, args[1:])
         return
     names = args or list(CASES)
+    refs = {"muon": ref}
     for name in names:
         case = CASES[name]
+        particle = case.get("physics", "muon")
+        if particle not in refs:
+            # Another physics in a private copy of the reference library.
+            p = os.path.join(os.path.dirname(path), "golden_%s.pumas" %
+                             particle)
+            with open(p, "wb") as f:
+                f.write(pumas_gb300.default_dump(particle))
+            refs[particle] = oracle.Reference(p, private=True)
+        r = refs[particle]
         s0 = make_states(name)
-        geo = oracle_geometry(ref, case["geometry"])
+        geo = oracle_geometry(r, case["geometry"])
         cfg = oracle_config(case["config"], case["seed"])
-        s1, r1 = ref.transport(cfg, geo, s0, 0, 8)
+        s1, r1 = r.transport(cfg, geo, s0, 0, 8)
         np.savez_compressed(os.path.join(HERE, name + ".npz"), initial=s0,
                             final=s1, results=r1)
         print("%-28s %5d events, %7.1f steps/event, status %s" % (

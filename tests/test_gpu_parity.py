@@ -23,8 +23,8 @@ import numpy as np
 import pytest
 
 from cases import CASES, make_states
-from conftest import (GOLDEN, compare, gpu_context, gpu_geometry,
-                      oracle_config, oracle_geometry)
+from conftest import (GOLDEN, case_physics, compare, gpu_context,
+                      gpu_geometry, oracle_config, oracle_geometry)
 
 pytestmark = pytest.mark.gpu
 
@@ -82,9 +82,9 @@ _golden_tally = {}
 
 
 @pytest.mark.parametrize("name", sorted(CASES))
-def test_gpu_matches_reference_golden(gpu_physics, name):
+def test_gpu_matches_reference_golden(request, name):
     data = np.load(os.path.join(GOLDEN, name + ".npz"))
-    s1, r1 = run_gpu(gpu_physics, name, data["initial"])
+    s1, r1 = run_gpu(case_physics(request, name), name, data["initial"])
     same, close = check(name, s1, r1, data["final"], data["results"])
     n = len(close)
     _golden_tally[name] = (int(close.sum()), n)

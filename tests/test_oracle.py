@@ -14,7 +14,8 @@ import numpy as np
 import pytest
 
 from cases import CASES, has_locals, make_states
-from conftest import GOLDEN, compare, oracle_config, oracle_geometry
+from conftest import (GOLDEN, case_oracle, compare, oracle_config,
+                      oracle_geometry)
 
 RANGE, PROPER_TIME, KINETIC, STOPPING, STRAGGLING = 0, 1, 2, 3, 4
 CSDA, MIXED = 0, 1
@@ -75,9 +76,10 @@ def test_philox_oracle_matches_numpy(port):
 
 
 @pytest.mark.parametrize("name", sorted(CASES))
-def test_port_matches_golden(port, name):
+def test_port_matches_golden(request, name):
     if has_locals(name):
         pytest.skip("the C restatement covers uniform media only")
+    port = case_oracle(request, name, "port")
     data = np.load(os.path.join(GOLDEN, name + ".npz"))
     case = CASES[name]
     s0 = data["initial"]
@@ -114,9 +116,11 @@ def test_reference_reproduces_locals_golden(reference, name):
 
 
 @pytest.mark.parametrize("name", sorted(CASES))
-def test_port_matches_reference_fresh_events(port, reference, name):
+def test_port_matches_reference_fresh_events(request, reference, name):
     if has_locals(name):
         pytest.skip("the C restatement covers uniform media only")
+    port = case_oracle(request, name, "port")
+    reference = case_oracle(request, name, "reference")
     case = CASES[name]
     s0 = make_states(name, n=64, first_event=100000)
     geo_p = oracle_geometry(port, case["geometry"])
