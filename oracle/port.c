@@ -18,9 +18,12 @@
  * (pumas.c:2167-2196), whose layout mirrors `struct pumas_physics`
  * (pumas.c:660-806) on an LP64 little-endian host.
  *
- * Not restated (not on the configured path): magnetic fields
- * (pumas.c:4968-5171, 6352-6382, 6833-6911), non-uniform locals with a step
- * limit, the recorder, tau specific tables, non-default DCS models.
+ * Media with local properties (density profiles and uniform fields of
+ * struct gpumas_locals) follow transport_set_locals (pumas.c:5528-5552),
+ * the magnetic steps (pumas.c:6352-6382, 6833-6911) and the closed form
+ * CSDA deflection (pumas.c:4968-5171). Muon and tau dumps both load.
+ *
+ * Not restated: the recorder, non-default DCS models.
  */
 #include <float.h>
 #include <math.h>
@@ -32,6 +35,7 @@
 #include <omp.h>
 #endif
 
+#include "gp_math.cuh"
 #include "oracle.h"
 #include "philox.h"
 
@@ -52,6 +56,7 @@
 #define PION_MASS 0.13957018
 #define AVOGADRO_NUMBER 6.02214076E+23
 #define PI_ 3.14159265358979323846
+#define LARMOR_FACTOR 0.299792458
 
 #define MODE_DISABLED -1
 #define MODE_CSDA 0
@@ -117,6 +122,7 @@ struct port_physics {
         const float *DCS, *DCS_x, *DCS_env;
         const double *Xt, *Kt, *a_max, *b_max, *Mu0, *Mu0_dK, *Lb, *Lb_dK;
         const double *Ms1, *Ms1_dK;
+        const double * Li;
         const int * elements_in;
         const double * material_density;
         struct port_element * element;
@@ -224,6 +230,7 @@ int oracle_port_load(const void * dump, int64_t size)
         p->DCS_env = F(28);
         p->Xt = D(29);
         p->Kt = D(30);
+        p->Li = D(31);
         p->a_max = D(33);
         p->b_max = D(34);
         p->Mu0 = D(35);
@@ -590,6 +597,10 @@ struct port_ctx {
         int randn_done;
         double randn_next;
         int steps;
+        /* Field of the current medium (struct medium_locals,
+         * pumas.c:396-403). */
+        double magnet[3];
+        int magnetized;
 };
 
 static inline double rnd(struct port_ctx * c)
@@ -627,12 +638,168 @@ static inline int medium_material(const struct port_ctx * c, int medium)
         return c->geometry->media[medium].material;
 }
 
+/* transport_set_locals (pumas.c:5528-5552) with the locals callback of the
+ * media's descriptors (struct gpumas_locals), evaluated as the reference
+ * harness's callback does: sets *density and the field, returns the step
+ * limit (0 for a uniform medium). */
+static double set_locals(struct port_ctx * c, int medium,
+    const struct oracle_state * s, double * density)
+{
+        const struct gpumas_locals * l = c->geometry->locals;
+        c->magnet[0] = c->magnet[1] = c->magnet[2] = 0.;
+        c->magnetized = 0;
+        if (l == NULL) {
+                *density = medium_density(c, medium);
+                return 0.;
+        }
+        l += medium;
+        double size = 0.;
+        *density = c->geometry->media[medium].density;
+        if (l->model == GPUMAS_DENSITY_EXPONENTIAL) {
+                *density = l->rho0 * gp_exp(gpumas_locals_exponent(l,
+                                         s->position));
+                size = gpumas_locals_size(l, s->direction);
+        }
+        if (*density <= 0.)
+                *density = ph->material_density[medium_material(c, medium)];
+        memcpy(c->magnet, l->magnet, sizeof(c->magnet));
+        c->magnetized = ((l->magnet[0] != 0.) || (l->magnet[1] != 0.) ||
+                            (l->magnet[2] != 0.)) ? 1 : 0;
+        return size * c->cfg->accuracy;
+}
+
 /* ------------------------------------------------------------------------ */
 /* Deterministic CSDA transport in an infinite uniform medium               */
 /* (transport_with_csda, pumas.c:4777-4949; no magnetic field).             */
 /* ------------------------------------------------------------------------ */
+/* cel_magnetic_rotation (pumas.c:3849-3883). */
+static double cel_magnetic_rotation(int material, double kinetic)
+{
+        const int imax = ph->n_energies - 1;
+        const double factor = LARMOR_FACTOR / ph->mass;
+        const double * T = ph->T + ROW(0, material);
+        if (kinetic <= ph->K[0]) return T[imax] * factor;
+        if (kinetic >= ph->K[imax]) return 0.;
+        const double t = interpolate(ph->K, T, ph->T_dK + ROW(0, material),
+            kinetic);
+        return (T[imax] - t) * factor;
+}
+
+/* csda_magnetic_transport (pumas.c:5095-5171), with the reference's
+ * polynomial fits of cos and sin. */
+static int csda_magnetic_transport(int material, double density,
+    double magnet, double charge, double kinetic, double phase, double * x,
+    double * y, double * z)
+{
+        const int imax = ph->n_energies - 1;
+        double k0 = kinetic;
+        int i1, i2;
+        if (kinetic <= ph->K[0]) {
+                k0 = ph->K[0];
+                i1 = 0;
+                i2 = 1;
+        } else if (kinetic >= ph->K[imax]) {
+                *y = 0.0;
+                *x = *z = -(cel_grammage(MODE_CSDA, material, kinetic) -
+                    ph->X[ROW(0, material) + imax]);
+                return RC_SUCCESS;
+        } else {
+                i1 = table_index(ph->K, k0);
+                i2 = i1 + 1;
+        }
+        static const double poly_x[8] = { 1.000000000e+000, 0.000000000e+000,
+                -5.000000000e-001, -1.048969541e-002, 5.597396438e-002,
+                -6.401353612e-003, -4.495849930e-004, 6.583532135e-005 };
+        static const double poly_y[8] = { 0.000000000e+000, 1.000000000e+000,
+                -1.400755143e-002, -1.350173383e-001, -2.838778336e-002,
+                2.123237056e-002, -3.094290091e-003, 1.409012754e-004 };
+        if (fabs(phase) > 2.0 * PI_) return RC_VALUE_ERROR;
+        const double * L = ph->Li + (long)material * 8 * ph->n_energies;
+        const double a = -magnet * charge / density;
+        double x1 = 0., x2 = 0., y1 = 0., y2 = 0., u = 1.;
+        int j;
+        for (j = 0; j < 8; j++) {
+                const double l1 = L[j * ph->n_energies + i1];
+                const double l2 = L[j * ph->n_energies + i2];
+                x1 += u * poly_x[j] * l1;
+                y1 += u * poly_y[j] * l1;
+                x2 += u * poly_x[j] * l2;
+                y2 += u * poly_y[j] * l2;
+                u *= a;
+        }
+        const double z1 = L[i1], z2 = L[i2];
+        const double h = (k0 - ph->K[i1]) / (ph->K[i2] - ph->K[i1]);
+        *x = (x1 + h * (x2 - x1)) / density;
+        *y = (y1 + h * (y2 - y1)) / density;
+        *z = (z1 + h * (z2 - z1)) / density;
+        return RC_SUCCESS;
+}
+
+/* transport_csda_deflect (pumas.c:4968-5075). */
+static int csda_deflect(struct port_ctx * c, struct oracle_state * state,
+    int material, double density, double ki, double distance)
+{
+        const double charge = state->charge;
+        const double kf = state->energy;
+        double * const position = state->position;
+        double * const direction = state->direction;
+        const double * const m = c->magnet;
+        const double b0 = sqrt(m[0] * m[0] + m[1] * m[1] + m[2] * m[2]);
+        const double b0_i = 1.0 / b0;
+        double ex[3], ey[3], ez[3];
+        ey[0] = (direction[2] * m[1] - direction[1] * m[2]) * b0_i;
+        ey[1] = (direction[0] * m[2] - direction[2] * m[0]) * b0_i;
+        ey[2] = (direction[1] * m[0] - direction[0] * m[1]) * b0_i;
+        const double d = b0_i * b0_i * (m[0] * direction[0] +
+                                           m[1] * direction[1] +
+                                           m[2] * direction[2]);
+        int k;
+        for (k = 0; k < 3; k++) {
+                ez[k] = m[k] * d;
+                ex[k] = direction[k] - ez[k];
+        }
+        const double a = -b0 * charge / density;
+        const double pi = a * cel_magnetic_rotation(material, ki);
+        const double pf = a * cel_magnetic_rotation(material, kf);
+        const double dp = pf - pi;
+        const double ps = fabs(pi + pf);
+        if (ps == 0.) return RC_SUCCESS;
+        const double dp0 = fabs(dp);
+        double dx, dy, dz;
+        if ((dp0 < 1E-02) && (dp0 / ps < 1E-02)) {
+                dz = (ki >= kf) ? distance : -distance;
+                const double sixth = 1 / 6.0;
+                dx = dz * (1.0 - sixth * dp * dp);
+                dy = 0.5 * dz * dp;
+        } else {
+                double xi, yi, zi, xf, yf, zf;
+                int rc = csda_magnetic_transport(material, density, b0, charge,
+                    ki, pi, &xi, &yi, &zi);
+                if (rc != RC_SUCCESS) return rc;
+                rc = csda_magnetic_transport(material, density, b0, charge, kf,
+                    pf, &xf, &yf, &zf);
+                if (rc != RC_SUCCESS) return rc;
+                const double si = sin(pi);
+                const double ci = cos(pi);
+                xf -= xi;
+                yf -= yi;
+                dx = ci * xf + si * yf;
+                dy = -si * xf + ci * yf;
+                dz = zf - zi;
+        }
+        for (k = 0; k < 3; k++)
+                position[k] += dx * ex[k] + dy * ey[k] + dz * ez[k];
+        const double sn = sin(dp);
+        const double cs = cos(dp);
+        for (k = 0; k < 3; k++)
+                direction[k] = cs * ex[k] + sn * ey[k] + ez[k];
+        return RC_SUCCESS;
+}
+
+/* transport_with_csda (pumas.c:4777-4949): with a field, the closed form
+ * deflection; *status gets its return code. */
 static int transport_with_csda(struct port_ctx * c, struct oracle_state * state,
-    int material, double density)
+    int material, double density, int * status)
 {
         const struct oracle_config * cfg = c->cfg;
         const double ki = state->energy;
@@ -757,6 +924,11 @@ static int transport_with_csda(struct port_ctx * c, struct oracle_state * state,
         if (cfg->decay == MODE_WEIGHTED)
                 state->weight *= exp(-fabs(ti - state->time) / ph->ctau);
 
+        if (c->magnetized) {
+                *status = csda_deflect(c, state, material, density, ki,
+                    distance);
+                return event;
+        }
         const double path =
             (cfg->direction == MODE_FORWARD) ? distance : -distance;
         state->position[0] += path * state->direction[0];
@@ -2735,7 +2907,8 @@ static void transport_limit(struct port_ctx * c,
  * uniform locals. Returns the end step medium index in *out_medium. */
 static int step_transport(struct port_ctx * c, struct oracle_state * state,
     int straight, int medium, double density, double grammage_max,
-    double step_max_medium, int * out_medium)
+    double step_max_medium, double * step_max_locals, double * density_end,
+    int * out_medium)
 {
         const struct oracle_config * cfg = c->cfg;
         const int scheme = cfg->energy_loss;
@@ -2750,6 +2923,7 @@ static int step_transport(struct port_ctx * c, struct oracle_state * state,
 
         double step_loc;
         double invlb1 = 0.;
+        double rLarmor0 = 0., uT0[3] = { 0., 0., 0. };
         if (!straight) {
                 double r = cfg->accuracy;
                 const double k_threshold = 1E+09;
@@ -2771,6 +2945,27 @@ static int step_transport(struct port_ctx * c, struct oracle_state * state,
                         const double stepT = cfg->accuracy / invlb1;
                         if (stepT < step_loc) step_loc = stepT;
                 }
+                /* Larmor radius and deflection direction
+                 * (pumas.c:6352-6382). */
+                if (c->magnetized) {
+                        const double * const B = c->magnet;
+                        uT0[0] = direction[1] * B[2] - direction[2] * B[1];
+                        uT0[1] = direction[2] * B[0] - direction[0] * B[2];
+                        uT0[2] = direction[0] * B[1] - direction[1] * B[0];
+                        const double BT = sqrt(uT0[0] * uT0[0] +
+                            uT0[1] * uT0[1] + uT0[2] * uT0[2]);
+                        if (BT != 0.) {
+                                rLarmor0 = momentum / (BT * LARMOR_FACTOR);
+                                const double pinv = 1. / momentum;
+                                uT0[0] *= pinv;
+                                uT0[1] *= pinv;
+                                uT0[2] *= pinv;
+                        }
+                }
+                if (rLarmor0 > 0.) {
+                        const double stepM = cfg->accuracy * rLarmor0;
+                        if (stepM < step_loc) step_loc = stepM;
+                }
         } else {
                 if (grammage_max <= 0.)
                         step_loc = 1E+09 * density_i;
@@ -2783,6 +2978,8 @@ static int step_transport(struct port_ctx * c, struct oracle_state * state,
         double step = (step_max_medium <= 0) ?
             step_loc :
             (step_max_medium < step_loc ? step_max_medium : step_loc);
+        if ((*step_max_locals > 0.) && (step > *step_max_locals))
+                step = *step_max_locals;
 
         *out_medium = medium;
         int event = EV_NONE;
@@ -2840,14 +3037,22 @@ static int step_transport(struct port_ctx * c, struct oracle_state * state,
                 event = EV_MEDIUM;
                 *out_medium = end_medium;
         }
+
+        /* End step locals (pumas.c:6488-6503), at the last point inside
+         * the medium when the step crosses a boundary. */
+        double Bi[3] = { 0., 0., 0. };
+        if (c->magnetized) memcpy(Bi, c->magnet, sizeof(Bi));
+        double density1 = density;
+        if (*step_max_locals > 0.) {
+                *step_max_locals = set_locals(c, medium, state, &density1);
+                if (density1 <= 0.) return RC_DENSITY_ERROR;
+        }
         if (event & EV_MEDIUM) {
                 position[0] = end_position[0];
                 position[1] = end_position[1];
                 position[2] = end_position[2];
         }
 
-        /* Uniform locals: the end step density is the start one. */
-        const double density1 = density;
         double k1 = state->energy, dk = 0.;
         const double dX = 0.5 * step * (density + density1);
         if ((scheme >= MODE_CSDA) && (scheme <= MODE_MIXED)) {
@@ -2976,16 +3181,18 @@ static int step_transport(struct port_ctx * c, struct oracle_state * state,
         const double Xi = state->grammage;
         state->grammage += dX;
         const double sf0 = step;
+        double h_int = 0.;
         if ((grammage_max > 0.) && (state->grammage >= grammage_max)) {
                 const double dX_ = grammage_max - Xi;
                 if ((fabs(density - density1) <= FLT_EPSILON) ||
                     (sf0 <= FLT_EPSILON)) {
                         step = dX_ * density_i;
+                        h_int = dX_ / (state->grammage - Xi);
                 } else {
                         const double drho = density1 - density;
                         double tmp = density * density + 2. * dX_ * drho / sf0;
                         tmp = (tmp > FLT_EPSILON) ? sqrt(tmp) : 0;
-                        const double h_int = (tmp - density) / drho;
+                        h_int = (tmp - density) / drho;
                         step *= h_int;
                 }
                 state->grammage = grammage_max;
@@ -3102,6 +3309,67 @@ static int step_transport(struct port_ctx * c, struct oracle_state * state,
                         c->step_invlb1 = density1 * invlb1_;
                 }
         }
+        *density_end = density1;
+
+        /* End point field and magnetic deflection (pumas.c:6833-6911). */
+        double rLarmor1 = 0., uT1[3] = { 0., 0., 0. };
+        if (c->magnetized) {
+                double B[3] = { c->magnet[0], c->magnet[1], c->magnet[2] };
+                int magnetized = c->magnetized;
+                if (h_int > 0.) {
+                        B[0] = Bi[0] + h_int * (B[0] - Bi[0]);
+                        B[1] = Bi[1] + h_int * (B[1] - Bi[1]);
+                        B[2] = Bi[2] + h_int * (B[2] - Bi[2]);
+                        magnetized =
+                            (B[0] * B[0] + B[1] * B[1] + B[2] * B[2] == 0.);
+                }
+                if (magnetized != 0) {
+                        uT1[0] = direction[1] * B[2] - direction[2] * B[1];
+                        uT1[1] = direction[2] * B[0] - direction[0] * B[2];
+                        uT1[2] = direction[0] * B[1] - direction[1] * B[0];
+                        const double BT = sqrt(uT1[0] * uT1[0] +
+                            uT1[1] * uT1[1] + uT1[2] * uT1[2]);
+                        if (BT != 0.) {
+                                const double p = (state->energy <= 0) ?
+                                    momentum :
+                                    sqrt(state->energy *
+                                        (state->energy + 2. * ph->mass));
+                                rLarmor1 = p / (BT * LARMOR_FACTOR);
+                                const double pinv = 1. / p;
+                                uT1[0] *= pinv;
+                                uT1[1] *= pinv;
+                                uT1[2] *= pinv;
+                        }
+                }
+        }
+        if ((rLarmor0 > 0.) || (rLarmor1 > 0.)) {
+                const double u[3] = { direction[0], direction[1],
+                        direction[2] };
+                const double theta0 =
+                    (rLarmor0 > 0.) ? state->charge * step / rLarmor0 : 0.;
+                const double theta1 =
+                    (rLarmor1 > 0.) ? state->charge * step / rLarmor1 : 0.;
+                double theta = 0.5 * (theta0 + theta1);
+                if (cfg->direction == MODE_BACKWARD) theta = -theta;
+                double cs = cos(theta);
+                double sn = sin(theta);
+                double v[3];
+                int i;
+                for (i = 0; i < 3; i++) v[i] = 0.5 * (uT0[i] + uT1[i]);
+                double nrmv = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+                if (nrmv > 0.) {
+                        nrmv = 1. / sqrt(nrmv);
+                        for (i = 0; i < 3; i++) v[i] *= nrmv;
+                } else {
+                        cs = 1.;
+                        sn = 0.;
+                }
+                for (i = 0; i < 3; i++) direction[i] = cs * u[i] + sn * v[i];
+                const double norm = 1. / sqrt(direction[0] * direction[0] +
+                                             direction[1] * direction[1] +
+                                             direction[2] * direction[2]);
+                for (i = 0; i < 3; i++) direction[i] *= norm;
+        }
 
         if ((invlb1 > 0.) || (c->step_invlb1 > 0.)) {
                 double ilb1 = 0.25 * step * (invlb1 + c->step_invlb1);
@@ -3119,14 +3387,15 @@ static int step_transport(struct port_ctx * c, struct oracle_state * state,
  * recorder. Returns the end event and updates *medium_ptr. */
 static int transport_with_stepping(struct port_ctx * c,
     struct oracle_state * state, int * medium_ptr, double density,
-    double step_max_medium, int * status)
+    double step_max_medium, double step_max_locals, int * status)
 {
         const struct oracle_config * cfg = c->cfg;
         int medium = *medium_ptr;
         int material = medium_material(c, medium);
         const int scheme = cfg->energy_loss;
         int straight = ((cfg->scattering == MODE_DISABLED) &&
-                           (scheme <= MODE_MIXED)) ? 1 : 0;
+                           (scheme <= MODE_MIXED) &&
+                           (step_max_locals <= 0.) && !c->magnetized) ? 1 : 0;
         c->step_event = EV_NONE;
         double ti = state->time;
         double wi = state->weight;
@@ -3169,8 +3438,13 @@ static int transport_with_stepping(struct port_ctx * c,
                                 step_max_medium += 0.5 * STEP_MIN;
                 }
                 int new_medium = -1;
-                step_transport(c, state, straight, medium, density,
-                    grammage_max, step_max_medium, &new_medium);
+                const int rc = step_transport(c, state, straight, medium,
+                    density, grammage_max, step_max_medium, &step_max_locals,
+                    &density, &new_medium);
+                if (rc != RC_SUCCESS) {
+                        *status = rc;
+                        return c->step_event;
+                }
                 step_index++;
                 if (!c->step_event) continue;
 
@@ -3205,13 +3479,28 @@ static int transport_with_stepping(struct port_ctx * c,
                                 transport_do_ehs(c, state, material);
                                 if (cfg->event & c->step_event) break;
                         }
+                        /* Locals update (pumas.c:5403-5414). */
+                        if (step_max_locals > 0.) {
+                                step_max_locals =
+                                    set_locals(c, medium, state, &density);
+                                if (density <= 0.) {
+                                        *status = RC_DENSITY_ERROR;
+                                        return c->step_event;
+                                }
+                        }
                 } else if (c->step_event & EV_MEDIUM) {
                         medium = new_medium;
                         if ((medium < 0) || (cfg->event & EV_MEDIUM)) break;
                         material = medium_material(c, medium);
-                        density = medium_density(c, medium);
+                        step_max_locals = set_locals(c, medium, state, &density);
+                        if (density <= 0.) {
+                                *status = RC_DENSITY_ERROR;
+                                return c->step_event;
+                        }
                         straight = ((cfg->scattering == MODE_DISABLED) &&
-                                       (scheme <= MODE_MIXED)) ? 1 : 0;
+                                       (scheme <= MODE_MIXED) &&
+                                       (step_max_locals <= 0.) &&
+                                       !c->magnetized) ? 1 : 0;
                         const int tmp_scheme =
                             scheme > MODE_DISABLED ? scheme : MODE_CSDA;
                         c->step_X_limit = (cfg->event & EV_LIMIT_ENERGY) ?
@@ -3283,7 +3572,10 @@ static int context_transport(struct port_ctx * c, struct oracle_state * state,
                 return RC_SUCCESS;
         } else if (step_max_medium > 0.)
                 step_max_medium += 0.5 * STEP_MIN;
-        const double density = medium_density(c, medium);
+        double density;
+        const double step_max_locals = set_locals(c, medium, state, &density);
+        if ((step_max_locals > 0.) && (step_max_locals < step_max_medium))
+                step_max_medium = step_max_locals;
         if (density <= 0.) return RC_DENSITY_ERROR;
 
         if (cfg->decay == MODE_RANDOMISED) {
@@ -3293,7 +3585,8 @@ static int context_transport(struct port_ctx * c, struct oracle_state * state,
 
         int do_stepping = 1;
         int e = EV_NONE, status = RC_SUCCESS;
-        if ((step_max_medium <= 0.) && (cfg->energy_loss <= MODE_CSDA)) {
+        if ((step_max_medium <= 0.) && (step_max_locals <= 0.) &&
+            (cfg->energy_loss <= MODE_CSDA)) {
                 if ((cfg->energy_loss == MODE_DISABLED) &&
                     ((cfg->event & EV_LIMIT) == 0)) {
                         return RC_MISSING_LIMIT;
@@ -3303,11 +3596,11 @@ static int context_transport(struct port_ctx * c, struct oracle_state * state,
                 }
         }
         if (do_stepping) {
-                e = transport_with_stepping(
-                    c, state, &medium, density, step_max_medium, &status);
+                e = transport_with_stepping(c, state, &medium, density,
+                    step_max_medium, step_max_locals, &status);
         } else {
                 e = transport_with_csda(
-                    c, state, medium_material(c, medium), density);
+                    c, state, medium_material(c, medium), density, &status);
         }
         *event = e;
         media[1] = medium;

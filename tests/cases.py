@@ -246,8 +246,8 @@ def particle(name):
 
 
 def has_locals(name):
-    """Whether a case's media have local properties, which the C
-    restatement does not cover (its oracle is the reference itself)."""
+    """Whether a case's media have local properties (density profiles,
+    magnetic fields)."""
     return CASES[name]["geometry"].get("locals") is not None
 
 

@@ -77,8 +77,6 @@ def test_philox_oracle_matches_numpy(port):
 
 @pytest.mark.parametrize("name", sorted(CASES))
 def test_port_matches_golden(request, name):
-    if has_locals(name):
-        pytest.skip("the C restatement covers uniform media only")
     port = case_oracle(request, name, "port")
     data = np.load(os.path.join(GOLDEN, name + ".npz"))
     case = CASES[name]
@@ -117,8 +115,6 @@ def test_reference_reproduces_locals_golden(reference, name):
 
 @pytest.mark.parametrize("name", sorted(CASES))
 def test_port_matches_reference_fresh_events(request, reference, name):
-    if has_locals(name):
-        pytest.skip("the C restatement covers uniform media only")
     port = case_oracle(request, name, "port")
     reference = case_oracle(request, name, "reference")
     case = CASES[name]
