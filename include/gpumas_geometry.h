@@ -66,7 +66,8 @@ enum gpumas_geometry_kind {
  * uniform density override in kg/m^3. A null or negative density selects the
  * material's default density. This is the device form of `struct
  * pumas_medium` (pumas.h:363-376) with a locals callback that returns a
- * constant density, no magnetic field and no step limit (pumas.c:5528-5552).
+ * constant density, no magnetic field and no step limit (pumas.c:5528-5552);
+ * density profiles and fields are given by struct gpumas_locals.
  */
 struct gpumas_medium {
         int material;

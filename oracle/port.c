@@ -669,8 +669,9 @@ static double set_locals(struct port_ctx * c, int medium,
 }
 
 /* ------------------------------------------------------------------------ */
-/* Deterministic CSDA transport in an infinite uniform medium               */
-/* (transport_with_csda, pumas.c:4777-4949; no magnetic field).             */
+/* Deterministic CSDA transport in an infinite uniform medium, with the     */
+/* closed form deflection of a uniform field (pumas.c:3849-3883,            */
+/* 4777-5171).                                                              */
 /* ------------------------------------------------------------------------ */
 /* cel_magnetic_rotation (pumas.c:3849-3883). */
 static double cel_magnetic_rotation(int material, double kinetic)
