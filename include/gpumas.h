@@ -232,6 +232,28 @@ int gpumas_context_create(struct gpumas_context ** context,
 /** Destroy a context and its device buffers (pumas_context_destroy, pumas.h:1326). */
 void gpumas_context_destroy(struct gpumas_context ** context);
 
+/** Set the key of the context's random stream
+ * (pumas_context_random_seed_set, pumas.h:1240-1241). With a NULL seed the
+ * key is drawn from the OS random stream (/dev/urandom), whose failure
+ * returns GPUMAS_RETURN_PATH_ERROR. A new context has the key 0. */
+int gpumas_context_random_seed_set(
+    struct gpumas_context * context, const uint64_t * seed);
+
+/** Get the key of the context's random stream
+ * (pumas_context_random_seed_get, pumas.h:1265-1266). */
+int gpumas_context_random_seed_get(
+    const struct gpumas_context * context, uint64_t * seed);
+
+/** The physics of a context (pumas_context_physics_get, pumas.h:1337). */
+const struct gpumas_physics * gpumas_context_physics_get(
+    const struct gpumas_context * context);
+
+/** Minimum kinetic transfer of DELs, relative (pumas_physics_cutoff,
+ * pumas.h:993), and elastic ratio (pumas_physics_elastic_ratio,
+ * pumas.h:1005); 0 for a NULL physics. */
+double gpumas_physics_cutoff(const struct gpumas_physics * physics);
+double gpumas_physics_elastic_ratio(const struct gpumas_physics * physics);
+
 /**
  * Set the geometry (replaces the `medium` callback). The descriptor and its
  * arrays are copied to the device; media materials are checked against the

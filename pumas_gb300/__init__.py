@@ -387,6 +387,18 @@ class Context:
     seed = property(lambda self: self._c.seed,
                     lambda self, v: setattr(self._c, "seed", int(v)))
 
+    def random_seed_set(self, seed=None):
+        """Set the random stream's key (pumas_context_random_seed_set); with
+        None, a key drawn from the OS random stream. Returns the key."""
+        lib = self._lib
+        f = lib.gpumas_context_random_seed_set
+        f.restype = ctypes.c_int
+        f.argtypes = [ctypes.POINTER(_Context),
+                      ctypes.POINTER(ctypes.c_uint64)]
+        key = None if seed is None else ctypes.byref(ctypes.c_uint64(seed))
+        _check(f(self._ptr, key), "gpumas_context_random_seed_set")
+        return self.seed
+
     def set_geometry(self, geometry):
         _check(self._lib.gpumas_context_geometry_set(
             self._ptr, ctypes.byref(geometry.c)),

@@ -721,6 +721,17 @@ extern "C" int gpumas_physics_info(const struct gpumas_physics * physics,
         return GPUMAS_RETURN_SUCCESS;
 }
 
+extern "C" double gpumas_physics_cutoff(const struct gpumas_physics * physics)
+{
+        return (physics == NULL) ? 0. : physics->tables.cutoff;
+}
+
+extern "C" double gpumas_physics_elastic_ratio(
+    const struct gpumas_physics * physics)
+{
+        return (physics == NULL) ? 0. : physics->tables.elastic_ratio;
+}
+
 extern "C" int gpumas_physics_particle(const struct gpumas_physics * physics,
     int * particle, double * lifetime, double * mass)
 {

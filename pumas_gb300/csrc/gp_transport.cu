@@ -10,6 +10,7 @@
  * done on the device and reported in the per event status.
  */
 #include <cuda_runtime.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -140,6 +141,40 @@ extern "C" int gpumas_context_create(struct gpumas_context ** context,
         }
         *context = &c->api;
         return GPUMAS_RETURN_SUCCESS;
+}
+
+extern "C" int gpumas_context_random_seed_set(
+    struct gpumas_context * context, const uint64_t * seed)
+{
+        if (context == NULL) return GPUMAS_RETURN_VALUE_ERROR;
+        if (seed != NULL) {
+                context->seed = *seed;
+                return GPUMAS_RETURN_SUCCESS;
+        }
+        FILE * stream = fopen("/dev/urandom", "rb");
+        if (stream == NULL) return GPUMAS_RETURN_PATH_ERROR;
+        uint64_t s;
+        const size_t n = fread(&s, sizeof(s), 1, stream);
+        fclose(stream);
+        if (n != 1) return GPUMAS_RETURN_PATH_ERROR;
+        context->seed = s;
+        return GPUMAS_RETURN_SUCCESS;
+}
+
+extern "C" int gpumas_context_random_seed_get(
+    const struct gpumas_context * context, uint64_t * seed)
+{
+        if ((context == NULL) || (seed == NULL))
+                return GPUMAS_RETURN_VALUE_ERROR;
+        *seed = context->seed;
+        return GPUMAS_RETURN_SUCCESS;
+}
+
+extern "C" const struct gpumas_physics * gpumas_context_physics_get(
+    const struct gpumas_context * context)
+{
+        if (context == NULL) return NULL;
+        return ((const gp_context *)context)->physics;
 }
 
 extern "C" void gpumas_context_destroy(struct gpumas_context ** context)

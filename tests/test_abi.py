@@ -55,3 +55,37 @@ def test_no_product_import_of_oracle():
                 assert "import oracle" not in text
                 assert "oracle/" not in text
                 assert "liboracle" not in text
+
+
+def test_random_seed_set_get():
+    """pumas_context_random_seed_set / _get semantics on the public context
+    record (no device needed): a given key is kept, NULL draws one from the
+    OS."""
+    import ctypes
+    import pumas_gb300 as pg
+    lib = pg.library()
+    ctx = pg._Context()
+    u64 = ctypes.c_uint64
+    lib.gpumas_context_random_seed_set.restype = ctypes.c_int
+    lib.gpumas_context_random_seed_set.argtypes = [
+        ctypes.POINTER(pg._Context), ctypes.POINTER(u64)]
+    lib.gpumas_context_random_seed_get.restype = ctypes.c_int
+    lib.gpumas_context_random_seed_get.argtypes = [
+        ctypes.POINTER(pg._Context), ctypes.POINTER(u64)]
+    assert lib.gpumas_context_random_seed_set(
+        ctypes.byref(ctx), ctypes.byref(u64(0x0123456789ABCDEF))) == 0
+    got = u64()
+    assert lib.gpumas_context_random_seed_get(
+        ctypes.byref(ctx), ctypes.byref(got)) == 0
+    assert got.value == 0x0123456789ABCDEF == ctx.seed
+    draws = set()
+    for _ in range(3):
+        assert lib.gpumas_context_random_seed_set(ctypes.byref(ctx),
+                                                  None) == 0
+        draws.add(ctx.seed)
+    assert len(draws) == 3
+    assert lib.gpumas_context_random_seed_get(None, ctypes.byref(got)) == \
+        pg.RETURN_VALUE_ERROR
+    lib.gpumas_physics_cutoff.restype = ctypes.c_double
+    lib.gpumas_physics_cutoff.argtypes = [ctypes.c_void_p]
+    assert lib.gpumas_physics_cutoff(None) == 0.
