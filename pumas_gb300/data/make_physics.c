@@ -9,7 +9,12 @@
  * dump that is shipped as package data, so that machines without the
  * reference can still load the tables.
  *
- * usage: make_physics <materials.xml> <dedx directory> <output dump> [tau]
+ * usage: make_physics <materials.xml> <dedx directory> <output dump>
+ *            [muon|tau [<bremsstrahlung> <pair production> <photonuclear>]]
+ *
+ * The optional model names select the DCS models of
+ * struct pumas_physics_settings (pumas.h:721-815); the default is SSR, SSR,
+ * DRSS.
  */
 #include <stdio.h>
 #include <stdlib.h>
@@ -27,8 +32,14 @@ int main(int argc, char * argv[])
         const enum pumas_particle particle =
             ((argc > 4) && (strcmp(argv[4], "tau") == 0)) ?
             PUMAS_PARTICLE_TAU : PUMAS_PARTICLE_MUON;
-        if (pumas_physics_create(&physics, particle, argv[1], argv[2], NULL) !=
-            PUMAS_RETURN_SUCCESS)
+        struct pumas_physics_settings settings = { 0 };
+        if (argc > 7) {
+                settings.bremsstrahlung = argv[5];
+                settings.pair_production = argv[6];
+                settings.photonuclear = argv[7];
+        }
+        if (pumas_physics_create(&physics, particle, argv[1], argv[2],
+                &settings) != PUMAS_RETURN_SUCCESS)
                 return EXIT_FAILURE;
         FILE * stream = fopen(argv[3], "wb");
         if (stream == NULL) return EXIT_FAILURE;
