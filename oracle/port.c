@@ -23,7 +23,9 @@
  * the magnetic steps (pumas.c:6352-6382, 6833-6911) and the closed form
  * CSDA deflection (pumas.c:4968-5171). Muon and tau dumps both load.
  *
- * Not restated: the recorder, non-default DCS models.
+ * DCS models: bremsstrahlung SSR, KKP, ABB; pair production SSR, KKP;
+ * photonuclear DRSS (pumas.h:742-771). Not restated: the recorder, the BM
+ * and BBKS photonuclear models.
  */
 #include <float.h>
 #include <math.h>
@@ -114,6 +116,9 @@ struct port_physics {
         char * blob;
         int n_energies, n_materials, n_composites, n_elements, n_components;
         int max_components, n_table_dcs, particle;
+        /* DCS models: bremsstrahlung 0 SSR, 1 KKP, 2 ABB; pair production
+         * 0 SSR, 1 KKP (the names of the dump, pumas.c:2167-2196). */
+        int model_brems, model_pair;
         double ctau, mass, cutoff, elastic_ratio;
         const double *K, *K_dX, *K_dNI_in, *K_dNI_el;
         const double *X, *X_dK, *X_dT, *T, *T_dK, *dE, *dE_dK;
@@ -274,9 +279,15 @@ int oracle_port_load(const void * dump, int64_t size)
         const uint64_t * nptr = (const uint64_t *)(b + off[49]);
         for (i = 0; i < p->n_materials; i++)
                 p->material_name[i] = b + (int64_t)(nptr[i] - base) + 528;
-        /* Only the default DCS models are restated. */
-        if ((strcmp(b + off[50], "SSR") != 0) ||
-            (strcmp(b + off[51], "SSR") != 0) ||
+        /* The restated DCS models. */
+        const char * brems = b + off[50];
+        const char * pair = b + off[51];
+        p->model_brems = (strcmp(brems, "SSR") == 0) ? 0 :
+            (strcmp(brems, "KKP") == 0) ? 1 :
+            (strcmp(brems, "ABB") == 0) ? 2 : -1;
+        p->model_pair = (strcmp(pair, "SSR") == 0) ? 0 :
+            (strcmp(pair, "KKP") == 0) ? 1 : -1;
+        if ((p->model_brems < 0) || (p->model_pair < 0) ||
             (strcmp(b + off[52], "DRSS") != 0) ||
             ((p->particle != 0) && (p->particle != 1))) {
                 port_free(p);
@@ -1749,6 +1760,207 @@ static double dcs_pair_production_SSR(
         return (I < 0) ? 0. : I;
 }
 
+/* ------------------------------------------------------------------------ */
+/* Other DCS models of struct pumas_physics_settings (pumas.h:742-771).      */
+/* ------------------------------------------------------------------------ */
+
+/* dcs_bremsstrahlung_KKP (pumas.c:13759-13810). */
+static double dcs_bremsstrahlung_KKP(
+    double Z, double A, double mu, double K, double q)
+{
+        if ((Z <= 0) || (A <= 0) || (mu <= 0) || (K <= 0) || (q <= 0))
+                return 0.;
+        const double Z13 = pow(Z, 1. / 3.);
+        const double sqrte = 1.648721271;
+        if (q >= K + mu * (1. - 0.75 * sqrte * Z13)) return 0.;
+        const double me = ELECTRON_MASS;
+        const double phie_factor = mu / (me * me * sqrte);
+        const double rem = 5.63588E-13 * me / mu;
+        const double BZ_n = radiation_logarithm(Z) / Z13;
+        const double BZ_e = (Z == 1.) ? 446. : 1429. / (Z13 * Z13);
+        const double D_n = 1.54 * pow(A, 0.27);
+        const double E = K + mu;
+        const double dcs_factor = 7.297182E-07 * rem * rem * Z / E;
+        const double delta_factor = 0.5 * mu * mu / E;
+        const double qe_max = E / (1. + 0.5 * mu * mu / (me * E));
+        const double nu = q / E;
+        const double delta = delta_factor * nu / (1. - nu);
+        const double muD_factor = mu + delta * (D_n * sqrte - 2.);
+        /* Nuclear, inelastic nuclear and electron screening terms. */
+        double Phi_n = log(BZ_n * muD_factor /
+            (D_n * (me + delta * sqrte * BZ_n)));
+        if (Phi_n < 0.) Phi_n = 0.;
+        double Phi_x = 0.;
+        if (Z >= 2) {
+                Phi_x = log(mu * D_n / muD_factor);
+                if (Phi_x < 0.) Phi_x = 0.;
+        }
+        double Phi_e = 0.;
+        if (q < qe_max) {
+                Phi_e = log(BZ_e * mu /
+                    ((1. + delta * phie_factor) * (me + delta * sqrte * BZ_e)));
+                if (Phi_e < 0.) Phi_e = 0.;
+        }
+        const double dcs = dcs_factor * (Z * Phi_n + Phi_x + Phi_e) *
+            (4. / 3. * (1. / nu - 1.) + nu);
+        return (dcs < 0.) ? 0. : dcs;
+}
+
+/* dcs_bremsstrahlung_ABB (pumas.c:13824-13905), in MeV internally, with the
+ * constants of pumas.c:13827-13830. */
+static double dcs_bremsstrahlung_ABB(
+    double Z, double A, double m, double K, double q)
+{
+        if ((Z <= 0) || (A <= 0) || (m <= 0) || (K <= 0) || (q <= 0))
+                return 0.;
+        const double Z13 = pow(Z, 1. / 3.);
+        if (q >= K + m * (1. - 0.75 * SSR_SQRTE * Z13)) return 0.;
+        const double energy = (K + m) * 1E+03;
+        const double v = q * 1E+03 / energy;
+        m *= 1E+03;
+        /* Screening constants and the nuclear form factor terms (eq. 2.18,
+         * 2.19, 2.30). */
+        const double Z3 = 1. / Z13;
+        const double a1 = 184.15 * Z3 / (SSR_SQRTE * SSR_ME);
+        const double a2 = 1194 * Z3 * Z3 / (SSR_SQRTE * SSR_ME);
+        const double qc = 1.9 * SSR_MMU * Z3;
+        double aux = 2 * m / qc;
+        const double zeta = sqrt(1 + aux * aux);
+        const double delta = m * m * v / (2 * energy * (1 - v));
+        const double x1 = a1 * delta;
+        const double x2 = a2 * delta;
+        double aux1, aux2, d1, d2;
+        if (Z == 1) {
+                d1 = 0;
+                d2 = 0;
+        } else {
+                aux1 = log(m / qc);
+                aux2 = 0.5 * zeta * log((zeta + 1) / (zeta - 1));
+                d1 = aux1 + aux2;
+                d2 = aux1 + 0.5 * ((3 - zeta * zeta) * aux2 + aux * aux);
+        }
+        /* Atomic screening functions (eq. 2.20, 2.21). */
+        aux = m * a1;
+        aux1 = log(aux * aux / (1 + x1 * x1));
+        aux = m * a2;
+        aux2 = log(aux * aux / (1 + x2 * x2));
+        double psi1 = 0.5 * ((1 + aux1) + (1 + aux2) / Z);
+        double psi2 = 0.5 * ((2. / 3 + aux1) + (2. / 3 + aux2) / Z);
+        aux1 = x1 * atan(1 / x1);
+        aux2 = x2 * atan(1 / x2);
+        psi1 -= aux1 + aux2 / Z;
+        aux = x1 * x1;
+        psi2 += 2 * aux * (1 - aux1 + 0.75 * log(aux / (1 + aux)));
+        aux = x2 * x2;
+        psi2 += 2 * aux * (1 - aux2 + 0.75 * log(aux / (1 + aux))) / Z;
+        psi1 -= d1;
+        psi2 -= d2;
+        const double result =
+            (2 - 2 * v + v * v) * psi1 - (2. / 3) * (1 - v) * psi2;
+        if (result < 0) return 0;
+        aux = 2 * (SSR_ME / m) * SSR_RE * Z;
+        return aux * aux * (ALPHA_EM / q) * result * 1E-04;
+}
+
+/* dcs_pair_production_KKP (pumas.c:14255-14373): integral over
+ * t = ln(1 - rho) with the 12 point Gauss-Legendre nodes, electron and muon
+ * terms, and the atomic electrons' form factor. */
+static double dcs_pair_production_KKP(
+    double Z, double A_, double mass, double K, double q)
+{
+        if ((Z <= 0) || (A_ <= 0) || (mass <= 0) || (K <= 0) || (q <= 0))
+                return 0.;
+        double qmin, qmax;
+        dcs_pair_production_range(Z, mass, K, &qmin, &qmax);
+        if ((q < qmin) || (q > qmax)) return 0.;
+        const double nu = q / (K + mass);
+        const double r = mass / ELECTRON_MASS;
+        const double beta = 0.5 * nu * nu / (1. - nu);
+        const double xi_factor = 0.5 * r * r * beta;
+        const double A = radiation_logarithm(Z);
+        const double Z13 = pow(Z, 1. / 3.);
+        const double AZ13 = A / Z13;
+        const double sqrte = 1.6487212707;
+        const double cL = 2. * sqrte * ELECTRON_MASS * AZ13;
+        const double cLe = 2.25 * Z13 * Z13 / (r * r);
+        const double gamma = 1. + K / mass;
+        const double x0 = 4. * ELECTRON_MASS / q;
+        const double x1 = 6. / (gamma * (gamma - q / mass));
+        const double argmin =
+            (x0 + 2. * (1. - x0) * x1) / (1. + (1. - x1) * sqrt(1. - x0));
+        if ((argmin >= 1.) || (argmin <= 0.)) return 0.;
+        const double tmin = log(argmin);
+        double I = 0.;
+        int i;
+        for (i = 0; i < 12; i++) {
+                const double eps = exp(gl12_x[i] * tmin);
+                const double rho = 1. - eps;
+                const double rho2 = rho * rho;
+                const double rho21 = eps * (2. - eps);
+                const double xi = xi_factor * rho21;
+                const double xi_i = 1. / xi;
+                double Be;
+                if (xi >= 1E+03)
+                        Be = 0.5 * xi_i *
+                            ((3 - rho2) + 2. * beta * (1. + rho2));
+                else
+                        Be = ((2. + rho2) * (1. + beta) + xi * (3. + rho2)) *
+                                log(1. + xi_i) +
+                            (rho21 - beta) / (1. + xi) - 3. - rho2;
+                const double Ye = (5. - rho2 + 4. * beta * (1. + rho2)) /
+                    (2. * (1. + 3. * beta) * log(3. + xi_i) - rho2 -
+                        2. * beta * (2. - rho2));
+                const double xe = (1. + xi) * (1. + Ye);
+                const double cLi = cL / rho21;
+                const double Le = log(AZ13 * sqrt(xe) * q / (q + cLi * xe)) -
+                    0.5 * log(1. + cLe * xe);
+                double Phi_e = Be * Le;
+                if (Phi_e < 0.) Phi_e = 0.;
+                double Bmu;
+                if (xi <= 1E-03)
+                        Bmu = 0.5 * xi * (5. - rho2 + beta * (3. + rho2));
+                else
+                        Bmu = ((1. + rho2) * (1. + 1.5 * beta) -
+                                  xi_i * (1. + 2. * beta) * rho21) *
+                                log(1. + xi) +
+                            xi * (rho21 - beta) / (1. + xi) +
+                            (1. + 2. * beta) * rho21;
+                const double Ymu = (4. + rho2 + 3. * beta * (1. + rho2)) /
+                    ((1. + rho2) * (1.5 + 2. * beta) * log(3. + xi) + 1. -
+                        1.5 * rho2);
+                const double xmu = (1. + xi) * (1. + Ymu);
+                const double Lmu =
+                    log(r * AZ13 * q / (1.5 * Z13 * (q + cLi * xmu)));
+                double Phi_mu = Bmu * Lmu;
+                if (Phi_mu < 0.) Phi_mu = 0.;
+                I -= (Phi_e + Phi_mu / (r * r)) * (1. - rho) * gl12_w[i] *
+                    tmin;
+        }
+        double zeta = 0.;
+        if (gamma > 35.) {
+                double gamma1, gamma2;
+                if (Z == 1.) {
+                        gamma1 = 4.4E-05;
+                        gamma2 = 4.8E-05;
+                } else {
+                        gamma1 = 1.95E-05;
+                        gamma2 = 5.30E-05;
+                }
+                zeta = 0.073 * log(gamma / (1. + gamma1 * gamma * Z13 * Z13)) -
+                    0.26;
+                if (zeta <= 0.)
+                        zeta = 0.;
+                else
+                        zeta /= 0.058 * log(gamma /
+                                                (1. + gamma2 * gamma * Z13)) -
+                            0.14;
+        }
+        const double E = K + mass;
+        const double dcs =
+            1.794664E-34 * Z * (Z + zeta) * (E - q) * I / (q * E);
+        return (dcs < 0.) ? 0. : dcs;
+}
+
 /* dcs_photonuclear_f2p_ALLM97 (pumas.c:14626-14673). */
 static double dcs_photonuclear_f2p_ALLM97(double x, double Q2)
 {
@@ -1902,12 +2114,21 @@ static double dcs_process(int process, const struct port_element * e,
     double K, double q)
 {
         switch (process) {
-        case 0:
-                return dcs_bremsstrahlung_SSR(e->Z, e->A, ph->mass, K, q) *
-                    1E+03 * AVOGADRO_NUMBER * (ph->mass + K) / e->A;
-        case 1:
-                return dcs_pair_production_SSR(e->Z, e->A, ph->mass, K, q) *
-                    1E+03 * AVOGADRO_NUMBER * (ph->mass + K) / e->A;
+        case 0: {
+                double (*f)(double, double, double, double, double) =
+                    (ph->model_brems == 1) ? &dcs_bremsstrahlung_KKP :
+                    (ph->model_brems == 2) ? &dcs_bremsstrahlung_ABB :
+                                             &dcs_bremsstrahlung_SSR;
+                return f(e->Z, e->A, ph->mass, K, q) * 1E+03 *
+                    AVOGADRO_NUMBER * (ph->mass + K) / e->A;
+        }
+        case 1: {
+                double (*f)(double, double, double, double, double) =
+                    (ph->model_pair == 1) ? &dcs_pair_production_KKP :
+                                            &dcs_pair_production_SSR;
+                return f(e->Z, e->A, ph->mass, K, q) * 1E+03 *
+                    AVOGADRO_NUMBER * (ph->mass + K) / e->A;
+        }
         case 2: {
                 double qmin, qmax;
                 dcs_photonuclear_range(ph->mass, K, &qmin, &qmax);

@@ -240,9 +240,53 @@ CASES["tau_rock_backward"] = dict(
     states=lambda n, s, f: _states(n, s, f, 1E+04, 1E+06, z0=999.999))
 
 
+# Non-default DCS models (pumas.h:742-771): KKP bremsstrahlung and pair
+# production, and ABB bremsstrahlung, with the DRSS photonuclear model.
+CASES["models_kkp_rock_slab"] = dict(
+    physics="muon_kkp",
+    config=_cfg(STRAGGLED, MIXED, FWD, event=LIMIT_ENERGY, limit_energy=1.),
+    geometry=ROCK_SLAB, n=200, seed=51,
+    states=lambda n, s, f: W.rock_slab(n, s, f))
+CASES["models_kkp_stack_backward"] = dict(
+    physics="muon_kkp",
+    config=_cfg(STRAGGLED, MIXED, BWD),
+    geometry=STACK, n=150, seed=52,
+    states=lambda n, s, f: _states(n, s, f, 1., 1E+04, z0=399.999))
+CASES["models_abb_stack_forward"] = dict(
+    physics="muon_abb",
+    config=_cfg(STRAGGLED, MIXED, FWD, event=LIMIT_ENERGY, limit_energy=1.),
+    geometry=STACK, n=200, seed=53,
+    states=lambda n, s, f: _states(n, s, f, 1., 1E+04))
+
+
 def particle(name):
-    """Physics of a case: "muon" (default) or "tau"."""
+    """Physics of a case: "muon" (default), "tau", or a muon physics with
+    non-default DCS models ("muon_kkp", "muon_abb")."""
     return CASES[name].get("physics", "muon")
+
+
+# Physics that the GPU engine loads; the others are pinned on the CPU
+# oracles only.
+DEVICE_PHYSICS = ("muon", "tau")
+
+
+def on_device(name):
+    return particle(name) in DEVICE_PHYSICS
+
+
+def physics_dump(name):
+    """Bytes of a physics dump: the shipped muon and tau dumps, or the test
+    fixtures with non-default DCS models (tests/golden/physics_*.pumas.gz,
+    made by tests/golden/make_golden.py physics)."""
+    import gzip
+    import os
+    from pumas_gb300 import default_dump
+    if name in ("muon", "tau"):
+        return default_dump(name)
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden",
+                        "physics_%s.pumas.gz" % name)
+    with gzip.open(path, "rb") as f:
+        return f.read()
 
 
 def has_locals(name):

@@ -58,20 +58,11 @@ def tau_dump():
 
 
 @pytest.fixture(scope="session")
-def tau_port(tau_dump):
-    """The C restatement with the tau physics, in its own copy of the
-    library (the physics is a global of the library)."""
-    import oracle
-    oracle.build_port()
-    return oracle.Port(tau_dump, private=True)
-
-
-@pytest.fixture(scope="session")
-def tau_reference(reference, tau_dump, tmp_path_factory):
-    import oracle
-    path = tmp_path_factory.mktemp("phys") / "tau.pumas"
-    path.write_bytes(tau_dump)
-    return oracle.Reference(str(path), private=True)
+def oracle_cache():
+    """Oracles of physics other than the default muon one, by (kind,
+    physics), each in its own copy of the library (the physics is a global
+    of the library)."""
+    return {}
 
 
 @pytest.fixture(scope="session")
@@ -81,15 +72,32 @@ def gpu_tau_physics(gpu_physics, tau_dump):
 
 
 def case_oracle(request, name, kind):
-    """The oracle fixture (`port` or `reference`) with a case's physics."""
-    from cases import particle
+    """The oracle (`port` or `reference`) with a case's physics."""
+    import oracle
+    from cases import particle, physics_dump
     p = particle(name)
-    return request.getfixturevalue(kind if p == "muon" else p + "_" + kind)
+    base = request.getfixturevalue(kind)
+    if p == "muon":
+        return base
+    cache = request.getfixturevalue("oracle_cache")
+    if (kind, p) not in cache:
+        dump = physics_dump(p)
+        if kind == "port":
+            cache[kind, p] = oracle.Port(dump, private=True)
+        else:
+            path = request.getfixturevalue("tmp_path_factory").mktemp(
+                "phys") / (p + ".pumas")
+            path.write_bytes(dump)
+            cache[kind, p] = oracle.Reference(str(path), private=True)
+    return cache[kind, p]
 
 
 def case_physics(request, name):
-    """The GPU physics fixture of a case."""
-    from cases import particle
+    """The GPU physics fixture of a case; cases whose physics the engine
+    does not load are skipped."""
+    from cases import on_device, particle
+    if not on_device(name):
+        pytest.skip("the engine loads the default DCS models only")
     p = particle(name)
     return request.getfixturevalue(
         "gpu_physics" if p == "muon" else "gpu_%s_physics" % p)

@@ -9,8 +9,13 @@ against the reference's own outputs.
 usage: python tests/golden/make_golden.py [case ...]   (default: all cases)
        python tests/golden/make_golden.py frames [case ...]   (recorder
        frames of the cases of RECORD_CASES)
+       python tests/golden/make_golden.py physics   (the physics dumps with
+       non-default DCS models of PHYSICS_MODELS, by the reference's
+       pumas_physics_create)
 """
+import gzip
 import os
+import subprocess
 import sys
 
 import numpy as np
@@ -22,7 +27,7 @@ sys.path.insert(0, os.path.dirname(HERE))
 
 import oracle  # noqa: E402
 import pumas_gb300  # noqa: E402
-from cases import CASES, make_states  # noqa: E402
+from cases import CASES, make_states, physics_dump  # noqa: E402
 from conftest import oracle_config, oracle_geometry  # noqa: E402
 
 
@@ -34,6 +39,41 @@ RECORD_CASES = [
     ("stack_backward_straggled", 0, 24, 32),
     ("terrain_backward", 25, 16, 64),
 ]
+
+
+# Physics dumps of the cases with non-default DCS models: name ->
+# (bremsstrahlung, pair production, photonuclear).
+PHYSICS_MODELS = {
+    "muon_kkp": ("KKP", "KKP", "DRSS"),
+    "muon_abb": ("ABB", "SSR", "DRSS"),
+}
+
+
+def make_physics():
+    """Build the dumps of PHYSICS_MODELS with the reference library."""
+    ref = oracle.REFERENCE_DIR
+    build = os.path.join(ROOT, "pumas_gb300", "data", "_build")
+    exe = os.path.join(build, "make_physics")
+    os.makedirs(build, exist_ok=True)
+    subprocess.check_call([
+        "cc", "-O3", "-std=c99", "-ffp-contract=off",
+        "-I" + os.path.join(ref, "include"), "-o", exe,
+        os.path.join(ROOT, "pumas_gb300", "data", "make_physics.c"),
+        os.path.join(ref, "src", "pumas.c"), "-lm"])
+    mdf = os.path.join(ROOT, "pumas_gb300", "data", "materials.xml")
+    for name, models in PHYSICS_MODELS.items():
+        dedx = os.path.join(build, "dedx-" + name)
+        os.makedirs(dedx, exist_ok=True)
+        raw = os.path.join(build, name + ".pumas")
+        subprocess.check_call([exe, mdf, dedx, raw, "muon"] + list(models))
+        with open(raw, "rb") as f, gzip.GzipFile(
+                physics_file(name), "wb", 9, mtime=0) as g:
+            g.write(f.read())
+        print("wrote", physics_file(name))
+
+
+def physics_file(name):
+    return os.path.join(HERE, "physics_%s.pumas.gz" % name)
 
 
 def record_file(name, period):
@@ -70,6 +110,9 @@ def main():
     if args and args[0] == "frames":
         make_frames(ref, args[1:])
         return
+    if args and args[0] == "physics":
+        make_physics()
+        return
     names = args or list(CASES)
     refs = {"muon": ref}
     for name in names:
@@ -80,7 +123,7 @@ def main():
             p = os.path.join(os.path.dirname(path), "golden_%s.pumas" %
                              particle)
             with open(p, "wb") as f:
-                f.write(pumas_gb300.default_dump(particle))
+                f.write(physics_dump(particle))
             refs[particle] = oracle.Reference(p, private=True)
         r = refs[particle]
         s0 = make_states(name)

@@ -22,7 +22,7 @@ import os
 import numpy as np
 import pytest
 
-from cases import CASES, make_states
+from cases import CASES, make_states, on_device
 from conftest import (GOLDEN, case_physics, compare, gpu_context,
                       gpu_geometry, oracle_config, oracle_geometry)
 
@@ -101,7 +101,7 @@ def test_gpu_matches_reference_golden(request, name):
 
 def test_gpu_golden_aggregate():
     """At least 99.9 % of all golden events within tolerance."""
-    if len(_golden_tally) < len(CASES):
+    if len(_golden_tally) < len([n for n in CASES if on_device(n)]):
         pytest.skip("per case golden tests not run")
     good = sum(v[0] for v in _golden_tally.values())
     total = sum(v[1] for v in _golden_tally.values())

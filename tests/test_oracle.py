@@ -156,3 +156,17 @@ def test_port_edge_cases(port):
                         event=1, limit_energy=1., accuracy=0., seed=1)
     s, r = port.transport(bad, geo, s0[:1])
     assert r["status"][0] == 1           # PUMAS_RETURN_ACCURACY_ERROR
+
+
+@pytest.mark.parametrize("name", ["models_kkp_rock_slab",
+                                  "models_abb_stack_forward"])
+def test_dcs_model_changes_the_transport(port, request, name):
+    """The same events with the default models end elsewhere: the model
+    cases exercise their own DCS."""
+    data = np.load(os.path.join(GOLDEN, name + ".npz"))
+    case = CASES[name]
+    geo = oracle_geometry(port, case["geometry"])
+    cfg = oracle_config(case["config"], case["seed"])
+    s1, r1 = port.transport(cfg, geo, data["initial"], 0, 4)
+    same, _ = compare(s1, r1, data["final"], data["results"])
+    assert same.mean() < 0.5
