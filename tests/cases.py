@@ -241,7 +241,8 @@ CASES["tau_rock_backward"] = dict(
 
 
 # Non-default DCS models (pumas.h:742-771): KKP bremsstrahlung and pair
-# production, and ABB bremsstrahlung, with the DRSS photonuclear model.
+# production with BM photonuclear; ABB bremsstrahlung with BBKS
+# photonuclear; BBKS for taus.
 CASES["models_kkp_rock_slab"] = dict(
     physics="muon_kkp",
     config=_cfg(STRAGGLED, MIXED, FWD, event=LIMIT_ENERGY, limit_energy=1.),
@@ -257,11 +258,16 @@ CASES["models_abb_stack_forward"] = dict(
     config=_cfg(STRAGGLED, MIXED, FWD, event=LIMIT_ENERGY, limit_energy=1.),
     geometry=STACK, n=200, seed=53,
     states=lambda n, s, f: _states(n, s, f, 1., 1E+04))
+CASES["models_bbks_tau_stack"] = dict(
+    physics="tau_bbks",
+    config=_cfg(STRAGGLED, MIXED, FWD, decay=RANDOMISED),
+    geometry=STACK, n=200, seed=54,
+    states=lambda n, s, f: _states(n, s, f, 1E+05, 1E+08))
 
 
 def particle(name):
-    """Physics of a case: "muon" (default), "tau", or a muon physics with
-    non-default DCS models ("muon_kkp", "muon_abb")."""
+    """Physics of a case: "muon" (default), "tau", or a physics with
+    non-default DCS models ("muon_kkp", "muon_abb", "tau_bbks")."""
     return CASES[name].get("physics", "muon")
 
 

@@ -42,10 +42,11 @@ RECORD_CASES = [
 
 
 # Physics dumps of the cases with non-default DCS models: name ->
-# (bremsstrahlung, pair production, photonuclear).
+# (particle, bremsstrahlung, pair production, photonuclear).
 PHYSICS_MODELS = {
-    "muon_kkp": ("KKP", "KKP", "DRSS"),
-    "muon_abb": ("ABB", "SSR", "DRSS"),
+    "muon_kkp": ("muon", "KKP", "KKP", "BM"),
+    "muon_abb": ("muon", "ABB", "SSR", "BBKS"),
+    "tau_bbks": ("tau", "SSR", "SSR", "BBKS"),
 }
 
 
@@ -65,7 +66,7 @@ def make_physics():
         dedx = os.path.join(build, "dedx-" + name)
         os.makedirs(dedx, exist_ok=True)
         raw = os.path.join(build, name + ".pumas")
-        subprocess.check_call([exe, mdf, dedx, raw, "muon"] + list(models))
+        subprocess.check_call([exe, mdf, dedx, raw] + list(models))
         with open(raw, "rb") as f, gzip.GzipFile(
                 physics_file(name), "wb", 9, mtime=0) as g:
             g.write(f.read())
