@@ -1,7 +1,7 @@
 /*
  * gp_models.cuh -- the non-default DCS models of PUMAS
  * (struct pumas_physics_settings, pumas.h:742-771), as code that compiles
- * both as C (the CPU oracle, oracle/port.c) and as CUDA (the engine):
+ * both as C (host) and as CUDA (the engine):
  *
  *   bremsstrahlung  KKP (Kelner, Kokoulin & Petrukhin), ABB (Andreev,
  *                   Bezrukov & Bugaev);
@@ -14,7 +14,7 @@
  *
  * Each function cites the reference lines it follows; their arithmetic is
  * kept in the reference's order so that the host build reproduces the
- * reference bit for bit (the oracle's golden cases check it). The device
+ * reference bit for bit (the golden cases of the tests check it). The device
  * build calls the CUDA math library, within an ulp of the host's.
  * Element data that the callers hold (the radiation logarithm) and the
  * Gauss-Legendre nodes are passed as arguments.
