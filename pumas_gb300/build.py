@@ -20,7 +20,7 @@ INCLUDE = os.path.join(ROOT, "include")
 
 SOURCES = ["gp_physics.cu", "gp_transport.cu", "gp_batch.cu"]
 HEADERS = ["gp_internal.h", "gp_device.cuh", "gp_math.cuh",
-           "gp_math_tables.h", "gp_io.cuh", "gp_context.h"]
+           "gp_math_tables.h", "gp_models.cuh", "gp_io.cuh", "gp_context.h"]
 
 NVCC_FLAGS = [
     "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo",

@@ -807,7 +807,7 @@ static __device__ __forceinline__ double gp_pn_value(
     const gp_tables & T, const gp_pn & s)
 {
         const gp_element & el = T.element[s.target];
-        const double d2 = gp_photonuclear_d2(T, el, s.ki, s.q, s.Q2);
+        const double d2 = gp_photonuclear_ddcs(T, el, s.ki, s.q, s.Q2);
         return (s.phase == PN_REJECT) ? d2 * s.Q2 : -d2 * s.Q2;
 }
 

@@ -32,6 +32,7 @@
 #include <stdint.h>
 
 #include "gp_math.cuh"
+#include "gp_models.cuh"
 
 #include "gpumas.h"
 #include "gp_internal.h"
@@ -1065,6 +1066,17 @@ static __device__ double gp_photonuclear_d2(const gp_tables & T,
         return cf * F2A * dds / q;
 }
 
+/* The doubly differential cross section of the photonuclear polar angle
+ * sampler: the BM model's for BM, else DRSS's (dcs_photonuclear_ddcs,
+ * pumas.c:15159-15170). */
+GPD double gp_photonuclear_ddcs(const gp_tables & T, const gp_element & el,
+    double K, double q, double Q2)
+{
+        if (T.model_photo == 2)
+                return gpm_photonuclear_d2_BM(el.Z, el.A, T.mass, K, q, Q2);
+        return gp_photonuclear_d2(T, el, K, q, Q2);
+}
+
 /* dcs_photonuclear_DRSS (pumas.c:15002-15083, mode 0). */
 static __device__ double gp_dcs_photonuclear(const gp_tables & T,
     const gp_element & el, double K, double q)
@@ -1128,17 +1140,30 @@ static __device__ double gp_dcs_process(const gp_tables & T, int process,
 {
         const double m = T.mass;
         if (process == 0) {
-                return gp_dcs_bremsstrahlung(T, el, K, q) * 1E+03 *
-                    GP_AVOGADRO * (m + K) / el.A;
+                /* The dump's model (struct pumas_physics_settings). */
+                const double d = (T.model_brems == 0) ?
+                    gp_dcs_bremsstrahlung(T, el, K, q) :
+                    (T.model_brems == 1) ?
+                    gpm_bremsstrahlung_KKP(el.Z, el.A, m, K, q, el.rad_log) :
+                    gpm_bremsstrahlung_ABB(el.Z, el.A, m, K, q);
+                return d * 1E+03 * GP_AVOGADRO * (m + K) / el.A;
         } else if (process == 1) {
-                return gp_dcs_pair_production(T, el, K, q) * 1E+03 *
-                    GP_AVOGADRO * (m + K) / el.A;
+                const double d = (T.model_pair == 0) ?
+                    gp_dcs_pair_production(T, el, K, q) :
+                    gpm_pair_production_KKP(el.Z, el.A, m, K, q, el.rad_log,
+                        gp_gl12_x, gp_gl12_w);
+                return d * 1E+03 * GP_AVOGADRO * (m + K) / el.A;
         } else if (process == 2) {
                 double qmin, qmax;
                 gp_photonuclear_range(m, K, qmin, qmax);
                 if ((q < qmin) || (q > qmax)) return 0.;
-                return gp_dcs_photonuclear(T, el, K, q) * 1E+03 *
-                    GP_AVOGADRO * (m + K) / el.A;
+                const double d = (T.model_photo == 0) ?
+                    gp_dcs_photonuclear(T, el, K, q) :
+                    (T.model_photo == 1) ?
+                    gpm_photonuclear_BBKS(el.Z, el.A, m, K, q) :
+                    gpm_photonuclear_BM(el.Z, el.A, m, K, q, gp_gl9_x,
+                        gp_gl9_w);
+                return d * 1E+03 * GP_AVOGADRO * (m + K) / el.A;
         } else {
                 return gp_electronic_dcs(el.Z, el.I, m, K, q) * (m + K) *
                     GP_AVOGADRO / (el.A * 1E-03);
@@ -1470,7 +1495,7 @@ GPD double gp_polar_objective(const gp_tables & T, const gp_element & el,
     double K, double q, double lnQ2)
 {
         const double Q2 = gp_exp(lnQ2);
-        return -gp_photonuclear_d2(T, el, K, q, Q2) * Q2;
+        return -gp_photonuclear_ddcs(T, el, K, q, Q2) * Q2;
 }
 
 /* math_find_minimum_brent (pumas.c:12233-12325); as in the reference the
@@ -1631,7 +1656,7 @@ static __device__ __forceinline__ double gp_polar_photonuclear(const gp_tables &
         for (i = 0; i < 100; i++) {
                 const double u = gp_random(e);
                 Q2 = Q2min * gp_exp(rQ2 * u);
-                const double r = gp_photonuclear_d2(T, el, ki, q, Q2) * Q2;
+                const double r = gp_photonuclear_ddcs(T, el, ki, q, Q2) * Q2;
                 if (gp_random(e) * fopt <= r) break;
         }
         if (i == 100) return 0.;

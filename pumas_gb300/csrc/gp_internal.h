@@ -119,6 +119,10 @@ struct __align__(16) gp_node {
 
 struct gp_tables {
         int n_energies, n_materials, n_elements, n_components, n_table_dcs;
+        /* DCS models (struct pumas_physics_settings, pumas.h:742-771):
+         * bremsstrahlung 0 SSR, 1 KKP, 2 ABB; pair production 0 SSR,
+         * 1 KKP; photonuclear 0 DRSS, 1 BBKS, 2 BM. */
+        int model_brems, model_pair, model_photo;
         double ctau, mass, cutoff, elastic_ratio;
         const double *K, *K_dX, *K_dNI_in, *K_dNI_el;
         const double *X, *X_dK, *X_dT, *T, *T_dK, *dE, *dE_dK;

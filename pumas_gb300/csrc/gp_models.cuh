@@ -25,7 +25,9 @@
 #include <math.h>
 
 #ifdef __CUDACC__
-#define GPM_HD static __host__ __device__ __forceinline__
+/* Out of line on the device: the default models' kernels keep their
+ * registers. */
+#define GPM_HD static __host__ __device__ __noinline__
 #ifdef __CUDA_ARCH__
 #define GPM_TABLE static __device__ const
 #else

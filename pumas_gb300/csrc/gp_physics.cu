@@ -297,6 +297,7 @@ static void bake_nodes(const double * x, int n, struct gp_node * out)
 struct parsed {
         int n_energies, n_materials, n_composites, n_elements, n_components;
         int max_components, n_table_dcs, particle;
+        int model_brems, model_pair, model_photo;
         double ctau, mass, cutoff, elastic_ratio;
         int64_t off[53];
 };
@@ -332,9 +333,20 @@ static int parse_blob(const char * b, int64_t size, struct parsed * p)
         if ((p->n_energies < 3) || (p->n_materials < 1) ||
             (p->n_elements < 1) || (p->max_components > GP_MAX_COMPONENTS))
                 return GPUMAS_RETURN_FORMAT_ERROR;
-        if ((strcmp(b + p->off[50], "SSR") != 0) ||
-            (strcmp(b + p->off[51], "SSR") != 0) ||
-            (strcmp(b + p->off[52], "DRSS") != 0))
+        /* The DCS models of the dump (pumas.c:2167-2196). */
+        const char * brems = b + p->off[50];
+        const char * pair = b + p->off[51];
+        const char * photo = b + p->off[52];
+        p->model_brems = (strcmp(brems, "SSR") == 0) ? 0 :
+            (strcmp(brems, "KKP") == 0) ? 1 :
+            (strcmp(brems, "ABB") == 0) ? 2 : -1;
+        p->model_pair = (strcmp(pair, "SSR") == 0) ? 0 :
+            (strcmp(pair, "KKP") == 0) ? 1 : -1;
+        p->model_photo = (strcmp(photo, "DRSS") == 0) ? 0 :
+            (strcmp(photo, "BBKS") == 0) ? 1 :
+            (strcmp(photo, "BM") == 0) ? 2 : -1;
+        if ((p->model_brems < 0) || (p->model_pair < 0) ||
+            (p->model_photo < 0))
                 return GPUMAS_RETURN_MODEL_ERROR;
         /* Muons or taus (enum pumas_particle, pumas.h:45-50). */
         if ((p->particle != GPUMAS_PARTICLE_MUON) &&
@@ -588,6 +600,9 @@ static int physics_from_blob(
         t->n_elements = ne;
         t->n_components = nc;
         t->n_table_dcs = p.n_table_dcs;
+        t->model_brems = p.model_brems;
+        t->model_pair = p.model_pair;
+        t->model_photo = p.model_photo;
         t->ctau = p.ctau;
         t->mass = p.mass;
         t->cutoff = p.cutoff;

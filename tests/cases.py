@@ -271,13 +271,13 @@ def particle(name):
     return CASES[name].get("physics", "muon")
 
 
-# Physics that the GPU engine loads; the others are pinned on the CPU
-# oracles only.
-DEVICE_PHYSICS = ("muon", "tau")
+# Physics with non-default DCS models: their GPU golden cases run in
+# tests/test_zy_models.py, after the other GPU tests.
+MODEL_PHYSICS = ("muon_kkp", "muon_abb", "tau_bbks")
 
 
-def on_device(name):
-    return particle(name) in DEVICE_PHYSICS
+def has_models(name):
+    return particle(name) in MODEL_PHYSICS
 
 
 def physics_dump(name):

@@ -92,15 +92,25 @@ def case_oracle(request, name, kind):
     return cache[kind, p]
 
 
+@pytest.fixture(scope="session")
+def gpu_physics_cache():
+    """GPU physics of the cases with non-default DCS models, by name."""
+    return {}
+
+
 def case_physics(request, name):
-    """The GPU physics fixture of a case; cases whose physics the engine
-    does not load are skipped."""
-    from cases import on_device, particle
-    if not on_device(name):
-        pytest.skip("the engine loads the default DCS models only")
+    """The GPU physics of a case."""
+    from cases import particle, physics_dump
     p = particle(name)
-    return request.getfixturevalue(
-        "gpu_physics" if p == "muon" else "gpu_%s_physics" % p)
+    if p in ("muon", "tau"):
+        return request.getfixturevalue(
+            "gpu_physics" if p == "muon" else "gpu_%s_physics" % p)
+    request.getfixturevalue("gpu_physics")
+    cache = request.getfixturevalue("gpu_physics_cache")
+    if p not in cache:
+        import pumas_gb300
+        cache[p] = pumas_gb300.Physics(physics_dump(p))
+    return cache[p]
 
 
 def oracle_geometry(orc, spec):

@@ -22,7 +22,7 @@ import os
 import numpy as np
 import pytest
 
-from cases import CASES, make_states, on_device
+from cases import CASES, has_models, make_states
 from conftest import (GOLDEN, case_physics, compare, gpu_context,
                       gpu_geometry, oracle_config, oracle_geometry)
 
@@ -81,13 +81,13 @@ def statistical_check(a, b):
 _golden_tally = {}
 
 
-@pytest.mark.parametrize("name", sorted(CASES))
-def test_gpu_matches_reference_golden(request, name):
+def golden_check(request, name):
+    """Run a golden case on the GPU and check it against the reference's
+    fixture; returns (events within tolerance, events)."""
     data = np.load(os.path.join(GOLDEN, name + ".npz"))
     s1, r1 = run_gpu(case_physics(request, name), name, data["initial"])
     same, close = check(name, s1, r1, data["final"], data["results"])
     n = len(close)
-    _golden_tally[name] = (int(close.sum()), n)
     assert np.all(r1["status"] == 0)
     cfg = CASES[name]["config"]
     if cfg["energy_loss"] == 0 and cfg["scattering"] == -1:
@@ -97,11 +97,22 @@ def test_gpu_matches_reference_golden(request, name):
         assert close.mean() >= 0.98, "%s: %d / %d events outside 1e-9" % (
             name, n - close.sum(), n)
         statistical_check(s1, data["final"])
+    return int(close.sum()), n
+
+
+# Golden cases of the default DCS models; those of the other models run in
+# test_zy_models.py.
+GOLDEN_CASES = sorted(n for n in CASES if not has_models(n))
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_gpu_matches_reference_golden(request, name):
+    _golden_tally[name] = golden_check(request, name)
 
 
 def test_gpu_golden_aggregate():
     """At least 99.9 % of all golden events within tolerance."""
-    if len(_golden_tally) < len([n for n in CASES if on_device(n)]):
+    if len(_golden_tally) < len(GOLDEN_CASES):
         pytest.skip("per case golden tests not run")
     good = sum(v[0] for v in _golden_tally.values())
     total = sum(v[1] for v in _golden_tally.values())
