@@ -70,7 +70,7 @@ def parse():
                    help="drain threshold in slots (0: off, <0: automatic)")
     p.add_argument("--workload", default="rock_slab",
                    choices=["rock_slab", "slab_jobs", "terrain",
-                            "plain_csda", "serve"])
+                            "plain_csda", "serve", "atmosphere"])
     p.add_argument("--jobs", type=int, default=8192)
     p.add_argument("--job-scale", type=float, default=0.01,
                    help="slab_jobs: factor on the events per job")
@@ -78,6 +78,8 @@ def parse():
                    help="slab_jobs: plain comparison on every n-th job")
     p.add_argument("--per-direction", type=int, default=10_000,
                    help="terrain: events per direction")
+    p.add_argument("--atm-events", type=int, default=1_000_000,
+                   help="atmosphere: events per step")
     p.add_argument("--rates", default="100,300,1000,3000,10000",
                    help="serve: Poisson arrival rates (requests/s)")
     p.add_argument("--serve-seconds", type=float, default=2.0)
@@ -620,6 +622,78 @@ def run_terrain(args, rank, world, local):
     print(json.dumps(line), flush=True)
 
 
+def run_atmosphere(args, rank, world, local):
+    """Muons from 15 km through the exponential atmosphere with the
+    geomagnetic field into 200 m of rock: media with local properties,
+    transported by the one thread per event kernel that carries them."""
+    import numpy as np
+    import torch
+    import pumas_gb300 as pg
+    from pumas_gb300 import workloads as W
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    physics = pg.Physics()
+    ctx = pg.Context(physics)
+    W.apply_config(ctx, W.config_dict("atmosphere"))
+    ctx.seed = args.seed
+    ctx.set_geometry(W.atmosphere_geometry(physics))
+    n = args.atm_events
+    first = rank_first_event(rank)
+    s0 = W.atmosphere(n, seed=args.seed, first_event=first)
+    ev = DeviceEvents(s0, dev)
+    stream = torch.cuda.Stream(device=dev)
+
+    def step(k):
+        ev.restore(stream)
+        rc = ctx.transport_device(n, ev.soa(), first, stream.cuda_stream)
+        if rc != 0:
+            raise RuntimeError("transport_device: %d" % rc)
+
+    for k in range(args.warmup):
+        step(k)
+    stream.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clocks:
+        e0.record(stream)
+        for k in range(args.steps):
+            step(k)
+        e1.record(stream)
+        stream.synchronize()
+    ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, dev, world)
+    res = ev.result_records()
+    steps_total = float(res["steps"].sum())
+    st = ctx.stats()
+    if rank != 0:
+        return
+    line = base_line(args, world, "events/s", world * n / (ms * 1E-03),
+                     "events/s", ms, {
+                         "workload": "atmosphere: forward straggled + mixed "
+                                     "scattering from 15 km through an "
+                                     "exponential atmosphere (12 km scale "
+                                     "height, geomagnetic field) into 200 m "
+                                     "of StandardRock, 1 GeV - 1 TeV, stop "
+                                     "at 1 GeV or exit",
+                         "events_per_step": n})
+    cpu = None
+    if not args.no_baseline:
+        sub = max(1, n // 100)
+        cpu = port_baseline("atmosphere", s0[:sub],
+                            W.config_dict("atmosphere"), W.atmosphere_spec(),
+                            args.seed, first, "the first %d events" % sub)
+    line.update({
+        "cpu_baseline": cpu,
+        "steps_per_s": steps_total / (ms * 1E-03),
+        "steps_per_event": steps_total / n,
+        "event_errors": int(np.count_nonzero(res["status"])),
+        "gpu_launches": st["launches"],
+        "roofline": None,
+        "clocks": clocks.summary()})
+    print(json.dumps(line), flush=True)
+
+
 def run_plain_csda(args, rank, world, local):
     """Deterministic CSDA in infinite rock: one thread per event, streaming
     8 B in and 32 B out per event (HBM roofline)."""
@@ -710,7 +784,8 @@ def main():
         torch.cuda.set_device(local)
         pg.library(build=True)
         fn = {"slab_jobs": run_slab_jobs, "terrain": run_terrain,
-              "plain_csda": run_plain_csda}.get(args.workload)
+              "plain_csda": run_plain_csda,
+              "atmosphere": run_atmosphere}.get(args.workload)
         if fn is None:
             from pumas_gb300 import serving
             return serving.bench(args, rank, world, local)

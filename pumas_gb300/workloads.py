@@ -14,12 +14,14 @@ so that any subset of events can be regenerated independently:
 * ``terrain``: backward transport from a detector under a synthetic
   heightmap, see ``terrain_geometry``.
 * ``slab_jobs``: batched uneven jobs of slab stacks, see ``slab_jobs``.
+* ``atmosphere``: muons from the sky through an exponential atmosphere with
+  the geomagnetic field into rock, see ``atmosphere_geometry``.
 """
 import numpy as np
 
 from . import (MODE_BACKWARD, MODE_CSDA, MODE_DISABLED, MODE_FORWARD,
                MODE_MIXED, MODE_STRAGGLED, MODE_WEIGHTED, EVENT_LIMIT_ENERGY,
-               EVENT_NONE, STATE_DTYPE, Geometry)
+               EVENT_NONE, STATE_DTYPE, DENSITY_EXPONENTIAL, Geometry)
 
 M0, M1 = np.uint64(0xD2511F53), np.uint64(0xCD9E8D57)
 W0, W1 = np.uint64(0x9E3779B9), np.uint64(0xBB67AE85)
@@ -104,6 +106,51 @@ def rock_slab_geometry(physics_or_index):
     return Geometry.slabs([0., 1000.], [rock])
 
 
+# The exponential atmosphere of the reference's examples/pumas/geometry.c
+# (76-97): 1.205 kg/m^3 at sea level, 12 km scale height, geomagnetic field
+# (0, 20, -40) uT, over 200 m of rock, up to 20 km.
+ATMOSPHERE_LOCALS = dict(model=DENSITY_EXPONENTIAL, rho0=1.205,
+                         axis=(0., 0., 1.), h0=0., lambda_=12E+03,
+                         eps=5E-02, magnet=(0., 2E-05, -4E-05))
+ATMOSPHERE_Z = (-200., 0., 20E+03)
+
+
+def atmosphere_geometry(physics_or_index):
+    """Two slabs: StandardRock (uniform) under the atmosphere (Air with the
+    exponential density and the field)."""
+    rock = _material(physics_or_index, "StandardRock")
+    air = _material(physics_or_index, "Air")
+    return Geometry.slabs(list(ATMOSPHERE_Z), [rock, air],
+                          locals=[dict(), dict(ATMOSPHERE_LOCALS)])
+
+
+def atmosphere_spec():
+    """The atmosphere geometry as a plain dict (for oracles and tests)."""
+    return dict(kind=1, media=[("StandardRock", 0.), ("Air", 0.)],
+                slab_z=list(ATMOSPHERE_Z), slab_media=[0, 1],
+                locals=[dict(), dict(ATMOSPHERE_LOCALS)])
+
+
+def atmosphere(n, seed=1, first_event=0, emin=1., emax=1E+03, z0=15E+03):
+    """Initial states of the atmosphere workload: mu+ / mu- by event id
+    parity at altitude z0 with momenta pointing down, zenith angle cosine
+    uniform in [0.2, 1], uniform azimuth, kinetic energy log-uniform in
+    [emin, emax]."""
+    ev = np.arange(first_event, first_event + n, dtype=np.uint64)
+    s = np.zeros(n, dtype=STATE_DTYPE)
+    s["charge"] = np.where(ev % 2 == 1, 1., -1.)
+    s["energy"] = _log_uniform(seed, ev, 0, emin, emax)
+    s["weight"] = 1.
+    s["position"][:, 2] = z0
+    c = 0.2 + 0.8 * uniform(seed, 1, ev, 1)
+    phi = 2. * np.pi * uniform(seed, 1, ev, 2)
+    st = np.sqrt(1. - c * c)
+    s["direction"][:, 0] = st * np.cos(phi)
+    s["direction"][:, 1] = st * np.sin(phi)
+    s["direction"][:, 2] = -c
+    return s
+
+
 def _material(physics_or_index, name):
     if isinstance(physics_or_index, dict):
         return physics_or_index[name]
@@ -117,6 +164,11 @@ def config_dict(kind):
                     scattering=MODE_DISABLED, event=EVENT_LIMIT_ENERGY,
                     limit_energy=1., accuracy=1E-02)
     if kind == "rock_slab":
+        return dict(energy_loss=MODE_STRAGGLED, decay=MODE_WEIGHTED,
+                    direction=MODE_FORWARD, scattering=MODE_MIXED,
+                    event=EVENT_LIMIT_ENERGY, limit_energy=1.,
+                    accuracy=1E-02)
+    if kind == "atmosphere":
         return dict(energy_loss=MODE_STRAGGLED, decay=MODE_WEIGHTED,
                     direction=MODE_FORWARD, scattering=MODE_MIXED,
                     event=EVENT_LIMIT_ENERGY, limit_energy=1.,

@@ -125,3 +125,43 @@ def test_bench_rank_helpers():
     import bench
     assert bench.rank_first_event(0) == 0
     assert bench.rank_first_event(3) == 3 * 10 ** 12
+
+
+def test_atmosphere_workload_on_the_oracle():
+    """The atmosphere workload of the bench, through the CPU oracle: every
+    event ends cleanly, some reach the rock, and the CPU baseline helper
+    reports a rate."""
+    import bench
+    import oracle
+    import pumas_gb300 as pg
+    s0 = W.atmosphere(64, seed=7)
+    assert np.all(s0["direction"][:, 2] <= -0.2)
+    oracle.build_port()
+    port = oracle.Port(pg.default_dump())
+    spec = W.atmosphere_spec()
+    media = [(port.material_index(m), d) for m, d in spec["media"]]
+    geo = oracle.make_geometry(spec["kind"], media, **{
+        k: v for k, v in spec.items() if k not in ("kind", "media")})
+    cfg = oracle.Config(seed=7, **W.config_dict("atmosphere"))
+    s1, r1 = port.transport(cfg, geo, s0, 0, 1)
+    assert np.all(r1["status"] == 0)
+    assert np.any(r1["medium_out"] == 0) or np.any(s1["position"][:, 2] < 0.)
+    assert np.mean(r1["steps"]) > 10.
+    cpu = bench.port_baseline("atmosphere", s0, W.config_dict("atmosphere"),
+                              spec, 7, 0, "64 events")
+    assert cpu["value"] > 0. and cpu["kind"] == "port"
+
+
+def test_atmosphere_geometry_descriptor():
+    """The bench's device geometry: the ctypes descriptor carries the
+    locals of both media."""
+    g = W.atmosphere_geometry({"StandardRock": 0, "Air": 2})
+    c = g.c
+    assert c.kind == 1 and c.n_slabs == 2 and c.n_media == 2
+    assert [c.slab_z[i] for i in range(3)] == list(W.ATMOSPHERE_Z)
+    assert (c.media[0].material, c.media[1].material) == (0, 2)
+    air, rock = c.locals[1], c.locals[0]
+    assert rock.model == 0 and list(rock.magnet) == [0., 0., 0.]
+    assert air.model == 1 and air.rho0 == 1.205 and air.lambda_ == 12E+03
+    assert list(air.axis) == [0., 0., 1.] and air.eps == 5E-02
+    assert list(air.magnet) == [0., 2E-05, -4E-05]
