@@ -89,3 +89,35 @@ def test_random_seed_set_get():
     lib.gpumas_physics_cutoff.restype = ctypes.c_double
     lib.gpumas_physics_cutoff.argtypes = [ctypes.c_void_p]
     assert lib.gpumas_physics_cutoff(None) == 0.
+
+
+def test_loader_checks_dumps_before_the_device():
+    """gpumas_physics_load checks a dump's format, DCS model names and
+    particle before any device call: malformed dumps fail with the
+    reference's codes, on a machine without a GPU too."""
+    import ctypes
+    import struct
+    import pumas_gb300 as pg
+    lib = pg.library()
+    load = lib.gpumas_physics_load
+    load.restype = ctypes.c_int
+    load.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.c_char_p,
+                     ctypes.c_size_t]
+    ptr = ctypes.c_void_p()
+    assert load(ctypes.byref(ptr), bytes(100), 100) == pg.RETURN_FORMAT_ERROR
+    dump = pg.default_dump()
+    assert load(ctypes.byref(ptr), dump, 7) == pg.RETURN_FORMAT_ERROR
+    # The blob follows an 8 byte tag and size; its pointer table starts at
+    # byte 80 and its data at byte 528 (pumas.c:2167-2196).
+    ptrs = struct.unpack_from("53Q", dump, 8 + 80)
+    pair = 8 + ptrs[51] - ptrs[0] + 528
+    assert dump[pair:pair + 4] == b"SSR\0"
+    bad = bytearray(dump)
+    bad[pair:pair + 3] = b"XYZ"
+    assert load(ctypes.byref(ptr), bytes(bad), len(bad)) == \
+        pg.RETURN_MODEL_ERROR
+    bad = bytearray(dump)
+    struct.pack_into("i", bad, 8 + 40, 7)
+    assert load(ctypes.byref(ptr), bytes(bad), len(bad)) == \
+        pg.RETURN_UNKNOWN_PARTICLE
+    assert not ptr.value
