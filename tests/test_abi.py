@@ -121,3 +121,27 @@ def test_loader_checks_dumps_before_the_device():
     assert load(ctypes.byref(ptr), bytes(bad), len(bad)) == \
         pg.RETURN_UNKNOWN_PARTICLE
     assert not ptr.value
+
+
+def test_loader_accepts_tau_and_model_dumps():
+    """The shipped tau dump and the dumps with non-default DCS models pass
+    the loader's checks: without a GPU the load stops at the first device
+    call (GPUMAS_RETURN_DEVICE_ERROR); with one it succeeds."""
+    import ctypes
+    import pumas_gb300 as pg
+    from cases import physics_dump
+    lib = pg.library()
+    load = lib.gpumas_physics_load
+    load.restype = ctypes.c_int
+    load.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.c_char_p,
+                     ctypes.c_size_t]
+    destroy = lib.gpumas_physics_destroy
+    destroy.restype = None
+    destroy.argtypes = [ctypes.POINTER(ctypes.c_void_p)]
+    for name in ("muon", "tau", "muon_kkp", "muon_abb", "tau_bbks"):
+        dump = physics_dump(name)
+        ptr = ctypes.c_void_p()
+        rc = load(ctypes.byref(ptr), dump, len(dump))
+        assert rc in (pg.RETURN_SUCCESS, pg.RETURN_DEVICE_ERROR), (name, rc)
+        if ptr.value:
+            destroy(ctypes.byref(ptr))
