@@ -86,6 +86,14 @@ def parse():
     p.add_argument("--serve-scale", type=float, default=1E-03)
     p.add_argument("--autotune", action="store_true",
                    help="slab_jobs: tune the pool on every 8th job first")
+    p.add_argument("--no-c3", action="store_true",
+                   help="rock_slab: skip the batched jobs sub-object")
+    p.add_argument("--no-c4", action="store_true",
+                   help="rock_slab: skip the serving sub-object")
+    p.add_argument("--c3-scale", type=float, default=0.1,
+                   help="rock_slab: event scale of the batched jobs")
+    p.add_argument("--e2e-steps", type=int, default=5,
+                   help="timed end to end calls (at most --steps)")
     return p.parse_args()
 
 
@@ -187,8 +195,11 @@ def fp64_peak_tflops(torch):
     return best
 
 
-def cpu_baseline(n_events, seed, first_event=0):
-    """All-core OpenMP run of the C restatement on a bounded sample."""
+def cpu_baseline(n_events, seed, first_event=0, single=True):
+    """All-core OpenMP run of the C restatement on a bounded sample, with
+    the host's core count and, on a smaller sample, the one thread rate
+    (so that the per core speed and the thread scaling can be read from
+    the line)."""
     import numpy as np
     import oracle
     import pumas_gb300 as pg
@@ -204,12 +215,23 @@ def cpu_baseline(n_events, seed, first_event=0):
     t0 = time.perf_counter()
     _, r = port.transport(cfg, geo, s0, first_event, threads)
     dt = time.perf_counter() - t0
-    return {"value": n_events / dt, "unit": "events/s", "cores": threads,
-            "kind": "port",
-            "steps_per_s": float(r["steps"].sum()) / dt,
-            "sample": "%d events of the rock slab workload (first event "
-                      "id %d), %.1f s wall on %d OpenMP threads"
-                      % (n_events, first_event, dt, threads)}
+    out = {"value": n_events / dt, "unit": "events/s", "cores": threads,
+           "kind": "port",
+           "steps_per_s": float(r["steps"].sum()) / dt,
+           "nproc": os.cpu_count(), "omp_max_threads": threads,
+           "sample": "%d events of the rock slab workload (first event "
+                     "id %d), %.1f s wall on %d OpenMP threads"
+                     % (n_events, first_event, dt, threads)}
+    if single:
+        m = max(1, n_events // (4 * threads))
+        t0 = time.perf_counter()
+        port.transport(cfg, geo, s0[:m], first_event, 1)
+        d1 = time.perf_counter() - t0
+        out["one_thread"] = {"value": m / d1, "unit": "events/s",
+                             "sample": "the first %d events of the same "
+                                       "sample on 1 thread, %.1f s" % (m, d1)}
+        out["thread_scaling"] = out["value"] / out["one_thread"]["value"]
+    return out
 
 
 def run_reference_arm(args, rank, world):
@@ -219,7 +241,8 @@ def run_reference_arm(args, rank, world):
     vals, steps = [], []
     base = None
     for k in range(args.warmup + args.steps):
-        r = cpu_baseline(n, args.seed, first_event=k * n)
+        r = cpu_baseline(n, args.seed, first_event=k * n,
+                         single=(k == args.warmup + args.steps - 1))
         if k >= args.warmup:
             vals.append(r["value"])
             steps.append(r["steps_per_s"])
@@ -238,7 +261,10 @@ def run_reference_arm(args, rank, world):
         "steps_per_s": sum(steps) / len(steps),
         "cpu_baseline": {"value": value, "unit": "events/s",
                          "cores": base["cores"], "kind": "port",
-                         "sample": base["sample"]},
+                         "sample": base["sample"], "nproc": base["nproc"],
+                         "omp_max_threads": base["omp_max_threads"],
+                         "one_thread": base.get("one_thread"),
+                         "thread_scaling": base.get("thread_scaling")},
         "e2e": {"value": value, "unit": "events/s",
                 "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -267,7 +293,9 @@ class DeviceEvents:
         self.cols["decayed"] = torch.from_numpy(
             np.ascontiguousarray(states["decayed"])).to(dev)
         self.work = {k: v.clone() for k, v in self.cols.items()}
-        self.results = torch.zeros((self.n, 32), dtype=torch.uint8,
+        import pumas_gb300 as pg
+        self.rsize = pg.RESULT_DTYPE.itemsize
+        self.results = torch.zeros((self.n, self.rsize), dtype=torch.uint8,
                                    device=dev)
 
     def restore(self, stream=None):
@@ -285,7 +313,7 @@ class DeviceEvents:
                          for k in range(3)]
         d["direction"] = [w["direction%d" % k].data_ptr() + 8 * offset
                           for k in range(3)]
-        d["result"] = self.results.data_ptr() + 32 * offset
+        d["result"] = self.results.data_ptr() + self.rsize * offset
         return d
 
     def result_records(self):
@@ -323,18 +351,21 @@ def base_line(args, world, metric, value, unit, ms_per_step, config,
             "data": "synthetic", "config": config}
 
 
-def run_slab_jobs(args, rank, world, local):
-    """Batched uneven jobs: every job of the slab-stack workload in one
-    engine run (one pool, CUDA graph batches) against one plain
-    one-thread-per-event launch per job, on the same device-resident
-    events."""
+def measure_slab_jobs(args, physics, dev, scale, steps, warmup,
+                      plain_stride=8, cpu_stride=100, baseline=True,
+                      autotune=False):
+    """Batched uneven jobs (the slab-stack workload at `scale` times its
+    events per job): every job in one engine run (one pool, CUDA graph
+    batches) per step, against one plain one-thread-per-event launch per
+    job on every plain_stride-th job, and the C restatement over all host
+    cores on every cpu_stride-th job, whose events are also compared with
+    the GPU's. Returns a dict of the measurements."""
     import numpy as np
     import torch
     import pumas_gb300 as pg
+    from pumas_gb300 import serving
     from pumas_gb300 import workloads as W
-    dev = torch.device("cuda", local)
-    physics = pg.Physics()
-    jobs = W.slab_jobs(args.jobs, seed=args.seed, event_scale=args.job_scale)
+    jobs = W.slab_jobs(args.jobs, seed=args.seed, event_scale=scale)
     t0 = time.perf_counter()
     ctxs, states, offsets = [], [], []
     off = 0
@@ -353,8 +384,10 @@ def run_slab_jobs(args, rank, world, local):
     spec = [(c, job["n"], None, job["first_event"])
             for c, job in zip(ctxs, jobs)]
     tuned = None
-    if args.autotune:
-        from pumas_gb300 import autotune
+    pool = dict(pool_slots=args.pool_slots, max_inner=args.max_inner,
+                batch=args.batch, tail=args.tail)
+    if autotune:
+        from pumas_gb300 import autotune as at
 
         def sample_run(eng):
             ev.restore()
@@ -362,38 +395,25 @@ def run_slab_jobs(args, rank, world, local):
                      enumerate(zip(spec, offsets)) if k % 8 == 0])
             torch.cuda.synchronize()
 
-        tuned = autotune.tune(physics, sample_run)
-        autotune.save(tuned)
-        args.pool_slots = tuned["pool_slots"]
-        args.max_inner = tuned["max_inner"]
-        args.batch = tuned["batch"]
-        args.tail = tuned["tail"]
-    eng = pg.Engine(physics, pool_slots=args.pool_slots,
-                    max_inner=args.max_inner, batch=args.batch,
-                    max_jobs=len(jobs) + 1, tail=args.tail)
+        tuned = at.tune(physics, sample_run)
+        at.save(tuned)
+        pool = {k: tuned[k] for k in pool}
+    eng = pg.Engine(physics, max_jobs=len(jobs) + 1, **pool)
 
-    def batched():
+    def batched(sub=None):
         ev.restore()
         torch.cuda.synchronize()
         t = time.perf_counter()
-        eng.run([(c, n, ev.soa(o), fe)
-                 for (c, n, _, fe), o in zip(spec, offsets)])
+        ks = range(len(jobs)) if sub is None else sub
+        eng.run([(spec[k][0], spec[k][1], ev.soa(offsets[k]), spec[k][3])
+                 for k in ks])
         torch.cuda.synchronize()
         return time.perf_counter() - t
 
     stream = torch.cuda.Stream(device=dev)
     # The one-launch-per-job comparison runs on every plain_stride-th job
     # (the plain form takes minutes on the whole set), both ways.
-    sub = list(range(0, len(jobs), args.plain_stride))
-
-    def batched_subset():
-        ev.restore()
-        torch.cuda.synchronize()
-        t = time.perf_counter()
-        eng.run([(spec[k][0], spec[k][1], ev.soa(offsets[k]), spec[k][3])
-                 for k in sub])
-        torch.cuda.synchronize()
-        return time.perf_counter() - t
+    sub = list(range(0, len(jobs), plain_stride))
 
     def plain():
         ev.restore()
@@ -413,85 +433,107 @@ def run_slab_jobs(args, rank, world, local):
 
     for c in ctxs:
         c.tuning(engine=pg.ENGINE_PLAIN)
-    for _ in range(max(1, args.warmup // 3)):
-        batched()
+    for _ in range(warmup):
+        batched(sub)
     st0 = eng.stats()
-    with ClockSampler(local) as clocks:
-        tb = [batched() for _ in range(args.steps)]
+    tb = [batched() for _ in range(steps)]
     st1 = eng.stats()
     res = ev.result_records()
+    fin = ev.final_states()
     steps_total = float(res["steps"].sum())
-    bad = int(np.count_nonzero(res["status"]))
     n = len(s0)
     n_sub = sum(jobs[k]["n"] for k in sub)
     idx_sub = np.concatenate([np.arange(offsets[k], offsets[k] + jobs[k]["n"])
                               for k in sub])
-    tbs = batched_subset()
+    tbs = batched(sub)
     tp = plain()
     res_p = ev.result_records()
     same = bool(np.array_equal(res_p[idx_sub], res[idx_sub]))
     tb_m = sum(tb) / len(tb)
-    kernel_ms = (st1["kernel_ms"] - st0["kernel_ms"]) / args.steps
+    kernel_ms = (st1["kernel_ms"] - st0["kernel_ms"]) / steps
+    out = {"jobs": len(jobs), "events": n, "event_scale": scale,
+           "events_per_job": [int(min(j["n"] for j in jobs)),
+                              int(max(j["n"] for j in jobs))],
+           "setup_s": setup_s, "batched_s": tb_m,
+           "value": n / tb_m, "unit": "events/s",
+           "steps_per_s": steps_total / tb_m,
+           "steps_per_event": steps_total / n,
+           "event_errors": int(np.count_nonzero(res["status"])),
+           "kernel_ms": kernel_ms,
+           "gpu_launches": (st1["launches"] - st0["launches"]) // steps,
+           "plain": {"value": n_sub / tp, "unit": "events/s",
+                     "ms": tp * 1E+03, "jobs": len(sub), "events": n_sub,
+                     "batched_same_jobs": n_sub / tbs,
+                     "detail": "every %d-th job: one gp_kernel_plain "
+                               "launch per job on one stream, against one "
+                               "engine run of the same jobs" % plain_stride,
+                     "identical_results": same},
+           "batched_over_plain": tp / tbs,
+           "engine": dict(pool, autotuned=None if tuned is None else {
+               "sample": "every 8th job", "trials": tuned["trials"]})}
+    if baseline:
+        cpu, parity = slab_jobs_cpu(jobs, ctxs, states, fin, res, offsets,
+                                    cpu_stride)
+        out["cpu_baseline"] = cpu
+        out["batched_over_cpu"] = out["value"] / cpu["value"]
+        out["parity_cpu_sample"] = parity
+    return out
+
+
+def run_slab_jobs(args, rank, world, local):
+    """Batched uneven jobs (C3), as its own bench line."""
+    import torch
+    import pumas_gb300 as pg
+    dev = torch.device("cuda", local)
+    physics = pg.Physics()
+    with ClockSampler(local) as clocks:
+        m = measure_slab_jobs(args, physics, dev, args.job_scale, args.steps,
+                              max(1, args.warmup // 3), args.plain_stride,
+                              baseline=not args.no_baseline,
+                              autotune=args.autotune)
     peak = fp64_peak_tflops(torch)
-    achieved = F_STEP * steps_total / (kernel_ms * 1E-03) * 1E-12
+    achieved = F_STEP * m["steps_per_s"] * m["batched_s"] / (
+        m["kernel_ms"] * 1E-03) * 1E-12
     if rank != 0:
         return
-    line = base_line(args, world, "events/s", world * n / tb_m, "events/s",
-                     tb_m * 1E+03, {
+    line = base_line(args, world, "events/s", world * m["value"],
+                     "events/s", m["batched_s"] * 1E+03, {
                          "workload": "slab_jobs: %d uneven jobs, 1-8 slabs "
                                      "of rock / water / iron, 50/50 "
                                      "forward / backward, straggled + "
-                                     "mixed" % len(jobs),
-                         "events_per_step": n,
-                         "event_scale": args.job_scale,
-                         "events_per_job": [int(min(j["n"] for j in jobs)),
-                                            int(max(j["n"] for j in jobs))],
-                         "setup_s": setup_s})
-    cpu = None
-    if not args.no_baseline:
-        cpu = slab_jobs_cpu(jobs, ctxs, states, args.seed)
-    line.update({
-        "cpu_baseline": cpu,
-        "impl_detail": "one engine run per step (all jobs in one slot "
-                       "pool, CUDA graph batches)",
-        "steps_per_s": steps_total / tb_m,
-        "steps_per_event": steps_total / n,
-        "event_errors": bad,
-        "plain": {"value": n_sub / tp, "unit": "events/s",
-                  "ms": tp * 1E+03, "jobs": len(sub), "events": n_sub,
-                  "batched_same_jobs": n_sub / tbs,
-                  "detail": "every %d-th job: one gp_kernel_plain launch "
-                            "per job on one stream, against one engine "
-                            "run of the same jobs" % args.plain_stride,
-                  "identical_results": same},
-        "batched_over_plain": tp / tbs,
-        "engine": {"pool_slots": args.pool_slots or 1048576,
-                   "max_inner": args.max_inner or 8,
-                   "batch": args.batch or 16, "tail": args.tail,
-                   "autotuned": None if tuned is None else {
-                       "sample": "every 8th job",
-                       "trials": tuned["trials"]}},
-        "kernel_ms": kernel_ms,
-        "gpu_launches": (st1["launches"] - st0["launches"]) // args.steps,
-        "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak,
-                     "unit": "TFLOP/s", "frac": achieved / peak,
-                     "traffic": None, "f_step": F_STEP},
-        "clocks": clocks.summary()})
+                                     "mixed" % m["jobs"],
+                         "events_per_step": m["events"],
+                         "event_scale": m["event_scale"],
+                         "events_per_job": m["events_per_job"],
+                         "setup_s": m["setup_s"]})
+    line.update({k: v for k, v in m.items() if k not in (
+        "jobs", "events", "event_scale", "events_per_job", "setup_s",
+        "value", "unit")})
+    line["impl_detail"] = ("one engine run per step (all jobs in one slot "
+                           "pool, CUDA graph batches)")
+    line["roofline"] = {"bound": "fp64", "achieved": achieved, "peak": peak,
+                        "unit": "TFLOP/s", "frac": achieved / peak,
+                        "traffic": None, "f_step": F_STEP}
+    line["clocks"] = clocks.summary()
     print(json.dumps(line), flush=True)
 
 
-def slab_jobs_cpu(jobs, ctxs, states, seed, stride=100):
+def slab_jobs_cpu(jobs, ctxs, states, fin, res, offsets, stride=100):
     """The C restatement with OpenMP over all host cores on every
     `stride`-th job of the slab-stack workload (a seeded 1 % job subset),
-    scaled to events/s."""
+    scaled to events/s; its events are compared with the GPU's final
+    states `fin` and results `res` (fraction within 1e-9)."""
+    import numpy as np
     import oracle
     import pumas_gb300 as pg
+    from pumas_gb300 import serving
     from pumas_gb300 import workloads as W
     oracle.build_port()
     port = oracle.Port(pg.default_dump())
     threads = port.max_threads()
     n = 0
     dt = 0.
+    n_close = n_same = 0
     for k in range(0, len(jobs), stride):
         job = jobs[k]
         mats = [port.material_index(m) for m in job["materials"]]
@@ -500,15 +542,38 @@ def slab_jobs_cpu(jobs, ctxs, states, seed, stride=100):
             slab_medium=list(range(len(mats))))
         cfg = oracle.Config(seed=ctxs[k].seed, **W.slab_job_config(job))
         t = time.perf_counter()
-        port.transport(cfg, geo, states[k], job["first_event"], threads)
+        b, rb = port.transport(cfg, geo, states[k], job["first_event"],
+                               threads)
         dt += time.perf_counter() - t
+        sl = slice(offsets[k], offsets[k] + job["n"])
+        same, close = serving.agreement(fin[sl], res[sl], b, rb)
+        n_same += int(same.sum())
+        n_close += int(close.sum())
         n += job["n"]
-    return {"value": n / dt, "unit": "events/s", "cores": threads,
-            "kind": "port",
-            "sample": "every %d-th job (%d jobs, %d events), %.1f s on %d "
-                      "OpenMP threads, one job after the other"
-                      % (stride, (len(jobs) + stride - 1) // stride, n, dt,
-                         threads)}
+    cpu = {"value": n / dt, "unit": "events/s", "cores": threads,
+           "kind": "port", "nproc": os.cpu_count(),
+           "sample": "every %d-th job (%d jobs, %d events), %.1f s on %d "
+                     "OpenMP threads, one job after the other"
+                     % (stride, (len(jobs) + stride - 1) // stride, n, dt,
+                        threads)}
+    parity = {"events": n, "within_1e-9": n_close, "bit_identical": n_same,
+              "fraction_within_1e-9": n_close / max(n, 1)}
+    return cpu, parity
+
+
+def port_transport(states, cfg_dict, geometry_spec, seed, first_event):
+    """The C restatement with OpenMP over all host cores: final states and
+    results of `states` with event ids from first_event."""
+    import oracle
+    import pumas_gb300 as pg
+    oracle.build_port()
+    port = oracle.Port(pg.default_dump())
+    media = [(port.material_index(m), d) for m, d in geometry_spec["media"]]
+    kw = {k: v for k, v in geometry_spec.items()
+          if k not in ("kind", "media")}
+    geo = oracle.make_geometry(geometry_spec["kind"], media, **kw)
+    cfg = oracle.Config(seed=seed, **cfg_dict)
+    return port.transport(cfg, geo, states, first_event, port.max_threads())
 
 
 def port_baseline(name, states, cfg_dict, geometry_spec, seed, first_event,
@@ -597,8 +662,9 @@ def run_terrain(args, rank, world, local):
                                      "1e8 GeV"
                                      % args.per_direction,
                          "events_per_step": n, "setup_s": setup_s})
-    cpu = None
+    cpu = parity = None
     if not args.no_baseline:
+        from pumas_gb300 import serving
         # Every 100th initial state, over all directions, transported with
         # event ids 0 .. n/100 - 1 (a sample of the same distribution).
         sub = np.arange(0, n, 100)
@@ -606,8 +672,20 @@ def run_terrain(args, rank, world, local):
                             W.terrain_spec(), args.seed, 0,
                             "every 100th initial state (%d events)"
                             % len(sub))
+        # Parity: the first events of the workload with their own event
+        # ids, against the GPU's final states.
+        m = min(n, 20000)
+        b, rb = port_transport(s0[:m], W.config_dict("terrain"),
+                               W.terrain_spec(), args.seed, 0)
+        same, close = serving.agreement(fin[:m], res[:m], b, rb)
+        parity = {"events": m, "within_1e-9": int(close.sum()),
+                  "bit_identical": int(same.sum()),
+                  "fraction_within_1e-9": float(close.mean()),
+                  "sample": "the first %d events (event ids 0 .. %d)"
+                            % (m, m - 1)}
     line.update({
         "cpu_baseline": cpu,
+        "parity_cpu_sample": parity,
         "steps_per_s": steps_total / (ms * 1E-03),
         "steps_per_event": steps_total / n,
         "event_errors": int(np.count_nonzero(res["status"])),
@@ -825,7 +903,8 @@ def main():
     cols["decayed"] = torch.from_numpy(
         np.ascontiguousarray(s0["decayed"])).to(dev)
     work = {k: v.clone() for k, v in cols.items()}
-    results = torch.zeros((n, 32), dtype=torch.uint8, device=dev)
+    results = torch.zeros((n, pg.RESULT_DTYPE.itemsize), dtype=torch.uint8,
+                          device=dev)
     soa = {f: work[f].data_ptr() for f in
            ("charge", "energy", "distance", "grammage", "time", "weight",
             "decayed")}
@@ -883,7 +962,7 @@ def main():
                            pin_memory=True)
         hview = np.frombuffer(host.numpy(), dtype=pg.STATE_DTYPE)
         e2e_ms = []
-        for k in range(1 + args.steps):
+        for k in range(1 + min(args.steps, args.e2e_steps)):
             hview[:] = s0
             torch.cuda.synchronize()
             t0 = time.perf_counter()
@@ -923,6 +1002,21 @@ def main():
     if rank == 0 and not args.no_baseline:
         base = cpu_baseline(args.cpu_events or 200_000, args.seed,
                             first_event=first)
+    # The batched-jobs and serving targets, measured once after the timed
+    # region on this rank's GPU.
+    c3 = c4 = None
+    if rank == 0 and not args.no_c3:
+        c3 = measure_slab_jobs(args, physics, dev, args.c3_scale, 1, 1,
+                               baseline=not args.no_baseline)
+        c3["workload"] = ("slab_jobs: %d uneven jobs, 1-8 slabs of rock / "
+                          "water / iron, 50/50 forward / backward, "
+                          "straggled + mixed, events per job x %g"
+                          % (c3["jobs"], c3["event_scale"]))
+    if rank == 0 and not args.no_c4:
+        from pumas_gb300 import serving
+        c4 = serving.sweep(physics, [float(x) for x in
+                                     args.rates.split(",")],
+                           args.serve_seconds, args.serve_scale, args.seed)
     if rank != 0:
         return
     line = {
@@ -945,6 +1039,7 @@ def main():
         "engine": tuning,
         "e2e": e2e, "roofline": roofline, "cpu_baseline": base,
         "clocks": clocks.summary(),
+        "c3": c3, "c4": c4,
     }
     print(json.dumps(line), flush=True)
 

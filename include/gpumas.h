@@ -123,9 +123,15 @@ struct gpumas_result {
         /** Number of geometric step proposals (medium callback calls with a
          * step argument, pumas.c:3182, 5281). */
         int steps;
-        int pad;
-        /** Number of random draws consumed. */
+        /** Box-Muller cache of the event's normal deviates at the end of
+         * the call (step_randn, pumas.c:7016-7029): 1 when `randn_next`
+         * holds the second deviate of a pair, else 0. */
+        int randn_done;
+        /** Position of the event's random stream at the end of the call:
+         * the number of draws consumed since its first call. */
         uint64_t draws;
+        /** The cached deviate, meaningful when randn_done is 1. */
+        double randn_next;
 };
 
 /** Structure of arrays view of events in device memory. Every pointer
@@ -348,6 +354,41 @@ int gpumas_context_tuning_get(
     const struct gpumas_context * context, struct gpumas_tuning * tuning);
 
 /**
+ * Failure detection of the rejection samplings. The reference's rejection
+ * loops have no bound (pumas.c:5839, 6115, 6126, 6241, 6918, 6973, 11208);
+ * on the device each of them stops after `max_trials` trials and the event
+ * ends with GPUMAS_RETURN_INTERNAL_ERROR in its result, the other events of
+ * the call going on unchanged. A new context has 100 000 trials; 0 restores
+ * that default, negative values return GPUMAS_RETURN_VALUE_ERROR. No
+ * counterpart in the reference.
+ */
+int gpumas_context_trials_set(struct gpumas_context * context,
+    int max_trials);
+int gpumas_context_trials_get(const struct gpumas_context * context,
+    int * max_trials);
+
+/**
+ * Events transported over several calls. A reference context keeps its
+ * random engine and its Box-Muller cache from one pumas_context_transport
+ * call to the next (struct simulation_context, pumas.c:426-477; reset only
+ * at creation, pumas.c:2607-2609), so that an event transported in several
+ * calls -- switching energy loss and scattering modes at an energy
+ * threshold, as in examples/pumas/geometry.c:269-312 -- continues its
+ * random sequence. Here each event's random stream is keyed by (seed, event
+ * id). With `carry` set to 1, every transport call starts each event where
+ * its gpumas_result entry says -- stream position `draws`, Box-Muller cache
+ * `randn_done` and `randn_next`, all zero before the first call -- and
+ * leaves the end values there for the next call; the results array is then
+ * required (GPUMAS_RETURN_VALUE_ERROR without it). With 0, the default,
+ * each call starts every event's stream afresh, as a new reference context
+ * per event would. Results of an event over a chain of calls do not depend
+ * on the engine or on what runs beside it.
+ */
+int gpumas_context_carry_set(struct gpumas_context * context, int carry);
+int gpumas_context_carry_get(
+    const struct gpumas_context * context, int * carry);
+
+/**
  * Allocation free form of gpumas_context_transport_device. It has no
  * counterpart in the reference: it exists for callers that cannot allocate
  * device memory while they transport (a host whose allocator owns the GPU
@@ -361,12 +402,17 @@ int gpumas_context_tuning_get(
  * cudaFree; events, of any number n, stream through the slots as in the
  * pool engine and give the same results.
  *
- * The first call on a device looks up the device address of the array
- * (cudaGetSymbolAddress with that device current): make it before any
- * stream capture. Every call shares the array and clears it at its start,
- * so calls that overlap on the GPU (other streams or threads) race and must
- * be serialised by the caller. The call synchronises `stream` before it
- * returns.
+ * The array is reserved on a device when a physics is loaded there
+ * (gpumas_physics_load or gpumas_physics_upload, with that device current:
+ * the CUDA runtime loads the library's device code, and with it the array,
+ * at its first use on a device). Transport calls on that device then only
+ * look up the array's address. Every call shares the array and clears it
+ * at its start, so calls that overlap on the GPU (other streams or threads)
+ * race and must be serialised by the caller. The call waits for `stream`
+ * (cudaStreamSynchronize) between its batches of iterations, so it must not
+ * be made while `stream` is being captured into a CUDA graph. Slots beyond
+ * the number of events are not used; the engine parameters of the context
+ * (gpumas_context_tuning_set: max_inner, tail) apply as in the pool engine.
  */
 #define GPUMAS_STATIC_SLOTS 32768
 int gpumas_context_transport_device_static(struct gpumas_context * context,
@@ -429,7 +475,7 @@ int gpumas_engine_submit(struct gpumas_engine * engine,
 
 /**
  * Queue a job whose events are `pumas_state` records in host memory. The
- * events are copied into the engine's state budget (136 bytes per event)
+ * events are copied into the engine's state budget (144 bytes per event)
  * and back into `states` (and `results`, if not NULL) when the job
  * completes, before its ticket is reported. Returns
  * GPUMAS_RETURN_MEMORY_ERROR, with no side effect, when the budget has no
@@ -491,7 +537,10 @@ int gpumas_bench_dfma(double * tflops);
  * replace the CUDA library functions in the transport, see gp_math.cuh).
  * fn = 2 evaluates the single precision screen of thinned candidates,
  * gp_neglog_beyond(u, p, q, r), for n quadruples x[4 i] .. x[4 i + 3]:
- * y[i] is 1 when it rules the candidate out, else 0. */
+ * y[i] is 1 when it rules the candidate out, else 0. fn = 3 and fn = 4
+ * evaluate the single precision logarithm and exponential of the DCS
+ * interpolation (gp_libmf.cuh: the build host C library's logf and expf on
+ * the DCS domains) at (float)x[i]. */
 int gpumas_math_eval(int fn, size_t n, const double * x, double * y);
 
 /* ------------------------------------------------------------------------ */

@@ -24,7 +24,10 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_LIB = os.path.join(HERE, "_build", "liboracle_port.so")
 REF_LIB = os.path.join(HERE, "_ref", "libpumas_ref.so")
-REFERENCE_DIR = os.environ.get("PUMAS_REFERENCE", "/root/reference")
+# The reference checkout: PUMAS_REFERENCE, else a directory named
+# "reference" beside this repository.
+REFERENCE_DIR = os.environ.get("PUMAS_REFERENCE", os.path.normpath(
+    os.path.join(HERE, "..", "..", "reference")))
 
 # pumas_state layout (pumas.h:289-309), padded to 8 bytes.
 STATE_DTYPE = np.dtype([
@@ -35,7 +38,8 @@ STATE_DTYPE = np.dtype([
 
 RESULT_DTYPE = np.dtype([
     ("event", "i4"), ("medium_in", "i4"), ("medium_out", "i4"),
-    ("status", "i4"), ("steps", "i4"), ("pad", "i4"), ("draws", "u8")])
+    ("status", "i4"), ("steps", "i4"), ("randn_done", "i4"),
+    ("draws", "u8"), ("randn_next", "f8")])
 
 
 # struct oracle_frame (oracle.h): a state, the medium index and the event.
@@ -81,7 +85,8 @@ class Config(ctypes.Structure):
         ("event", ctypes.c_int),
         ("limit_energy", ctypes.c_double), ("limit_distance", ctypes.c_double),
         ("limit_grammage", ctypes.c_double), ("limit_time", ctypes.c_double),
-        ("accuracy", ctypes.c_double), ("seed", ctypes.c_uint64)]
+        ("accuracy", ctypes.c_double), ("seed", ctypes.c_uint64),
+        ("carry", ctypes.c_int)]
 
 
 def make_geometry(kind, media, **kw):
@@ -193,11 +198,15 @@ class _Oracle:
         return v.value
 
     def transport(self, config, geometry, states, first_event=0,
-                  n_threads=1):
+                  n_threads=1, results=None):
         """Transport a copy of `states` (STATE_DTYPE); returns the final
-        states and the per event results."""
+        states and the per event results. With config.carry, each event
+        continues the random state of `results` (a previous call's)."""
         s = np.array(states, dtype=STATE_DTYPE, copy=True, order="C")
-        r = np.zeros(len(s), dtype=RESULT_DTYPE)
+        if results is None:
+            r = np.zeros(len(s), dtype=RESULT_DTYPE)
+        else:
+            r = np.array(results, dtype=RESULT_DTYPE, copy=True, order="C")
         rc = self._transport(ctypes.byref(config), ctypes.byref(geometry),
                              len(s), first_event, s.ctypes.data,
                              r.ctypes.data, n_threads)

@@ -47,6 +47,10 @@ struct oracle_config {
         double limit_time;
         double accuracy;
         uint64_t seed;
+        /* Each event continues the random stream and Box-Muller cache of
+         * its previous call, read from its oracle_result entry, as one
+         * reference context per event kept across calls would. */
+        int carry;
 };
 
 /* Per event outputs besides the state. */
@@ -56,8 +60,9 @@ struct oracle_result {
         int medium_out; /* end medium index, -1 for none */
         int status;     /* enum pumas_return of the transport call */
         int steps;      /* number of geometric step proposals */
-        int pad;
-        uint64_t draws; /* number of random draws */
+        int randn_done; /* Box-Muller cache at the end of the call */
+        uint64_t draws; /* stream position: random draws since the start */
+        double randn_next;
 };
 
 /* A recorded frame (struct pumas_frame, pumas.h:378-395) with the medium

@@ -87,6 +87,15 @@ struct oracle_stream {
         double next;
 };
 
+/* Continue the stream at draw n (the position a previous transport call of
+ * the same event left it at). */
+static inline void oracle_stream_seek(struct oracle_stream * s, uint64_t n)
+{
+        s->n = n;
+        s->next = 0.;
+        if (n & 1) s->next = oracle_uniform(s->seed, 0u, s->event, n);
+}
+
 static inline double oracle_stream_draw(struct oracle_stream * s)
 {
         double u;

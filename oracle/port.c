@@ -3696,16 +3696,22 @@ int oracle_port_transport(const struct oracle_config * cfg,
                 c.rng.seed = cfg->seed;
                 c.rng.event = first_event + k;
                 c.rng.n = 0;
+                struct oracle_result * r = results + k;
+                if (cfg->carry) {
+                        oracle_stream_seek(&c.rng, r->draws);
+                        c.randn_done = r->randn_done;
+                        c.randn_next = r->randn_next;
+                }
                 int event, media[2];
                 const int rc = context_transport(&c, states + k, &event, media);
-                struct oracle_result * r = results + k;
                 r->event = event;
                 r->medium_in = media[0];
                 r->medium_out = media[1];
                 r->status = rc;
                 r->steps = c.steps;
-                r->pad = 0;
+                r->randn_done = c.randn_done;
                 r->draws = c.rng.n;
+                r->randn_next = c.randn_next;
         }
         return RC_SUCCESS;
 }

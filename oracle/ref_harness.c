@@ -233,6 +233,7 @@ int oracle_ref_transport(const struct oracle_config * cfg,
 #pragma omp for schedule(dynamic, 256)
 #endif
                         for (k = 0; k < n; k++) {
+                                struct oracle_result * r = results + k;
                                 data->stream.seed = cfg->seed;
                                 data->stream.event = first_event + k;
                                 data->stream.n = 0;
@@ -240,6 +241,14 @@ int oracle_ref_transport(const struct oracle_config * cfg,
                                 data->steps = 0;
                                 context_->randn_done = 0;
                                 context_->randn_next = 0.;
+                                if (cfg->carry) {
+                                        /* The event's own context as a
+                                         * previous call left it. */
+                                        oracle_stream_seek(
+                                            &data->stream, r->draws);
+                                        context_->randn_done = r->randn_done;
+                                        context_->randn_next = r->randn_next;
+                                }
 
                                 enum pumas_event event = PUMAS_EVENT_NONE;
                                 struct pumas_medium * m[2] = { NULL, NULL };
@@ -248,7 +257,6 @@ int oracle_ref_transport(const struct oracle_config * cfg,
                                 const enum pumas_return rck =
                                     pumas_context_transport(
                                         context, s, &event, m);
-                                struct oracle_result * r = results + k;
                                 r->event = event;
                                 r->medium_in = (m[0] == NULL) ? -1 :
                                     (int)((struct ref_medium *)m[0] - media);
@@ -256,8 +264,9 @@ int oracle_ref_transport(const struct oracle_config * cfg,
                                     (int)((struct ref_medium *)m[1] - media);
                                 r->status = rck;
                                 r->steps = data->steps;
-                                r->pad = 0;
+                                r->randn_done = context_->randn_done;
                                 r->draws = data->stream.n;
+                                r->randn_next = context_->randn_next;
                         }
                         pumas_context_destroy(&context);
                 }
@@ -344,8 +353,9 @@ int oracle_ref_transport_record(const struct oracle_config * cfg,
                     (int)((struct ref_medium *)m[1] - media);
                 r->status = rck;
                 r->steps = data->steps;
-                r->pad = 0;
+                r->randn_done = context_->randn_done;
                 r->draws = data->stream.n;
+                r->randn_next = context_->randn_next;
                 length[k] = recorder->length;
                 const struct pumas_frame * f = recorder->first;
                 int j;

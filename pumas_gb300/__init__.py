@@ -61,7 +61,8 @@ STATE_DTYPE = np.dtype([
     ("pad", "i4")])
 RESULT_DTYPE = np.dtype([
     ("event", "i4"), ("medium_in", "i4"), ("medium_out", "i4"),
-    ("status", "i4"), ("steps", "i4"), ("pad", "i4"), ("draws", "u8")])
+    ("status", "i4"), ("steps", "i4"), ("randn_done", "i4"),
+    ("draws", "u8"), ("randn_next", "f8")])
 # struct gpumas_frame: a recorded state, its medium index and event flags.
 FRAME_DTYPE = np.dtype([("state", STATE_DTYPE), ("medium", "i4"),
                         ("event", "i4")])
@@ -206,6 +207,12 @@ def library(build=False):
             ctypes.POINTER(_Context), ctypes.POINTER(_Tuning)]
         lib.gpumas_context_tuning_get.argtypes = [
             ctypes.POINTER(_Context), ctypes.POINTER(_Tuning)]
+        lib.gpumas_context_trials_set.argtypes = [ctypes.POINTER(_Context), i]
+        lib.gpumas_context_carry_set.argtypes = [ctypes.POINTER(_Context), i]
+        lib.gpumas_context_carry_get.argtypes = [
+            ctypes.POINTER(_Context), ctypes.POINTER(i)]
+        lib.gpumas_context_trials_get.argtypes = [
+            ctypes.POINTER(_Context), ctypes.POINTER(i)]
         lib.gpumas_engine_create.argtypes = [
             pp, vp, ctypes.POINTER(_Tuning), i, sz]
         lib.gpumas_engine_destroy.argtypes = [pp]
@@ -231,6 +238,8 @@ def library(build=False):
                   "gpumas_context_transport",
                   "gpumas_context_transport_device", "gpumas_context_stats",
                   "gpumas_context_tuning_set", "gpumas_context_tuning_get",
+                  "gpumas_context_trials_set", "gpumas_context_trials_get",
+                  "gpumas_context_carry_set", "gpumas_context_carry_get",
                   "gpumas_bench_dfma", "gpumas_random_fill",
                   "gpumas_engine_create", "gpumas_engine_submit",
                   "gpumas_engine_submit_host", "gpumas_engine_step",
@@ -406,11 +415,16 @@ class Context:
             "gpumas_context_geometry_set")
         self.geometry = geometry
 
-    def transport(self, states, first_event=0, check=False):
+    def transport(self, states, first_event=0, check=False, results=None):
         """Transport a copy of `states`; returns (states, results). With
-        `check`, a non-success per event return code raises."""
+        `check`, a non-success per event return code raises. With `carry`
+        set, each event continues the random state of `results` (those of
+        its previous call; zeros for a first call)."""
         s = np.array(states, dtype=STATE_DTYPE, copy=True, order="C")
-        r = np.zeros(len(s), dtype=RESULT_DTYPE)
+        if results is None:
+            r = np.zeros(len(s), dtype=RESULT_DTYPE)
+        else:
+            r = np.array(results, dtype=RESULT_DTYPE, copy=True, order="C")
         rc = self._lib.gpumas_context_transport(
             self._ptr, len(s), s.ctypes.data, r.ctypes.data, first_event)
         if rc != RETURN_SUCCESS and (check or rc >= RETURN_DEVICE_ERROR or
@@ -465,6 +479,35 @@ class Context:
         self._lib.gpumas_context_tuning_get(self._ptr, ctypes.byref(t))
         return {"engine": t.engine, "pool_slots": t.pool_slots,
                 "max_inner": t.max_inner, "batch": t.batch, "tail": t.tail}
+
+    @property
+    def carry(self):
+        """Whether transport calls continue each event's random stream and
+        Box-Muller cache from its results (gpumas_context_carry_set)."""
+        c = ctypes.c_int()
+        _check(self._lib.gpumas_context_carry_get(self._ptr, ctypes.byref(c)),
+               "gpumas_context_carry_get")
+        return bool(c.value)
+
+    @carry.setter
+    def carry(self, on):
+        _check(self._lib.gpumas_context_carry_set(self._ptr, int(bool(on))),
+               "gpumas_context_carry_set")
+
+    @property
+    def max_trials(self):
+        """Trials of a rejection sampling before an event fails with
+        RETURN_INTERNAL_ERROR (gpumas_context_trials_set)."""
+        n = ctypes.c_int()
+        _check(self._lib.gpumas_context_trials_get(self._ptr,
+                                                   ctypes.byref(n)),
+               "gpumas_context_trials_get")
+        return n.value
+
+    @max_trials.setter
+    def max_trials(self, n):
+        _check(self._lib.gpumas_context_trials_set(self._ptr, int(n)),
+               "gpumas_context_trials_set")
 
     def stats(self):
         st = _Stats()

@@ -20,12 +20,16 @@ INCLUDE = os.path.join(ROOT, "include")
 
 SOURCES = ["gp_physics.cu", "gp_transport.cu", "gp_batch.cu"]
 HEADERS = ["gp_internal.h", "gp_device.cuh", "gp_math.cuh",
-           "gp_math_tables.h", "gp_models.cuh", "gp_io.cuh", "gp_context.h"]
+           "gp_math_tables.h", "gp_models.cuh", "gp_io.cuh", "gp_context.h",
+           "gp_libmf.cuh", "gen_libmf_tables.c"]
+# Generated into the build directory by gen_libmf_tables.c from the build
+# host's C library (the one the CPU oracles link).
+LIBMF_TABLES = os.path.join(BUILD, "gp_libmf_tables.h")
 
 NVCC_FLAGS = [
     "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo",
     "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
-    "-I" + INCLUDE, "-I" + CSRC,
+    "-I" + INCLUDE, "-I" + CSRC, "-I" + BUILD,
 ]
 
 
@@ -45,12 +49,37 @@ def _stale():
         return True
     t = os.path.getmtime(LIB)
     deps = [os.path.join(CSRC, s) for s in _sources() + HEADERS] + [
-        os.path.join(INCLUDE, h) for h in ("gpumas.h", "gpumas_geometry.h")]
+        os.path.join(INCLUDE, h) for h in ("gpumas.h", "gpumas_geometry.h")
+    ] + [LIBMF_TABLES]
     return any(os.path.exists(d) and os.path.getmtime(d) > t for d in deps)
+
+
+def libmf_tables(force=False):
+    """Write gp_libmf_tables.h: the arguments where the build host's C
+    library logf / expf differ from the engine's correctly rounded single
+    precision results, over the domains of the DCS evaluation."""
+    src = os.path.join(CSRC, "gen_libmf_tables.c")
+    if (not force and os.path.exists(LIBMF_TABLES) and
+            os.path.getmtime(LIBMF_TABLES) >= max(
+                os.path.getmtime(src),
+                os.path.getmtime(os.path.join(CSRC, "gp_math.cuh")),
+                os.path.getmtime(os.path.join(CSRC, "gp_math_tables.h")))):
+        return LIBMF_TABLES
+    os.makedirs(BUILD, exist_ok=True)
+    exe = os.path.join(BUILD, "gen_libmf_tables")
+    subprocess.check_call([
+        os.environ.get("CC", "gcc"), "-O2", "-std=gnu99",
+        "-ffp-contract=off", "-I" + CSRC, "-o", exe, src, "-lm"])
+    tmp = LIBMF_TABLES + ".tmp"
+    with open(tmp, "w") as f:
+        subprocess.check_call([exe], stdout=f)
+    os.replace(tmp, LIBMF_TABLES)
+    return LIBMF_TABLES
 
 
 def build(force=False, verbose=False, extra_flags=()):
     """Compile and link libgpumas.so if any source changed."""
+    libmf_tables()
     if not force and not _stale():
         return LIB
     os.makedirs(BUILD, exist_ok=True)

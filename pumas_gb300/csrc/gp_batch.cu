@@ -82,6 +82,11 @@ struct gp_pool {
 
 struct gp_counters {
         unsigned long long cursor;
+        /* Slot visits routed so far (continuous step phases ended, and
+         * events run to their end by the drain): a batch of iterations that
+         * leaves it and the cursor unchanged while events remain is a
+         * stall, which the host loops turn into an error. */
+        unsigned long long progress;
         int active;
         int n_done;
         int n_del[2];
@@ -253,12 +258,21 @@ __device__ __forceinline__ void gp_finish(const gp_pool & pool, int slot,
         gp_job_event_done(X, cnt, PI(SI_JOB));
 }
 
+/* Count one unit of progress per calling lane, with one atomic per warp. */
+__device__ __forceinline__ void gp_progress(gp_counters * cnt)
+{
+        cg::coalesced_group g = cg::coalesced_threads();
+        if (g.thread_rank() == 0)
+                atomicAdd(&cnt->progress, (unsigned long long)g.size());
+}
+
 /* Route a slot to its next phase. */
 __device__ __forceinline__ void gp_route(const gp_pool & pool, int slot,
     const gp_launch * X, const gp_job & J, gp_counters * cnt,
     int * del_list, int * ehs_list, int parity, int next, gp_event & e,
     gp_loop & L, int event)
 {
+        gp_progress(cnt);
         if (next == GP_NEXT_DONE) {
                 gp_finish(pool, slot, X, J, cnt, e, event, L.medium);
                 return;
@@ -311,8 +325,7 @@ static __device__ __forceinline__ int gp_refill(const gp_tables & T,
                 job = gp_job_of(X, idx);
                 const gp_job & J = X->jobs[job];
                 const unsigned long long k = idx - J.begin;
-                J.io.load((size_t)k, e);
-                gp_event_init(e, J.cfg.seed, J.first_event + k);
+                J.io.begin((size_t)k, J.cfg, J.first_event + k, e);
                 int medium_in, event = GPUMAS_EVENT_NONE;
                 const int next = gp_transport_begin(
                     T, J.cfg, *J.geometry, e, L, event, medium_in);
@@ -358,7 +371,8 @@ __global__ void __launch_bounds__(128, 1) gp_pool_drain(
         if (!tail) return;
         const gp_tables & T = *Tp;
         int * dcursor = &cnt->drain_next[parity];
-        for (long guard = 0; guard < (1L << 40); guard++) {
+        /* Each pass takes a new slot index: at most P + 1 passes. */
+        for (long guard = 0; guard <= pool.P; guard++) {
                 cg::coalesced_group w = cg::coalesced_threads();
                 int base = 0;
                 if (w.thread_rank() == 0)
@@ -373,8 +387,13 @@ __global__ void __launch_bounds__(128, 1) gp_pool_drain(
                 gp_slot_load(pool, slot, J.cfg, e, L);
                 int event = GPUMAS_EVENT_NONE;
                 int next = GP_NEXT_STEP;
-                for (long s_ = 0; (s_ < (1L << 40)) && (next != GP_NEXT_DONE);
-                     s_++) {
+                /* An event ends within GP_MAX_STEPS steps, each followed by
+                 * at most one DEL and one EHS. */
+                for (long s_ = 0; next != GP_NEXT_DONE; s_++) {
+                        if (s_ > 3L * GP_MAX_STEPS) {
+                                e.status = GPUMAS_RETURN_INTERNAL_ERROR;
+                                break;
+                        }
                         if (next == GP_NEXT_STEP)
                                 next = gp_stepping_step(
                                     T, J.cfg, *J.geometry, e, L, event);
@@ -383,6 +402,7 @@ __global__ void __launch_bounds__(128, 1) gp_pool_drain(
                         else
                                 next = gp_stepping_ehs(T, J.cfg, e, L, event);
                 }
+                gp_progress(cnt);
                 gp_finish(pool, slot, X, J, cnt, e, event, L.medium);
         }
 }
@@ -405,7 +425,11 @@ __global__ void __launch_bounds__(128, GP_STEP_MIN_BLOCKS) gp_pool_step(
         gp_loop L;
         const gp_job * J = X->jobs;
         int slot = -1, k = 0, exhausted = 0;
-        for (long guard = 0; guard < (1L << 40); guard++) {
+        /* Every pass steps each lane that holds a slot; a lane takes at
+         * most P slots (distinct cursor positions), each for at most
+         * max_inner steps. */
+        const long passes = (long)pool.P * max_inner + 2;
+        for (long guard = 0; guard < passes; guard++) {
                 while ((slot < 0) && !exhausted) {
                         cg::coalesced_group w = cg::coalesced_threads();
                         int base = 0;
@@ -825,7 +849,10 @@ __global__ void __launch_bounds__(128, GP_POOL_MIN_BLOCKS) gp_pool_polar(
         gp_pn s;
         const gp_job * J = X->jobs;
         int slot = -1;
-        for (int guard = 0; guard < (1 << 30); guard++) {
+        /* A lane takes at most count events, each needing at most two
+         * searches of 202 evaluations and 100 rejection trials. */
+        const long passes = 1024L * (count + 1);
+        for (long guard = 0; guard < passes; guard++) {
                 if (slot < 0) {
                         /* Take events until one needs a sampling. */
                         while (true) {
@@ -1136,7 +1163,19 @@ struct gpumas_engine {
         /* Statistics. */
         cudaEvent_t t0, t1;
         struct gpumas_engine_stats stats;
+        /* Progress seen after the last batch (stall detection). */
+        unsigned long long seen_cursor, seen_progress;
 };
+
+/* Whether the counters moved since the last batch; records them. */
+static int gp_moved(unsigned long long * cursor, unsigned long long * progress,
+    const gp_counters & c)
+{
+        const int moved = (c.cursor != *cursor) || (c.progress != *progress);
+        *cursor = c.cursor;
+        *progress = c.progress;
+        return moved;
+}
 
 static int gp_fifo_push(gpumas_engine * g, int ticket)
 {
@@ -1173,6 +1212,7 @@ static int gp_engine_pool(gpumas_engine * g, int P)
         gp_pool_carve((char *)g->d_pool, P, &g->view);
         if (g->h_counters != NULL) memset(g->h_counters, 0,
             sizeof(gp_counters));
+        g->seen_cursor = g->seen_progress = 0;
         g->grid_step = gp_step_wave(P, 128);
         rc = gp_check(cudaMemsetAsync(g->view.pool.i + (size_t)SI_PHASE * P,
             0, (size_t)P * sizeof(int), g->stream));
@@ -1349,6 +1389,7 @@ static int gp_engine_restart(gpumas_engine * g)
         g->n_uploaded = 0;
         g->n_reported = 0;
         g->total = 0;
+        g->seen_cursor = g->seen_progress = 0;
         memset(g->h_counters, 0, sizeof(gp_counters));
         return gp_check(cudaMemsetAsync(
             g->view.counters, 0, sizeof(gp_counters), g->stream));
@@ -1413,6 +1454,7 @@ static int gp_engine_batch(gpumas_engine * g)
 {
         cudaStream_t s = g->stream;
         int rc = GPUMAS_RETURN_SUCCESS;
+        const int launched = g->busy;
         if (g->n_uploaded < g->n_jobs) {
                 const int k0 = g->n_uploaded, k = g->n_jobs - g->n_uploaded;
                 rc = gp_check(cudaMemcpyAsync(g->d_jobs + k0, g->h_jobs + k0,
@@ -1457,6 +1499,12 @@ static int gp_engine_batch(gpumas_engine * g)
         }
         g->busy = !((g->h_counters->cursor >= g->total) &&
             (g->h_counters->active == 0));
+        /* A batch that neither took an event from the queue nor moved one
+         * while events remain is a stall (no kernel makes progress): fail
+         * instead of looping. */
+        if (!gp_moved(&g->seen_cursor, &g->seen_progress, *g->h_counters) &&
+            launched && g->busy)
+                return GPUMAS_RETURN_INTERNAL_ERROR;
 
         /* Jobs completed during the batch, in completion order. */
         const int nd = g->h_counters->n_done;
@@ -1573,7 +1621,7 @@ extern "C" int gpumas_engine_submit(struct gpumas_engine * engine,
                     (a.position[0] == NULL) || (a.position[1] == NULL) ||
                     (a.position[2] == NULL) || (a.direction[0] == NULL) ||
                     (a.direction[1] == NULL) || (a.direction[2] == NULL) ||
-                    (a.decayed == NULL))
+                    (a.decayed == NULL) || (cfg.carry && (a.result == NULL)))
                         return GPUMAS_RETURN_VALUE_ERROR;
         }
         rc = gp_engine_room(g);
@@ -1600,6 +1648,8 @@ extern "C" int gpumas_engine_submit_host(struct gpumas_engine * engine,
         const gpumas_geometry * geometry;
         int rc = gp_engine_context(g, context, &cfg, &geometry);
         if (rc != GPUMAS_RETURN_SUCCESS) return rc;
+        if (cfg.carry && (n > 0) && (results == NULL))
+                return GPUMAS_RETURN_VALUE_ERROR;
         rc = gp_engine_room(g);
         if (rc != GPUMAS_RETURN_SUCCESS) return rc;
         gp_job_host info;
@@ -1619,6 +1669,10 @@ extern "C" int gpumas_engine_submit_host(struct gpumas_engine * engine,
                 rc = gp_check(cudaMemcpyAsync(io.aos.states, states,
                     n * sizeof(gpumas_state), cudaMemcpyHostToDevice,
                     g->stream));
+                if ((rc == GPUMAS_RETURN_SUCCESS) && cfg.carry)
+                        rc = gp_check(cudaMemcpyAsync(io.aos.results, results,
+                            n * sizeof(gpumas_result), cudaMemcpyHostToDevice,
+                            g->stream));
                 if (rc != GPUMAS_RETURN_SUCCESS) {
                         gp_arena_free(&g->arena, offset, bytes);
                         return rc;
@@ -1674,10 +1728,10 @@ extern "C" int gpumas_engine_run(struct gpumas_engine * engine,
                 }
                 if (rc != GPUMAS_RETURN_SUCCESS) return rc;
         }
-        for (long it = 0; g->inflight > 0 || g->busy; it++) {
+        while (g->inflight > 0 || g->busy) {
+                /* Ends: every batch moves an event or fails (stall). */
                 const int rc = gp_engine_batch(g);
                 if (rc != GPUMAS_RETURN_SUCCESS) return rc;
-                if (it > (1L << 40)) return GPUMAS_RETURN_INTERNAL_ERROR;
         }
         /* Completions of a run are not reported as tickets. */
         g->fifo_n = 0;
@@ -1735,12 +1789,9 @@ extern "C" int gp_pool_transport(gp_context * c, const gp_config * cfg,
                 rc = gp_engine_append(g, *cfg, c->d_geometry, *io, n, first,
                     info, &ticket);
         }
-        for (long it = 0; (rc == GPUMAS_RETURN_SUCCESS) &&
-             (g->inflight > 0 || g->busy);
-             it++) {
+        /* Ends: every batch moves an event or fails (stall). */
+        while ((rc == GPUMAS_RETURN_SUCCESS) && (g->inflight > 0 || g->busy))
                 rc = gp_engine_batch(g);
-                if (it > (1L << 40)) rc = GPUMAS_RETURN_INTERNAL_ERROR;
-        }
         g->fifo_n = 0;
         g->fifo_head = 0;
         g->stream = own;
@@ -1762,8 +1813,12 @@ extern "C" int gp_pool_transport(gp_context * c, const gp_config * cfg,
 /* arenas, a plugin embedded in a framework that forbids allocation on its  */
 /* hot path, or code that must not pay (or fail on) a cudaMalloc in the     */
 /* middle of a run. For them the slot pool of the pool engine also exists   */
-/* as one static device array, reserved when the library is loaded on a     */
-/* device and kept until the process exits.                                 */
+/* as one static device array. The CUDA runtime loads the library's device  */
+/* code on a device lazily, at its first use there, and reserves the array  */
+/* then: gp_static_reserve does that when a physics is loaded onto the      */
+/* device (gpumas_physics_load / _upload), where the caller allocates       */
+/* anyway, so that the transport calls themselves allocate nothing. The     */
+/* array is kept until the process exits.                                   */
 /* ------------------------------------------------------------------------ */
 
 /* Largest pool of the allocation free entry point, in event slots
@@ -1783,24 +1838,26 @@ extern "C" int gp_pool_transport(gp_context * c, const gp_config * cfg,
 
 static __device__ __align__(256) unsigned char gp_static_pool[GP_STATIC_BYTES];
 
-/* Device address of gp_static_pool on each device, found once per device
- * with that device current (a host side use of the symbol itself is not a
- * device address). */
-#define GP_STATIC_DEVICES 64
-static void * gp_static_address[GP_STATIC_DEVICES];
-
-static int gp_static_setup(int device, void ** address)
+/* Device address of gp_static_pool on the current device (a host side use
+ * of the symbol itself is not a device address). The lookup loads this
+ * file's device code on the current device if it is not loaded yet, which
+ * reserves the array there. It is made at every call: once the code is
+ * loaded it is a table lookup of the runtime, safe from several host
+ * threads, and it stays right after a device reset. */
+static int gp_static_setup(void ** address)
 {
-        if ((device < 0) || (device >= GP_STATIC_DEVICES))
+        void * ptr = NULL;
+        if (cudaGetSymbolAddress(&ptr, gp_static_pool) != cudaSuccess)
                 return GPUMAS_RETURN_DEVICE_ERROR;
-        if (gp_static_address[device] == NULL) {
-                void * ptr = NULL;
-                if (cudaGetSymbolAddress(&ptr, gp_static_pool) != cudaSuccess)
-                        return GPUMAS_RETURN_DEVICE_ERROR;
-                gp_static_address[device] = ptr;
-        }
-        *address = gp_static_address[device];
+        *address = ptr;
         return GPUMAS_RETURN_SUCCESS;
+}
+
+/* Reserve the static array on the current device (at physics load). */
+extern "C" int gp_static_reserve(void)
+{
+        void * ptr = NULL;
+        return gp_static_setup(&ptr);
 }
 
 extern "C" int gpumas_context_transport_device_static(
@@ -1821,16 +1878,17 @@ extern "C" int gpumas_context_transport_device_static(
         int rc = gp_config_check(context, c->physics, &cfg);
         if (rc != GPUMAS_RETURN_SUCCESS) return rc;
         if (n == 0) return GPUMAS_RETURN_SUCCESS;
+        if (cfg.carry && (events->result == NULL))
+                return GPUMAS_RETURN_VALUE_ERROR;
 
-        int device = 0;
-        if (cudaGetDevice(&device) != cudaSuccess)
-                return GPUMAS_RETURN_DEVICE_ERROR;
         void * base = NULL;
-        rc = gp_static_setup(device, &base);
+        rc = gp_static_setup(&base);
         if (rc != GPUMAS_RETURN_SUCCESS) return rc;
 
-        /* Carve the static array: the pool of P slots, then the job. */
-        const int P = pool_slots;
+        /* Carve the static array: the pool of P slots, then the job. No more
+         * slots than events, as in gp_pool_transport. */
+        int P = pool_slots;
+        if ((size_t)P > n) P = (int)((n + 127) / 128 * 128);
         gp_pool_view v;
         gp_pool_carve((char *)base, P, &v);
         gp_job * job = (gp_job *)((char *)base + GP_STATIC_POOL_BYTES);
@@ -1863,9 +1921,11 @@ extern "C" int gpumas_context_transport_device_static(
         h.job_done = job_done;
         h.done_list = done_list;
         h.n_jobs = 1;
-        h.max_inner = (c->tuning.max_inner > 0) ? c->tuning.max_inner : 1;
+        const unsigned int grid_step = gp_step_wave(P, 128);
+        h.max_inner = (c->tuning.max_inner > 0) ? c->tuning.max_inner : 8;
         h.total = n;
-        h.tail_slots = 0;
+        h.tail_slots = (c->tuning.tail > 0) ? c->tuning.tail :
+            (c->tuning.tail < 0) ? (int)(grid_step * 128) : 0;
         if (rc == GPUMAS_RETURN_SUCCESS)
                 rc = gp_check(cudaMemcpyAsync(job, &hj, sizeof(hj),
                     cudaMemcpyHostToDevice, s));
@@ -1876,9 +1936,9 @@ extern "C" int gpumas_context_transport_device_static(
                 rc = gp_check(cudaStreamSynchronize(s));
         if (rc != GPUMAS_RETURN_SUCCESS) return rc;
 
-        const unsigned int grid_step = gp_step_wave(P, 128);
         const int batch = 16;
-        for (long it = 0;; it++) {
+        unsigned long long seen_cursor = 0, seen_progress = 0;
+        for (;;) {
                 for (int k = 0; k < batch; k++)
                         gp_iteration(c->d_tables, v, grid_step, k & 1, s);
                 rc = gp_check(cudaGetLastError());
@@ -1890,7 +1950,10 @@ extern "C" int gpumas_context_transport_device_static(
                         rc = gp_check(cudaStreamSynchronize(s));
                 if (rc != GPUMAS_RETURN_SUCCESS) return rc;
                 if ((hc.cursor >= n) && (hc.active == 0)) break;
-                if (it > (1L << 40)) return GPUMAS_RETURN_INTERNAL_ERROR;
+                /* A batch that neither took an event from the queue nor
+                 * moved one is a stall: fail instead of looping. */
+                if (!gp_moved(&seen_cursor, &seen_progress, hc))
+                        return GPUMAS_RETURN_INTERNAL_ERROR;
         }
         return GPUMAS_RETURN_SUCCESS;
 }

@@ -40,6 +40,8 @@ struct gp_context {
         struct gp_tuning tuning;
         struct gpumas_recorder recorder; /* frames, if recording */
         int recording;
+        int max_trials; /* rejection sampling cap (gp_config.max_trials) */
+        int carry;      /* continue events across calls (gp_config.carry) */
 };
 
 

@@ -32,6 +32,7 @@
 #include <stdint.h>
 
 #include "gp_math.cuh"
+#include "gp_libmf.cuh"
 #include "gp_models.cuh"
 
 #include "gpumas.h"
@@ -55,8 +56,9 @@
 #define GP_DBL_EPSILON 2.2204460492503131E-16
 #define GP_DBL_MAX 1.7976931348623157E+308
 
-/* Iteration cap of the reference's unbounded rejection loops. */
-#define GP_MAX_REJECTIONS 100000
+/* Default iteration cap of the reference's unbounded rejection loops
+ * (gp_config.max_trials, gpumas_context_trials_set). */
+#define GP_MAX_REJECTIONS_DEFAULT 100000
 
 #define GPD static __device__ __forceinline__
 
@@ -74,6 +76,13 @@ struct gp_config {
         double limit_energy, limit_distance, limit_grammage, limit_time;
         double accuracy;
         uint64_t seed;
+        /* Trials of a rejection sampling before the event fails with
+         * GPUMAS_RETURN_INTERNAL_ERROR (GP_MAX_REJECTIONS_DEFAULT by
+         * default). */
+        int max_trials;
+        /* Events continue the random stream and Box-Muller cache of their
+         * previous call, read from their result entry (gpumas_result). */
+        int carry;
 };
 
 /* ------------------------------------------------------------------------ */
@@ -1170,9 +1179,10 @@ static __device__ double gp_dcs_process(const gp_tables & T, int process,
         }
 }
 
-/* Single precision log and exp, rounded from double precision. */
-GPD float gp_logf(float x) { return (float)gp_log((double)x); }
-GPD float gp_expf(float x) { return (float)gp_exp((double)x); }
+/* Single precision log and exp with the C library's results on the DCS
+ * domains (gp_libmf.cuh). */
+GPD float gp_logf(float x) { return gp_libm_logf(x); }
+GPD float gp_expf(float x) { return gp_libm_expf(x); }
 
 /* dcs_evaluate (pumas.c:11243-11347). */
 static __device__ double gp_dcs_evaluate(const gp_tables & T, int process,
@@ -1705,8 +1715,9 @@ static __device__ __forceinline__ double gp_polar(const gp_tables & T, gp_event 
 /* ------------------------------------------------------------------------ */
 
 /* dcs_ionisation_randomise (pumas.c:11185-11226). */
-static __device__ __forceinline__ double gp_ionisation_randomise(const gp_tables & T, gp_event & e,
-    const gp_element & el, double K, double xlow)
+static __device__ __forceinline__ double gp_ionisation_randomise(const gp_tables & T,
+    const gp_config & cfg, gp_event & e, const gp_element & el, double K,
+    double xlow)
 {
         const double P2 = K * (K + 2. * T.mass);
         const double E = K + T.mass;
@@ -1725,7 +1736,7 @@ static __device__ __forceinline__ double gp_ionisation_randomise(const gp_tables
         const double p2 = 1. / Wmin - 1. / Wmax;
         double q = 0.;
         int trials;
-        for (trials = 0; trials < GP_MAX_REJECTIONS; trials++) {
+        for (trials = 0; trials < cfg.max_trials; trials++) {
                 double z = gp_random(e) * (p0 + p2);
                 if (z <= p0) {
                         z /= p0;
@@ -1738,7 +1749,7 @@ static __device__ __forceinline__ double gp_ionisation_randomise(const gp_tables
                 const double r1 = r0 - a1 / q;
                 if (gp_random(e) * r0 <= r1) break;
         }
-        if (trials == GP_MAX_REJECTIONS) e.status = GPUMAS_RETURN_INTERNAL_ERROR;
+        if (trials == cfg.max_trials) e.status = GPUMAS_RETURN_INTERNAL_ERROR;
         return K - q;
 }
 
@@ -1817,11 +1828,11 @@ static __device__ __forceinline__ void gp_del_target(const gp_tables & T, const 
         }
         double zeta = 0.;
         int trials;
-        for (trials = 0; trials < GP_MAX_REJECTIONS; trials++) {
+        for (trials = 0; trials < cfg.max_trials; trials++) {
                 zeta = gp_random(e) * stot;
                 if ((zeta > 0.) && (zeta < stot)) break;
         }
-        if (trials == GP_MAX_REJECTIONS) e.status = GPUMAS_RETURN_INTERNAL_ERROR;
+        if (trials == cfg.max_trials) e.status = GPUMAS_RETURN_INTERNAL_ERROR;
         /* The energy transfer and the weight share a union in the reference
          * (struct del_info, pumas.c:643-655): the selection below evaluates
          * the DCS at an energy transfer equal to stot (pumas.c:6250). */
@@ -1861,7 +1872,7 @@ static __device__ __forceinline__ bool gp_del_forward(const gp_tables & T, const
         process = ip;
         if (ip == 3) {
                 e.energy = gp_ionisation_randomise(
-                    T, e, el, e.energy, T.cutoff);
+                    T, cfg, e, el, e.energy, T.cutoff);
                 return true;
         }
         double qmin, qmax;
@@ -1967,7 +1978,7 @@ static __device__ __forceinline__ bool gp_del_reverse(const gp_tables & T, const
                 const double x0 = pow(xf, a1);
                 const double x1 = pow(xmax, a1);
                 int trials;
-                for (trials = 0; trials < GP_MAX_REJECTIONS; trials++) {
+                for (trials = 0; trials < cfg.max_trials; trials++) {
                         const double z = gp_random(e);
                         const double tmp = x0 + z * (x1 - x0);
                         r = pow(tmp, 1. / a1);
@@ -1975,7 +1986,7 @@ static __device__ __forceinline__ bool gp_del_reverse(const gp_tables & T, const
                         w_bias = (x1 - x0) * r / (a1 * tmp);
                         break;
                 }
-                if (trials == GP_MAX_REJECTIONS) {
+                if (trials == cfg.max_trials) {
                         e.status = GPUMAS_RETURN_INTERNAL_ERROR;
                         return false;
                 }
@@ -2134,7 +2145,7 @@ static __device__ __forceinline__ void gp_do_ehs(const gp_tables & T, const gp_c
         }
         double mu1 = mu0;
         int trials;
-        for (trials = 0; trials < GP_MAX_REJECTIONS; trials++) {
+        for (trials = 0; trials < cfg.max_trials; trials++) {
                 const double zeta = gp_random(e);
                 const double tmp = 1. + A - zeta * (1 - mu0);
                 if (tmp <= 0.) continue;
@@ -2152,7 +2163,7 @@ static __device__ __forceinline__ void gp_do_ehs(const gp_tables & T, const gp_c
                 ratio *= ratio * (1. - fspin * mu1);
                 if (gp_random(e) <= ratio) break;
         }
-        if (trials == GP_MAX_REJECTIONS) e.status = GPUMAS_RETURN_INTERNAL_ERROR;
+        if (trials == cfg.max_trials) e.status = GPUMAS_RETURN_INTERNAL_ERROR;
         const double gamma = fCM[0];
         const double tau = fCM[1];
         double mu;
@@ -2199,8 +2210,8 @@ static __device__ __forceinline__ void gp_fluctuate(const gp_tables & T, const g
                         do {
                                 u = gp_randn(e);
                         } while ((fabs(u) > 3.) &&
-                            (++trials < GP_MAX_REJECTIONS));
-                        if (trials == GP_MAX_REJECTIONS)
+                            (++trials < cfg.max_trials));
+                        if (trials == cfg.max_trials)
                                 e.status = GPUMAS_RETURN_INTERNAL_ERROR;
                         u *= 1. / 1.015387;
                         k1 += u * dk1;
@@ -2825,8 +2836,8 @@ static __device__ __forceinline__ int gp_step(const gp_tables & T, const gp_conf
                 int trials = 0;
                 do {
                         mu = -ilb1 * gp_log(gp_random(e));
-                } while ((mu > 1.) && (++trials < GP_MAX_REJECTIONS));
-                if (trials == GP_MAX_REJECTIONS)
+                } while ((mu > 1.) && (++trials < cfg.max_trials));
+                if (trials == cfg.max_trials)
                         e.status = GPUMAS_RETURN_INTERNAL_ERROR;
                 gp_rotate(e, mu);
         }
@@ -3444,6 +3455,23 @@ static __device__ __forceinline__ int gp_transport_csda(const gp_tables & T, con
         if (rec != NULL)
                 gp_rec_frame(rec, e, medium, event | GPUMAS_EVENT_STOP);
         return event;
+}
+
+/* Continue an event's random stream at draw n, with the Box-Muller cache
+ * of its previous call (the per context state that the reference keeps
+ * between transport calls, pumas.c:426-477). */
+GPD void gp_event_carry(gp_event & e, uint64_t n, int randn_done,
+    double randn_next)
+{
+        e.n = (uint32_t)n;
+        if (e.n & 1u) {
+                uint32_t x[4];
+                gp_philox(e.n >> 1, 0u, (uint32_t)e.id,
+                    (uint32_t)(e.id >> 32), e.k0, e.k1, x);
+                e.rnext = gp_word_to_uniform(x[2], x[3]);
+        }
+        e.randn_done = randn_done;
+        e.randn_next = randn_next;
 }
 
 /* Prepare the event context for a new transport call. */

@@ -161,6 +161,9 @@ extern "C" {
 #endif
 int gp_physics_tables(const struct gpumas_physics * physics,
     struct gp_tables * tables);
+/* Reserve the static slot pool of the allocation free entry point on the
+ * current device (gp_batch.cu). */
+int gp_static_reserve(void);
 #ifdef __cplusplus
 }
 #endif

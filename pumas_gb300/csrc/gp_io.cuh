@@ -10,6 +10,23 @@
 /* ------------------------------------------------------------------------ */
 /* Event I/O: array of pumas_state structures or structure of arrays.       */
 /* ------------------------------------------------------------------------ */
+/* Per event results, with the random state that a following call of a
+ * carrying context continues. */
+__device__ __forceinline__ void gp_result_store(gpumas_result & out,
+    const gp_event & e, int event, int m_in, int m_out)
+{
+        gpumas_result r;
+        r.event = event;
+        r.medium_in = m_in;
+        r.medium_out = m_out;
+        r.status = e.status;
+        r.steps = e.steps;
+        r.randn_done = e.randn_done;
+        r.draws = e.n;
+        r.randn_next = e.randn_next;
+        out = r;
+}
+
 struct gp_io_aos {
         gpumas_state * states;
         gpumas_result * results;
@@ -43,17 +60,13 @@ struct gp_io_aos {
                         s.direction[k] = e.dir[k];
                 }
                 s.decayed = e.decayed;
-                if (results != NULL) {
-                        gpumas_result r;
-                        r.event = event;
-                        r.medium_in = m_in;
-                        r.medium_out = m_out;
-                        r.status = e.status;
-                        r.steps = e.steps;
-                        r.pad = 0;
-                        r.draws = e.n;
-                        results[i] = r;
-                }
+                if (results != NULL) gp_result_store(results[i], e, event,
+                    m_in, m_out);
+        }
+        __device__ void load_carry(size_t i, gp_event & e) const
+        {
+                const gpumas_result & r = results[i];
+                gp_event_carry(e, r.draws, r.randn_done, r.randn_next);
         }
 };
 
@@ -87,17 +100,13 @@ struct gp_io_soa {
                         a.direction[k][i] = e.dir[k];
                 }
                 a.decayed[i] = e.decayed;
-                if (a.result != NULL) {
-                        gpumas_result r;
-                        r.event = event;
-                        r.medium_in = m_in;
-                        r.medium_out = m_out;
-                        r.status = e.status;
-                        r.steps = e.steps;
-                        r.pad = 0;
-                        r.draws = e.n;
-                        a.result[i] = r;
-                }
+                if (a.result != NULL) gp_result_store(a.result[i], e, event,
+                    m_in, m_out);
+        }
+        __device__ void load_carry(size_t i, gp_event & e) const
+        {
+                const gpumas_result & r = a.result[i];
+                gp_event_carry(e, r.draws, r.randn_done, r.randn_next);
         }
 };
 
@@ -121,6 +130,23 @@ struct gp_io {
                         aos.store(i, e, event, m_in, m_out);
                 else
                         soa.store(i, e, event, m_in, m_out);
+        }
+        /* Start event i's stream where its previous call left it. */
+        __device__ void load_carry(size_t i, gp_event & e) const
+        {
+                if (aos.states != NULL)
+                        aos.load_carry(i, e);
+                else
+                        soa.load_carry(i, e);
+        }
+        /* An event's setup for a call: state, stream and, when the config
+         * carries, the random state of its previous call. */
+        __device__ void begin(size_t i, const gp_config & cfg, uint64_t id,
+            gp_event & e) const
+        {
+                load(i, e);
+                gp_event_init(e, cfg.seed, id);
+                if (cfg.carry) load_carry(i, e);
         }
 };
 

@@ -666,6 +666,13 @@ static int physics_from_blob(
         t->k.allm_lq0 = log(0.52544 / 0.06527);
         t->k.pair_me_m2 = pow(0.5109989461 / (p.mass * 1E+03), 2.);
 
+        /* Reserve the slot pool of the allocation free entry point on this
+         * device now, while the caller allocates anyway. */
+        if (gp_static_reserve() != GPUMAS_RETURN_SUCCESS) {
+                gpumas_physics_destroy(&ph);
+                return GPUMAS_RETURN_DEVICE_ERROR;
+        }
+
         *out = ph;
         return GPUMAS_RETURN_SUCCESS;
 }

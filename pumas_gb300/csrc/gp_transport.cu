@@ -34,8 +34,7 @@ __global__ void __launch_bounds__(128, 1) gp_kernel_plain(
         const gp_tables & T = *Tp;
         const gpumas_geometry & g = *gp;
         gp_event e;
-        io.load(i, e);
-        gp_event_init(e, cfg.seed, first_event + i);
+        io.begin(i, cfg, first_event + i, e);
         int event, m_in, m_out;
         gp_transport(T, cfg, g, e, event, m_in, m_out);
         io.store(i, e, event, m_in, m_out);
@@ -56,8 +55,7 @@ __global__ void __launch_bounds__(128, 1) gp_kernel_plain_ext(
         const gp_tables & T = *Tp;
         const gpumas_geometry & g = *gp;
         gp_event e;
-        io.load(i, e);
-        gp_event_init(e, cfg.seed, first_event + i);
+        io.begin(i, cfg, first_event + i, e);
         gp_rec r;
         r.frames = recording ?
             recorder.frames + i * (size_t)recorder.max_frames : NULL;
@@ -114,6 +112,7 @@ extern "C" int gpumas_context_create(struct gpumas_context ** context,
         c->tuning.max_inner = 8;
         c->tuning.batch = 16;
         c->tuning.tail = 0;
+        c->max_trials = GP_MAX_REJECTIONS_DEFAULT;
         if (extra_memory > 0) {
                 c->extra = calloc(1, extra_memory);
                 c->api.user_data = c->extra;
@@ -351,6 +350,8 @@ extern "C" int gp_config_check(const struct gpumas_context * context,
         cfg->limit_time = context->limit.time;
         cfg->accuracy = context->accuracy;
         cfg->seed = context->seed;
+        cfg->max_trials = ((const gp_context *)context)->max_trials;
+        cfg->carry = ((const gp_context *)context)->carry;
         return GPUMAS_RETURN_SUCCESS;
 }
 
@@ -438,6 +439,43 @@ extern "C" int gpumas_context_tuning_set(
         return GPUMAS_RETURN_SUCCESS;
 }
 
+extern "C" int gpumas_context_trials_set(
+    struct gpumas_context * context, int max_trials)
+{
+        if ((context == NULL) || (max_trials < 0))
+                return GPUMAS_RETURN_VALUE_ERROR;
+        ((gp_context *)context)->max_trials = (max_trials > 0) ?
+            max_trials : GP_MAX_REJECTIONS_DEFAULT;
+        return GPUMAS_RETURN_SUCCESS;
+}
+
+extern "C" int gpumas_context_carry_set(
+    struct gpumas_context * context, int carry)
+{
+        if ((context == NULL) || (carry < 0) || (carry > 1))
+                return GPUMAS_RETURN_VALUE_ERROR;
+        ((gp_context *)context)->carry = carry;
+        return GPUMAS_RETURN_SUCCESS;
+}
+
+extern "C" int gpumas_context_carry_get(
+    const struct gpumas_context * context, int * carry)
+{
+        if ((context == NULL) || (carry == NULL))
+                return GPUMAS_RETURN_VALUE_ERROR;
+        *carry = ((const gp_context *)context)->carry;
+        return GPUMAS_RETURN_SUCCESS;
+}
+
+extern "C" int gpumas_context_trials_get(
+    const struct gpumas_context * context, int * max_trials)
+{
+        if ((context == NULL) || (max_trials == NULL))
+                return GPUMAS_RETURN_VALUE_ERROR;
+        *max_trials = ((const gp_context *)context)->max_trials;
+        return GPUMAS_RETURN_SUCCESS;
+}
+
 extern "C" int gpumas_context_tuning_get(
     const struct gpumas_context * context, struct gpumas_tuning * tuning)
 {
@@ -464,6 +502,8 @@ extern "C" int gpumas_context_transport_device(struct gpumas_context * context,
         int rc = gp_config_check(context, c->physics, &cfg);
         if (rc != GPUMAS_RETURN_SUCCESS) return rc;
         if (n == 0) return GPUMAS_RETURN_SUCCESS;
+        if (cfg.carry && (events->result == NULL))
+                return GPUMAS_RETURN_VALUE_ERROR;
         gp_io io;
         memset(&io, 0, sizeof(io));
         io.soa.a = *events;
@@ -482,6 +522,7 @@ extern "C" int gpumas_context_transport(struct gpumas_context * context,
         if (rc != GPUMAS_RETURN_SUCCESS) return rc;
         if (n == 0) return GPUMAS_RETURN_SUCCESS;
         if (states == NULL) return GPUMAS_RETURN_VALUE_ERROR;
+        if (cfg.carry && (results == NULL)) return GPUMAS_RETURN_VALUE_ERROR;
 
         const size_t sz_s = n * sizeof(gpumas_state);
         const size_t sz_r = n * sizeof(gpumas_result);
@@ -502,6 +543,9 @@ extern "C" int gpumas_context_transport(struct gpumas_context * context,
         cudaStream_t s = c->stream;
         rc = gp_check(cudaMemcpyAsync(
             io.aos.states, states, sz_s, cudaMemcpyHostToDevice, s));
+        if ((rc == GPUMAS_RETURN_SUCCESS) && cfg.carry)
+                rc = gp_check(cudaMemcpyAsync(io.aos.results, results, sz_r,
+                    cudaMemcpyHostToDevice, s));
         if (rc != GPUMAS_RETURN_SUCCESS) return rc;
         rc = gp_run(c, cfg, io, n, first_event, s, 0);
         if (rc != GPUMAS_RETURN_SUCCESS) return rc;
@@ -601,6 +645,9 @@ __global__ void gp_kernel_math(int fn, size_t n, const double * x, double * y)
         if (fn == 2) {
                 const double * a = x + 4 * i;
                 y[i] = gp_neglog_beyond(a[0], a[1], a[2], a[3]);
+        } else if (fn >= 3) {
+                const float f = (float)x[i];
+                y[i] = (fn == 3) ? gp_libm_logf(f) : gp_libm_expf(f);
         } else {
                 y[i] = (fn == 0) ? gp_log(x[i]) : gp_exp(x[i]);
         }
@@ -609,7 +656,7 @@ __global__ void gp_kernel_math(int fn, size_t n, const double * x, double * y)
 extern "C" int gpumas_math_eval(int fn, size_t n, const double * x,
     double * y)
 {
-        if ((x == NULL) || (y == NULL) || (n == 0) || (fn < 0) || (fn > 2))
+        if ((x == NULL) || (y == NULL) || (n == 0) || (fn < 0) || (fn > 4))
                 return GPUMAS_RETURN_VALUE_ERROR;
         const size_t nx = (fn == 2) ? 4 * n : n;
         double * d = NULL;

@@ -2,10 +2,11 @@
 # Regenerate muon.pumas and tau.pumas (the physics dumps shipped with the
 # package) from materials.xml with the reference library's
 # pumas_physics_create.
-# Needs the reference sources (REFERENCE, default /root/reference).
+# Needs the reference sources (REFERENCE, default: a directory named
+# "reference" beside this repository).
 set -e
 HERE=$(cd "$(dirname "$0")" && pwd)
-REFERENCE=${REFERENCE:-/root/reference}
+REFERENCE=${REFERENCE:-$(cd "$HERE/../../.." && pwd)/reference}
 BUILD="$HERE/_build"
 cc -O3 -std=c99 -ffp-contract=off -I"$REFERENCE/include" \
     -o "$BUILD/make_physics" "$HERE/make_physics.c" "$REFERENCE/src/pumas.c" -lm

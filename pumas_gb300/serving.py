@@ -224,29 +224,26 @@ def percentiles(values):
             "p99": float(np.percentile(v, 99))}
 
 
-def bench(args, rank, world, local):
-    """Serving sweep: Poisson arrivals at each rate of args.rates for
-    args.serve_seconds, continuous batching against the plain
-    one-launch-per-request baseline, p50/p95/p99 latency in ms."""
-    import json
-
-    import pumas_gb300 as pg
-    physics = pg.Physics()
-    mix = RequestMix(physics, seed=args.seed, scale=args.serve_scale)
-    server = Server(physics, pool_slots=args.pool_slots or 65536,
-                    max_inner=args.max_inner or 8, batch=args.batch or 4)
-    rates = [float(x) for x in args.rates.split(",")]
-    rng_seed = args.seed
+def sweep(physics, rates, seconds=2.0, scale=1E-03, seed=7,
+          pool_slots=65536, max_inner=8, batch=4, plain_max=300):
+    """Serving sweep: Poisson arrivals at each rate (requests/s) for
+    `seconds`, continuous batching against the plain one-launch-per-request
+    baseline (on at most plain_max requests of each rate), p50/p95/p99
+    latency in ms. Returns the sweep and the highest sustained rate (served
+    throughput at least 90 % of the offered rate) with its p99."""
+    mix = RequestMix(physics, seed=seed, scale=scale)
+    server = Server(physics, pool_slots=pool_slots, max_inner=max_inner,
+                    batch=batch)
     # Warm-up: a few requests through both paths.
     warm = [mix.make(10 ** 9 + i) for i in range(20)]
     serve_open_loop(server, warm, np.zeros(len(warm)))
     plain_serve([mix.make(10 ** 9 + i) for i in range(5)], np.zeros(5))
-    sweep = []
+    out = []
     best = None
     base = 0
     for rate in rates:
-        n = max(1, int(round(rate * args.serve_seconds)))
-        gaps = -np.log(W.uniform(rng_seed, 5, np.arange(
+        n = max(1, int(round(rate * seconds)))
+        gaps = -np.log(W.uniform(seed, 5, np.arange(
             base, base + n, dtype=np.uint64), 0)) / rate
         arrivals = np.cumsum(gaps) - gaps[0]
         reqs = [mix.make(base + i) for i in range(n)]
@@ -260,9 +257,9 @@ def bench(args, rank, world, local):
                  "events_per_s": events / wall,
                  "latency_ms": percentiles(lat), "event_errors": errors,
                  "sustained": bool(n / wall >= 0.9 * rate)}
-        # The plain baseline on the same arrivals (bounded: at most 300
-        # requests, the first ones).
-        m = min(n, 300)
+        # The plain baseline on the same arrivals (bounded: the first
+        # plain_max requests).
+        m = min(n, plain_max)
         preqs = [mix.make(base + i) for i in range(m)]
         pwall = plain_serve(preqs, arrivals[:m])
         n_ev = n_same = n_close = 0
@@ -279,27 +276,49 @@ def bench(args, rank, world, local):
                           "events_compared": n_ev,
                           "bit_identical_events": n_same,
                           "events_within_1e-9": n_close}
-        sweep.append(entry)
+        out.append(entry)
         if entry["sustained"]:
             best = entry
         base += n
+    return {"sweep": out,
+            "highest_sustained_rate": best["rate"] if best else None,
+            "p99_ms_at_highest_sustained": (best["latency_ms"]["p99"]
+                                            if best else None),
+            "throughput_rps_at_highest_sustained": (
+                best["throughput_rps"] if best else None),
+            "engine": server.engine.stats(),
+            "config": {"event_scale": scale, "seconds_per_rate": seconds,
+                       "state_budget_gb": 40, "pool_slots": pool_slots,
+                       "mix": "70 % slab-stack jobs, 30 % terrain flux "
+                              "queries (1-256 directions)"}}
+
+
+def bench(args, rank, world, local):
+    """Serving sweep over args.rates as its own bench line."""
+    import json
+
+    import pumas_gb300 as pg
+    physics = pg.Physics()
+    rates = [float(x) for x in args.rates.split(",")]
+    r = sweep(physics, rates, args.serve_seconds, args.serve_scale,
+              args.seed, args.pool_slots or 65536, args.max_inner or 8,
+              args.batch or 4)
     if rank != 0:
         return
-    top = best or sweep[0]
+    top = None
+    for e in r["sweep"]:
+        if e["rate"] == r["highest_sustained_rate"]:
+            top = e
+    top = top or r["sweep"][0]
     line = {"metric": "requests/s at p99 latency", "value":
             top["throughput_rps"], "unit": "requests/s", "n_gpus": world,
             "steps": len(rates), "warmup": 1,
             "ms_per_step": 1E+03 * top["wall_s"],
             "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "serve: Poisson arrivals, 70 %% slab-"
-                                   "stack jobs, 30 %% terrain flux queries "
-                                   "(1-256 directions), events x %g"
-                                   % args.serve_scale,
-                       "state_budget_gb": 40,
-                       "pool_slots": args.pool_slots or 65536},
-            "highest_sustained_rate": best["rate"] if best else None,
-            "p99_ms_at_highest_sustained": (best["latency_ms"]["p99"]
-                                            if best else None),
-            "sweep": sweep, "engine": server.engine.stats()}
+            "config": dict(r["config"], workload="serve: Poisson arrivals, "
+                           "70 %% slab-stack jobs, 30 %% terrain flux "
+                           "queries (1-256 directions), events x %g"
+                           % args.serve_scale)}
+    line.update({k: v for k, v in r.items() if k != "config"})
     print(json.dumps(line), flush=True)

@@ -308,3 +308,76 @@ def make_states(name, n=None, first_event=0):
 
 def material_indices(index_of, geometry):
     return [(index_of(m), d) for m, d in geometry["media"]]
+
+
+# Events transported over several calls (the carry of gpumas_result): the
+# two-regime loop of examples/pumas/geometry.c:269-312. Backward muons from a
+# detector at the bottom of a rock layer under the atmosphere: below 100 GeV
+# a detailed simulation (straggled energy loss, mixed scattering, energy
+# limit 100 GeV), above it a fast one (mixed energy loss, no scattering, up
+# to 1000 times the largest detector energy); the loop ends when the muon
+# leaves the geometry or reaches that energy. Each call continues the
+# random stream and Box-Muller cache of the event's previous call, as one
+# reference context per event does.
+FLT_EPSILON = 1.1920928955078125E-07
+CHAIN = dict(
+    geometry=dict(kind=1, media=[("StandardRock", 0.), ("Air", 0.)],
+                  slab_z=[0., 90., 10000.], slab_media=[0, 1]),
+    n=200, seed=61, first_event=4000, energy_min=1., energy_max=1E+03)
+CHAIN_THRESHOLD = CHAIN["energy_max"] * 1E+03
+CHAIN_LOW = _cfg(STRAGGLED, MIXED, BWD, event=LIMIT_ENERGY,
+                 limit_energy=1E+02)
+CHAIN_HIGH = _cfg(MIXED, DISABLED, BWD, event=LIMIT_ENERGY,
+                  limit_energy=CHAIN_THRESHOLD)
+
+
+def chain_states(n=None, seed=None, first=None):
+    """Detector muons as examples/pumas/geometry.c:227-253 draws them: energy
+    log-uniform with weight kf ln(Emax / Emin) times 2 for the charge, random
+    charge, direction at an elevation drawn here uniformly in [5, 90] deg."""
+    c = CHAIN
+    n = c["n"] if n is None else n
+    seed = c["seed"] if seed is None else seed
+    first = c["first_event"] if first is None else first
+    ev = np.arange(first, first + n, dtype=np.uint64)
+    rk = np.log(c["energy_max"] / c["energy_min"])
+    kf = c["energy_min"] * np.exp(rk * W.uniform(seed, 1, ev, 0))
+    # Energies within FLT_EPSILON below 100 GeV would take the fast regime
+    # at once in the loop of the example; keep them out of the sample.
+    kf = np.where(np.abs(kf - 1E+02) < 1E-05, 1.01E+02, kf)
+    elev = np.radians(5. + 85. * W.uniform(seed, 1, ev, 1))
+    s = np.zeros(n, dtype=STATE_DTYPE)
+    s["charge"] = np.where(W.uniform(seed, 1, ev, 2) > 0.5, 1., -1.)
+    s["energy"] = kf
+    s["weight"] = kf * rk * 2.
+    cos_theta = np.cos(0.5 * np.pi - elev)
+    s["direction"][:, 0] = -np.sqrt(1. - cos_theta * cos_theta)
+    s["direction"][:, 2] = -cos_theta
+    return s
+
+
+def run_chain(transport, states, max_calls=16):
+    """Run the loop of examples/pumas/geometry.c:269-312 over a batch.
+
+    `transport(config, states, results)` transports every event of the
+    batch with a carrying context of settings `config` and returns the new
+    (states, results). The loop calls the detailed and the fast settings in
+    turn on the whole batch. In a call whose regime does not apply to an
+    event, the event returns at once without a random draw: above the
+    energy limit of a backward transport (transport_limit,
+    pumas.c:5576-5596) or outside the geometry (pumas.c:3187-3195). So each
+    event sees the same sequence of effective calls as in the example's
+    per-event loop. Returns (states, results, calls)."""
+    from pumas_gb300 import RESULT_DTYPE
+    s = np.array(states, copy=True)
+    r = np.zeros(len(s), dtype=RESULT_DTYPE)
+    calls = 0
+    while calls < max_calls:
+        for cfg in (CHAIN_LOW, CHAIN_HIGH):
+            s, r = transport(cfg, s, r)
+            calls += 1
+        out = (r["event"] == 16) & (r["medium_out"] == -1)
+        done = out | (s["energy"] >= CHAIN_THRESHOLD - FLT_EPSILON)
+        if np.all(done):
+            break
+    return s, r, calls

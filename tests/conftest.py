@@ -17,6 +17,26 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300)")
 
 
+# Parity fractions reported by the GPU tests: name -> (events within
+# tolerance, events). Printed at the end of the run.
+PARITY_REPORT = {}
+
+
+def pytest_terminal_summary(terminalreporter):
+    if not PARITY_REPORT:
+        return
+    tr = terminalreporter
+    tr.section("parity: events within 1e-9 on every field, weight included")
+    good = total = 0
+    for name in sorted(PARITY_REPORT):
+        g, n = PARITY_REPORT[name]
+        good += g
+        total += n
+        tr.write_line("%-40s %8d / %-8d %.5f" % (name, g, n, g / max(n, 1)))
+    tr.write_line("%-40s %8d / %-8d %.5f" % ("all", good, total,
+                                            good / max(total, 1)))
+
+
 @pytest.fixture(scope="session")
 def dump():
     import pumas_gb300

@@ -12,6 +12,9 @@ usage: python tests/golden/make_golden.py [case ...]   (default: all cases)
        python tests/golden/make_golden.py physics   (the physics dumps with
        non-default DCS models of PHYSICS_MODELS, by the reference's
        pumas_physics_create)
+       python tests/golden/make_golden.py chain   (events transported over
+       several calls, the loop of examples/pumas/geometry.c:269-312, see
+       tests/cases.py CHAIN)
 """
 import gzip
 import os
@@ -27,7 +30,8 @@ sys.path.insert(0, os.path.dirname(HERE))
 
 import oracle  # noqa: E402
 import pumas_gb300  # noqa: E402
-from cases import CASES, make_states, physics_dump  # noqa: E402
+from cases import (CASES, CHAIN, chain_states, make_states,  # noqa: E402
+                   physics_dump, run_chain)
 from conftest import oracle_config, oracle_geometry  # noqa: E402
 
 
@@ -99,6 +103,32 @@ def make_frames(ref, names=None):
             name, period, length.mean(), length.max()))
 
 
+CHAIN_FILE = os.path.join(HERE, "chain_geometry_loop.npz")
+
+
+def chain_transport(impl, seed, first_event):
+    """The `transport` callable of cases.run_chain on a CPU oracle: every
+    call carries each event's random state from its previous call."""
+    geo = oracle_geometry(impl, CHAIN["geometry"])
+
+    def transport(cfg, states, results):
+        c = oracle_config(cfg, seed)
+        c.carry = 1
+        return impl.transport(c, geo, states, first_event, 8, results)
+    return transport
+
+
+def make_chain(ref):
+    """The reference's final states after the loop of CHAIN."""
+    s0 = chain_states()
+    s1, r1, calls = run_chain(
+        chain_transport(ref, CHAIN["seed"], CHAIN["first_event"]), s0)
+    np.savez_compressed(CHAIN_FILE, initial=s0, final=s1, results=r1,
+                        calls=calls)
+    print("chain: %d events, %d calls, %.1f draws/event" % (
+        len(s0), calls, r1["draws"].mean()))
+
+
 def main():
     oracle.build_reference()
     dump = pumas_gb300.default_dump()
@@ -113,6 +143,9 @@ def main():
         return
     if args and args[0] == "physics":
         make_physics()
+        return
+    if args and args[0] == "chain":
+        make_chain(ref)
         return
     names = args or list(CASES)
     refs = {"muon": ref}

@@ -1,5 +1,7 @@
-"""The engine's table-driven logarithm and exponential, and its single
-precision screen of thinned candidates (gp_math.cuh).
+"""The engine's table-driven logarithm and exponential, its single
+precision screen of thinned candidates (gp_math.cuh), and the single
+precision logarithm and exponential of the DCS interpolation, which return
+the C library's logf / expf results (gp_libmf.cuh).
 
 They replace the CUDA library functions in the transport (fewer double
 precision instructions on a GPU whose FP64 rate is 1/64 of its FP32 rate).
@@ -18,22 +20,39 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 CSRC = os.path.join(ROOT, "pumas_gb300", "csrc")
 
 
+# Domains of the C library corrections (gen_libmf_tables.c), as float bit
+# patterns [u0, u1): logf of q / K, logf of energy ratios, expf of
+# logarithms of DCS values.
+LIBMF_DOMAINS = [(3, 0x3B800000, 0x3F800000), (3, 0x3F800000, 0x3FC00000),
+                 (4, 0xC0000000, 0xC2800000)]
+
+
 @pytest.fixture(scope="module")
-def host(tmp_path_factory):
+def host_lib(tmp_path_factory):
+    from pumas_gb300 import build as engine_build
+    engine_build.libmf_tables()
     lib = str(tmp_path_factory.mktemp("math") / "libmath_host.so")
     subprocess.check_call([
-        "gcc", "-O2", "-std=c99", "-ffp-contract=off", "-fPIC", "-shared",
-        "-I" + CSRC, "-o", lib, os.path.join(ROOT, "tests", "math_host.c"),
-        "-lm"])
+        "gcc", "-O2", "-std=gnu99", "-ffp-contract=off", "-fPIC", "-shared",
+        "-I" + CSRC, "-I" + engine_build.BUILD, "-o", lib,
+        os.path.join(ROOT, "tests", "math_host.c"), "-lm"])
     h = ctypes.CDLL(lib)
     h.math_host_eval.argtypes = [ctypes.c_int, ctypes.c_size_t,
                                  ctypes.c_void_p, ctypes.c_void_p]
     h.math_host_eval.restype = None
+    h.math_host_libmf_mismatch.argtypes = [
+        ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32,
+        ctypes.POINTER(ctypes.c_float)]
+    h.math_host_libmf_mismatch.restype = ctypes.c_long
+    return h
 
+
+@pytest.fixture(scope="module")
+def host(host_lib):
     def run(fn, x):
         x = np.ascontiguousarray(x, dtype=np.float64)
         y = np.empty(len(x))
-        h.math_host_eval(fn, len(x), x.ctypes.data, y.ctypes.data)
+        host_lib.math_host_eval(fn, len(x), x.ctypes.data, y.ctypes.data)
         return y
     return run
 
@@ -156,3 +175,72 @@ def test_device_screen(host, gpu_physics):
     s = y == 1.
     assert not np.any(s & ~screen_exact(host, x))
     assert np.mean(s == (host(2, x) == 1.)) > 0.999
+
+
+@pytest.mark.parametrize("fn,u0,u1", LIBMF_DOMAINS)
+def test_libmf_equals_c_library(host_lib, fn, u0, u1):
+    """On every float of each DCS domain, the corrected single precision
+    logarithm / exponential returns the bit pattern of this host's C
+    library logf / expf (the functions the reference calls in dcs_evaluate,
+    pumas.c:11279-11343)."""
+    first = ctypes.c_float(0.)
+    n = host_lib.math_host_libmf_mismatch(fn, u0, u1, ctypes.byref(first))
+    assert n == 0, "%d mismatches, first at %r" % (n, first.value)
+
+
+def libmf_arguments(seed=13, n=400000):
+    """Float arguments of the DCS domains: random bit patterns, the first
+    and last float of every correction bucket, and a few values outside the
+    domains; returned as doubles with the function index."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for fn, u0, u1 in LIBMF_DOMAINS:
+        u = np.concatenate([
+            rng.integers(u0, u1, n, dtype=np.uint64),
+            np.arange(u0, u1, 4096, dtype=np.uint64),
+            np.arange(u0 + 4095, u1, 4096, dtype=np.uint64)])
+        x = u.astype(np.uint32).view(np.float32).astype(np.float64)
+        out.append((fn, x))
+    out.append((3, np.array([1E-05, 0.001, 1.5, 3., 1E+06])))
+    out.append((4, np.array([-1., -0.5, -70., -100., 0., 1.])))
+    return out
+
+
+def libmf_inside(fn, x):
+    """Whether float arguments x lie in one of fn's correction domains."""
+    u = x.astype(np.float32).view(np.uint32).astype(np.int64)
+    inside = np.zeros(len(x), bool)
+    for f, u0, u1 in LIBMF_DOMAINS:
+        if f == fn:
+            inside |= (u >= u0) & (u < u1)
+    return inside
+
+
+def test_libmf_host_arguments(host):
+    """The sampled arguments of the device test give the C library's
+    results on the host too (a sanity check of the argument generator)."""
+    for fn, x in libmf_arguments(n=20000):
+        inside = libmf_inside(fn, x)
+        y = host(fn, x)
+        ref = host(fn + 2, x)
+        assert np.array_equal(y[inside], ref[inside])
+
+
+@pytest.mark.gpu
+def test_device_libmf_equals_c_library(host, gpu_physics):
+    """On the device, the single precision logarithm and exponential of the
+    DCS interpolation return this host's C library logf / expf results on
+    the sampled arguments of the DCS domains, and equal the host build of
+    the same code everywhere."""
+    import pumas_gb300 as pg
+    lib = pg.library()
+    lib.gpumas_math_eval.argtypes = [ctypes.c_int, ctypes.c_size_t,
+                                     ctypes.c_void_p, ctypes.c_void_p]
+    lib.gpumas_math_eval.restype = ctypes.c_int
+    for fn, x in libmf_arguments():
+        y = np.empty_like(x)
+        assert lib.gpumas_math_eval(fn, len(x), x.ctypes.data,
+                                    y.ctypes.data) == 0
+        assert np.array_equal(y, host(fn, x))
+        inside = libmf_inside(fn, x)
+        assert np.array_equal(y[inside], host(fn + 2, x)[inside])

@@ -170,3 +170,47 @@ def test_dcs_model_changes_the_transport(port, request, name):
     s1, r1 = port.transport(cfg, geo, data["initial"], 0, 4)
     same, _ = compare(s1, r1, data["final"], data["results"])
     assert same.mean() < 0.5
+
+
+def _chain(impl, seed, first, carry=1):
+    from cases import CHAIN, run_chain, chain_states
+    geo = oracle_geometry(impl, CHAIN["geometry"])
+
+    def transport(cfg, states, results):
+        c = oracle_config(cfg, seed)
+        c.carry = carry
+        return impl.transport(c, geo, states, first, 4, results)
+    n = CHAIN["n"] if first == CHAIN["first_event"] else 64
+    s0 = chain_states(n=n, seed=seed, first=first)
+    return (s0,) + run_chain(transport, s0)
+
+
+def test_port_chain_matches_golden(port):
+    """Events transported over several calls (the loop of
+    examples/pumas/geometry.c:269-312, each call continuing the random
+    stream and Box-Muller cache of the event's previous call): the C
+    restatement reproduces the reference's fixture bit for bit."""
+    from cases import CHAIN
+    data = np.load(os.path.join(GOLDEN, "chain_geometry_loop.npz"))
+    s0, s1, r1, calls = _chain(port, CHAIN["seed"], CHAIN["first_event"])
+    assert np.array_equal(s0, data["initial"])
+    assert calls == int(data["calls"])
+    same, _ = compare(s1, r1, data["final"], data["results"])
+    assert same.all(), "%d / %d events differ" % ((~same).sum(), len(same))
+    for f in ("draws", "randn_done", "randn_next"):
+        assert np.array_equal(r1[f], data["results"][f]), f
+    # The carry matters: the fast regime consumes draws, and restarting
+    # the stream at each call replays those of the detailed regime.
+    _, s2, r2, _ = _chain(port, CHAIN["seed"], CHAIN["first_event"], carry=0)
+    both = s0["energy"] < 1E+02
+    assert np.any(s2["energy"][both] != s1["energy"][both])
+    assert np.array_equal(s2["energy"][~both], s1["energy"][~both])
+
+
+def test_port_chain_matches_reference_fresh_events(port, reference):
+    from cases import CHAIN
+    a = _chain(port, CHAIN["seed"] + 1, 70000)
+    b = _chain(reference, CHAIN["seed"] + 1, 70000)
+    same, _ = compare(a[1], a[2], b[1], b[2])
+    assert same.all()
+    assert np.array_equal(a[2]["draws"], b[2]["draws"])

@@ -4,10 +4,12 @@ Some callers cannot allocate device memory while they transport -- a host
 whose allocator owns the GPU memory, a plugin whose framework forbids
 allocation on its hot path. gpumas_context_transport_device_static serves
 them: its slot pool is a static device array of the library instead of a
-cudaMalloc'ed one. This checks, through the C ABI, that it gives the same
-results as gpumas_context_transport_device on two calls in a row (the second
-call reuses the array the first one left behind), and that pool sizes above
-the static maximum are refused.
+cudaMalloc'ed one, reserved on a device when a physics is loaded there.
+This checks, through the C ABI, that it gives the same results as
+gpumas_context_transport_device, bit for bit, on two calls in a row (the
+second call reuses the array the first one left behind) and with the
+default (largest) pool, and that pool sizes above the static maximum or not
+a multiple of 128 are refused.
 
 Collected last on purpose (file name), so that a run stopping at the first
 failure has run every other test before this one.
@@ -34,7 +36,9 @@ def _columns(torch, states):
             np.ascontiguousarray(states["direction"][:, k])).to(dev)
     cols["decayed"] = torch.from_numpy(
         np.ascontiguousarray(states["decayed"])).to(dev)
-    cols["result"] = torch.zeros((len(states), 32), dtype=torch.uint8,
+    import pumas_gb300 as pg
+    cols["result"] = torch.zeros((len(states), pg.RESULT_DTYPE.itemsize),
+                                 dtype=torch.uint8,
                                  device=dev)
     return cols
 
@@ -77,7 +81,7 @@ def test_static_pool_matches_device_entry_point(gpu_physics):
     ctx.tuning(engine=pg.ENGINE_POOL, pool_slots=4096, max_inner=2)
 
     n = 6000
-    for call in range(2):
+    for call, slots in enumerate((2048, 2048, 0)):
         first = 1000 + call * n
         s0 = W.rock_slab(n, seed=17, first_event=first)
         a_cols = _columns(torch, s0)
@@ -96,7 +100,7 @@ def test_static_pool_matches_device_entry_point(gpu_physics):
         assert rc == 0
         torch.cuda.synchronize()
         soa = _soa(pg, b_cols)
-        rc = fn(ctx._ptr, n, ctypes.byref(soa), first, 2048, None)
+        rc = fn(ctx._ptr, n, ctypes.byref(soa), first, slots, None)
         assert rc == 0
         torch.cuda.synchronize()
         a, b = _host(pg, a_cols), _host(pg, b_cols)
@@ -105,16 +109,20 @@ def test_static_pool_matches_device_entry_point(gpu_physics):
                 continue
             x, y = a[k], b[k]
             assert np.all(np.abs(x - y) <= RTOL * np.maximum(np.abs(x), 1.)), k
+            # The same kernels run the same events: bit for bit.
+            assert x.tobytes() == y.tobytes(), k
         ra, rb = a["result"], b["result"]
         for f in ("event", "medium_in", "medium_out", "status", "steps",
                   "draws"):
             assert np.array_equal(ra[f], rb[f]), f
         assert np.all(rb["status"] == 0)
 
-    # Pool sizes above the static maximum are refused.
+    # Pool sizes above the static maximum, or not a multiple of 128, are
+    # refused.
     soa = _soa(pg, _columns(torch, W.rock_slab(128, seed=1)))
-    assert fn(ctx._ptr, 128, ctypes.byref(soa), 0,
-              2 * pg_static_slots(), None) == pg.RETURN_VALUE_ERROR
+    for slots in (2 * pg_static_slots(), pg_static_slots() + 128, 200, -128):
+        assert fn(ctx._ptr, 128, ctypes.byref(soa), 0, slots,
+                  None) == pg.RETURN_VALUE_ERROR
 
 
 def pg_static_slots():
