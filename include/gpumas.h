@@ -160,9 +160,11 @@ struct gpumas_physics;
  * Load physics tables from the bytes of a `pumas_physics_dump` stream
  * (pumas.c:2167-2196; replaces pumas_physics_load, pumas.h:980-981) and
  * upload them to the current CUDA device. The dump must come from an LP64
- * little-endian host (tag 13) with the default DCS models (SSR, SSR, DRSS)
- * for muons; otherwise GPUMAS_RETURN_FORMAT_ERROR or
- * GPUMAS_RETURN_MODEL_ERROR is returned.
+ * little-endian host (tag 13), for muons or taus, with any of the
+ * reference's DCS models (bremsstrahlung SSR, KKP or ABB; pair production
+ * SSR or KKP; photonuclear DRSS, BBKS or BM); otherwise
+ * GPUMAS_RETURN_FORMAT_ERROR or GPUMAS_RETURN_MODEL_ERROR (an unknown
+ * model name) is returned.
  */
 int gpumas_physics_load(
     struct gpumas_physics ** physics, const void * dump, size_t size);
@@ -189,8 +191,8 @@ int gpumas_physics_info(const struct gpumas_physics * physics,
 
 /** Transported particle (GPUMAS_PARTICLE_MUON or GPUMAS_PARTICLE_TAU), its
  * proper lifetime c tau in m and its mass in GeV/c^2. Replaces
- * `pumas_physics_particle` (pumas.h:1106-1108). The particle comes from
- * the physics dump: both are tabulated with the default models. */
+ * `pumas_physics_particle` (pumas.h:1106-1108). The particle, and the DCS
+ * models, come from the physics dump. */
 int gpumas_physics_particle(const struct gpumas_physics * physics,
     int * particle, double * lifetime, double * mass);
 
@@ -522,6 +524,54 @@ struct gpumas_stats {
 };
 int gpumas_context_stats(
     const struct gpumas_context * context, struct gpumas_stats * stats);
+
+/* ------------------------------------------------------------------------ */
+/* Errors.                                                                  */
+/* ------------------------------------------------------------------------ */
+
+/** A library function, as given to an error handler (pumas_function_t,
+ * pumas.h:519). */
+typedef void gpumas_function_t(void);
+
+/** An error handler (pumas_handler_cb, pumas.h:532-533): the return code,
+ * the library function that returned it and a message. */
+typedef void gpumas_handler_cb(
+    int rc, gpumas_function_t * caller, const char * message);
+
+/**
+ * Set or clear the error handler (pumas_error_handler_set, pumas.h:1133).
+ * Every function of this header that returns a code other than
+ * GPUMAS_RETURN_SUCCESS calls the handler, if one is set, with that code,
+ * then returns the code. Unlike the reference, whose default handler
+ * prints the error and exits the process (pumas.c:871-889), this library
+ * has no handler until one is set and never exits. The handler is shared
+ * by all threads; setting it is not thread safe.
+ */
+void gpumas_error_handler_set(gpumas_handler_cb * handler);
+
+/** The current error handler, NULL if none (pumas_error_handler_get,
+ * pumas.h:1144). */
+gpumas_handler_cb * gpumas_error_handler_get(void);
+
+/**
+ * Catch errors (pumas_error_catch, pumas.h:1163): with a non-zero `enable`,
+ * the following errors do not call the handler; the first one is recorded
+ * until gpumas_error_raise. With 0, catching stops without raising.
+ */
+void gpumas_error_catch(int enable);
+
+/**
+ * Raise a caught error (pumas_error_raise, pumas.h:1184): returns the code
+ * of the first error caught since gpumas_error_catch, or
+ * GPUMAS_RETURN_SUCCESS, and calls the handler with it if one is set.
+ * Catching stops. Without a previous gpumas_error_catch, returns (and
+ * reports) GPUMAS_RETURN_RAISE_ERROR.
+ */
+int gpumas_error_raise(void);
+
+/** The name of a library function given to an error handler, or NULL
+ * (pumas_error_function, pumas.h:1120). */
+const char * gpumas_error_function(gpumas_function_t * function);
 
 /* ------------------------------------------------------------------------ */
 /* Diagnostics.                                                             */

@@ -47,7 +47,7 @@ RETURN_INDEX_ERROR, RETURN_PHYSICS_ERROR, RETURN_INTERNAL_ERROR = 7, 8, 9
 RETURN_FORMAT_ERROR, RETURN_MEDIUM_ERROR, RETURN_MEMORY_ERROR = 11, 12, 13
 RETURN_MODEL_ERROR, RETURN_MISSING_LIMIT = 14, 15
 RETURN_UNKNOWN_MATERIAL, RETURN_UNKNOWN_PARTICLE = 22, 23
-RETURN_VALUE_ERROR = 24
+RETURN_RAISE_ERROR, RETURN_VALUE_ERROR = 18, 24
 RETURN_DEVICE_ERROR = 64
 
 GEOMETRY_UNIFORM, GEOMETRY_SLABS, GEOMETRY_HEIGHTMAP = 0, 1, 2

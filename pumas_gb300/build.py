@@ -18,7 +18,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libgpumas.so")
 INCLUDE = os.path.join(ROOT, "include")
 
-SOURCES = ["gp_physics.cu", "gp_transport.cu", "gp_batch.cu"]
+SOURCES = ["gp_physics.cu", "gp_transport.cu", "gp_batch.cu", "gp_errors.cu"]
 HEADERS = ["gp_internal.h", "gp_device.cuh", "gp_math.cuh",
            "gp_math_tables.h", "gp_models.cuh", "gp_io.cuh", "gp_context.h",
            "gp_libmf.cuh", "gen_libmf_tables.c"]

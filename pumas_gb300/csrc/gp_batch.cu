@@ -1565,7 +1565,7 @@ extern "C" void gpumas_engine_destroy(struct gpumas_engine ** engine)
         *engine = NULL;
 }
 
-extern "C" int gpumas_engine_create(struct gpumas_engine ** engine,
+extern "C" int gp_api_engine_create(struct gpumas_engine ** engine,
     const struct gpumas_physics * physics,
     const struct gpumas_tuning * tuning, int max_jobs, size_t state_budget)
 {
@@ -1603,7 +1603,7 @@ static int gp_engine_room(gpumas_engine * g)
                                            GPUMAS_RETURN_MEMORY_ERROR;
 }
 
-extern "C" int gpumas_engine_submit(struct gpumas_engine * engine,
+extern "C" int gp_api_engine_submit(struct gpumas_engine * engine,
     const struct gpumas_job * job, int * ticket)
 {
         if ((engine == NULL) || (job == NULL) || (ticket == NULL))
@@ -1635,7 +1635,7 @@ extern "C" int gpumas_engine_submit(struct gpumas_engine * engine,
             job->first_event, info, ticket);
 }
 
-extern "C" int gpumas_engine_submit_host(struct gpumas_engine * engine,
+extern "C" int gp_api_engine_submit_host(struct gpumas_engine * engine,
     const struct gpumas_context * context, size_t n,
     struct gpumas_state * states, struct gpumas_result * results,
     uint64_t first_event, int * ticket)
@@ -1687,7 +1687,7 @@ extern "C" int gpumas_engine_submit_host(struct gpumas_engine * engine,
             ticket);
 }
 
-extern "C" int gpumas_engine_step(struct gpumas_engine * engine,
+extern "C" int gp_api_engine_step(struct gpumas_engine * engine,
     int max_done, int * done, int * n_done, int * pending)
 {
         if ((engine == NULL) || ((max_done > 0) && (done == NULL)))
@@ -1707,7 +1707,7 @@ extern "C" int gpumas_engine_step(struct gpumas_engine * engine,
         return rc;
 }
 
-extern "C" int gpumas_engine_run(struct gpumas_engine * engine,
+extern "C" int gp_api_engine_run(struct gpumas_engine * engine,
     size_t n_jobs, const struct gpumas_job * jobs)
 {
         if ((engine == NULL) || ((n_jobs > 0) && (jobs == NULL)))
@@ -1715,14 +1715,14 @@ extern "C" int gpumas_engine_run(struct gpumas_engine * engine,
         gpumas_engine * g = engine;
         for (size_t k = 0; k < n_jobs; k++) {
                 int ticket;
-                int rc = gpumas_engine_submit(g, jobs + k, &ticket);
+                int rc = gp_api_engine_submit(g, jobs + k, &ticket);
                 if (rc == GPUMAS_RETURN_MEMORY_ERROR) {
                         /* Table full: drain it, then go on. */
                         while ((rc == GPUMAS_RETURN_MEMORY_ERROR) &&
                             (g->inflight > 0)) {
                                 rc = gp_engine_batch(g);
                                 if (rc == GPUMAS_RETURN_SUCCESS)
-                                        rc = gpumas_engine_submit(
+                                        rc = gp_api_engine_submit(
                                             g, jobs + k, &ticket);
                         }
                 }
@@ -1739,7 +1739,7 @@ extern "C" int gpumas_engine_run(struct gpumas_engine * engine,
         return GPUMAS_RETURN_SUCCESS;
 }
 
-extern "C" int gpumas_engine_stats(const struct gpumas_engine * engine,
+extern "C" int gp_api_engine_stats(const struct gpumas_engine * engine,
     struct gpumas_engine_stats * stats)
 {
         if ((engine == NULL) || (stats == NULL))
@@ -1860,7 +1860,7 @@ extern "C" int gp_static_reserve(void)
         return gp_static_setup(&ptr);
 }
 
-extern "C" int gpumas_context_transport_device_static(
+extern "C" int gp_api_context_transport_device_static(
     struct gpumas_context * context, size_t n,
     const struct gpumas_soa * events, uint64_t first_event, int pool_slots,
     void * stream)

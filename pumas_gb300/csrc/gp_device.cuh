@@ -2461,9 +2461,11 @@ static __device__ __forceinline__ int gp_step(const gp_tables & T, const gp_conf
         const double sgn = (cfg.direction == GPUMAS_MODE_FORWARD) ? 1. : -1.;
         const double sd0 = sgn * e.dir[0], sd1 = sgn * e.dir[1],
                      sd2 = sgn * e.dir[2];
-        e.pos[0] += step * sd0;
-        e.pos[1] += step * sd1;
-        e.pos[2] += step * sd2;
+        /* Separate roundings, as the reference's position update
+         * (pumas.c:6416-6418): the position accumulates over the track. */
+        e.pos[0] = GP_ADD(e.pos[0], GP_MUL(step, sd0));
+        e.pos[1] = GP_ADD(e.pos[1], GP_MUL(step, sd1));
+        e.pos[2] = GP_ADD(e.pos[2], GP_MUL(step, sd2));
 
         int end_medium = gp_locate(g, e);
         /* Where the end step locals are evaluated when the step crosses a
@@ -2475,9 +2477,9 @@ static __device__ __forceinline__ int gp_step(const gp_tables & T, const gp_conf
                 const double step_min = (step < GP_STEP_MIN) ? step : GP_STEP_MIN;
                 const double pi0 = e.pos[0], pi1 = e.pos[1], pi2 = e.pos[2];
                 double s1 = 0., s2 = -step_min;
-                e.pos[0] = pi0 + s2 * sd0;
-                e.pos[1] = pi1 + s2 * sd1;
-                e.pos[2] = pi2 + s2 * sd2;
+                e.pos[0] = GP_ADD(pi0, GP_MUL(s2, sd0));
+                e.pos[1] = GP_ADD(pi1, GP_MUL(s2, sd1));
+                e.pos[2] = GP_ADD(pi2, GP_MUL(s2, sd2));
                 int tmp_medium = gp_locate(g, e);
                 if (tmp_medium != medium) {
                         if (tmp_medium != end_medium) end_medium = tmp_medium;
@@ -2485,9 +2487,9 @@ static __device__ __forceinline__ int gp_step(const gp_tables & T, const gp_conf
                         s2 = -step;
                         while (fabs(s1 - s2) > GP_STEP_MIN) {
                                 double s3 = 0.5 * (s1 + s2);
-                                e.pos[0] = pi0 + s3 * sd0;
-                                e.pos[1] = pi1 + s3 * sd1;
-                                e.pos[2] = pi2 + s3 * sd2;
+                                e.pos[0] = GP_ADD(pi0, GP_MUL(s3, sd0));
+                                e.pos[1] = GP_ADD(pi1, GP_MUL(s3, sd1));
+                                e.pos[2] = GP_ADD(pi2, GP_MUL(s3, sd2));
                                 tmp_medium = gp_locate(g, e);
                                 if (tmp_medium == medium) {
                                         s2 = s3;
@@ -2499,13 +2501,13 @@ static __device__ __forceinline__ int gp_step(const gp_tables & T, const gp_conf
                         }
                         step += s1;
                         if (loc != NULL) {
-                                pl[0] = pi0 + s2 * sd0;
-                                pl[1] = pi1 + s2 * sd1;
-                                pl[2] = pi2 + s2 * sd2;
+                                pl[0] = GP_ADD(pi0, GP_MUL(s2, sd0));
+                                pl[1] = GP_ADD(pi1, GP_MUL(s2, sd1));
+                                pl[2] = GP_ADD(pi2, GP_MUL(s2, sd2));
                         }
-                        e.pos[0] = pi0 + s1 * sd0;
-                        e.pos[1] = pi1 + s1 * sd1;
-                        e.pos[2] = pi2 + s1 * sd2;
+                        e.pos[0] = GP_ADD(pi0, GP_MUL(s1, sd0));
+                        e.pos[1] = GP_ADD(pi1, GP_MUL(s1, sd1));
+                        e.pos[2] = GP_ADD(pi2, GP_MUL(s1, sd2));
                 } else {
                         if (loc != NULL) {
                                 pl[0] = e.pos[0];
@@ -2722,9 +2724,9 @@ static __device__ __forceinline__ int gp_step(const gp_tables & T, const gp_conf
                         }
                 }
                 const double ds_ = step - sf0;
-                e.pos[0] += ds_ * sd0;
-                e.pos[1] += ds_ * sd1;
-                e.pos[2] += ds_ * sd2;
+                e.pos[0] = GP_ADD(e.pos[0], GP_MUL(ds_, sd0));
+                e.pos[1] = GP_ADD(e.pos[1], GP_MUL(ds_, sd1));
+                e.pos[2] = GP_ADD(e.pos[2], GP_MUL(ds_, sd2));
         }
 
         int decayed = 0;
@@ -2763,15 +2765,19 @@ static __device__ __forceinline__ int gp_step(const gp_tables & T, const gp_conf
                 if (event != GPUMAS_EVENT_LIMIT_TIME) {
                         const double Tf =
                             gp_cel_proper_time(T, scheme, material, k1);
-                        e.time += fabs(Tf - Ti) * density_i;
+                        /* Rounded as the reference's accumulation. */
+                        e.time = GP_ADD(e.time,
+                            GP_MUL(fabs(Tf - Ti), density_i));
                 }
         } else {
                 const double p_f =
                     (k1 <= 0) ? momentum : sqrt(k1 * (k1 + 2. * T.mass));
                 const double ti = e.time;
-                /* 1 / momentum + 1 / p_f with one division. */
-                e.time += 0.5 * step * T.mass *
-                    ((momentum + p_f) / (momentum * p_f));
+                /* Correctly rounded reciprocals, products and sums: the
+                 * time accumulates over the whole track, so it is rounded
+                 * as the reference's expression is (pumas.c:6759-6760). */
+                e.time = GP_ADD(e.time, GP_MUL(GP_MUL(GP_MUL(0.5, step),
+                    T.mass), GP_ADD(__drcp_rn(momentum), __drcp_rn(p_f))));
                 if ((time_max > 0.) && (e.time >= time_max)) {
                         event = GPUMAS_EVENT_LIMIT_TIME;
                         e.time = time_max;
@@ -2807,9 +2813,9 @@ static __device__ __forceinline__ int gp_step(const gp_tables & T, const gp_conf
         }
         if (event == GPUMAS_EVENT_LIMIT_TIME) {
                 const double ds_ = step - sf1;
-                e.pos[0] += ds_ * sd0;
-                e.pos[1] += ds_ * sd1;
-                e.pos[2] += ds_ * sd2;
+                e.pos[0] = GP_ADD(e.pos[0], GP_MUL(ds_, sd0));
+                e.pos[1] = GP_ADD(e.pos[1], GP_MUL(ds_, sd1));
+                e.pos[2] = GP_ADD(e.pos[2], GP_MUL(ds_, sd2));
         }
 
         e.step_event = event;

@@ -677,7 +677,7 @@ static int physics_from_blob(
         return GPUMAS_RETURN_SUCCESS;
 }
 
-extern "C" int gpumas_physics_load(
+extern "C" int gp_api_physics_load(
     struct gpumas_physics ** physics, const void * dump, size_t size)
 {
         if (physics == NULL) return GPUMAS_RETURN_PHYSICS_ERROR;
@@ -693,7 +693,7 @@ extern "C" int gpumas_physics_load(
             physics, (const char *)dump + 8, blob_size);
 }
 
-extern "C" int gpumas_physics_upload(
+extern "C" int gp_api_physics_upload(
     struct gpumas_physics ** physics, const void * pumas_physics)
 {
         if (physics == NULL) return GPUMAS_RETURN_PHYSICS_ERROR;
@@ -719,7 +719,7 @@ extern "C" void gpumas_physics_destroy(struct gpumas_physics ** physics)
         *physics = NULL;
 }
 
-extern "C" int gpumas_physics_material_index(
+extern "C" int gp_api_physics_material_index(
     const struct gpumas_physics * physics, const char * name, int * index)
 {
         if (physics == NULL) return GPUMAS_RETURN_PHYSICS_ERROR;
@@ -732,7 +732,7 @@ extern "C" int gpumas_physics_material_index(
         return GPUMAS_RETURN_UNKNOWN_MATERIAL;
 }
 
-extern "C" int gpumas_physics_info(const struct gpumas_physics * physics,
+extern "C" int gp_api_physics_info(const struct gpumas_physics * physics,
     int * n_materials, int * n_elements, double * cutoff, double * mass)
 {
         if (physics == NULL) return GPUMAS_RETURN_PHYSICS_ERROR;
@@ -754,7 +754,7 @@ extern "C" double gpumas_physics_elastic_ratio(
         return (physics == NULL) ? 0. : physics->tables.elastic_ratio;
 }
 
-extern "C" int gpumas_physics_particle(const struct gpumas_physics * physics,
+extern "C" int gp_api_physics_particle(const struct gpumas_physics * physics,
     int * particle, double * lifetime, double * mass)
 {
         if (physics == NULL) return GPUMAS_RETURN_PHYSICS_ERROR;

@@ -89,7 +89,7 @@ __global__ void gp_kernel_random(uint64_t seed, uint32_t domain,
 /* Contexts.                                                                */
 /* ------------------------------------------------------------------------ */
 
-extern "C" int gpumas_context_create(struct gpumas_context ** context,
+extern "C" int gp_api_context_create(struct gpumas_context ** context,
     const struct gpumas_physics * physics, int extra_memory)
 {
         if (context == NULL) return GPUMAS_RETURN_VALUE_ERROR;
@@ -142,7 +142,7 @@ extern "C" int gpumas_context_create(struct gpumas_context ** context,
         return GPUMAS_RETURN_SUCCESS;
 }
 
-extern "C" int gpumas_context_random_seed_set(
+extern "C" int gp_api_context_random_seed_set(
     struct gpumas_context * context, const uint64_t * seed)
 {
         if (context == NULL) return GPUMAS_RETURN_VALUE_ERROR;
@@ -160,7 +160,7 @@ extern "C" int gpumas_context_random_seed_set(
         return GPUMAS_RETURN_SUCCESS;
 }
 
-extern "C" int gpumas_context_random_seed_get(
+extern "C" int gp_api_context_random_seed_get(
     const struct gpumas_context * context, uint64_t * seed)
 {
         if ((context == NULL) || (seed == NULL))
@@ -294,7 +294,7 @@ extern "C" int gp_geometry_upload(const struct gpumas_physics * physics,
         return GPUMAS_RETURN_SUCCESS;
 }
 
-extern "C" int gpumas_context_geometry_set(
+extern "C" int gp_api_context_geometry_set(
     struct gpumas_context * context, const struct gpumas_geometry * geometry)
 {
         if (context == NULL) return GPUMAS_RETURN_VALUE_ERROR;
@@ -403,7 +403,7 @@ static int gp_run(gp_context * c, const gp_config & cfg, const gp_io & io,
         return rc;
 }
 
-extern "C" int gpumas_context_recorder_set(
+extern "C" int gp_api_context_recorder_set(
     struct gpumas_context * context, const struct gpumas_recorder * recorder)
 {
         if (context == NULL) return GPUMAS_RETURN_VALUE_ERROR;
@@ -421,7 +421,7 @@ extern "C" int gpumas_context_recorder_set(
         return GPUMAS_RETURN_SUCCESS;
 }
 
-extern "C" int gpumas_context_tuning_set(
+extern "C" int gp_api_context_tuning_set(
     struct gpumas_context * context, const struct gpumas_tuning * tuning)
 {
         if ((context == NULL) || (tuning == NULL))
@@ -439,7 +439,7 @@ extern "C" int gpumas_context_tuning_set(
         return GPUMAS_RETURN_SUCCESS;
 }
 
-extern "C" int gpumas_context_trials_set(
+extern "C" int gp_api_context_trials_set(
     struct gpumas_context * context, int max_trials)
 {
         if ((context == NULL) || (max_trials < 0))
@@ -449,7 +449,7 @@ extern "C" int gpumas_context_trials_set(
         return GPUMAS_RETURN_SUCCESS;
 }
 
-extern "C" int gpumas_context_carry_set(
+extern "C" int gp_api_context_carry_set(
     struct gpumas_context * context, int carry)
 {
         if ((context == NULL) || (carry < 0) || (carry > 1))
@@ -458,7 +458,7 @@ extern "C" int gpumas_context_carry_set(
         return GPUMAS_RETURN_SUCCESS;
 }
 
-extern "C" int gpumas_context_carry_get(
+extern "C" int gp_api_context_carry_get(
     const struct gpumas_context * context, int * carry)
 {
         if ((context == NULL) || (carry == NULL))
@@ -467,7 +467,7 @@ extern "C" int gpumas_context_carry_get(
         return GPUMAS_RETURN_SUCCESS;
 }
 
-extern "C" int gpumas_context_trials_get(
+extern "C" int gp_api_context_trials_get(
     const struct gpumas_context * context, int * max_trials)
 {
         if ((context == NULL) || (max_trials == NULL))
@@ -476,7 +476,7 @@ extern "C" int gpumas_context_trials_get(
         return GPUMAS_RETURN_SUCCESS;
 }
 
-extern "C" int gpumas_context_tuning_get(
+extern "C" int gp_api_context_tuning_get(
     const struct gpumas_context * context, struct gpumas_tuning * tuning)
 {
         if ((context == NULL) || (tuning == NULL))
@@ -490,7 +490,7 @@ extern "C" int gpumas_context_tuning_get(
         return GPUMAS_RETURN_SUCCESS;
 }
 
-extern "C" int gpumas_context_transport_device(struct gpumas_context * context,
+extern "C" int gp_api_context_transport_device(struct gpumas_context * context,
     size_t n, const struct gpumas_soa * events, uint64_t first_event,
     void * stream)
 {
@@ -510,7 +510,7 @@ extern "C" int gpumas_context_transport_device(struct gpumas_context * context,
         return gp_run(c, cfg, io, n, first_event, (cudaStream_t)stream, 0);
 }
 
-extern "C" int gpumas_context_transport(struct gpumas_context * context,
+extern "C" int gp_api_context_transport(struct gpumas_context * context,
     size_t n, struct gpumas_state * states, struct gpumas_result * results,
     uint64_t first_event)
 {
@@ -578,7 +578,7 @@ extern "C" int gpumas_context_transport(struct gpumas_context * context,
         return rc;
 }
 
-extern "C" int gpumas_context_stats(
+extern "C" int gp_api_context_stats(
     const struct gpumas_context * context, struct gpumas_stats * stats)
 {
         if ((context == NULL) || (stats == NULL))
@@ -609,7 +609,7 @@ __global__ void gp_kernel_dfma(double * out, int iters, double a, double b)
         if (s == 12345.678) out[0] = s;
 }
 
-extern "C" int gpumas_bench_dfma(double * tflops)
+extern "C" int gp_api_bench_dfma(double * tflops)
 {
         if (tflops == NULL) return GPUMAS_RETURN_VALUE_ERROR;
         int device, sms = 0;
@@ -653,7 +653,7 @@ __global__ void gp_kernel_math(int fn, size_t n, const double * x, double * y)
         }
 }
 
-extern "C" int gpumas_math_eval(int fn, size_t n, const double * x,
+extern "C" int gp_api_math_eval(int fn, size_t n, const double * x,
     double * y)
 {
         if ((x == NULL) || (y == NULL) || (n == 0) || (fn < 0) || (fn > 4))
@@ -676,7 +676,7 @@ extern "C" int gpumas_math_eval(int fn, size_t n, const double * x,
         return rc;
 }
 
-extern "C" int gpumas_random_fill(uint64_t seed, uint32_t domain,
+extern "C" int gp_api_random_fill(uint64_t seed, uint32_t domain,
     uint64_t event, uint64_t first, size_t n, double * out)
 {
         if ((out == NULL) || (n == 0)) return GPUMAS_RETURN_VALUE_ERROR;

@@ -145,3 +145,71 @@ def test_loader_accepts_tau_and_model_dumps():
         assert rc in (pg.RETURN_SUCCESS, pg.RETURN_DEVICE_ERROR), (name, rc)
         if ptr.value:
             destroy(ctypes.byref(ptr))
+
+
+def test_error_handler_catch_raise():
+    """The error API of the reference (pumas_error_handler_set, _catch,
+    _raise, _function; pumas.h:1110-1184) on errors that happen before any
+    device call: the installed handler gets the code, the failing function
+    and a message and the code is returned; caught errors are held until
+    raised; the library never exits, with or without a handler."""
+    import ctypes
+    import pumas_gb300 as pg
+    lib = pg.library()
+    HANDLER = ctypes.CFUNCTYPE(None, ctypes.c_int, ctypes.c_void_p,
+                               ctypes.c_char_p)
+    lib.gpumas_error_handler_set.argtypes = [HANDLER]
+    lib.gpumas_error_handler_set.restype = None
+    lib.gpumas_error_handler_get.restype = ctypes.c_void_p
+    lib.gpumas_error_catch.argtypes = [ctypes.c_int]
+    lib.gpumas_error_catch.restype = None
+    lib.gpumas_error_raise.restype = ctypes.c_int
+    lib.gpumas_error_function.argtypes = [ctypes.c_void_p]
+    lib.gpumas_error_function.restype = ctypes.c_char_p
+    load = lib.gpumas_physics_load
+    load.restype = ctypes.c_int
+    load.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.c_char_p,
+                     ctypes.c_size_t]
+    calls = []
+
+    def on_error(rc, caller, message):
+        calls.append((rc, lib.gpumas_error_function(caller), message))
+
+    handler = HANDLER(on_error)
+    ptr = ctypes.c_void_p()
+    try:
+        # No handler: the code only.
+        assert lib.gpumas_error_handler_get() is None
+        assert load(ctypes.byref(ptr), bytes(100), 100) == \
+            pg.RETURN_FORMAT_ERROR
+        lib.gpumas_error_handler_set(handler)
+        assert lib.gpumas_error_handler_get() is not None
+        assert load(ctypes.byref(ptr), bytes(100), 100) == \
+            pg.RETURN_FORMAT_ERROR
+        assert calls == [(pg.RETURN_FORMAT_ERROR, b"gpumas_physics_load",
+                          b"gpumas_physics_load returned "
+                          b"GPUMAS_RETURN_FORMAT_ERROR (11)")]
+        # Caught errors: the first one is raised, the handler called once.
+        calls.clear()
+        lib.gpumas_error_catch(1)
+        assert load(None, bytes(100), 100) == pg.RETURN_PHYSICS_ERROR
+        assert load(ctypes.byref(ptr), bytes(100), 100) == \
+            pg.RETURN_FORMAT_ERROR
+        assert calls == []
+        assert lib.gpumas_error_raise() == pg.RETURN_PHYSICS_ERROR
+        assert [c[:2] for c in calls] == [
+            (pg.RETURN_PHYSICS_ERROR, b"gpumas_physics_load")]
+        # Raise without catch.
+        calls.clear()
+        assert lib.gpumas_error_raise() == pg.RETURN_RAISE_ERROR
+        assert [c[:2] for c in calls] == [
+            (pg.RETURN_RAISE_ERROR, b"gpumas_error_raise")]
+        # A catch with no error raises success, without a call.
+        calls.clear()
+        lib.gpumas_error_catch(1)
+        assert lib.gpumas_error_raise() == pg.RETURN_SUCCESS
+        assert calls == []
+    finally:
+        lib.gpumas_error_catch(0)
+        lib.gpumas_error_handler_set(HANDLER(0))
+    assert lib.gpumas_error_handler_get() is None

@@ -278,3 +278,32 @@ def test_gpu_carry_requires_results(gpu_physics):
     assert rc == pg.RETURN_VALUE_ERROR
     assert ctx._lib.gpumas_context_carry_set(
         ctx._ptr, 2) == pg.RETURN_VALUE_ERROR
+
+
+def test_gpu_statistics_north_star_size(gpu_physics, port):
+    """The rock slab workload at its full size, 1e7 events, on the GPU;
+    the C restatement over all host cores on a seeded subset of 1e6 of
+    them (event ids 0 .. 999 999: initial states are drawn per event id,
+    so any block of ids is a random sample). At least 99.9 % of the
+    subset within 1e-9 on every field, and KS / chi-square tests (p > 0.01)
+    between the GPU's 1e7 final states and the subset's CPU final
+    states."""
+    import oracle
+    from pumas_gb300 import workloads as W
+    n, m = 10_000_000, 1_000_000
+    s0 = W.rock_slab(n, seed=23, first_event=0)
+    ctx = gpu_context(gpu_physics, W.config_dict("rock_slab"), 23,
+                      W.rock_slab_geometry(gpu_physics))
+    a, ra = ctx.transport(s0, 0)
+    assert np.all(ra["status"] == 0)
+    rock = port.material_index("StandardRock")
+    geo = oracle.make_geometry(1, [(rock, 0.)], slab_z=[0., 1000.],
+                               slab_medium=[0])
+    cfg = oracle.Config(seed=23, **W.config_dict("rock_slab"))
+    b, rb = port.transport(cfg, geo, s0[:m], 0, port.max_threads())
+    same, close = compare(a[:m], ra[:m], b, rb, RTOL)
+    PARITY_REPORT["rock slab 1e7 (first 1e6 on the CPU)"] = (
+        int(close.sum()), m)
+    assert close.mean() >= 0.999, "%d / %d outside 1e-9" % (
+        (~close).sum(), m)
+    statistical_check(a, b)
