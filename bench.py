@@ -70,7 +70,8 @@ def parse():
                    help="drain threshold in slots (0: off, <0: automatic)")
     p.add_argument("--workload", default="rock_slab",
                    choices=["rock_slab", "slab_jobs", "terrain",
-                            "plain_csda", "serve", "atmosphere"])
+                            "plain_csda", "serve", "atmosphere",
+                            "tabulate"])
     p.add_argument("--jobs", type=int, default=8192)
     p.add_argument("--job-scale", type=float, default=0.01,
                    help="slab_jobs: factor on the events per job")
@@ -851,6 +852,64 @@ def run_plain_csda(args, rank, world, local):
     print(json.dumps(line), flush=True)
 
 
+def run_tabulate(args, rank, world, local):
+    """Device table builder: the per element DEL tables of the shipped
+    physics (4 materials, 7 elements, 194 energies) recomputed from its
+    elements and energy grid -- 5 432 restricted cross sections of 180 DCS
+    evaluations each and 3 x 7 x 194 DCS table rows of 36 points -- per
+    step, against the C restatement over all host cores. The e2e time is
+    the whole gpumas_physics_tabulate call, host arrays included."""
+    import numpy as np
+    import torch
+    import oracle
+    import pumas_gb300 as pg
+    dump = pg.default_dump()
+    physics = pg.Physics(dump)
+    for _ in range(args.warmup):
+        physics.tabulate()
+    ms, wall = [], []
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            r = physics.tabulate()
+            wall.append(time.perf_counter() - t0)
+            ms.append(r["ms"])
+    evals = 3 * physics.n_elements * physics.n_energies * (
+        180 + physics.n_table_dcs)
+    ms_m = sum(ms) / len(ms)
+    cpu = None
+    if not args.no_baseline and rank == 0:
+        oracle.build_port()
+        port = oracle.Port(dump)
+        threads = port.max_threads()
+        t0 = time.perf_counter()
+        port.dcs_tabulate(threads)
+        dt = time.perf_counter() - t0
+        cpu = {"value": 1. / dt, "unit": "tabulations/s", "cores": threads,
+               "kind": "port", "nproc": os.cpu_count(),
+               "sample": "one tabulation of the shipped physics, %.2f s on "
+                         "%d OpenMP threads" % (dt, threads)}
+    if rank != 0:
+        return
+    line = base_line(args, world, "tabulations/s", 1E+03 / ms_m,
+                     "tabulations/s", ms_m, {
+                         "workload": "tabulate: per element DEL tables of "
+                                     "the shipped physics (CSn, CSn_dK, DCS "
+                                     "tables, envelope exponents)",
+                         "dcs_evaluations": evals})
+    line.update({
+        "dcs_evaluations_per_s": evals / (ms_m * 1E-03),
+        "e2e": {"value": 1. / (sum(wall) / len(wall)),
+                "unit": "tabulations/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": int(r["csn"].nbytes +
+                                          r["csn_dk"].nbytes +
+                                          r["dcs"].nbytes +
+                                          r["alpha"].nbytes)},
+        "cpu_baseline": cpu, "gpu_launches": 6, "roofline": None,
+        "clocks": clocks.summary()})
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local = dist_info()
@@ -862,8 +921,8 @@ def main():
         torch.cuda.set_device(local)
         pg.library(build=True)
         fn = {"slab_jobs": run_slab_jobs, "terrain": run_terrain,
-              "plain_csda": run_plain_csda,
-              "atmosphere": run_atmosphere}.get(args.workload)
+              "plain_csda": run_plain_csda, "atmosphere": run_atmosphere,
+              "tabulate": run_tabulate}.get(args.workload)
         if fn is None:
             from pumas_gb300 import serving
             return serving.bench(args, rank, world, local)

@@ -177,6 +177,24 @@ int gpumas_physics_load(
 int gpumas_physics_upload(
     struct gpumas_physics ** physics, const void * pumas_physics);
 
+/**
+ * Tabulate on the device the per element DEL tables of a physics, from its
+ * own elements, energy grid, cutoff and DCS models, as the reference's
+ * pumas_physics_create does (pumas.c:10704-10737, 11358-11438,
+ * 11629-11735): the restricted cross sections CSn (180 point Gauss-Legendre
+ * integrals of the DCS in ln q, the analytic one for ionisation) and their
+ * PCHIP slopes over the energy grid, for the 4 DEL processes, n_elements x
+ * n_energies each, in the reference's layout [process][element][row]; the
+ * single precision DCS interpolation tables of the 3 radiative processes,
+ * [process][element][row][n_table_dcs][2] (logarithm of the DCS and slope
+ * in ln(q / K)); and the exponents of their envelopes, [process][element]
+ * [row]. All arrays are in host memory. `ms`, if not NULL, receives the
+ * device time in ms. The tables a physics was loaded with can be compared
+ * with these: they come from the same definitions.
+ */
+int gpumas_physics_tabulate(const struct gpumas_physics * physics,
+    double * csn, double * csn_dk, float * dcs, float * alpha, float * ms);
+
 /** Release the device image (pumas_physics_destroy, pumas.h:924). */
 void gpumas_physics_destroy(struct gpumas_physics ** physics);
 

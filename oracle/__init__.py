@@ -251,6 +251,52 @@ class Reference(_Oracle):
             raise RuntimeError("reference load error %d" % rc)
 
 
+def _port_dcs_tables(self):
+    """The per element DEL tables of the loaded dump: CSn and CSn_dK
+    [4, n_elements, n_energies], DCS tables [3, n_elements, n_energies,
+    n_table_dcs, 2], envelope exponents [3, n_elements, n_energies] and the
+    DCS grid."""
+    f = self.lib.oracle_port_dcs_tables
+    f.restype = ctypes.c_int
+    dims = (ctypes.c_int * 3)()
+    f(dims, None, None, None, None, None)
+    nel, ne, nx = dims
+    csn = np.zeros((4, nel, ne))
+    dk = np.zeros((4, nel, ne))
+    dcs = np.zeros((3, nel, ne, nx, 2), dtype=np.float32)
+    alpha = np.zeros((3, nel, ne), dtype=np.float32)
+    x = np.zeros(nx, dtype=np.float32)
+    rc = f(dims, csn.ctypes.data_as(ctypes.c_void_p),
+           dk.ctypes.data_as(ctypes.c_void_p),
+           dcs.ctypes.data_as(ctypes.c_void_p),
+           alpha.ctypes.data_as(ctypes.c_void_p),
+           x.ctypes.data_as(ctypes.c_void_p))
+    if rc != 0:
+        raise RuntimeError("oracle tables error %d" % rc)
+    return {"csn": csn, "csn_dk": dk, "dcs": dcs, "alpha": alpha, "x": x}
+
+
+def _reference_dcs_tables(self, shape):
+    """The same tables (but CSn_dK) computed by the reference's own
+    functions on its loaded physics; `shape` = (n_elements, n_energies,
+    n_table_dcs). Returns the tables and the wall times (s) of the cross
+    sections and of the DCS rows."""
+    nel, ne, nx = shape
+    f = self.lib.oracle_ref_dcs_tables
+    f.restype = ctypes.c_int
+    csn = np.zeros((4, nel, ne))
+    dcs = np.zeros((3, nel, ne, nx, 2), dtype=np.float32)
+    alpha = np.zeros((3, nel, ne), dtype=np.float32)
+    t = np.zeros(2)
+    rc = f(csn.ctypes.data_as(ctypes.c_void_p),
+           dcs.ctypes.data_as(ctypes.c_void_p),
+           alpha.ctypes.data_as(ctypes.c_void_p),
+           t.ctypes.data_as(ctypes.c_void_p))
+    if rc != 0:
+        raise RuntimeError("reference tables error %d" % rc)
+    return {"csn": csn, "dcs": dcs, "alpha": alpha}, t
+
+
 def _reference_record(self, config, geometry, states, first_event, period,
                       max_frames):
     """Transport with the reference's frame recorder; returns (states,
@@ -274,6 +320,26 @@ def _reference_record(self, config, geometry, states, first_event, period,
 
 
 Reference.transport_record = _reference_record
+Reference.dcs_tables = _reference_dcs_tables
+
+
+def _port_dcs_tabulate(self, n_threads=1):
+    """The C restatement of the device table builder on the loaded
+    physics: the tables of dcs_tables (without the DCS grid), computed."""
+    t = self.dcs_tables()
+    f = self.lib.oracle_port_dcs_tabulate
+    f.restype = ctypes.c_int
+    out = {k: np.zeros_like(t[k]) for k in ("csn", "csn_dk", "dcs",
+                                            "alpha")}
+    rc = f(*[out[k].ctypes.data_as(ctypes.c_void_p) for k in
+             ("csn", "csn_dk", "dcs", "alpha")], ctypes.c_int(n_threads))
+    if rc != 0:
+        raise RuntimeError("oracle tabulation error %d" % rc)
+    return out
+
+
+Port.dcs_tabulate = _port_dcs_tabulate
+Port.dcs_tables = _port_dcs_tables
 
 
 def reference_available():

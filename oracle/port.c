@@ -3667,6 +3667,293 @@ static int context_transport(struct port_ctx * c, struct oracle_state * state,
         return status;
 }
 
+/* The per element DEL tables of the loaded dump (the reference's own
+ * pumas_physics_create output), in the dump's layout: CSn and CSn_dK
+ * [4][n_elements][n_energies], the DCS tables [3][n_elements][n_energies]
+ * [n_table_dcs][2], the envelope exponents [3][n_elements][n_energies] and
+ * the DCS grid. Returns the sizes through dims[3] = {n_elements,
+ * n_energies, n_table_dcs} when the arrays are NULL. */
+int oracle_port_dcs_tables(int * dims, double * csn, double * csn_dk,
+    float * dcs, float * alpha, float * x)
+{
+        if (ph == NULL) return RC_PHYSICS_ERROR;
+        const int nel = ph->n_elements, nE = ph->n_energies;
+        const int nx = ph->n_table_dcs;
+        dims[0] = nel;
+        dims[1] = nE;
+        dims[2] = nx;
+        if (csn == NULL) return RC_SUCCESS;
+        const size_t n4 = 4 * (size_t)nel * nE, n3 = 3 * (size_t)nel * nE;
+        memcpy(csn, ph->CSn, n4 * sizeof(double));
+        memcpy(csn_dk, ph->CSn_dK, n4 * sizeof(double));
+        memcpy(dcs, ph->DCS, n3 * 2 * nx * sizeof(float));
+        size_t i;
+        for (i = 0; i < n3; i++) alpha[i] = ph->DCS_env[2 * i];
+        memcpy(x, ph->DCS_x, nx * sizeof(float));
+        return RC_SUCCESS;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Per element DEL tables (the device table builder's CPU restatement).     */
+/* ------------------------------------------------------------------------ */
+
+/* math_diff3 (pumas.c:9944-9955). */
+static double tab_diff3(
+    double x0, double x1, double x2, double y0, double y1, double y2)
+{
+        const double h1 = x1 - x0;
+        const double h2 = x2 - x0;
+        const double delta = h1 * h2 * (h2 - h1);
+        const double c1 = h2 * h2 / delta;
+        const double c2 = -h1 * h1 / delta;
+        const double c0 = -(c1 + c2);
+        return c0 * y0 + c1 * y1 + c2 * y2;
+}
+
+/* math_pchip_initialise without known derivatives (pumas.c:9958-10023). */
+static void tab_pchip(int n, const double * x, const double * y, double * m)
+{
+        if (n >= 3) {
+                m[0] = (y[1] - y[0]) / (x[1] - x[0]);
+                n--;
+                x++;
+                y++;
+                m++;
+        }
+        if (n == 1) {
+                m[0] = 0;
+        } else if (n == 2) {
+                const double d = (y[1] - y[0]) / (x[1] - x[0]);
+                m[0] = m[1] = d;
+        } else {
+                int i;
+                for (i = 1; i < n - 1; i++) {
+                        const double h1 = x[i] - x[i - 1];
+                        const double h2 = x[i + 1] - x[i];
+                        const double S1 = (y[i] - y[i - 1]) / h1;
+                        const double S2 = (y[i + 1] - y[i]) / h2;
+                        const double tmp = S1 * S2;
+                        if (tmp > 0) {
+                                const double a =
+                                    (h1 + 2 * h2) / (3 * (h1 + h2));
+                                m[i] = tmp / ((1 - a) * S1 + a * S2);
+                        } else {
+                                m[i] = 0.;
+                        }
+                }
+                m[0] = tab_diff3(x[0], x[1], x[2], y[0], y[1], y[2]);
+                m[n - 1] = tab_diff3(x[n - 1], x[n - 2], x[n - 3], y[n - 1],
+                    y[n - 2], y[n - 3]);
+        }
+}
+
+/* The restricted cross section of a DEL process: compute_dcs_integral in
+ * mode 0 with 180 points from cutoff K to K (pumas.c:10837-10888,
+ * 10730-10732), a 6 point Gauss-Legendre rule on equal intervals of ln q
+ * (math_gauss_quad, pumas.c:12410-12450), and the analytic integral of the
+ * ionisation DCS (dcs_ionisation_integrate, pumas.c:11140-11183). */
+static double tab_csn(int process, const struct port_element * e, double K)
+{
+        static const double xg[6] = { 0.0337652428984240, 0.1693953067668678,
+                0.3806904069584016, 0.6193095930415985, 0.8306046932331322,
+                0.9662347571015760 };
+        static const double wg[6] = { 0.0856622461895852, 0.1803807865240693,
+                0.2339569672863455, 0.2339569672863455, 0.1803807865240693,
+                0.0856622461895852 };
+        const double xlow = ph->cutoff, xhigh = 1.;
+        if (process == 3) {
+                const double P2 = K * (K + 2. * ph->mass);
+                const double E = K + ph->mass;
+                const double Wr = 2. * ELECTRON_MASS * P2 /
+                    (ph->mass * ph->mass +
+                        ELECTRON_MASS * (ELECTRON_MASS + 2. * E));
+                const double qlow = K * xlow, qhigh = K * xhigh;
+                double Wmax = Wr;
+                if (Wmax < qlow) return 0.;
+                if (Wmax > qhigh) Wmax = qhigh;
+                double Wmin = (13.6 / 19.2) * e->I;
+                if (qlow >= Wmin) Wmin = qlow;
+                if (Wmax <= Wmin) return 0.;
+                const double E2 = E * E;
+                const double beta2 = P2 / E2;
+                const double a0 = 0.5 / E2;
+                const double a1 = beta2 / Wr;
+                const double I = a0 * (Wmax - Wmin) - a1 * log(Wmax / Wmin) +
+                    1. / Wmin - 1. / Wmax;
+                return 2 * PI_ * ELECTRON_MASS * ELECTRON_RADIUS *
+                    ELECTRON_RADIUS * e->Z * AVOGADRO_NUMBER /
+                    (e->A * 1E-03 * beta2) * I;
+        }
+        double qmin = 0, qmax;
+        if (process == 2) {
+                const double M = 0.5 * (NEUTRON_MASS + PROTON_MASS);
+                const double mpi = PION_MASS;
+                qmin = mpi + 0.5 * mpi * mpi / M;
+                qmax = K + ph->mass - 0.5 * (M + ph->mass * ph->mass / M);
+        } else {
+                const double Z13 = pow(e->Z, 1. / 3.);
+                const double sqrte = 1.648721271;
+                qmax = K + ph->mass * (1. - 0.75 * sqrte * Z13);
+                if (process == 1) qmin = 4 * ELECTRON_MASS;
+        }
+        double qlow = xlow * K;
+        if (qlow < qmin) qlow = qmin;
+        double qhigh = xhigh * K;
+        if (qhigh > qmax) qhigh = qmax;
+        if (qlow >= qhigh) return 0.;
+        const int n_itv = 30;
+        double x0 = log(qlow);
+        const double h = (log(qhigh) - x0) / n_itv;
+        double s = 0.;
+        int i, j;
+        for (i = 0; i < n_itv; i++, x0 += h) {
+                for (j = 0; j < 6; j++) {
+                        const double xi = x0 + xg[j] * h;
+                        const double wi = wg[j] * h;
+                        const double qi = exp(xi);
+                        const double y = dcs_process(process, e, K, qi) * qi;
+                        s += y * wi;
+                }
+        }
+        return s / (K + ph->mass);
+}
+
+/* One row of the DCS table (dcs_tabulate_row, pumas.c:11358-11438). */
+static void tab_dcs_row(int process, int iel, int row, const double * x,
+    double cs, float * data, float * alpha)
+{
+        const int n = ph->n_table_dcs;
+        int i;
+        if (cs <= 0.) {
+                for (i = 0; i < 2 * n; i++) data[i] = 0.f;
+                *alpha = 0.f;
+                return;
+        }
+        const double K = ph->K[row];
+        const struct port_element * e = ph->element + iel;
+        double y[64], m[64];
+        int imin = n, imax = n - 1;
+        for (i = 0; i < n; i++) {
+                const double d = dcs_process(process, e, K, K * exp(x[i]));
+                if (d > 0) {
+                        if (i < imin) imin = i;
+                        y[i] = log(d);
+                } else if (imin < n) {
+                        imax = i - 1;
+                        break;
+                }
+        }
+        if (imin <= imax)
+                tab_pchip(imax - imin + 1, x + imin, y + imin, m + imin);
+        double qmin, qmax;
+        if (process == 2) {
+                dcs_photonuclear_range(ph->mass, K, &qmin, &qmax);
+                qmin += qmin;
+        } else {
+                dcs_pair_production_range(e->Z, ph->mass, K, &qmin, &qmax);
+                if (process == 0)
+                        qmin = 0.5 * ph->cutoff * K;
+                else
+                        qmin *= 4;
+        }
+        const double qrev = 0.6 * K;
+        qmax *= 0.5;
+        if (qmax > qrev) qmax = qrev;
+        const double xmin = log(qmin / K), xmax = log(qmax / K);
+        int ia0 = imax, ia1 = imin;
+        for (i = 0; i < n; i++) {
+                if ((i >= imin) && (i <= imax)) {
+                        data[2 * i] = (float)y[i];
+                        data[2 * i + 1] = (float)m[i];
+                        if ((x[i] > xmin) && (x[i] < xmax)) {
+                                if (ia0 > i) ia0 = i;
+                                if (ia1 < i) ia1 = i;
+                        }
+                } else {
+                        data[2 * i] = 0.f;
+                        data[2 * i + 1] = 0.f;
+                }
+        }
+        if ((ia0 < ia1) && (ia0 < n - 1)) {
+                const int ia = (3 * ia0 + ia1) / 4;
+                double a = -m[ia];
+                if (fabs(a - 1.) <= 0.1) a = 1.;
+                *alpha = (float)a;
+        } else {
+                *alpha = 0.f;
+        }
+}
+
+/* The per element DEL tables of the loaded physics computed from its
+ * elements, energy grid and DCS models, as the device table builder does
+ * (gp_tabulate.cu), with OpenMP over processes, elements and rows: CSn and
+ * CSn_dK [4][n_elements][n_energies], the DCS tables and the envelope
+ * exponents (layouts of oracle_port_dcs_tables). */
+int oracle_port_dcs_tabulate(double * csn, double * csn_dk, float * dcs,
+    float * alpha, int n_threads)
+{
+        if (ph == NULL) return RC_PHYSICS_ERROR;
+        const int nel = ph->n_elements, nE = ph->n_energies;
+        const int n = ph->n_table_dcs;
+        if (n > 64) return RC_VALUE_ERROR;
+        /* The DCS sampling grid of compute_dcs_table (pumas.c:11643-11672). */
+        double x[64];
+        const int p = 20, m = n - p;
+        double xrev;
+        int i;
+        if (m > 0) {
+                xrev = 0.6;
+                const double x0 = log(ph->cutoff);
+                const double dx = log(xrev / ph->cutoff) / (m - 1);
+                for (i = 0; i < m; i++) x[i] = x0 + i * dx;
+        } else {
+                xrev = ph->cutoff;
+        }
+        const double dxmin = 1E-03;
+        const double dx = log((0.95 - xrev) / dxmin) / ((m > 0) ? p : p - 1);
+        for (i = 0; i < p; i++) x[n - 1 - i] = log(0.95 - dxmin * exp(i * dx));
+
+        long k;
+        const long n4 = 4L * nel * nE, n3 = 3L * nel * nE;
+#ifdef _OPENMP
+        if (n_threads <= 0) n_threads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 8) num_threads(n_threads)
+#endif
+        for (k = 0; k < n4; k++) {
+                const int row = (int)(k % nE);
+                const int iel = (int)((k / nE) % nel);
+                const int process = (int)(k / ((long)nE * nel));
+                csn[k] = (row == 0) ? 0. :
+                    tab_csn(process, ph->element + iel, ph->K[row]);
+        }
+        for (k = 0; k < 4L * nel; k++)
+                tab_pchip(nE, ph->K, csn + k * nE, csn_dk + k * nE);
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 8) num_threads(n_threads)
+#endif
+        for (k = 0; k < n3; k++) {
+                const int row = (int)(k % nE);
+                const int iel = (int)((k / nE) % nel);
+                const int process = (int)(k / ((long)nE * nel));
+                tab_dcs_row(process, iel, row, x, csn[k],
+                    dcs + k * 2 * n, alpha + k);
+        }
+        for (k = 0; k < 3L * nel; k++) {
+                float * a = alpha + k * nE;
+                int n0 = 0, row;
+                float a0 = 0.f;
+                for (row = 0; row < nE; row++) {
+                        if (a[row] > 0.f) {
+                                n0 = row;
+                                a0 = a[row];
+                                break;
+                        }
+                }
+                for (row = 0; row < n0; row++) a[row] = a0;
+        }
+        return RC_SUCCESS;
+}
+
 int oracle_port_max_threads(void)
 {
 #ifdef _OPENMP

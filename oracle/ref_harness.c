@@ -374,3 +374,97 @@ int oracle_ref_transport_record(const struct oracle_config * cfg,
         free(media);
         return PUMAS_RETURN_SUCCESS;
 }
+
+/* The per element DEL tables computed by the reference's own functions on
+ * the loaded physics (its elements, energy grid and DCS models): the
+ * restricted cross sections of compute_cel_and_del (pumas.c:10722-10737)
+ * and the DCS table rows of compute_dcs_table without the envelope maxima
+ * (pumas.c:11629-11699: dcs_tabulate_row and the low energy exponents), in
+ * the dump's layouts (see oracle_port_dcs_tables). The DCS table rows read
+ * the cross sections of the loaded physics, as in the reference. The wall
+ * time of each part goes to seconds[2]. */
+int oracle_ref_dcs_tables(double * csn, float * dcs, float * alpha,
+    double * seconds)
+{
+        if (ref_physics == NULL) return PUMAS_RETURN_PHYSICS_ERROR;
+        struct pumas_physics * physics = ref_physics;
+        const int nel = physics->n_elements, nE = physics->n_energies;
+        const int n = physics->n_table_dcs;
+        double t0 = omp_get_wtime();
+        int ip, iel, row;
+        for (ip = 0; ip < N_DEL_PROCESSES; ip++) {
+                dcs_function_t * f = dcs_get(ip);
+                for (iel = 0; iel < nel; iel++) {
+                        for (row = 0; row < nE; row++) {
+                                csn[(ip * nel + iel) * nE + row] = (row == 0) ?
+                                    0. :
+                                    compute_dcs_integral(physics, 0,
+                                        physics->element[iel],
+                                        physics->table_K[row], f,
+                                        physics->cutoff, 1, 180);
+                        }
+                }
+        }
+        double t1 = omp_get_wtime();
+        seconds[0] = t1 - t0;
+
+        /* The sampling grid and work space of compute_dcs_table. */
+        struct dcs_tabulate_work * work =
+            malloc(sizeof(*work) + 3 * n * sizeof(*work->x));
+        if (work == NULL) return PUMAS_RETURN_MEMORY_ERROR;
+        work->x = work->data;
+        work->y = work->x + n;
+        work->m = work->y + n;
+        const int p = DCS_MODEL_N_REVERSE;
+        const int m = n - p;
+        double xrev;
+        int i;
+        if (m > 0) {
+                xrev = DCS_MODEL_X_REVERSE;
+                const double x0 = log(physics->cutoff);
+                const double dx = log(xrev / physics->cutoff) / (m - 1);
+                for (i = 0; i < m; i++) work->x[i] = x0 + i * dx;
+        } else {
+                xrev = physics->cutoff;
+        }
+        const double dxmin = DCS_MODEL_DXMIN;
+        const double dx = log((DCS_MODEL_MAX_FRACTION - xrev) / dxmin) /
+            ((m > 0) ? p : p - 1);
+        for (i = 0; i < p; i++)
+                work->x[n - 1 - i] =
+                    log(DCS_MODEL_MAX_FRACTION - dxmin * exp(i * dx));
+        for (ip = 0; ip < N_DEL_PROCESSES - 1; ip++) {
+                for (iel = 0; iel < nel; iel++) {
+                        /* Envelopes start at zero, as in a fresh
+                         * pumas_physics_create: rows without cross section
+                         * are not written by dcs_tabulate_row. */
+                        for (row = 0; row < nE; row++)
+                                table_get_dcs_envelope(
+                                    physics, ip, iel, row)[0] = 0.f;
+                        for (row = 0; row < nE; row++)
+                                dcs_tabulate_row(physics, ip, iel, row, work);
+                        int n0 = 0;
+                        float a0 = 0.f;
+                        for (row = 0; row < nE; row++) {
+                                const float * env = table_get_dcs_envelope(
+                                    physics, ip, iel, row);
+                                if (env[0] > 0.f) {
+                                        n0 = row;
+                                        a0 = env[0];
+                                        break;
+                                }
+                        }
+                        for (row = 0; row < nE; row++) {
+                                const float * env = table_get_dcs_envelope(
+                                    physics, ip, iel, row);
+                                alpha[(ip * nel + iel) * nE + row] =
+                                    (row < n0) ? a0 : env[0];
+                        }
+                }
+        }
+        free(work);
+        memcpy(dcs, physics->table_DCS,
+            (size_t)3 * nel * nE * 2 * n * sizeof(float));
+        seconds[1] = omp_get_wtime() - t1;
+        return PUMAS_RETURN_SUCCESS;
+}

@@ -279,12 +279,39 @@ class Physics:
         lib.gpumas_physics_info(self._ptr, ctypes.byref(nm), ctypes.byref(ne),
                                 ctypes.byref(cut), ctypes.byref(mass))
         self.n_materials, self.n_elements = nm.value, ne.value
+        # Grid sizes from the dump's header (read as gpumas_physics_load
+        # does): the energy rows and the DCS sampling points.
+        hdr = np.frombuffer(dump, dtype=np.int32, count=11, offset=8)
+        self.n_energies, self.n_table_dcs = int(hdr[1]), int(hdr[9])
         self.cutoff, self.mass = cut.value, mass.value
         part, ctau = ctypes.c_int(), ctypes.c_double()
         _check(lib.gpumas_physics_particle(self._ptr, ctypes.byref(part),
                                            ctypes.byref(ctau), None),
                "gpumas_physics_particle")
         self.particle, self.ctau = part.value, ctau.value
+
+    def tabulate(self):
+        """Tabulate on the device the per element DEL tables of this
+        physics (gpumas_physics_tabulate): CSn and CSn_dK [4, n_elements,
+        n_energies], DCS tables [3, n_elements, n_energies, n_table_dcs, 2],
+        envelope exponents [3, n_elements, n_energies], and the device time
+        in ms."""
+        ne = self.n_energies
+        nx = self.n_table_dcs
+        nel = self.n_elements
+        csn = np.zeros((4, nel, ne))
+        dk = np.zeros((4, nel, ne))
+        dcs = np.zeros((3, nel, ne, nx, 2), dtype=np.float32)
+        alpha = np.zeros((3, nel, ne), dtype=np.float32)
+        ms = ctypes.c_float(0.)
+        f = self._lib.gpumas_physics_tabulate
+        f.restype = ctypes.c_int
+        f.argtypes = [ctypes.c_void_p] * 5 + [ctypes.POINTER(ctypes.c_float)]
+        _check(f(self._ptr, csn.ctypes.data, dk.ctypes.data, dcs.ctypes.data,
+                 alpha.ctypes.data, ctypes.byref(ms)),
+               "gpumas_physics_tabulate")
+        return {"csn": csn, "csn_dk": dk, "dcs": dcs, "alpha": alpha,
+                "ms": ms.value}
 
     def material_index(self, name):
         idx = ctypes.c_int(-1)

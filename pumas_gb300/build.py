@@ -18,7 +18,11 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libgpumas.so")
 INCLUDE = os.path.join(ROOT, "include")
 
-SOURCES = ["gp_physics.cu", "gp_transport.cu", "gp_batch.cu", "gp_errors.cu"]
+SOURCES = ["gp_physics.cu", "gp_transport.cu", "gp_batch.cu", "gp_errors.cu",
+           "gp_tabulate.cu"]
+# Per file flags: the table builder rounds every expression as the
+# reference's C code does (no fused multiply-adds).
+FILE_FLAGS = {"gp_tabulate.cu": ["--fmad=false"]}
 HEADERS = ["gp_internal.h", "gp_device.cuh", "gp_math.cuh",
            "gp_math_tables.h", "gp_models.cuh", "gp_io.cuh", "gp_context.h",
            "gp_libmf.cuh", "gen_libmf_tables.c"]
@@ -87,8 +91,8 @@ def build(force=False, verbose=False, extra_flags=()):
 
     def compile_one(src):
         obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
-        cmd = [nvcc] + NVCC_FLAGS + list(extra_flags) + [
-            "-c", os.path.join(CSRC, src), "-o", obj]
+        cmd = [nvcc] + NVCC_FLAGS + FILE_FLAGS.get(src, []) + list(
+            extra_flags) + ["-c", os.path.join(CSRC, src), "-o", obj]
         if verbose:
             print(" ".join(cmd), flush=True)
         subprocess.check_call(cmd)

@@ -98,6 +98,8 @@ int gp_api_physics_material_index(const struct gpumas_physics * physics,
     const char * name, int * index);
 int gp_api_physics_info(const struct gpumas_physics * physics,
     int * n_materials, int * n_elements, double * cutoff, double * mass);
+int gp_api_physics_tabulate(const struct gpumas_physics * physics,
+    double * csn, double * csn_dk, float * dcs, float * alpha, float * ms);
 int gp_api_physics_particle(const struct gpumas_physics * physics,
     int * particle, double * lifetime, double * mass);
 int gp_api_context_create(struct gpumas_context ** context,
@@ -161,6 +163,7 @@ extern "C" const char * gpumas_error_function(gpumas_function_t * function)
         GP_NAME(gpumas_physics_material_index)
         GP_NAME(gpumas_physics_info)
         GP_NAME(gpumas_physics_particle)
+        GP_NAME(gpumas_physics_tabulate)
         GP_NAME(gpumas_context_create)
         GP_NAME(gpumas_context_random_seed_set)
         GP_NAME(gpumas_context_random_seed_get)
@@ -403,4 +406,12 @@ extern "C" int gpumas_random_fill(uint64_t seed, uint32_t domain,
 {
         return gp_report(gp_api_random_fill(seed, domain, event, first, n, out),
             (gpumas_function_t *)&gpumas_random_fill);
+}
+
+extern "C" int gpumas_physics_tabulate(const struct gpumas_physics * physics,
+    double * csn, double * csn_dk, float * dcs, float * alpha, float * ms)
+{
+        return gp_report(gp_api_physics_tabulate(physics, csn, csn_dk, dcs,
+                             alpha, ms),
+            (gpumas_function_t *)&gpumas_physics_tabulate);
 }

@@ -26,7 +26,8 @@ def pytest_terminal_summary(terminalreporter):
     if not PARITY_REPORT:
         return
     tr = terminalreporter
-    tr.section("parity: events within 1e-9 on every field, weight included")
+    tr.section("parity: events within 1e-9 on every field (weight included), "
+               "or table entries bit for bit")
     good = total = 0
     for name in sorted(PARITY_REPORT):
         g, n = PARITY_REPORT[name]

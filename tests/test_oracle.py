@@ -214,3 +214,43 @@ def test_port_chain_matches_reference_fresh_events(port, reference):
     same, _ = compare(a[1], a[2], b[1], b[2])
     assert same.all()
     assert np.array_equal(a[2]["draws"], b[2]["draws"])
+
+
+def test_reference_functions_reproduce_dump_dcs_tables(dump, port,
+                                                       tmp_path):
+    """The per element DEL tables of the shipped dump are those of the
+    reference functions that the device table builder restates
+    (compute_dcs_integral for CSn, dcs_tabulate_row and the low energy
+    envelope exponents of compute_dcs_table): recomputed by the reference
+    library on the loaded physics, they come out bit for bit. This pins
+    which reference code the device tabulation must follow."""
+    import oracle
+    if not oracle.reference_available() and not oracle.build_reference():
+        pytest.skip("reference sources not available")
+    path = tmp_path / "muon.pumas"
+    path.write_bytes(dump)
+    ref = oracle.Reference(str(path), private=True)
+    want = port.dcs_tables()
+    shape = want["csn"].shape[1:] + (len(want["x"]),)
+    got, seconds = ref.dcs_tables(shape)
+    assert np.array_equal(got["csn"], want["csn"])
+    assert np.array_equal(got["dcs"], want["dcs"])
+    assert np.array_equal(got["alpha"], want["alpha"])
+    assert np.all(seconds > 0.)
+
+
+@pytest.mark.parametrize("name", ["muon", "tau", "muon_kkp", "muon_abb",
+                                  "tau_bbks"])
+def test_port_tabulation_matches_dump(name):
+    """The C restatement of the device table builder (cross sections,
+    their slopes, DCS tables and envelope exponents from the physics'
+    elements, energy grid and DCS models) reproduces the tables that the
+    reference's pumas_physics_create wrote into each physics dump, bit for
+    bit."""
+    import oracle
+    from cases import physics_dump
+    port = oracle.Port(physics_dump(name), private=True)
+    want = port.dcs_tables()
+    got = port.dcs_tabulate(4)
+    for k in ("csn", "csn_dk", "dcs", "alpha"):
+        assert np.array_equal(got[k], want[k]), k

@@ -20,7 +20,7 @@ MODEL_CASES = sorted(n for n in CASES if has_models(n))
 @pytest.mark.parametrize("name", MODEL_CASES)
 def test_gpu_models_match_reference_golden(request, name):
     good, n = golden_check(request, name)
-    assert good >= 0.999 * n
+    assert good >= 0.999 * n    # all of them so far
 
 
 def test_model_physics_load(request):
