@@ -85,6 +85,9 @@ def parse():
                    help="serve: Poisson arrival rates (requests/s)")
     p.add_argument("--serve-seconds", type=float, default=2.0)
     p.add_argument("--serve-scale", type=float, default=1E-03)
+    p.add_argument("--serve-plain", type=int, default=300,
+                   help="serve: requests of each rate also served by the "
+                        "plain one-request-at-a-time server (0: none)")
     p.add_argument("--autotune", action="store_true",
                    help="slab_jobs: tune the pool on every 8th job first")
     p.add_argument("--no-c3", action="store_true",

@@ -468,3 +468,12 @@ int oracle_ref_dcs_tables(double * csn, float * dcs, float * alpha,
         seconds[1] = omp_get_wtime() - t1;
         return PUMAS_RETURN_SUCCESS;
 }
+
+/* The reference's loaded physics itself (a live struct pumas_physics, with
+ * pointers into this process) and its size in bytes. */
+const void * oracle_ref_physics(int * size)
+{
+        if (ref_physics == NULL) return NULL;
+        memcpy(size, ref_physics, sizeof(*size));
+        return ref_physics;
+}

@@ -274,14 +274,20 @@ class Physics:
         self._ptr = ctypes.c_void_p()
         _check(lib.gpumas_physics_load(ctypes.byref(self._ptr), dump,
                                        len(dump)), "gpumas_physics_load")
+        self._fill(dump[8:])
+
+    def _fill(self, blob):
+        """Sizes and particle of the loaded physics; `blob` starts with the
+        struct's header."""
+        lib = self._lib
         nm, ne = ctypes.c_int(), ctypes.c_int()
         cut, mass = ctypes.c_double(), ctypes.c_double()
         lib.gpumas_physics_info(self._ptr, ctypes.byref(nm), ctypes.byref(ne),
                                 ctypes.byref(cut), ctypes.byref(mass))
         self.n_materials, self.n_elements = nm.value, ne.value
-        # Grid sizes from the dump's header (read as gpumas_physics_load
+        # Grid sizes from the struct's header (read as gpumas_physics_load
         # does): the energy rows and the DCS sampling points.
-        hdr = np.frombuffer(dump, dtype=np.int32, count=11, offset=8)
+        hdr = np.frombuffer(blob, dtype=np.int32, count=11)
         self.n_energies, self.n_table_dcs = int(hdr[1]), int(hdr[9])
         self.cutoff, self.mass = cut.value, mass.value
         part, ctau = ctypes.c_int(), ctypes.c_double()
@@ -289,6 +295,22 @@ class Physics:
                                            ctypes.byref(ctau), None),
                "gpumas_physics_particle")
         self.particle, self.ctau = part.value, ctau.value
+
+    @classmethod
+    def upload(cls, address):
+        """Physics from a live struct pumas_physics at a host address
+        (gpumas_physics_upload)."""
+        self = cls.__new__(cls)
+        lib = library()
+        self._lib = lib
+        self._ptr = ctypes.c_void_p()
+        _check(lib.gpumas_physics_upload(ctypes.byref(self._ptr),
+                                         ctypes.c_void_p(address)),
+               "gpumas_physics_upload")
+        size = int(np.frombuffer((ctypes.c_char * 4).from_address(address),
+                                 dtype=np.int32)[0])
+        self._fill((ctypes.c_char * size).from_address(address).raw)
+        return self
 
     def tabulate(self):
         """Tabulate on the device the per element DEL tables of this

@@ -258,8 +258,14 @@ def sweep(physics, rates, seconds=2.0, scale=1E-03, seed=7,
                  "latency_ms": percentiles(lat), "event_errors": errors,
                  "sustained": bool(n / wall >= 0.9 * rate)}
         # The plain baseline on the same arrivals (bounded: the first
-        # plain_max requests).
+        # plain_max requests; none with plain_max = 0).
         m = min(n, plain_max)
+        if m == 0:
+            out.append(entry)
+            if entry["sustained"]:
+                best = entry
+            base += n
+            continue
         preqs = [mix.make(base + i) for i in range(m)]
         pwall = plain_serve(preqs, arrivals[:m])
         n_ev = n_same = n_close = 0
@@ -302,7 +308,7 @@ def bench(args, rank, world, local):
     rates = [float(x) for x in args.rates.split(",")]
     r = sweep(physics, rates, args.serve_seconds, args.serve_scale,
               args.seed, args.pool_slots or 65536, args.max_inner or 8,
-              args.batch or 4)
+              args.batch or 4, plain_max=args.serve_plain)
     if rank != 0:
         return
     top = None
