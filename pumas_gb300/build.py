@@ -2,9 +2,12 @@
 
 The CUDA sources under csrc/ are compiled for sm_103a only
 (``-gencode arch=compute_103a,code=sm_103a``) in parallel and linked into
-``pumas_gb300/_build/libgpumas.so``, inside the source tree. Host code is
-compiled without floating point contraction so that constants evaluated on
-the host match the reference's on every host architecture.
+``pumas_gb300/_build/libgpumas.so``, inside the source tree. Host and
+device code are compiled without floating point contraction
+(``-ffp-contract=off``, ``--fmad=false``): every product and sum is rounded
+on its own, as in the reference's C code, so that the transport reproduces
+the reference's roundings; fused multiply-adds appear only where the code
+asks for one (``fma``), in its own math functions and division steps.
 """
 import os
 import subprocess
@@ -20,9 +23,8 @@ INCLUDE = os.path.join(ROOT, "include")
 
 SOURCES = ["gp_physics.cu", "gp_transport.cu", "gp_batch.cu", "gp_errors.cu",
            "gp_tabulate.cu"]
-# Per file flags: the table builder rounds every expression as the
-# reference's C code does (no fused multiply-adds).
-FILE_FLAGS = {"gp_tabulate.cu": ["--fmad=false"]}
+# Per file flags (none at present).
+FILE_FLAGS = {}
 HEADERS = ["gp_internal.h", "gp_device.cuh", "gp_math.cuh",
            "gp_math_tables.h", "gp_models.cuh", "gp_io.cuh", "gp_context.h",
            "gp_libmf.cuh", "gen_libmf_tables.c"]
@@ -32,7 +34,8 @@ LIBMF_TABLES = os.path.join(BUILD, "gp_libmf_tables.h")
 
 NVCC_FLAGS = [
     "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo",
-    "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+    "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler",
+    "-ffp-contract=off",
     "-I" + INCLUDE, "-I" + CSRC, "-I" + BUILD,
 ]
 

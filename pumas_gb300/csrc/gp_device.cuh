@@ -62,9 +62,10 @@
 
 #define GPD static __device__ __forceinline__
 
-/* Products and sums rounded separately, as on the host: used where the
- * reference's expression cancels and a fused multiply-add would change the
- * result beyond the parity tolerance. */
+/* Products and sums rounded separately, as on the host. The library is
+ * built without contraction (--fmad=false) anyway; these mark the places
+ * where the reference's expression cancels and a fused multiply-add would
+ * change the result beyond the parity tolerance. */
 #define GP_MUL(a, b) __dmul_rn((a), (b))
 #define GP_ADD(a, b) __dadd_rn((a), (b))
 #define GP_SUB(a, b) __dsub_rn((a), (b))
@@ -228,12 +229,31 @@ GPD int gp_index(const gp_tables & T, int lut_id,
         return i1;
 }
 
+/* The correctly rounded quotient a / b from rb = 1 / b (correctly rounded):
+ * one residual correction of q0 = a rb, with the residual a - q0 b exact
+ * by a fused multiply-add (Markstein, IBM J. Res. Dev. 34 (1990) 111). */
+GPD double gp_quotient(double a, double b, double rb)
+{
+        const double q0 = GP_MUL(a, rb);
+        return fma(fma(-q0, b, a), rb, q0);
+}
+
+/* The cubic p0 + t (m0 + t (c2 + t c3)), every product and sum rounded on
+ * its own as in the reference's C code. */
+GPD double gp_horner3(double t, double p0, double m0, double c2, double c3)
+{
+        return GP_ADD(p0, GP_MUL(t, GP_ADD(m0, GP_MUL(t, GP_ADD(c2,
+            GP_MUL(t, c3))))));
+}
+
 /* math_pchip_interpolate (pumas.c:4118-4125). */
 GPD double gp_pchip(double t, double p0, double p1, double m0, double m1)
 {
-        const double c2 = -3 * (p0 - p1) - 2 * m0 - m1;
-        const double c3 = 2 * (p0 - p1) + m0 + m1;
-        return p0 + t * (m0 + t * (c2 + t * c3));
+        const double d = GP_SUB(p0, p1);
+        const double c2 =
+            GP_SUB(GP_SUB(GP_MUL(-3., d), GP_MUL(2., m0)), m1);
+        const double c3 = GP_ADD(GP_ADD(GP_MUL(2., d), m0), m1);
+        return gp_horner3(t, p0, m0, c2, c3);
 }
 
 /* table_interpolate_pchip (pumas.c:4146-4157). */
@@ -244,10 +264,10 @@ GPD double gp_interpolate(const gp_tables & T, int lut_id,
         const int i1 = gp_index(T, lut_id, X, x);
         const int i2 = i1 + 1;
         const double x1 = __ldg(X + i1);
-        const double dX = __ldg(X + i2) - x1;
-        const double t = (x - x1) / dX;
-        const double m1 = __ldg(M + i1) * dX;
-        const double m2 = (i2 > 1) ? __ldg(M + i2) * dX : m1;
+        const double dX = GP_SUB(__ldg(X + i2), x1);
+        const double t = __ddiv_rn(GP_SUB(x, x1), dX);
+        const double m1 = GP_MUL(__ldg(M + i1), dX);
+        const double m2 = (i2 > 1) ? GP_MUL(__ldg(M + i2), dX) : m1;
         return gp_pchip(t, __ldg(Y + i1), __ldg(Y + i2), m1, m2);
 }
 
@@ -257,12 +277,13 @@ GPD double gp_baked_row(const gp_tables & T, int grid, int cid, int i,
     double x)
 {
         const size_t ne = (size_t)T.n_energies;
-        const double2 nd = __ldg((const double2 *)(T.node + grid * ne + i));
-        const double t = (x - nd.x) * nd.y;
+        const double2 * n = (const double2 *)(T.node + grid * ne + i);
+        const double2 nd = __ldg(n);
+        const double t = gp_quotient(GP_SUB(x, nd.x), __ldg(&n[1].x), nd.y);
         const double2 * c = (const double2 *)(T.coef + cid * ne + i);
         const double2 c01 = __ldg(c);
         const double2 c23 = __ldg(c + 1);
-        return c01.x + t * (c01.y + t * (c23.x + t * c23.y));
+        return gp_horner3(t, c01.x, c01.y, c23.x, c23.y);
 }
 
 GPD double gp_baked(const gp_tables & T, int grid,
@@ -499,10 +520,13 @@ GPD double gp_coulomb_ehs_length(
                 return __ldg(Lb + imax) / p2;
         } else {
                 const int i1 = gp_index(T, GP_LUT_K, T.K, kinetic);
-                const double2 nd = __ldg((const double2 *)(T.node + i1));
-                const double h = (kinetic - nd.x) * nd.y;
+                const double2 * n = (const double2 *)(T.node + i1);
+                const double2 nd = __ldg(n);
+                const double h =
+                    gp_quotient(GP_SUB(kinetic, nd.x), __ldg(&n[1].x), nd.y);
                 const double l1 = __ldg(Lb + i1);
-                return (l1 + h * (__ldg(Lb + i1 + 1) - l1)) / p2;
+                return GP_ADD(l1, GP_MUL(h, GP_SUB(__ldg(Lb + i1 + 1), l1))) /
+                    p2;
         }
 }
 
@@ -1392,61 +1416,67 @@ GPD double gp_randn(gp_event & e)
         e.randn_done = !e.randn_done;
         if (!e.randn_done) return e.randn_next;
         const double r = sqrt(-2. * gp_log(gp_random(e)));
-        /* sin and cos of 2 pi u, without argument reduction. */
-        const double u2 = 2. * gp_random(e);
+        const double phi = GP_MUL(2. * GP_PI, gp_random(e));
         double s, c;
-        sincospi(u2, &s, &c);
-        e.randn_next = r * c;
-        return r * s;
+        sincos(phi, &s, &c);
+        e.randn_next = GP_MUL(r, c);
+        return GP_MUL(r, s);
 }
 
-/* step_rotate_direction (pumas.c:7042-7095). */
+/* step_rotate_direction (pumas.c:7042-7095), every product and sum
+ * rounded on its own as in the reference's C code. */
+GPD double gp_rnorm2(double a, double b)
+{
+        return __drcp_rn(sqrt(GP_ADD(GP_MUL(a, a), GP_MUL(b, b))));
+}
+
+GPD double gp_cross(double a, double b, double c, double d)
+{
+        return GP_SUB(GP_MUL(a, b), GP_MUL(c, d));
+}
+
 static __device__ __forceinline__ void gp_rotate(gp_event & e, double mu)
 {
         double * const direction = e.dir;
-        const double cos_theta = 1 - 2 * mu;
-        const double stsq = 4 * mu * (1. - mu);
+        const double cos_theta = GP_SUB(1., GP_MUL(2., mu));
+        const double stsq = GP_MUL(GP_MUL(4., mu), GP_SUB(1., mu));
         if (stsq <= 0.) return;
         const double st = sqrt(stsq);
         double u0x = 0., u0y = 0., u0z = 0.;
-        const double a0 = fabs(direction[0]);
-        const double a1 = fabs(direction[1]);
-        const double a2 = fabs(direction[2]);
+        const double d0 = direction[0], d1 = direction[1], d2 = direction[2];
+        const double a0 = fabs(d0);
+        const double a1 = fabs(d1);
+        const double a2 = fabs(d2);
         if (a0 > a1) {
                 if (a0 > a2) {
-                        const double nrm =
-                            rsqrt(direction[0] * direction[0] +
-                                direction[2] * direction[2]);
-                        u0x = -direction[2] * nrm, u0z = direction[0] * nrm;
+                        const double nrm = gp_rnorm2(d0, d2);
+                        u0x = GP_MUL(-d2, nrm), u0z = GP_MUL(d0, nrm);
                 } else {
-                        const double nrm =
-                            rsqrt(direction[1] * direction[1] +
-                                direction[2] * direction[2]);
-                        u0y = direction[2] * nrm, u0z = -direction[1] * nrm;
+                        const double nrm = gp_rnorm2(d1, d2);
+                        u0y = GP_MUL(d2, nrm), u0z = GP_MUL(-d1, nrm);
                 }
         } else {
                 if (a1 > a2) {
-                        const double nrm =
-                            rsqrt(direction[0] * direction[0] +
-                                direction[1] * direction[1]);
-                        u0x = direction[1] * nrm, u0y = -direction[0] * nrm;
+                        const double nrm = gp_rnorm2(d0, d1);
+                        u0x = GP_MUL(d1, nrm), u0y = GP_MUL(-d0, nrm);
                 } else {
-                        const double nrm =
-                            rsqrt(direction[1] * direction[1] +
-                                direction[2] * direction[2]);
-                        u0y = direction[2] * nrm, u0z = -direction[1] * nrm;
+                        const double nrm = gp_rnorm2(d1, d2);
+                        u0y = GP_MUL(d2, nrm), u0z = GP_MUL(-d1, nrm);
                 }
         }
-        const double u1x = u0y * direction[2] - u0z * direction[1];
-        const double u1y = u0z * direction[0] - u0x * direction[2];
-        const double u1z = u0x * direction[1] - u0y * direction[0];
-        /* sin and cos of pi (1 - 2 u); 1 - 2 u is exact. */
-        const double phi_pi = 1. - 2. * gp_random(e);
+        const double u1x = gp_cross(u0y, d2, u0z, d1);
+        const double u1y = gp_cross(u0z, d0, u0x, d2);
+        const double u1z = gp_cross(u0x, d1, u0y, d0);
+        /* phi = pi (1 - 2 u), 1 - 2 u being exact. */
+        const double phi = GP_MUL(GP_PI, 1. - 2. * gp_random(e));
         double sp, cp;
-        sincospi(phi_pi, &sp, &cp);
-        direction[0] = cos_theta * direction[0] + st * (cp * u0x + sp * u1x);
-        direction[1] = cos_theta * direction[1] + st * (cp * u0y + sp * u1y);
-        direction[2] = cos_theta * direction[2] + st * (cp * u0z + sp * u1z);
+        sincos(phi, &sp, &cp);
+        direction[0] = GP_ADD(GP_MUL(cos_theta, d0),
+            GP_MUL(st, GP_ADD(GP_MUL(cp, u0x), GP_MUL(sp, u1x))));
+        direction[1] = GP_ADD(GP_MUL(cos_theta, d1),
+            GP_MUL(st, GP_ADD(GP_MUL(cp, u0y), GP_MUL(sp, u1y))));
+        direction[2] = GP_ADD(GP_MUL(cos_theta, d2),
+            GP_MUL(st, GP_ADD(GP_MUL(cp, u0z), GP_MUL(sp, u1z))));
 }
 
 /* ------------------------------------------------------------------------ */

@@ -90,13 +90,17 @@ struct gp_lut {
  * dx = x[i+1] - x[i], m0 = m[i] dx, m1 = m[i+1] dx (m0 in row 0), then
  * c2 = -3 (y[i] - y[i+1]) - 2 m0 - m1 and c3 = 2 (y[i] - y[i+1]) + m0 + m1.
  * These are evaluated once on the host with the same expressions and
- * stored per row; a lookup is then p0 + t (m0 + t (c2 + t c3)) with
- * t = (v - x[i]) / dx, the division being replaced by the stored 1 / dx. */
+ * stored per row; a lookup is then p0 + t (m0 + t (c2 + t c3)), each
+ * product and sum rounded on its own as in the reference, with
+ * t = (v - x[i]) / dx. The quotient is the correctly rounded one, obtained
+ * from the stored 1 / dx with one residual correction (Markstein): q0 =
+ * (v - x[i]) (1 / dx), r = (v - x[i]) - q0 dx exactly by a fused
+ * multiply-add, t = q0 + r (1 / dx) rounded once. */
 struct __align__(32) gp_coef {
         double p0, m0, c2, c3;
 };
-struct __align__(16) gp_node {
-        double x, inv_dx;
+struct __align__(32) gp_node {
+        double x, inv_dx, dx, pad;
 };
 
 /* Identifiers of the baked interpolants, M materials, s a scheme in {0, 1}

@@ -288,10 +288,12 @@ static void bake_nodes(const double * x, int n, struct gp_node * out)
 {
         for (int i = 0; i < n - 1; i++) {
                 out[i].x = x[i];
-                out[i].inv_dx = 1. / (x[i + 1] - x[i]);
+                out[i].dx = x[i + 1] - x[i];
+                out[i].inv_dx = 1. / out[i].dx;
+                out[i].pad = 0.;
         }
         out[n - 1].x = x[n - 1];
-        out[n - 1].inv_dx = 0.;
+        out[n - 1].inv_dx = out[n - 1].dx = out[n - 1].pad = 0.;
 }
 
 struct parsed {

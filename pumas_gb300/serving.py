@@ -197,19 +197,20 @@ def agreement(a, ra, b, rb, rtol=1E-09):
     """Per event agreement of two transports of the same events: (bit
     identical, within rtol relative on energy, distance, grammage, time,
     weight, position and direction with identical end events, media and
-    status). An event's draws and operations do not depend on what runs
-    beside it; its roundings can differ by an ulp where the compiler fused
-    a multiply-add differently in the kernels that ran it (served engine
-    against one thread per event)."""
+    status). Scalars are compared relative to their magnitude, the position
+    and direction vectors relative to their norm (a near zero transverse
+    component is not held to rtol of itself)."""
     same = (a == b) & (ra == rb)
     close = np.ones(len(a), bool)
-    for f in ("energy", "distance", "grammage", "time", "weight", "position",
-              "direction"):
+    for f in ("energy", "distance", "grammage", "time", "weight"):
         x, y = a[f], b[f]
-        if x.ndim == 1:
-            x, y = x[:, None], y[:, None]
         scale = np.maximum(np.maximum(np.abs(x), np.abs(y)), 1E-300)
-        close &= np.all(np.abs(x - y) <= rtol * scale, axis=1)
+        close &= np.abs(x - y) <= rtol * scale
+    for f in ("position", "direction"):
+        x, y = a[f], b[f]
+        scale = np.maximum(np.maximum(np.linalg.norm(x, axis=1),
+                                      np.linalg.norm(y, axis=1)), 1E-300)
+        close &= np.linalg.norm(x - y, axis=1) <= rtol * scale
     for f in ("event", "medium_in", "medium_out", "status"):
         close &= ra[f] == rb[f]
     return same, close

@@ -78,9 +78,15 @@ def test_serving_agreement_and_percentiles():
     b["energy"][1] *= 1. + 1E-12      # an ulp-scale difference: close
     b["energy"][2] *= 1. + 1E-06      # a real difference
     rb["event"][3] = 1                # another end event
+    # Vectors are compared relative to their norm: a last bits difference
+    # of a near zero transverse component is close, a real deflection not.
+    a["position"][4] = b["position"][4] = (1E-08, 0., 1E+05)
+    b["position"][4, 0] = 2E-08
+    a["direction"][5] = b["direction"][5] = (0., 0., 1.)
+    b["direction"][5, 0] = 1E-06
     same, close = agreement(a, ra, b, rb)
-    assert list(np.where(~same)[0]) == [1, 2, 3]
-    assert list(np.where(~close)[0]) == [2, 3]
+    assert list(np.where(~same)[0]) == [1, 2, 3, 4, 5]
+    assert list(np.where(~close)[0]) == [2, 3, 5]
     p = percentiles(np.arange(1., 101.))
     assert p["p50"] == pytest.approx(50.5) and p["p99"] == pytest.approx(
         99.01)

@@ -6,10 +6,11 @@ slopes, DCS interpolation tables and envelope exponents -- are recomputed on
 the GPU from each physics' own elements, energy grid, cutoff and DCS models,
 and compared with the dump's (which tests/test_oracle.py shows to be the
 output of the reference functions that the device code restates). The DCS
-models run on the device with the engine's logarithm and exponential, so
-values agree to a few ulp: CSn within 1e-12 relative, CSn_dK within 1e-9 of
-its column's scale, and at least 99.9 % of the single precision table
-entries and envelope exponents bit for bit, the others within 16 ulp.
+models run on the device with the device's logarithm, arc tangent and
+power functions, so values agree to a few ulp: CSn within 1e-10 relative,
+CSn_dK within 1e-9 of its column's scale, and at least 99.9 % of the single
+precision table entries and envelope exponents bit for bit, the others
+within 16 ulp.
 """
 import numpy as np
 import pytest
@@ -44,7 +45,11 @@ def test_device_tabulation_matches_dump(request, name):
     assert np.array_equal(a == 0., b == 0.)
     nz = b != 0.
     rel = np.abs(a[nz] - b[nz]) / np.abs(b[nz])
-    assert rel.max() <= 1E-12, rel.max()
+    # The ABB bremsstrahlung DCS (pumas.c:13824-13905) is a difference of
+    # screening terms that cancel near the end point: a last bit difference
+    # in one of their logarithms or arc tangents moves the DCS there, and the
+    # integral, by up to about 1e-11.
+    assert rel.max() <= 1E-10, rel.max()
 
     a, b = got["csn_dk"], want["csn_dk"]
     scale = np.maximum(np.abs(b).max(axis=2, keepdims=True), 1E-300)
