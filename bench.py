@@ -81,9 +81,11 @@ def parse():
                    help="terrain: events per direction")
     p.add_argument("--atm-events", type=int, default=1_000_000,
                    help="atmosphere: events per step")
-    p.add_argument("--rates", default="100,300,1000,3000,10000",
+    p.add_argument("--rates",
+                   default="100,200,300,500,700,1000,1500,2000,3000,5000,"
+                           "10000",
                    help="serve: Poisson arrival rates (requests/s)")
-    p.add_argument("--serve-seconds", type=float, default=2.0)
+    p.add_argument("--serve-seconds", type=float, default=3.0)
     p.add_argument("--serve-scale", type=float, default=1E-03)
     p.add_argument("--serve-plain", type=int, default=300,
                    help="serve: requests of each rate also served by the "

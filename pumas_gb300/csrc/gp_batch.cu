@@ -48,10 +48,10 @@ namespace cg = cooperative_groups;
 #ifndef GP_POOL_MIN_BLOCKS
 #define GP_POOL_MIN_BLOCKS 1
 #endif
-/* The step kernel runs as one persistent wave: 3 blocks of 128 threads per
- * SM, i.e. at most 168 registers per thread. */
+/* The step kernel runs as one persistent wave: 4 blocks of 128 threads per
+ * SM, i.e. at most 128 registers per thread. */
 #ifndef GP_STEP_MIN_BLOCKS
-#define GP_STEP_MIN_BLOCKS 3
+#define GP_STEP_MIN_BLOCKS 4
 #endif
 
 /* Field layout of a slot: doubles, ints and 64 bit integers, each as an
@@ -67,11 +67,15 @@ enum gp_slot_int {
         SI_DECAYED, SI_STEP_FIRST, SI_STEP_EVENT, SI_STEP_FORESEEN,
         SI_RANDN_DONE, SI_STEPS, SI_STATUS, SI_MEDIUM, SI_MATERIAL,
         SI_STRAIGHT, SI_STEP_INDEX, SI_NEW_MEDIUM, SI_PHASE, SI_MEDIUM_IN,
-        SI_N_DRAWS, SI_POLAR_PROCESS, SI_POLAR_TARGET, SI_JOB, SI_N
+        SI_N_DRAWS, SI_POLAR_PROCESS, SI_POLAR_TARGET, SI_JOB, SI_EVENT_END,
+        SI_N
 };
 enum gp_slot_u64 { SU_ID, SU_SRC, SU_N };
 
 #define GP_EMPTY 0
+/* A slot whose event ended in the step kernel (GP_NEXT_DONE): its state
+ * and end event wait in the slot for the fill kernel, which writes them back
+ * to the job's output and frees the slot. */
 
 struct gp_pool {
         double * d;
@@ -266,18 +270,16 @@ __device__ __forceinline__ void gp_progress(gp_counters * cnt)
                 atomicAdd(&cnt->progress, (unsigned long long)g.size());
 }
 
-/* Route a slot to its next phase. */
+/* Route a slot to its next phase; an ended event waits in its slot for the
+ * fill kernel (GP_NEXT_DONE). */
 __device__ __forceinline__ void gp_route(const gp_pool & pool, int slot,
     const gp_launch * X, const gp_job & J, gp_counters * cnt,
     int * del_list, int * ehs_list, int parity, int next, gp_event & e,
     gp_loop & L, int event)
 {
         gp_progress(cnt);
-        if (next == GP_NEXT_DONE) {
-                gp_finish(pool, slot, X, J, cnt, e, event, L.medium);
-                return;
-        }
         gp_slot_store(pool, slot, e, L);
+        if (next == GP_NEXT_DONE) PI(SI_EVENT_END) = event;
         PI(SI_PHASE) = next;
         if (next == GP_NEXT_DEL)
                 gp_append(&cnt->n_del[parity], del_list, slot);
@@ -407,12 +409,42 @@ __global__ void __launch_bounds__(128, 1) gp_pool_drain(
         }
 }
 
+/* Slot turnover, one thread per slot: an event that ended in the previous
+ * step kernel (GP_NEXT_DONE) is written back to its job's output and its
+ * slot freed; an empty slot takes the next event of the queue
+ * (gp_refill: events that end before their first step are written back at
+ * once and the next one taken), which enters the step phase. */
+__global__ void __launch_bounds__(128, 1) gp_pool_fill(
+    const gp_tables * __restrict__ Tp, const gp_launch * __restrict__ X,
+    const gp_pool pool, gp_counters * cnt)
+{
+        const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+        if (slot >= pool.P) return;
+        const gp_tables & T = *Tp;
+        gp_event e;
+        gp_loop L;
+        int phase = PI(SI_PHASE);
+        if (phase == GP_NEXT_DONE) {
+                const gp_job & J = X->jobs[PI(SI_JOB)];
+                gp_slot_load(pool, slot, J.cfg, e, L);
+                gp_finish(pool, slot, X, J, cnt, e, PI(SI_EVENT_END),
+                    L.medium);
+                phase = GP_EMPTY;
+        }
+        if (phase != GP_EMPTY) return;
+        int job;
+        if (!gp_refill(T, X, pool, slot, cnt, e, L, job)) return;
+        gp_slot_store(pool, slot, e, L);
+        PI(SI_PHASE) = GP_NEXT_STEP;
+}
+
 /* Continuous steps. The kernel is persistent: each lane takes slots from a
- * cursor over the pool (refilling empty ones from the input), steps its
- * slot until the step ends on an event or after max_inner steps, routes it
- * to the next phase and takes the next slot. All lanes thus execute the step
- * together until the pool is exhausted, whatever the number of steps of
- * each event. */
+ * cursor over the pool, steps the slots in the step phase until the step
+ * ends on an event or after max_inner steps, routes them to the next phase
+ * and takes the next slot. All lanes thus execute the step together until
+ * the pool is exhausted, whatever the number of steps of each event. Slots
+ * are emptied and refilled by the fill kernel, which keeps the input and
+ * output code out of this one. */
 __global__ void __launch_bounds__(128, GP_STEP_MIN_BLOCKS) gp_pool_step(
     const gp_tables * __restrict__ Tp, const gp_launch * __restrict__ X,
     const gp_pool pool, gp_counters * cnt, int * del_list, int * ehs_list,
@@ -441,22 +473,13 @@ __global__ void __launch_bounds__(128, GP_STEP_MIN_BLOCKS) gp_pool_step(
                                 exhausted = 1;
                                 break;
                         }
-                        const int s_ = j;
                         {
-                                const int slot = s_;
-                                int job;
-                                if (PI(SI_PHASE) == GP_EMPTY) {
-                                        if (!gp_refill(T, X, pool, slot, cnt,
-                                                e, L, job))
-                                                continue;
-                                } else {
-                                        job = PI(SI_JOB);
-                                        gp_slot_load(pool, slot,
-                                            X->jobs[job].cfg, e, L);
-                                }
-                                J = X->jobs + job;
+                                const int slot = j;
+                                if (PI(SI_PHASE) != GP_NEXT_STEP) continue;
+                                J = X->jobs + PI(SI_JOB);
+                                gp_slot_load(pool, slot, J->cfg, e, L);
                         }
-                        slot = s_;
+                        slot = j;
                         k = 0;
                 }
                 if (!__any_sync(0xFFFFFFFFu, slot >= 0)) break;
@@ -984,9 +1007,10 @@ static unsigned int gp_step_wave(int P, int block)
         return (wave < grid) ? wave : grid;
 }
 
-/* Launch one pool iteration: list reset and drain, continuous steps, DELs,
- * photonuclear polar angles, hard elastic scatters. Lists 0-1 are the DEL
- * lists, 2-3 the EHS lists and 4-5 the polar lists of both parities. */
+/* Launch one pool iteration: list reset and drain, slot turnover,
+ * continuous steps, DELs, photonuclear polar angles, hard elastic scatters.
+ * Lists 0-1 are the DEL lists, 2-3 the EHS lists and 4-5 the polar lists of
+ * both parities. */
 /* A second stream and two events let the photonuclear polar kernel run
  * beside the EHS kernel: they work on disjoint slots (a DEL or an EHS per
  * slot and iteration), and the polar kernel's long per-lane chains of DDCS
@@ -1009,6 +1033,8 @@ static void gp_iteration(const gp_tables * d_tables, const gp_pool_view & v,
         int * polar_list = v.lists[4 + parity];
         gp_pool_drain<<<grid_step, block, 0, s>>>(d_tables, v.launch, v.pool,
             v.counters, parity);
+        gp_pool_fill<<<grid, block, 0, s>>>(d_tables, v.launch, v.pool,
+            v.counters);
         gp_pool_step<<<grid_step, block, 0, s>>>(d_tables, v.launch, v.pool,
             v.counters, del_list, ehs_list, parity);
         gp_pool_del<<<grid2, block, 0, s>>>(d_tables, v.launch, v.pool,
@@ -1027,6 +1053,19 @@ static void gp_iteration(const gp_tables * d_tables, const gp_pool_view & v,
                 cudaEventRecord(fork->join, fork->s2);
                 cudaStreamWaitEvent(s, fork->join, 0);
         }
+}
+
+/* Kernels per pool iteration, and the slot turnover that closes a batch of
+ * iterations: the events that ended in its last step kernel are written
+ * back before the host reads the counters. */
+#define GP_KERNELS_PER_ITERATION 6
+
+static void gp_batch_end(const gp_tables * d_tables, const gp_pool_view & v,
+    cudaStream_t s)
+{
+        const unsigned int grid = (v.pool.P + 127) / 128;
+        gp_pool_fill<<<grid, 128, 0, s>>>(d_tables, v.launch, v.pool,
+            v.counters);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -1255,6 +1294,7 @@ static int gp_engine_graph(gpumas_engine * g)
                 for (int k = 0; k < iters; k++)
                         gp_iteration(g->d_tables, g->view, g->grid_step,
                             k & 1, cap, &fork);
+                gp_batch_end(g->d_tables, g->view, cap);
                 rc = gp_check(cudaStreamEndCapture(cap, &g->graph));
         }
         if (rc == GPUMAS_RETURN_SUCCESS)
@@ -1484,7 +1524,8 @@ static int gp_engine_batch(gpumas_engine * g)
                 rc = gp_check(cudaGraphLaunch(g->exec, s));
                 cudaEventRecord(g->t1, s);
                 if (rc != GPUMAS_RETURN_SUCCESS) return rc;
-                g->stats.launches += 5 * g->graph_iters;
+                g->stats.launches +=
+                    GP_KERNELS_PER_ITERATION * g->graph_iters + 1;
                 g->stats.batches++;
         }
         rc = gp_check(cudaMemcpyAsync(g->h_counters, g->view.counters,
@@ -1941,6 +1982,7 @@ extern "C" int gp_api_context_transport_device_static(
         for (;;) {
                 for (int k = 0; k < batch; k++)
                         gp_iteration(c->d_tables, v, grid_step, k & 1, s);
+                gp_batch_end(c->d_tables, v, s);
                 rc = gp_check(cudaGetLastError());
                 gp_counters hc;
                 if (rc == GPUMAS_RETURN_SUCCESS)

@@ -226,12 +226,16 @@ def percentiles(values):
 
 
 def sweep(physics, rates, seconds=2.0, scale=1E-03, seed=7,
-          pool_slots=65536, max_inner=8, batch=4, plain_max=300):
-    """Serving sweep: Poisson arrivals at each rate (requests/s) for
-    `seconds`, continuous batching against the plain one-launch-per-request
-    baseline (on at most plain_max requests of each rate), p50/p95/p99
-    latency in ms. Returns the sweep and the highest sustained rate (served
-    throughput at least 90 % of the offered rate) with its p99."""
+          pool_slots=1 << 20, max_inner=8, batch=8, plain_max=300,
+          stop_after=2):
+    """Serving sweep: Poisson arrivals at each rate (requests/s, in
+    increasing order) for `seconds`, continuous batching against the plain
+    one-launch-per-request baseline (on at most plain_max requests of each
+    rate), p50/p95/p99 latency in ms. Returns the sweep and the highest
+    sustained rate (served throughput at least 90 % of the offered rate)
+    with its p99. After `stop_after` rates in a row that are not sustained
+    the server is saturated: the higher rates are listed as skipped (their
+    backlog would only grow)."""
     mix = RequestMix(physics, seed=seed, scale=scale)
     server = Server(physics, pool_slots=pool_slots, max_inner=max_inner,
                     batch=batch)
@@ -242,7 +246,11 @@ def sweep(physics, rates, seconds=2.0, scale=1E-03, seed=7,
     out = []
     best = None
     base = 0
+    missed = 0
     for rate in rates:
+        if stop_after and missed >= stop_after:
+            out.append({"rate": rate, "skipped": "saturated at lower rates"})
+            continue
         n = max(1, int(round(rate * seconds)))
         gaps = -np.log(W.uniform(seed, 5, np.arange(
             base, base + n, dtype=np.uint64), 0)) / rate
@@ -258,6 +266,7 @@ def sweep(physics, rates, seconds=2.0, scale=1E-03, seed=7,
                  "events_per_s": events / wall,
                  "latency_ms": percentiles(lat), "event_errors": errors,
                  "sustained": bool(n / wall >= 0.9 * rate)}
+        missed = 0 if entry["sustained"] else missed + 1
         # The plain baseline on the same arrivals (bounded: the first
         # plain_max requests; none with plain_max = 0).
         m = min(n, plain_max)
@@ -296,6 +305,7 @@ def sweep(physics, rates, seconds=2.0, scale=1E-03, seed=7,
             "engine": server.engine.stats(),
             "config": {"event_scale": scale, "seconds_per_rate": seconds,
                        "state_budget_gb": 40, "pool_slots": pool_slots,
+                       "batch": batch, "max_inner": max_inner,
                        "mix": "70 % slab-stack jobs, 30 % terrain flux "
                               "queries (1-256 directions)"}}
 
@@ -308,13 +318,13 @@ def bench(args, rank, world, local):
     physics = pg.Physics()
     rates = [float(x) for x in args.rates.split(",")]
     r = sweep(physics, rates, args.serve_seconds, args.serve_scale,
-              args.seed, args.pool_slots or 65536, args.max_inner or 8,
-              args.batch or 4, plain_max=args.serve_plain)
+              args.seed, args.pool_slots or (1 << 20), args.max_inner or 8,
+              args.batch or 8, plain_max=args.serve_plain)
     if rank != 0:
         return
     top = None
     for e in r["sweep"]:
-        if e["rate"] == r["highest_sustained_rate"]:
+        if e["rate"] == r["highest_sustained_rate"] and "skipped" not in e:
             top = e
     top = top or r["sweep"][0]
     line = {"metric": "requests/s at p99 latency", "value":
