@@ -76,6 +76,16 @@ enum gp_slot_u64 { SU_ID, SU_SRC, SU_N };
 /* A slot whose event ended in the step kernel (GP_NEXT_DONE): its state
  * and end event wait in the slot for the fill kernel, which writes them back
  * to the job's output and frees the slot. */
+/* Slots whose photonuclear polar angle was sampled beside the next
+ * iteration (the polar kernel runs on its own graph stream into the next
+ * iteration): back in the step phase (GP_POLAR_STEP) or emptied
+ * (GP_POLAR_EMPTY), tagged with the parity p of the iteration that listed
+ * them. The kernels of parity p, two iterations later and after the polar
+ * kernel has joined, take them as GP_NEXT_STEP and GP_EMPTY; those of the
+ * other parity, which can run while the polar kernel writes them, leave
+ * them alone, as they leave the slots still listed (GP_NEXT_DEL). */
+#define GP_POLAR_STEP(p) (5 + (p))
+#define GP_POLAR_EMPTY(p) (7 + (p))
 
 struct gp_pool {
         double * d;
@@ -249,17 +259,19 @@ __device__ __forceinline__ void gp_job_event_done(const gp_launch * X,
 }
 
 /* Finish an event: write its state and results back at its index in its
- * job and free the slot. */
+ * job and free the slot (phase `empty`: GP_EMPTY, or GP_POLAR_EMPTY from
+ * the polar kernel). */
 __device__ __forceinline__ void gp_finish(const gp_pool & pool, int slot,
     const gp_launch * X, const gp_job & J, gp_counters * cnt, gp_event & e,
-    int event, int medium_out)
+    int event, int medium_out, int empty = GP_EMPTY)
 {
         gp_stepping_end(J.cfg, e);
+        const int job = PI(SI_JOB);
         J.io.store((size_t)PU(SU_SRC), e, event, PI(SI_MEDIUM_IN),
             medium_out);
-        PI(SI_PHASE) = GP_EMPTY;
+        PI(SI_PHASE) = empty;
         atomicSub(&cnt->active, 1);
-        gp_job_event_done(X, cnt, PI(SI_JOB));
+        gp_job_event_done(X, cnt, job);
 }
 
 /* Count one unit of progress per calling lane, with one atomic per warp. */
@@ -344,9 +356,11 @@ static __device__ __forceinline__ int gp_refill(const gp_tables & T,
         }
 }
 
-/* First kernel of a pool iteration. Block 0 clears the other parity's
- * lists and cursors, which the previous iteration's kernels (before this
- * one in stream order) have consumed.
+/* First kernel of a pool iteration. Block 0 clears the other parity's DEL
+ * and EHS lists and cursors, which the previous iteration's kernels (before
+ * this one in stream order) have consumed, and this parity's polar list,
+ * consumed by the polar kernel of two iterations before (joined before this
+ * one).
  *
  * It also drains the pool: once no event is left in the queue and at most
  * tail_slots slots are active, regrouping by step kind would leave most
@@ -354,8 +368,8 @@ static __device__ __forceinline__ int gp_refill(const gp_tables & T,
  * slots and carries their events to the end, DELs and EHSs included (the
  * one thread per event scheme); an event's operations and draws are the
  * same either way. Otherwise the kernel returns at once. At the start of
- * an iteration every active slot is in the continuous step phase: the DEL,
- * polar and EHS kernels of the previous iteration set it back. */
+ * an iteration an active slot is in the continuous step phase, ended
+ * (GP_NEXT_DONE) or with the polar kernel of the previous iteration. */
 __global__ void __launch_bounds__(128, 1) gp_pool_drain(
     const gp_tables * __restrict__ Tp, const gp_launch * __restrict__ X,
     const gp_pool pool, gp_counters * cnt, int parity)
@@ -363,10 +377,10 @@ __global__ void __launch_bounds__(128, 1) gp_pool_drain(
         if ((blockIdx.x == 0) && (threadIdx.x == 0)) {
                 cnt->n_del[parity ^ 1] = 0;
                 cnt->n_ehs[parity ^ 1] = 0;
-                cnt->n_polar[parity ^ 1] = 0;
-                cnt->polar_next[parity ^ 1] = 0;
                 cnt->step_next[parity ^ 1] = 0;
                 cnt->drain_next[parity ^ 1] = 0;
+                cnt->n_polar[parity] = 0;
+                cnt->polar_next[parity] = 0;
         }
         const int tail = (X->tail_slots > 0) && (cnt->cursor >= X->total) &&
             (cnt->active <= X->tail_slots);
@@ -382,7 +396,10 @@ __global__ void __launch_bounds__(128, 1) gp_pool_drain(
                 base = w.shfl(base, 0);
                 const int slot = base + (int)w.thread_rank();
                 if (slot >= pool.P) return;
-                if (PI(SI_PHASE) != GP_NEXT_STEP) continue;
+                const int phase = PI(SI_PHASE);
+                if ((phase != GP_NEXT_STEP) &&
+                    (phase != GP_POLAR_STEP(parity)))
+                        continue;
                 const gp_job & J = X->jobs[PI(SI_JOB)];
                 gp_event e;
                 gp_loop L;
@@ -416,7 +433,7 @@ __global__ void __launch_bounds__(128, 1) gp_pool_drain(
  * once and the next one taken), which enters the step phase. */
 __global__ void __launch_bounds__(128, 1) gp_pool_fill(
     const gp_tables * __restrict__ Tp, const gp_launch * __restrict__ X,
-    const gp_pool pool, gp_counters * cnt)
+    const gp_pool pool, gp_counters * cnt, int parity)
 {
         const int slot = blockIdx.x * blockDim.x + threadIdx.x;
         if (slot >= pool.P) return;
@@ -431,7 +448,7 @@ __global__ void __launch_bounds__(128, 1) gp_pool_fill(
                     L.medium);
                 phase = GP_EMPTY;
         }
-        if (phase != GP_EMPTY) return;
+        if ((phase != GP_EMPTY) && (phase != GP_POLAR_EMPTY(parity))) return;
         int job;
         if (!gp_refill(T, X, pool, slot, cnt, e, L, job)) return;
         gp_slot_store(pool, slot, e, L);
@@ -475,7 +492,10 @@ __global__ void __launch_bounds__(128, GP_STEP_MIN_BLOCKS) gp_pool_step(
                         }
                         {
                                 const int slot = j;
-                                if (PI(SI_PHASE) != GP_NEXT_STEP) continue;
+                                const int phase = PI(SI_PHASE);
+                                if ((phase != GP_NEXT_STEP) &&
+                                    (phase != GP_POLAR_STEP(parity)))
+                                        continue;
                                 J = X->jobs + PI(SI_JOB);
                                 gp_slot_load(pool, slot, J->cfg, e, L);
                         }
@@ -858,13 +878,17 @@ static __device__ __forceinline__ double gp_pn_value(
         return (s.phase == PN_REJECT) ? d2 * s.Q2 : -d2 * s.Q2;
 }
 
-/* Deferred photonuclear polar angles: lanes refill from the list. */
+/* Deferred photonuclear polar angles: lanes refill from the list. With
+ * `side`, the kernel runs beside the next iteration and marks the slots it
+ * releases with this iteration's parity (GP_POLAR_STEP, GP_POLAR_EMPTY). */
 __global__ void __launch_bounds__(128, GP_POOL_MIN_BLOCKS) gp_pool_polar(
     const gp_tables * __restrict__ Tp, const gp_launch * __restrict__ X,
     const gp_pool pool, gp_counters * cnt, const int * __restrict__ list,
-    int parity)
+    int parity, int side)
 {
         const int count = cnt->n_polar[parity];
+        const int step = side ? GP_POLAR_STEP(parity) : GP_NEXT_STEP;
+        const int empty = side ? GP_POLAR_EMPTY(parity) : GP_EMPTY;
         const gp_tables & T = *Tp;
         int * cursor = &cnt->polar_next[parity];
         gp_event e;
@@ -893,10 +917,10 @@ __global__ void __launch_bounds__(128, GP_POOL_MIN_BLOCKS) gp_pool_polar(
                                     T, J->cfg, e, L, event);
                                 if (next == GP_NEXT_DONE) {
                                         gp_finish(pool, slot, X, *J, cnt, e,
-                                            event, L.medium);
+                                            event, L.medium, empty);
                                 } else {
                                         gp_slot_store(pool, slot, e, L);
-                                        PI(SI_PHASE) = GP_NEXT_STEP;
+                                        PI(SI_PHASE) = step;
                                 }
                                 slot = -1;
                         }
@@ -912,10 +936,10 @@ __global__ void __launch_bounds__(128, GP_POOL_MIN_BLOCKS) gp_pool_polar(
                                     T, J->cfg, e, L, event);
                                 if (next == GP_NEXT_DONE) {
                                         gp_finish(pool, slot, X, *J, cnt, e,
-                                            event, L.medium);
+                                            event, L.medium, empty);
                                 } else {
                                         gp_slot_store(pool, slot, e, L);
-                                        PI(SI_PHASE) = GP_NEXT_STEP;
+                                        PI(SI_PHASE) = step;
                                 }
                                 slot = -1;
                         }
@@ -1007,52 +1031,56 @@ static unsigned int gp_step_wave(int P, int block)
         return (wave < grid) ? wave : grid;
 }
 
-/* Launch one pool iteration: list reset and drain, slot turnover,
- * continuous steps, DELs, photonuclear polar angles, hard elastic scatters.
- * Lists 0-1 are the DEL lists, 2-3 the EHS lists and 4-5 the polar lists of
- * both parities. */
-/* A second stream and two events let the photonuclear polar kernel run
- * beside the EHS kernel: they work on disjoint slots (a DEL or an EHS per
- * slot and iteration), and the polar kernel's long per-lane chains of DDCS
- * evaluations keep few warps per SM busy. With fork == NULL the kernels run
- * one after the other on s. */
+/* Launch pool iteration k (list parity k & 1): list reset and drain, slot
+ * turnover, continuous steps, DELs, hard elastic scatters and photonuclear
+ * polar angles. Lists 0-1 are the DEL lists, 2-3 the EHS lists and 4-5 the
+ * polar lists of both parities.
+ *
+ * With fork == NULL every kernel runs on s, one after the other. With a
+ * fork, the polar kernel runs on a second stream from the end of the DEL
+ * kernel on into the next iteration: each of its lanes carries one event's
+ * chain of up to hundreds of DDCS evaluations, so it keeps few warps busy
+ * for about a millisecond, which the EHS kernel and the next iteration's
+ * step kernel now fill. Its slots (a few per thousand of the pool) sit out
+ * the next step kernel; iteration k + 2 waits for it before it starts. */
 struct gp_fork {
         cudaStream_t s2;
-        cudaEvent_t fork, join;
+        cudaEvent_t del_done, polar_done[2];
 };
 
 static void gp_iteration(const gp_tables * d_tables, const gp_pool_view & v,
-    unsigned int grid_step, int parity, cudaStream_t s,
+    unsigned int grid_step, int k, cudaStream_t s,
     const gp_fork * fork = NULL)
 {
         const int block = 128;
+        const int parity = k & 1;
+        const int side = (fork != NULL);
         const unsigned int grid = (v.pool.P + block - 1) / block;
         const unsigned int grid2 = (grid + 3) / 4;
         int * del_list = v.lists[parity];
         int * ehs_list = v.lists[2 + parity];
         int * polar_list = v.lists[4 + parity];
+        if (side && (k >= 2))
+                cudaStreamWaitEvent(s, fork->polar_done[parity], 0);
         gp_pool_drain<<<grid_step, block, 0, s>>>(d_tables, v.launch, v.pool,
             v.counters, parity);
         gp_pool_fill<<<grid, block, 0, s>>>(d_tables, v.launch, v.pool,
-            v.counters);
+            v.counters, parity);
         gp_pool_step<<<grid_step, block, 0, s>>>(d_tables, v.launch, v.pool,
             v.counters, del_list, ehs_list, parity);
         gp_pool_del<<<grid2, block, 0, s>>>(d_tables, v.launch, v.pool,
             v.counters, del_list, polar_list, parity);
         cudaStream_t sp = s;
-        if (fork != NULL) {
-                cudaEventRecord(fork->fork, s);
-                cudaStreamWaitEvent(fork->s2, fork->fork, 0);
+        if (side) {
+                cudaEventRecord(fork->del_done, s);
+                cudaStreamWaitEvent(fork->s2, fork->del_done, 0);
                 sp = fork->s2;
         }
         gp_pool_polar<<<grid2, block, 0, sp>>>(d_tables, v.launch, v.pool,
-            v.counters, polar_list, parity);
+            v.counters, polar_list, parity, side);
+        if (side) cudaEventRecord(fork->polar_done[parity], sp);
         gp_pool_ehs<<<grid2, block, 0, s>>>(d_tables, v.launch, v.pool,
             v.counters, ehs_list, parity);
-        if (fork != NULL) {
-                cudaEventRecord(fork->join, fork->s2);
-                cudaStreamWaitEvent(s, fork->join, 0);
-        }
 }
 
 /* Kernels per pool iteration, and the slot turnover that closes a batch of
@@ -1061,11 +1089,15 @@ static void gp_iteration(const gp_tables * d_tables, const gp_pool_view & v,
 #define GP_KERNELS_PER_ITERATION 6
 
 static void gp_batch_end(const gp_tables * d_tables, const gp_pool_view & v,
-    cudaStream_t s)
+    cudaStream_t s, const gp_fork * fork = NULL)
 {
+        if (fork != NULL) {
+                cudaStreamWaitEvent(s, fork->polar_done[0], 0);
+                cudaStreamWaitEvent(s, fork->polar_done[1], 0);
+        }
         const unsigned int grid = (v.pool.P + 127) / 128;
         gp_pool_fill<<<grid, 128, 0, s>>>(d_tables, v.launch, v.pool,
-            v.counters);
+            v.counters, 0);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -1279,28 +1311,27 @@ static int gp_engine_graph(gpumas_engine * g)
         if (rc != GPUMAS_RETURN_SUCCESS) return rc;
         gp_fork fork;
         memset(&fork, 0, sizeof(fork));
+        cudaEvent_t * events[3] = { &fork.del_done, &fork.polar_done[0],
+                &fork.polar_done[1] };
         rc = gp_check(cudaStreamCreateWithFlags(
             &fork.s2, cudaStreamNonBlocking));
-        if (rc == GPUMAS_RETURN_SUCCESS)
+        for (int q = 0; (q < 3) && (rc == GPUMAS_RETURN_SUCCESS); q++)
                 rc = gp_check(cudaEventCreateWithFlags(
-                    &fork.fork, cudaEventDisableTiming));
-        if (rc == GPUMAS_RETURN_SUCCESS)
-                rc = gp_check(cudaEventCreateWithFlags(
-                    &fork.join, cudaEventDisableTiming));
+                    events[q], cudaEventDisableTiming));
         if (rc == GPUMAS_RETURN_SUCCESS)
                 rc = gp_check(cudaStreamBeginCapture(
                     cap, cudaStreamCaptureModeThreadLocal));
         if (rc == GPUMAS_RETURN_SUCCESS) {
                 for (int k = 0; k < iters; k++)
-                        gp_iteration(g->d_tables, g->view, g->grid_step,
-                            k & 1, cap, &fork);
-                gp_batch_end(g->d_tables, g->view, cap);
+                        gp_iteration(g->d_tables, g->view, g->grid_step, k,
+                            cap, &fork);
+                gp_batch_end(g->d_tables, g->view, cap, &fork);
                 rc = gp_check(cudaStreamEndCapture(cap, &g->graph));
         }
         if (rc == GPUMAS_RETURN_SUCCESS)
                 rc = gp_check(cudaGraphInstantiate(&g->exec, g->graph, 0));
-        if (fork.join != NULL) cudaEventDestroy(fork.join);
-        if (fork.fork != NULL) cudaEventDestroy(fork.fork);
+        for (int q = 0; q < 3; q++)
+                if (*events[q] != NULL) cudaEventDestroy(*events[q]);
         if (fork.s2 != NULL) cudaStreamDestroy(fork.s2);
         cudaStreamDestroy(cap);
         if (rc == GPUMAS_RETURN_SUCCESS) g->graph_iters = iters;
@@ -1981,7 +2012,7 @@ extern "C" int gp_api_context_transport_device_static(
         unsigned long long seen_cursor = 0, seen_progress = 0;
         for (;;) {
                 for (int k = 0; k < batch; k++)
-                        gp_iteration(c->d_tables, v, grid_step, k & 1, s);
+                        gp_iteration(c->d_tables, v, grid_step, k, s);
                 gp_batch_end(c->d_tables, v, s);
                 rc = gp_check(cudaGetLastError());
                 gp_counters hc;
