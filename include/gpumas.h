@@ -415,7 +415,7 @@ int gpumas_context_carry_get(
  * memory, a plugin whose framework forbids allocation on its hot path).
  *
  * The slot pool lives in one static device array of the library, sized for
- * GPUMAS_STATIC_SLOTS slots (about 10 MB), which every GPU that loads the
+ * GPUMAS_STATIC_SLOTS slots (about 13 MB), which every GPU that loads the
  * library holds until the process exits. `pool_slots` must be a multiple of
  * 128 in [128, GPUMAS_STATIC_SLOTS], or 0 for the maximum; other values
  * return GPUMAS_RETURN_VALUE_ERROR. The call makes no cudaMalloc or

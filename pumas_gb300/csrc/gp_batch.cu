@@ -61,14 +61,15 @@ enum gp_slot_double {
         SD_POS0, SD_POS1, SD_POS2, SD_DIR0, SD_DIR1, SD_DIR2,
         SD_STEP_X_LIMIT, SD_STEP_INVLB1, SD_RANDN_NEXT, SD_LIFETIME, SD_RNEXT,
         SD_DENSITY, SD_TI, SD_WI, SD_XI, SD_XF, SD_DEI, SD_GRAMMAGE_MAX,
-        SD_STEP_MAX_MEDIUM, SD_POLAR_KI, SD_POLAR_KF, SD_N
+        SD_STEP_MAX_MEDIUM, SD_POLAR_KI, SD_POLAR_KF, SD_LOC_MAG0,
+        SD_LOC_MAG1, SD_LOC_MAG2, SD_LOC_DENSITY, SD_LOC_STEP_MAX, SD_N
 };
 enum gp_slot_int {
         SI_DECAYED, SI_STEP_FIRST, SI_STEP_EVENT, SI_STEP_FORESEEN,
         SI_RANDN_DONE, SI_STEPS, SI_STATUS, SI_MEDIUM, SI_MATERIAL,
         SI_STRAIGHT, SI_STEP_INDEX, SI_NEW_MEDIUM, SI_PHASE, SI_MEDIUM_IN,
         SI_N_DRAWS, SI_POLAR_PROCESS, SI_POLAR_TARGET, SI_JOB, SI_EVENT_END,
-        SI_N
+        SI_LOC_MAGNETIZED, SI_N
 };
 enum gp_slot_u64 { SU_ID, SU_SRC, SU_N };
 
@@ -236,6 +237,38 @@ __device__ __forceinline__ void gp_slot_store(const gp_pool & pool, int slot,
         PI(SI_NEW_MEDIUM) = L.new_medium;
 }
 
+/* Local properties of the current medium (struct gp_loc) of a slot whose
+ * job's geometry has locals (struct gpumas_locals): loaded into `loc`,
+ * whose address is returned, or NULL for the other jobs. The kernels are
+ * built twice: with LOC = 0 (no job with locals in the pool, the locals
+ * code compiled out) and LOC = 1. */
+template <int LOC>
+__device__ __forceinline__ gp_loc * gp_loc_load(const gp_pool & pool,
+    int slot, const gpumas_geometry * g, gp_loc & loc)
+{
+        if (!LOC || (g->locals == NULL)) return NULL;
+        loc.g = g;
+        loc.magnet[0] = PD(SD_LOC_MAG0);
+        loc.magnet[1] = PD(SD_LOC_MAG1);
+        loc.magnet[2] = PD(SD_LOC_MAG2);
+        loc.density = PD(SD_LOC_DENSITY);
+        loc.step_max = PD(SD_LOC_STEP_MAX);
+        loc.magnetized = PI(SI_LOC_MAGNETIZED);
+        return &loc;
+}
+
+__device__ __forceinline__ void gp_loc_store(const gp_pool & pool, int slot,
+    const gp_loc * loc)
+{
+        if (loc == NULL) return;
+        PD(SD_LOC_MAG0) = loc->magnet[0];
+        PD(SD_LOC_MAG1) = loc->magnet[1];
+        PD(SD_LOC_MAG2) = loc->magnet[2];
+        PD(SD_LOC_DENSITY) = loc->density;
+        PD(SD_LOC_STEP_MAX) = loc->step_max;
+        PI(SI_LOC_MAGNETIZED) = loc->magnetized;
+}
+
 /* Append `slot` to a compact list with one atomic per warp. */
 __device__ __forceinline__ void gp_append(int * count, int * list, int slot)
 {
@@ -320,9 +353,10 @@ __device__ __forceinline__ int gp_job_of(const gp_launch * X,
  * first step are finished here and the next one is taken. Returns 1 if the
  * slot now holds an event to step (e, L loaded, *job set), 0 if the queue
  * is empty. */
+template <int LOC>
 static __device__ __forceinline__ int gp_refill(const gp_tables & T,
     const gp_launch * X, const gp_pool & pool, int slot, gp_counters * cnt,
-    gp_event & e, gp_loop & L, int & job)
+    gp_event & e, gp_loop & L, int & job, gp_loc & loc, gp_loc *& lp)
 {
         const unsigned long long total = X->total;
         for (;;) {
@@ -341,8 +375,9 @@ static __device__ __forceinline__ int gp_refill(const gp_tables & T,
                 const unsigned long long k = idx - J.begin;
                 J.io.begin((size_t)k, J.cfg, J.first_event + k, e);
                 int medium_in, event = GPUMAS_EVENT_NONE;
+                lp = (LOC && (J.geometry->locals != NULL)) ? &loc : NULL;
                 const int next = gp_transport_begin(
-                    T, J.cfg, *J.geometry, e, L, event, medium_in);
+                    T, J.cfg, *J.geometry, e, L, event, medium_in, NULL, lp);
                 if (next == GP_NEXT_DONE) {
                         J.io.store((size_t)k, e, event, medium_in, L.medium);
                         gp_job_event_done(X, cnt, job);
@@ -370,6 +405,7 @@ static __device__ __forceinline__ int gp_refill(const gp_tables & T,
  * same either way. Otherwise the kernel returns at once. At the start of
  * an iteration an active slot is in the continuous step phase, ended
  * (GP_NEXT_DONE) or with the polar kernel of the previous iteration. */
+template <int LOC>
 __global__ void __launch_bounds__(128, 1) gp_pool_drain(
     const gp_tables * __restrict__ Tp, const gp_launch * __restrict__ X,
     const gp_pool pool, gp_counters * cnt, int parity)
@@ -403,7 +439,9 @@ __global__ void __launch_bounds__(128, 1) gp_pool_drain(
                 const gp_job & J = X->jobs[PI(SI_JOB)];
                 gp_event e;
                 gp_loop L;
+                gp_loc loc;
                 gp_slot_load(pool, slot, J.cfg, e, L);
+                gp_loc * lp = gp_loc_load<LOC>(pool, slot, J.geometry, loc);
                 int event = GPUMAS_EVENT_NONE;
                 int next = GP_NEXT_STEP;
                 /* An event ends within GP_MAX_STEPS steps, each followed by
@@ -414,12 +452,14 @@ __global__ void __launch_bounds__(128, 1) gp_pool_drain(
                                 break;
                         }
                         if (next == GP_NEXT_STEP)
-                                next = gp_stepping_step(
-                                    T, J.cfg, *J.geometry, e, L, event);
+                                next = gp_stepping_step(T, J.cfg,
+                                    *J.geometry, e, L, event, NULL, lp);
                         else if (next == GP_NEXT_DEL)
-                                next = gp_stepping_del(T, J.cfg, e, L, event);
+                                next = gp_stepping_del(
+                                    T, J.cfg, e, L, event, NULL, lp);
                         else
-                                next = gp_stepping_ehs(T, J.cfg, e, L, event);
+                                next = gp_stepping_ehs(
+                                    T, J.cfg, e, L, event, lp);
                 }
                 gp_progress(cnt);
                 gp_finish(pool, slot, X, J, cnt, e, event, L.medium);
@@ -431,6 +471,7 @@ __global__ void __launch_bounds__(128, 1) gp_pool_drain(
  * slot freed; an empty slot takes the next event of the queue
  * (gp_refill: events that end before their first step are written back at
  * once and the next one taken), which enters the step phase. */
+template <int LOC>
 __global__ void __launch_bounds__(128, 1) gp_pool_fill(
     const gp_tables * __restrict__ Tp, const gp_launch * __restrict__ X,
     const gp_pool pool, gp_counters * cnt, int parity)
@@ -450,8 +491,11 @@ __global__ void __launch_bounds__(128, 1) gp_pool_fill(
         }
         if ((phase != GP_EMPTY) && (phase != GP_POLAR_EMPTY(parity))) return;
         int job;
-        if (!gp_refill(T, X, pool, slot, cnt, e, L, job)) return;
+        gp_loc loc, * lp = NULL;
+        if (!gp_refill<LOC>(T, X, pool, slot, cnt, e, L, job, loc, lp))
+                return;
         gp_slot_store(pool, slot, e, L);
+        gp_loc_store(pool, slot, lp);
         PI(SI_PHASE) = GP_NEXT_STEP;
 }
 
@@ -462,6 +506,7 @@ __global__ void __launch_bounds__(128, 1) gp_pool_fill(
  * the pool is exhausted, whatever the number of steps of each event. Slots
  * are emptied and refilled by the fill kernel, which keeps the input and
  * output code out of this one. */
+template <int LOC>
 __global__ void __launch_bounds__(128, GP_STEP_MIN_BLOCKS) gp_pool_step(
     const gp_tables * __restrict__ Tp, const gp_launch * __restrict__ X,
     const gp_pool pool, gp_counters * cnt, int * del_list, int * ehs_list,
@@ -472,6 +517,7 @@ __global__ void __launch_bounds__(128, GP_STEP_MIN_BLOCKS) gp_pool_step(
         int * scursor = &cnt->step_next[parity];
         gp_event e;
         gp_loop L;
+        gp_loc loc, * lp = NULL;
         const gp_job * J = X->jobs;
         int slot = -1, k = 0, exhausted = 0;
         /* Every pass steps each lane that holds a slot; a lane takes at
@@ -498,6 +544,8 @@ __global__ void __launch_bounds__(128, GP_STEP_MIN_BLOCKS) gp_pool_step(
                                         continue;
                                 J = X->jobs + PI(SI_JOB);
                                 gp_slot_load(pool, slot, J->cfg, e, L);
+                                lp = gp_loc_load<LOC>(
+                                    pool, slot, J->geometry, loc);
                         }
                         slot = j;
                         k = 0;
@@ -505,10 +553,11 @@ __global__ void __launch_bounds__(128, GP_STEP_MIN_BLOCKS) gp_pool_step(
                 if (!__any_sync(0xFFFFFFFFu, slot >= 0)) break;
                 if (slot >= 0) {
                         int event = GPUMAS_EVENT_NONE;
-                        const int next = gp_stepping_step(
-                            T, J->cfg, *J->geometry, e, L, event);
+                        const int next = gp_stepping_step(T, J->cfg,
+                            *J->geometry, e, L, event, NULL, lp);
                         k++;
                         if ((next != GP_NEXT_STEP) || (k >= max_inner)) {
+                                gp_loc_store(pool, slot, lp);
                                 gp_route(pool, slot, X, *J, cnt, del_list,
                                     ehs_list, parity, next, e, L, event);
                                 slot = -1;
@@ -521,6 +570,7 @@ __global__ void __launch_bounds__(128, GP_STEP_MIN_BLOCKS) gp_pool_step(
  * Photonuclear polar angles (a Brent maximisation of the DDCS followed by a
  * rejection sampling, pumas.c:11874-11950) cost far more than the others
  * and are deferred to the polar list, so that they run in full warps. */
+template <int LOC>
 __global__ void __launch_bounds__(128, GP_POOL_MIN_BLOCKS) gp_pool_del(
     const gp_tables * __restrict__ Tp, const gp_launch * __restrict__ X,
     const gp_pool pool, gp_counters * cnt, const int * __restrict__ list,
@@ -551,11 +601,15 @@ __global__ void __launch_bounds__(128, GP_POOL_MIN_BLOCKS) gp_pool_del(
                         continue;
                 }
                 gp_do_del_polar(T, e, job);
-                const int next = gp_stepping_del_end(T, cfg, e, L, event);
+                gp_loc loc;
+                gp_loc * lp = gp_loc_load<LOC>(pool, slot, J.geometry, loc);
+                const int next =
+                    gp_stepping_del_end(T, cfg, e, L, event, lp);
                 if (next == GP_NEXT_DONE) {
                         gp_finish(pool, slot, X, J, cnt, e, event, L.medium);
                 } else {
                         gp_slot_store(pool, slot, e, L);
+                        gp_loc_store(pool, slot, lp);
                         PI(SI_PHASE) = GP_NEXT_STEP;
                 }
         }
@@ -881,6 +935,7 @@ static __device__ __forceinline__ double gp_pn_value(
 /* Deferred photonuclear polar angles: lanes refill from the list. With
  * `side`, the kernel runs beside the next iteration and marks the slots it
  * releases with this iteration's parity (GP_POLAR_STEP, GP_POLAR_EMPTY). */
+template <int LOC>
 __global__ void __launch_bounds__(128, GP_POOL_MIN_BLOCKS) gp_pool_polar(
     const gp_tables * __restrict__ Tp, const gp_launch * __restrict__ X,
     const gp_pool pool, gp_counters * cnt, const int * __restrict__ list,
@@ -913,13 +968,17 @@ __global__ void __launch_bounds__(128, GP_POOL_MIN_BLOCKS) gp_pool_polar(
                                 if (s.phase != PN_DONE) break;
                                 gp_rotate(e, s.mu);
                                 int event = GPUMAS_EVENT_NONE;
+                                gp_loc loc;
+                                gp_loc * lp = gp_loc_load<LOC>(
+                                    pool, slot, J->geometry, loc);
                                 const int next = gp_stepping_del_end(
-                                    T, J->cfg, e, L, event);
+                                    T, J->cfg, e, L, event, lp);
                                 if (next == GP_NEXT_DONE) {
                                         gp_finish(pool, slot, X, *J, cnt, e,
                                             event, L.medium, empty);
                                 } else {
                                         gp_slot_store(pool, slot, e, L);
+                                        gp_loc_store(pool, slot, lp);
                                         PI(SI_PHASE) = step;
                                 }
                                 slot = -1;
@@ -932,13 +991,17 @@ __global__ void __launch_bounds__(128, GP_POOL_MIN_BLOCKS) gp_pool_polar(
                         if (s.phase == PN_DONE) {
                                 gp_rotate(e, s.mu);
                                 int event = GPUMAS_EVENT_NONE;
+                                gp_loc loc;
+                                gp_loc * lp = gp_loc_load<LOC>(
+                                    pool, slot, J->geometry, loc);
                                 const int next = gp_stepping_del_end(
-                                    T, J->cfg, e, L, event);
+                                    T, J->cfg, e, L, event, lp);
                                 if (next == GP_NEXT_DONE) {
                                         gp_finish(pool, slot, X, *J, cnt, e,
                                             event, L.medium, empty);
                                 } else {
                                         gp_slot_store(pool, slot, e, L);
+                                        gp_loc_store(pool, slot, lp);
                                         PI(SI_PHASE) = step;
                                 }
                                 slot = -1;
@@ -947,6 +1010,7 @@ __global__ void __launch_bounds__(128, GP_POOL_MIN_BLOCKS) gp_pool_polar(
         }
 }
 
+template <int LOC>
 __global__ void __launch_bounds__(128, GP_POOL_MIN_BLOCKS) gp_pool_ehs(
     const gp_tables * __restrict__ Tp, const gp_launch * __restrict__ X,
     const gp_pool pool, gp_counters * cnt, const int * __restrict__ list,
@@ -962,12 +1026,15 @@ __global__ void __launch_bounds__(128, GP_POOL_MIN_BLOCKS) gp_pool_ehs(
                 gp_event e;
                 gp_loop L;
                 gp_slot_load(pool, slot, cfg, e, L);
+                gp_loc loc;
+                gp_loc * lp = gp_loc_load<LOC>(pool, slot, J.geometry, loc);
                 int event = GPUMAS_EVENT_NONE;
-                const int next = gp_stepping_ehs(T, cfg, e, L, event);
+                const int next = gp_stepping_ehs(T, cfg, e, L, event, lp);
                 if (next == GP_NEXT_DONE) {
                         gp_finish(pool, slot, X, J, cnt, e, event, L.medium);
                 } else {
                         gp_slot_store(pool, slot, e, L);
+                        gp_loc_store(pool, slot, lp);
                         PI(SI_PHASE) = GP_NEXT_STEP;
                 }
         }
@@ -1024,7 +1091,7 @@ static unsigned int gp_step_wave(int P, int block)
         cudaGetDevice(&device);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &per_sm, gp_pool_step, block, 0);
+            &per_sm, gp_pool_step<0>, block, 0);
         const unsigned int wave =
             (unsigned int)(sms * (per_sm > 0 ? per_sm : 1));
         const unsigned int grid = (P + block - 1) / block;
@@ -1048,6 +1115,7 @@ struct gp_fork {
         cudaEvent_t del_done, polar_done[2];
 };
 
+template <int LOC>
 static void gp_iteration(const gp_tables * d_tables, const gp_pool_view & v,
     unsigned int grid_step, int k, cudaStream_t s,
     const gp_fork * fork = NULL)
@@ -1062,25 +1130,25 @@ static void gp_iteration(const gp_tables * d_tables, const gp_pool_view & v,
         int * polar_list = v.lists[4 + parity];
         if (side && (k >= 2))
                 cudaStreamWaitEvent(s, fork->polar_done[parity], 0);
-        gp_pool_drain<<<grid_step, block, 0, s>>>(d_tables, v.launch, v.pool,
-            v.counters, parity);
-        gp_pool_fill<<<grid, block, 0, s>>>(d_tables, v.launch, v.pool,
-            v.counters, parity);
-        gp_pool_step<<<grid_step, block, 0, s>>>(d_tables, v.launch, v.pool,
-            v.counters, del_list, ehs_list, parity);
-        gp_pool_del<<<grid2, block, 0, s>>>(d_tables, v.launch, v.pool,
-            v.counters, del_list, polar_list, parity);
+        gp_pool_drain<LOC><<<grid_step, block, 0, s>>>(d_tables, v.launch,
+            v.pool, v.counters, parity);
+        gp_pool_fill<LOC><<<grid, block, 0, s>>>(d_tables, v.launch,
+            v.pool, v.counters, parity);
+        gp_pool_step<LOC><<<grid_step, block, 0, s>>>(d_tables, v.launch,
+            v.pool, v.counters, del_list, ehs_list, parity);
+        gp_pool_del<LOC><<<grid2, block, 0, s>>>(d_tables, v.launch,
+            v.pool, v.counters, del_list, polar_list, parity);
         cudaStream_t sp = s;
         if (side) {
                 cudaEventRecord(fork->del_done, s);
                 cudaStreamWaitEvent(fork->s2, fork->del_done, 0);
                 sp = fork->s2;
         }
-        gp_pool_polar<<<grid2, block, 0, sp>>>(d_tables, v.launch, v.pool,
-            v.counters, polar_list, parity, side);
+        gp_pool_polar<LOC><<<grid2, block, 0, sp>>>(d_tables, v.launch,
+            v.pool, v.counters, polar_list, parity, side);
         if (side) cudaEventRecord(fork->polar_done[parity], sp);
-        gp_pool_ehs<<<grid2, block, 0, s>>>(d_tables, v.launch, v.pool,
-            v.counters, ehs_list, parity);
+        gp_pool_ehs<LOC><<<grid2, block, 0, s>>>(d_tables, v.launch,
+            v.pool, v.counters, ehs_list, parity);
 }
 
 /* Kernels per pool iteration, and the slot turnover that closes a batch of
@@ -1088,6 +1156,7 @@ static void gp_iteration(const gp_tables * d_tables, const gp_pool_view & v,
  * back before the host reads the counters. */
 #define GP_KERNELS_PER_ITERATION 6
 
+template <int LOC>
 static void gp_batch_end(const gp_tables * d_tables, const gp_pool_view & v,
     cudaStream_t s, const gp_fork * fork = NULL)
 {
@@ -1096,7 +1165,7 @@ static void gp_batch_end(const gp_tables * d_tables, const gp_pool_view & v,
                 cudaStreamWaitEvent(s, fork->polar_done[1], 0);
         }
         const unsigned int grid = (v.pool.P + 127) / 128;
-        gp_pool_fill<<<grid, 128, 0, s>>>(d_tables, v.launch, v.pool,
+        gp_pool_fill<LOC><<<grid, 128, 0, s>>>(d_tables, v.launch, v.pool,
             v.counters, 0);
 }
 
@@ -1205,9 +1274,13 @@ struct gpumas_engine {
         int P;
         gp_pool_view view;
         unsigned int grid_step;
-        cudaGraph_t graph;
-        cudaGraphExec_t exec;
-        int graph_iters;
+        /* Batch graphs of the kernels built without (0) and with (1) the
+         * media's local properties; the second serves once a job with
+         * locals joined the table, until the table is emptied. */
+        cudaGraph_t graph[2];
+        cudaGraphExec_t exec[2];
+        int graph_iters[2];
+        int locals;
         /* Jobs: device table, completion counts and list. */
         int capacity;
         gp_job * d_jobs;
@@ -1270,10 +1343,12 @@ static int gp_fifo_push(gpumas_engine * g, int ticket)
 static int gp_engine_pool(gpumas_engine * g, int P)
 {
         if ((g->d_pool != NULL) && (g->P == P)) return GPUMAS_RETURN_SUCCESS;
-        if (g->exec != NULL) cudaGraphExecDestroy(g->exec);
-        if (g->graph != NULL) cudaGraphDestroy(g->graph);
-        g->exec = NULL;
-        g->graph = NULL;
+        for (int q = 0; q < 2; q++) {
+                if (g->exec[q] != NULL) cudaGraphExecDestroy(g->exec[q]);
+                if (g->graph[q] != NULL) cudaGraphDestroy(g->graph[q]);
+                g->exec[q] = NULL;
+                g->graph[q] = NULL;
+        }
         if (g->d_pool != NULL) cudaFree(g->d_pool);
         g->d_pool = NULL;
         g->P = 0;
@@ -1294,17 +1369,18 @@ static int gp_engine_pool(gpumas_engine * g, int P)
 }
 
 /* Capture `iters` iterations (an even number, for the list parity) as a
- * CUDA graph, once per pool. */
-static int gp_engine_graph(gpumas_engine * g)
+ * CUDA graph of the kernels without (loc = 0) or with the locals, once per
+ * pool. */
+static int gp_engine_graph(gpumas_engine * g, int loc)
 {
         const int batch = (g->tuning.batch > 0) ? g->tuning.batch : 16;
         const int iters = 2 * ((batch + 1) / 2);
-        if ((g->exec != NULL) && (g->graph_iters == iters))
+        if ((g->exec[loc] != NULL) && (g->graph_iters[loc] == iters))
                 return GPUMAS_RETURN_SUCCESS;
-        if (g->exec != NULL) cudaGraphExecDestroy(g->exec);
-        if (g->graph != NULL) cudaGraphDestroy(g->graph);
-        g->exec = NULL;
-        g->graph = NULL;
+        if (g->exec[loc] != NULL) cudaGraphExecDestroy(g->exec[loc]);
+        if (g->graph[loc] != NULL) cudaGraphDestroy(g->graph[loc]);
+        g->exec[loc] = NULL;
+        g->graph[loc] = NULL;
         cudaStream_t cap;
         int rc = gp_check(cudaStreamCreateWithFlags(
             &cap, cudaStreamNonBlocking));
@@ -1322,26 +1398,37 @@ static int gp_engine_graph(gpumas_engine * g)
                 rc = gp_check(cudaStreamBeginCapture(
                     cap, cudaStreamCaptureModeThreadLocal));
         if (rc == GPUMAS_RETURN_SUCCESS) {
-                for (int k = 0; k < iters; k++)
-                        gp_iteration(g->d_tables, g->view, g->grid_step, k,
-                            cap, &fork);
-                gp_batch_end(g->d_tables, g->view, cap, &fork);
-                rc = gp_check(cudaStreamEndCapture(cap, &g->graph));
+                for (int k = 0; k < iters; k++) {
+                        if (loc)
+                                gp_iteration<1>(g->d_tables, g->view,
+                                    g->grid_step, k, cap, &fork);
+                        else
+                                gp_iteration<0>(g->d_tables, g->view,
+                                    g->grid_step, k, cap, &fork);
+                }
+                if (loc)
+                        gp_batch_end<1>(g->d_tables, g->view, cap, &fork);
+                else
+                        gp_batch_end<0>(g->d_tables, g->view, cap, &fork);
+                rc = gp_check(cudaStreamEndCapture(cap, &g->graph[loc]));
         }
         if (rc == GPUMAS_RETURN_SUCCESS)
-                rc = gp_check(cudaGraphInstantiate(&g->exec, g->graph, 0));
+                rc = gp_check(cudaGraphInstantiate(
+                    &g->exec[loc], g->graph[loc], 0));
         for (int q = 0; q < 3; q++)
                 if (*events[q] != NULL) cudaEventDestroy(*events[q]);
         if (fork.s2 != NULL) cudaStreamDestroy(fork.s2);
         cudaStreamDestroy(cap);
-        if (rc == GPUMAS_RETURN_SUCCESS) g->graph_iters = iters;
+        if (rc == GPUMAS_RETURN_SUCCESS) g->graph_iters[loc] = iters;
         return rc;
 }
 
 static void gp_engine_free(gpumas_engine * g)
 {
-        if (g->exec != NULL) cudaGraphExecDestroy(g->exec);
-        if (g->graph != NULL) cudaGraphDestroy(g->graph);
+        for (int q = 0; q < 2; q++) {
+                if (g->exec[q] != NULL) cudaGraphExecDestroy(g->exec[q]);
+                if (g->graph[q] != NULL) cudaGraphDestroy(g->graph[q]);
+        }
         if (g->d_pool != NULL) cudaFree(g->d_pool);
         if (g->d_jobs != NULL) cudaFree(g->d_jobs);
         if (g->own_tables && (g->d_tables != NULL)) cudaFree(g->d_tables);
@@ -1457,6 +1544,7 @@ static int gp_engine_restart(gpumas_engine * g)
                 return GPUMAS_RETURN_SUCCESS;
         g->ticket0 += g->n_jobs;
         g->n_jobs = 0;
+        g->locals = 0;
         g->n_uploaded = 0;
         g->n_reported = 0;
         g->total = 0;
@@ -1472,8 +1560,10 @@ static int gp_engine_restart(gpumas_engine * g)
  * so that no lane can ever be given a position between two jobs. */
 static int gp_engine_append(gpumas_engine * g, const gp_config & cfg,
     const gpumas_geometry * geometry, const gp_io & io, size_t n,
-    uint64_t first_event, const gp_job_host & info, int * ticket)
+    uint64_t first_event, const gp_job_host & info, int * ticket,
+    int locals = 0)
 {
+        if (locals) g->locals = 1;
         gp_job & J = g->h_jobs[g->n_jobs];
         memset(&J, 0, sizeof(J));
         J.cfg = cfg;
@@ -1505,18 +1595,16 @@ extern "C" int gp_config_check(const struct gpumas_context * context,
 /* Checks and settings of a job's context. */
 static int gp_engine_context(gpumas_engine * g,
     const struct gpumas_context * context, gp_config * cfg,
-    const gpumas_geometry ** geometry)
+    const gpumas_geometry ** geometry, int * locals)
 {
         if (context == NULL) return GPUMAS_RETURN_VALUE_ERROR;
         const gp_context * c = (const gp_context *)context;
         if (c->physics != g->physics) return GPUMAS_RETURN_PHYSICS_ERROR;
         if (!c->has_geometry) return GPUMAS_RETURN_MEDIUM_ERROR;
-        /* Media with local properties run on the one thread per event
-         * kernel only (gpumas_context_transport). */
-        if (c->has_locals) return GPUMAS_RETURN_VALUE_ERROR;
         const int rc = gp_config_check(context, c->physics, cfg);
         if (rc != GPUMAS_RETURN_SUCCESS) return rc;
         *geometry = c->d_geometry;
+        *locals = c->has_locals;
         return GPUMAS_RETURN_SUCCESS;
 }
 
@@ -1549,14 +1637,15 @@ static int gp_engine_batch(gpumas_engine * g)
                     (g->tuning.tail < 0) ? (int)(g->grid_step * 128) : 0;
                 rc = gp_check(cudaMemcpyAsync(g->view.launch, h,
                     sizeof(gp_launch), cudaMemcpyHostToDevice, s));
-                if (rc == GPUMAS_RETURN_SUCCESS) rc = gp_engine_graph(g);
+                const int loc = g->locals;
+                if (rc == GPUMAS_RETURN_SUCCESS) rc = gp_engine_graph(g, loc);
                 if (rc != GPUMAS_RETURN_SUCCESS) return rc;
                 cudaEventRecord(g->t0, s);
-                rc = gp_check(cudaGraphLaunch(g->exec, s));
+                rc = gp_check(cudaGraphLaunch(g->exec[loc], s));
                 cudaEventRecord(g->t1, s);
                 if (rc != GPUMAS_RETURN_SUCCESS) return rc;
                 g->stats.launches +=
-                    GP_KERNELS_PER_ITERATION * g->graph_iters + 1;
+                    GP_KERNELS_PER_ITERATION * g->graph_iters[loc] + 1;
                 g->stats.batches++;
         }
         rc = gp_check(cudaMemcpyAsync(g->h_counters, g->view.counters,
@@ -1683,7 +1772,8 @@ extern "C" int gp_api_engine_submit(struct gpumas_engine * engine,
         gpumas_engine * g = engine;
         gp_config cfg;
         const gpumas_geometry * geometry;
-        int rc = gp_engine_context(g, job->context, &cfg, &geometry);
+        int locals;
+        int rc = gp_engine_context(g, job->context, &cfg, &geometry, &locals);
         if (rc != GPUMAS_RETURN_SUCCESS) return rc;
         if (job->n > 0) {
                 const gpumas_soa & a = job->events;
@@ -1704,7 +1794,7 @@ extern "C" int gp_api_engine_submit(struct gpumas_engine * engine,
         gp_job_host info;
         memset(&info, 0, sizeof(info));
         return gp_engine_append(g, cfg, geometry, io, job->n,
-            job->first_event, info, ticket);
+            job->first_event, info, ticket, locals);
 }
 
 extern "C" int gp_api_engine_submit_host(struct gpumas_engine * engine,
@@ -1718,7 +1808,8 @@ extern "C" int gp_api_engine_submit_host(struct gpumas_engine * engine,
         gpumas_engine * g = engine;
         gp_config cfg;
         const gpumas_geometry * geometry;
-        int rc = gp_engine_context(g, context, &cfg, &geometry);
+        int locals;
+        int rc = gp_engine_context(g, context, &cfg, &geometry, &locals);
         if (rc != GPUMAS_RETURN_SUCCESS) return rc;
         if (cfg.carry && (n > 0) && (results == NULL))
                 return GPUMAS_RETURN_VALUE_ERROR;
@@ -1756,7 +1847,7 @@ extern "C" int gp_api_engine_submit_host(struct gpumas_engine * engine,
                 info.in_arena = 1;
         }
         return gp_engine_append(g, cfg, geometry, io, n, first_event, info,
-            ticket);
+            ticket, locals);
 }
 
 extern "C" int gp_api_engine_step(struct gpumas_engine * engine,
@@ -1859,7 +1950,7 @@ extern "C" int gp_pool_transport(gp_context * c, const gp_config * cfg,
                 gp_job_host info;
                 memset(&info, 0, sizeof(info));
                 rc = gp_engine_append(g, *cfg, c->d_geometry, *io, n, first,
-                    info, &ticket);
+                    info, &ticket, c->has_locals);
         }
         /* Ends: every batch moves an event or fails (stall). */
         while ((rc == GPUMAS_RETURN_SUCCESS) && (g->inflight > 0 || g->busy))
@@ -1945,7 +2036,6 @@ extern "C" int gp_api_context_transport_device_static(
                 return GPUMAS_RETURN_VALUE_ERROR;
         gp_context * c = (gp_context *)context;
         if (!c->has_geometry) return GPUMAS_RETURN_MEDIUM_ERROR;
-        if (c->has_locals) return GPUMAS_RETURN_VALUE_ERROR;
         gp_config cfg;
         int rc = gp_config_check(context, c->physics, &cfg);
         if (rc != GPUMAS_RETURN_SUCCESS) return rc;
@@ -2011,9 +2101,18 @@ extern "C" int gp_api_context_transport_device_static(
         const int batch = 16;
         unsigned long long seen_cursor = 0, seen_progress = 0;
         for (;;) {
-                for (int k = 0; k < batch; k++)
-                        gp_iteration(c->d_tables, v, grid_step, k, s);
-                gp_batch_end(c->d_tables, v, s);
+                for (int k = 0; k < batch; k++) {
+                        if (c->has_locals)
+                                gp_iteration<1>(c->d_tables, v, grid_step, k,
+                                    s);
+                        else
+                                gp_iteration<0>(c->d_tables, v, grid_step, k,
+                                    s);
+                }
+                if (c->has_locals)
+                        gp_batch_end<1>(c->d_tables, v, s);
+                else
+                        gp_batch_end<0>(c->d_tables, v, s);
                 rc = gp_check(cudaGetLastError());
                 gp_counters hc;
                 if (rc == GPUMAS_RETURN_SUCCESS)

@@ -376,7 +376,9 @@ static int gp_run(gp_context * c, const gp_config & cfg, const gp_io & io,
         if (engine == 0) engine = gp_needs_stepping(c, cfg) ? 2 : 1;
         int rc;
         cudaEventRecord(c->t0, s);
-        if (c->recording || c->has_locals) {
+        /* The recorder runs on the one thread per event kernel; media with
+         * local properties run on it or on the slot pool. */
+        if (c->recording || (c->has_locals && (engine != 2))) {
                 const unsigned int grid =
                     (unsigned int)((n + gp_block - 1) / gp_block);
                 gp_kernel_plain_ext<<<grid, gp_block, 0, s>>>(c->d_tables,

@@ -7,8 +7,8 @@ Parity with the reference runs through the golden cases with locals of
 tests/cases.py in test_gpu_parity.py: the stepping cases atmosphere_* and
 iron_field, and the closed form CSDA deflection (transport_csda_deflect,
 pumas.c:4968-5171) of rock_csda_field*, water_csda_field_backward. This
-file covers the descriptor's layout, its checks and the entry points that
-do not take locals.
+file covers the descriptor's layout, its checks, and the slot pool engine
+against the one thread per event kernel on media with locals.
 """
 import ctypes
 import os
@@ -78,32 +78,47 @@ def test_bad_locals_are_refused(gpu_physics, bad):
 
 
 @pytest.mark.gpu
-def test_pool_entry_points_refuse_locals(gpu_physics):
-    """The slot pool engine and the static entry point run uniform media
-    only; a context with locals runs through gpumas_context_transport."""
+@pytest.mark.parametrize("name", ["atmosphere_forward", "atmosphere_backward",
+                                  "iron_field"])
+def test_pool_engine_runs_locals(gpu_physics, name):
+    """Media with local properties also run on the slot pool engine: the
+    context's transport with the pool tuning, and the engine's job queue
+    with a job of uniform media beside, give every event of the one thread
+    per event kernel bit for bit."""
     import pumas_gb300 as pg
-    case = CASES["atmosphere_forward"]
+    from cases import make_states
+    case = CASES[name]
     geo = gpu_geometry(gpu_physics, case["geometry"])
     ctx = gpu_context(gpu_physics, case["config"], case["seed"], geo)
-    eng = pg.Engine(gpu_physics, pool_slots=4096)
-    from cases import make_states
-    s0 = make_states("atmosphere_forward", n=8)
-    with pytest.raises(pg.PumasError) as e:
-        eng.submit_host(ctx, s0)
-    assert e.value.code == pg.RETURN_VALUE_ERROR
-    lib = pg.library()
-    fn = lib.gpumas_context_transport_device_static
-    fn.restype = ctypes.c_int
-    fn.argtypes = [ctypes.POINTER(pg._Context), ctypes.c_size_t,
-                   ctypes.POINTER(pg._Soa), ctypes.c_uint64, ctypes.c_int,
-                   ctypes.c_void_p]
-    soa = pg._Soa()
-    assert fn(ctx._ptr, 8, ctypes.byref(soa), 0, 0, None) == \
-        pg.RETURN_VALUE_ERROR
-
-    # A pool tuning does not move a context with locals off its kernel.
-    a, ra = ctx.transport(s0)
-    ctx.tuning(engine=pg.ENGINE_POOL, pool_slots=4096, max_inner=2)
-    b, rb = ctx.transport(s0)
+    s0 = make_states(name, n=400, first_event=3)
+    ctx.tuning(engine=pg.ENGINE_PLAIN)
+    a, ra = ctx.transport(s0, 3)
     assert ctx.stats()["launches"] == 1
-    assert np.array_equal(a, b) and np.array_equal(ra, rb)
+    ctx.tuning(engine=pg.ENGINE_POOL, pool_slots=4096, max_inner=2,
+               batch=4)
+    b, rb = ctx.transport(s0, 3)
+    assert ctx.stats()["launches"] > 1
+    assert a.tobytes() == b.tobytes()
+    assert ra.tobytes() == rb.tobytes()
+
+    rock = CASES["rock_slab"]
+    ctx2 = gpu_context(gpu_physics, rock["config"], rock["seed"],
+                       gpu_geometry(gpu_physics, rock["geometry"]))
+    s2 = make_states("rock_slab", n=300)
+    ctx2.tuning(engine=pg.ENGINE_PLAIN)
+    c, rc = ctx2.transport(s2, 0)
+    eng = pg.Engine(gpu_physics, pool_slots=4096, max_inner=2, batch=4,
+                    state_budget=1 << 28)
+    t2 = eng.submit_host(ctx2, s2, 0)
+    t1 = eng.submit_host(ctx, s0, 3)
+    done = set()
+    for _ in range(100000):
+        got, pending = eng.step()
+        done.update(got)
+        if {t1, t2} <= done:
+            break
+    assert {t1, t2} <= done
+    d, rd = eng.result(t1)
+    assert a.tobytes() == d.tobytes() and ra.tobytes() == rd.tobytes()
+    d, rd = eng.result(t2)
+    assert c.tobytes() == d.tobytes() and rc.tobytes() == rd.tobytes()

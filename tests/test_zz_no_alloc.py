@@ -131,3 +131,36 @@ def pg_static_slots():
     from conftest import ROOT
     text = open(os.path.join(ROOT, "include", "gpumas.h")).read()
     return int(re.search(r"#define GPUMAS_STATIC_SLOTS (\d+)", text).group(1))
+
+
+def test_static_pool_runs_locals(gpu_physics):
+    """Media with local properties through the static pool: every event as
+    on the one thread per event kernel, bit for bit."""
+    torch = pytest.importorskip("torch")
+    import pumas_gb300 as pg
+    from cases import CASES, make_states
+    from conftest import gpu_context, gpu_geometry
+
+    lib = pg.library()
+    fn = lib.gpumas_context_transport_device_static
+    fn.restype = ctypes.c_int
+    fn.argtypes = [ctypes.POINTER(pg._Context), ctypes.c_size_t,
+                   ctypes.POINTER(pg._Soa), ctypes.c_uint64, ctypes.c_int,
+                   ctypes.c_void_p]
+    case = CASES["atmosphere_forward"]
+    geo = gpu_geometry(gpu_physics, case["geometry"])
+    ctx = gpu_context(gpu_physics, case["config"], case["seed"], geo)
+    s0 = make_states("atmosphere_forward", n=300, first_event=11)
+    ctx.tuning(engine=pg.ENGINE_PLAIN)
+    a, ra = ctx.transport(s0, 11)
+    ctx.tuning(engine=pg.ENGINE_POOL, max_inner=2)
+    cols = _columns(torch, s0)
+    soa = _soa(pg, cols)
+    assert fn(ctx._ptr, len(s0), ctypes.byref(soa), 11, 2048, None) == 0
+    torch.cuda.synchronize()
+    b = _host(pg, cols)
+    assert a["energy"].tobytes() == b["energy"].tobytes()
+    assert a["time"].tobytes() == b["time"].tobytes()
+    assert a["position"][:, 2].tobytes() == b["p2"].tobytes()
+    assert a["direction"][:, 0].tobytes() == b["d0"].tobytes()
+    assert ra.tobytes() == b["result"].tobytes()
