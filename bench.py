@@ -26,6 +26,7 @@ One step transports the whole batch. Timed legs:
 import argparse
 import json
 import os
+import platform
 import subprocess
 import sys
 import threading
@@ -45,9 +46,14 @@ F_STEP = 680.4
 F_STEP_EXECUTED = 681.7
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum over every pool
 # kernel launch) per reference step, from one ncu launch list of two
-# 2e6-event rock slab batches (612.4 GB over 1.0957e9 steps); the traffic
+# 2e6-event rock slab batches (820.2 GB over 1.0957e9 steps); the traffic
 # of a batch is this times its steps.
-TRAFFIC_STEP = 559.0
+TRAFFIC_STEP = 749.0
+# The plain CSDA workload (closed form transport_with_csda, one thread per
+# event): FP64 flops per event (DADD and DMUL 1, DFMA 2) and DRAM bytes per
+# event, from one ncu capture of 2e7 events.
+F_CSDA = 101.0
+TRAFFIC_CSDA = 197.0
 
 
 def parse():
@@ -237,6 +243,23 @@ def cpu_baseline(n_events, seed, first_event=0, single=True):
                              "sample": "the first %d events of the same "
                                        "sample on 1 thread, %.1f s" % (m, d1)}
         out["thread_scaling"] = out["value"] / out["one_thread"]["value"]
+        # The reference computes the Coulomb functions of hard scatters in
+        # long double, which aarch64 implements in software (IEEE quad):
+        # the same sample through the port built with double there.
+        try:
+            dbl = oracle.PortDouble(pg.default_dump(), private=True)
+            t0 = time.perf_counter()
+            _, r2 = dbl.transport(cfg, geo, s0[:m], first_event, 1)
+            d2 = time.perf_counter() - t0
+            out["one_thread_coulomb_double"] = {
+                "value": m / d2, "unit": "events/s",
+                "same_steps": bool(np.array_equal(
+                    r2["steps"], r[:m]["steps"])),
+                "note": "the port with its Coulomb functions in double "
+                        "instead of the reference's long double (%s); "
+                        "not a baseline" % platform.machine()}
+        except (OSError, RuntimeError):
+            pass
     return out
 
 
@@ -824,6 +847,7 @@ def run_plain_csda(args, rank, world, local):
     hbm = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))[
         "hbm_gbs"] if os.path.exists(os.path.join(
             ROOT, "MEASURED_PEAKS.json")) else 6800.
+    peak = fp64_peak_tflops(torch)
     # 8 B in (kinetic energy) + 32 B out (energy, distance, grammage,
     # time) per event; position z is also written (8 B).
     algo = 48. * n
@@ -847,12 +871,15 @@ def run_plain_csda(args, rank, world, local):
     line.update({
         "cpu_baseline": cpu,
         "kernel_ms": kernel_ms,
-        "roofline": {"bound": "hbm",
-                     "achieved": algo / (kernel_ms * 1E-03) * 1E-09,
-                     "peak": hbm, "unit": "GB/s",
-                     "frac": algo / (kernel_ms * 1E-03) * 1E-09 / hbm,
-                     "traffic": None,
-                     "algorithmic_bytes_per_event": 48},
+        "roofline": {"bound": "fp64",
+                     "achieved": F_CSDA * n / (kernel_ms * 1E-03) * 1E-12,
+                     "peak": peak, "unit": "TFLOP/s",
+                     "frac": F_CSDA * n / (kernel_ms * 1E-03) * 1E-12 / peak,
+                     "traffic": TRAFFIC_CSDA * n, "flops_per_event": F_CSDA,
+                     "hbm": {"achieved": algo / (kernel_ms * 1E-03) * 1E-09,
+                             "peak": hbm, "unit": "GB/s",
+                             "frac": algo / (kernel_ms * 1E-03) * 1E-09 / hbm,
+                             "algorithmic_bytes_per_event": 48}},
         "gpu_launches": 1, "clocks": clocks.summary()})
     print(json.dumps(line), flush=True)
 

@@ -237,6 +237,13 @@ class Port(_Oracle):
         return self.lib.oracle_port_uniform(seed, domain, event, n)
 
 
+class PortDouble(Port):
+    """The C restatement with its Coulomb functions in double instead of the
+    reference's long double (port.c, ORACLE_COULOMB_DOUBLE): only for timing
+    how much of the CPU baseline the long double arithmetic costs."""
+    path = os.path.join(HERE, "_build", "liboracle_port_double.so")
+
+
 class Reference(_Oracle):
     """The reference library driven as an oracle (ref_harness.c)."""
     prefix = "oracle_ref"

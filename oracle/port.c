@@ -42,6 +42,19 @@
 #include "oracle.h"
 #include "philox.h"
 
+/* The reference computes the Coulomb pole reduction and transport
+ * coefficients in long double (pumas.c:7524-7683): 80 bit extended on
+ * x86-64, IEEE quad in software on aarch64. ORACLE_COULOMB_DOUBLE builds a
+ * copy in double, used only to show how much of the CPU baseline's time that
+ * costs on a given host; the oracle itself is the long double build. */
+#ifdef ORACLE_COULOMB_DOUBLE
+typedef double coulomb_real;
+#define coulomb_log log
+#else
+typedef long double coulomb_real;
+#define coulomb_log logl
+#endif
+
 /* ------------------------------------------------------------------------ */
 /* Constants (pumas.c:53-200) and public enum values (pumas.h:90-278).      */
 /* ------------------------------------------------------------------------ */
@@ -1282,45 +1295,45 @@ static void coulomb_frame_parameters(double Z, double A, double mass,
 
 /* coulomb_pole_reduction (pumas.c:7524-7576), in extended precision. */
 static void coulomb_pole_reduction(int n_parameters, const double * amplitude,
-    const double * screening, long double * a, long double * b,
-    long double * c)
+    const double * screening, coulomb_real * a, coulomb_real * b,
+    coulomb_real * c)
 {
         const int n = n_parameters - 1;
         int i, j;
         for (i = 0; i < n; i++) a[i] = b[i] = 0;
         for (i = 0; i < 4; i++) c[i] = 0;
         for (i = 0; i < n; i++) {
-                const long double Ai = amplitude[i];
-                const long double Bi = screening[i];
+                const coulomb_real Ai = amplitude[i];
+                const coulomb_real Bi = screening[i];
                 b[i] = Ai * Ai;
                 for (j = i + 1; j < n; j++) {
-                        const long double Aj = amplitude[j];
-                        const long double Bj = screening[j];
-                        const long double d = 2 * Ai * Aj / (Bj - Bi);
+                        const coulomb_real Aj = amplitude[j];
+                        const coulomb_real Bj = screening[j];
+                        const coulomb_real d = 2 * Ai * Aj / (Bj - Bi);
                         a[i] += d;
                         a[j] -= d;
                 }
         }
-        const long double N = screening[n];
-        long double Sa[4] = { 0, 0, 0, 0 }, Sb[4] = { 0, 0, 0, 0 };
+        const coulomb_real N = screening[n];
+        coulomb_real Sa[4] = { 0, 0, 0, 0 }, Sb[4] = { 0, 0, 0, 0 };
         for (i = 0; i < n; i++) {
-                const long double Bi = screening[i];
-                const long double x = 1. - Bi / N;
-                long double r = x;
+                const coulomb_real Bi = screening[i];
+                const coulomb_real x = 1. - Bi / N;
+                coulomb_real r = x;
                 for (j = 0; j < 4; j++) {
                         Sa[j] += a[i] / r;
                         r *= x;
                         Sb[j] += b[i] / r;
                 }
         }
-        long double tmp = 1;
+        coulomb_real tmp = 1;
         for (i = 0; i < 4; i++) {
                 c[i] = ((4 - i) * Sb[3 - i] / N - Sa[3 - i]) * tmp;
                 tmp *= N;
         }
         for (i = 0; i < n; i++) {
-                const long double Bi = screening[i];
-                long double d = 1. - Bi / N;
+                const coulomb_real Bi = screening[i];
+                coulomb_real d = 1. - Bi / N;
                 d *= d;
                 d *= d;
                 a[i] = (a[i] - 4 * b[i] / (N - Bi)) / d;
@@ -1330,44 +1343,44 @@ static void coulomb_pole_reduction(int n_parameters, const double * amplitude,
 
 /* coulomb_transport_coefficients (pumas.c:7623-7683). */
 static void coulomb_transport_coefficients(double mu_, double fspin,
-    int n_parameters, const double * screening, const long double * a,
-    const long double * b, const long double * c, double * coefficient)
+    int n_parameters, const double * screening, const coulomb_real * a,
+    const coulomb_real * b, const coulomb_real * c, double * coefficient)
 {
-        const long double S = fspin;
-        const long double mu = mu_;
+        const coulomb_real S = fspin;
+        const coulomb_real mu = mu_;
         const int n = n_parameters - 1;
         double cs0 = 0., cs1 = 0.;
         int i;
         for (i = 0; i < n; i++) {
-                const long double alp = screening[i];
-                const long double r = mu / (mu + alp);
-                const long double L = logl(1. + mu / alp);
-                const long double I0 = r / alp;
-                const long double J0 = L;
-                const long double I1 = L - r;
-                const long double J1 = -alp * L;
-                const long double I2 = mu + alp * (r - 2. * L);
-                const long double J2 = alp * (alp * L - mu);
+                const coulomb_real alp = screening[i];
+                const coulomb_real r = mu / (mu + alp);
+                const coulomb_real L = coulomb_log(1. + mu / alp);
+                const coulomb_real I0 = r / alp;
+                const coulomb_real J0 = L;
+                const coulomb_real I1 = L - r;
+                const coulomb_real J1 = -alp * L;
+                const coulomb_real I2 = mu + alp * (r - 2. * L);
+                const coulomb_real J2 = alp * (alp * L - mu);
                 cs0 += a[i] * (J0 - S * J1) + b[i] * (I0 - S * I1);
                 cs1 += a[i] * (J1 - S * J2) + b[i] * (I1 - S * I2);
         }
-        const long double N = screening[n];
-        const long double r = mu / (mu + N);
-        const long double L = logl(1. + mu / N);
-        const long double I0 = r / N;
-        const long double J0 = L;
-        const long double I1 = L - r;
-        const long double J1 = -N * L;
-        const long double I2 = mu + N * (r - 2. * L);
-        const long double J2 = N * (N * L - mu);
-        const long double rn = 1. / (1. + mu / N);
-        const long double K0 = (1. - rn) * (1. + rn) / (2 * N * N);
-        const long double L0 =
+        const coulomb_real N = screening[n];
+        const coulomb_real r = mu / (mu + N);
+        const coulomb_real L = coulomb_log(1. + mu / N);
+        const coulomb_real I0 = r / N;
+        const coulomb_real J0 = L;
+        const coulomb_real I1 = L - r;
+        const coulomb_real J1 = -N * L;
+        const coulomb_real I2 = mu + N * (r - 2. * L);
+        const coulomb_real J2 = N * (N * L - mu);
+        const coulomb_real rn = 1. / (1. + mu / N);
+        const coulomb_real K0 = (1. - rn) * (1. + rn) / (2 * N * N);
+        const coulomb_real L0 =
             (1. - rn) * ((1. + rn) * (1. + rn) - rn) / (3 * N * N * N);
-        const long double K1 = I0 - N * K0;
-        const long double L1 = K0 - N * L0;
-        const long double K2 = I1 - N * K1;
-        const long double L2 = K1 - N * L1;
+        const coulomb_real K1 = I0 - N * K0;
+        const coulomb_real L1 = K0 - N * L0;
+        const coulomb_real K2 = I1 - N * K1;
+        const coulomb_real L2 = K1 - N * L1;
         cs0 += c[0] * (J0 - S * J1) + c[1] * (I0 - S * I1) +
             c[2] * (K0 - S * K1) + c[3] * (L0 - S * L1);
         cs1 += c[0] * (J1 - S * J2) + c[1] * (I1 - S * I2) +
@@ -1378,8 +1391,8 @@ static void coulomb_transport_coefficients(double mu_, double fspin,
 
 /* coulomb_restricted_cs (pumas.c:7591-7609). */
 static double coulomb_restricted_cs(double mu, double fspin, int n_parameters,
-    const double * screening, const long double * a, const long double * b,
-    const long double * c)
+    const double * screening, const coulomb_real * a, const coulomb_real * b,
+    const coulomb_real * c)
 {
         if ((mu >= 1.) || (mu >= 1E+06 * screening[n_parameters - 1]))
                 return 0.;
@@ -2720,7 +2733,7 @@ struct coulomb_data {
         int n_parameters;
         double amplitude[3];
         double screening[4];
-        long double a[3], b[3], c[4];
+        coulomb_real a[3], b[3], c[4];
         double fspin;
         double fCM[2];
 };

@@ -535,9 +535,13 @@ GPD double gp_coulomb_ehs_length(
 /* ------------------------------------------------------------------------ */
 
 /* coulomb_screening_parameters (pumas.c:7203-7387) with the element's
- * Salvat amplitudes and exponents from the host. */
+ * Salvat amplitudes and exponents from the host. The reference stores the
+ * nuclear screening after the n atomic ones (screening[n]); here it is
+ * returned in N, so that every array index is a constant once the loops
+ * are unrolled and the arrays stay in registers. Returns n + 1. */
 GPD int gp_coulomb_screening(const gp_element & el, double mass,
-    double kinetic, double kinetic0, double * amplitude, double * screening)
+    double kinetic, double kinetic0, double * amplitude, double * screening,
+    double & N)
 {
         const double Z = el.Z;
         const double aZE = GP_ALPHA_EM * Z * (kinetic + mass);
@@ -568,7 +572,7 @@ GPD int gp_coulomb_screening(const gp_element & el, double mass,
                         screening[i] = d * a * a;
                 }
         }
-        screening[n] = 12. * d / (el.RN * el.RN);
+        N = 12. * d / (el.RN * el.RN);
         return n + 1;
 }
 
@@ -626,9 +630,9 @@ GPD void gp_coulomb_frame_parameters(double Ma, double mass, double kinetic,
         parameters[1] = sqrt(rM2 * (1. - betaCM2) + betaCM2);
 }
 
-/* coulomb_pole_reduction (pumas.c:7524-7576). */
+/* coulomb_pole_reduction (pumas.c:7524-7576), N = screening[n]. */
 GPD void gp_coulomb_pole_reduction(int n_parameters, const double * amplitude,
-    const double * screening, double * a, double * b, double * c)
+    const double * screening, double N, double * a, double * b, double * c)
 {
         const int n = n_parameters - 1;
         for (int i = 0; i < 3; i++) a[i] = b[i] = 0.;
@@ -646,7 +650,6 @@ GPD void gp_coulomb_pole_reduction(int n_parameters, const double * amplitude,
                         a[j] -= d;
                 }
         }
-        const double N = screening[n];
         double Sa[4] = { 0, 0, 0, 0 }, Sb[4] = { 0, 0, 0, 0 };
         for (int i = 0; i < 3; i++) {
                 if (i >= n) break;
@@ -674,9 +677,10 @@ GPD void gp_coulomb_pole_reduction(int n_parameters, const double * amplitude,
         }
 }
 
-/* coulomb_transport_coefficients, order 0 only (pumas.c:7623-7683). */
+/* coulomb_transport_coefficients, order 0 only (pumas.c:7623-7683),
+ * N = screening[n]. */
 GPD double gp_coulomb_cs0(double mu, double S, int n_parameters,
-    const double * screening, const double * a, const double * b,
+    const double * screening, double N, const double * a, const double * b,
     const double * c)
 {
         const int n = n_parameters - 1;
@@ -692,7 +696,6 @@ GPD double gp_coulomb_cs0(double mu, double S, int n_parameters,
                 const double J1 = -alp * L;
                 cs0 += a[i] * (J0 - S * J1) + b[i] * (I0 - S * I1);
         }
-        const double N = screening[n];
         const double r = mu / (mu + N);
         const double L = gp_log(1. + mu / N);
         const double I0 = r / N;
@@ -710,17 +713,17 @@ GPD double gp_coulomb_cs0(double mu, double S, int n_parameters,
         return cs0;
 }
 
-/* coulomb_restricted_cs (pumas.c:7591-7609). */
+/* coulomb_restricted_cs (pumas.c:7591-7609), N = screening[n]. */
 GPD double gp_coulomb_restricted_cs(double mu, double fspin, int n_parameters,
-    const double * screening, const double * a, const double * b,
+    const double * screening, double N, const double * a, const double * b,
     const double * c)
 {
-        if ((mu >= 1.) || (mu >= 1E+06 * screening[n_parameters - 1]))
+        if ((mu >= 1.) || (mu >= 1E+06 * N))
                 return 0.;
         const double cs0 =
-            gp_coulomb_cs0(1., fspin, n_parameters, screening, a, b, c);
+            gp_coulomb_cs0(1., fspin, n_parameters, screening, N, a, b, c);
         const double cs = gp_coulomb_cs0(mu, fspin, n_parameters, screening,
-            a, b, c);
+            N, a, b, c);
         if (cs > cs0)
                 return 0;
         else
@@ -2131,21 +2134,21 @@ static __device__ __forceinline__ void gp_do_ehs(const gp_tables & T, const gp_c
                 for (int i = 0; i < n_el; i++) {
                         const gp_element & el =
                             T.element[__ldg(T.comp_element + ic0 + i)];
-                        double kinetic0, fCM[2], amplitude[3], screening[4];
-                        double a[3], b[3], c[4];
+                        double kinetic0, fCM[2], amplitude[3], screening[3];
+                        double N, a[3], b[3], c[4];
                         gp_coulomb_frame_parameters(
                             el.Ma, T.mass, kinetic, kinetic0, fCM);
                         const int np = gp_coulomb_screening(el, T.mass,
-                            kinetic, kinetic0, amplitude, screening);
+                            kinetic, kinetic0, amplitude, screening, N);
                         gp_coulomb_pole_reduction(
-                            np, amplitude, screening, a, b, c);
+                            np, amplitude, screening, N, a, b, c);
                         const double normalisation =
                             __ldg(T.comp_fraction + ic0 + i) /
                             gp_coulomb_normalisation(
                                 el.Z, el.A, T.mass, kinetic, kinetic0);
                         cs_hard[i] = normalisation *
                             gp_coulomb_restricted_cs(
-                                mu0, fspin, np, screening, a, b, c);
+                                mu0, fspin, np, screening, N, a, b, c);
                         cs_tot += cs_hard[i];
                 }
                 const double cc0 = gp_random(e) * cs_tot;
@@ -2163,10 +2166,10 @@ static __device__ __forceinline__ void gp_do_ehs(const gp_tables & T, const gp_c
         }
 
         const gp_element & el = T.element[__ldg(T.comp_element + ic0 + ihard)];
-        double kinetic0, fCM[2], amplitude[3], screening[4];
+        double kinetic0, fCM[2], amplitude[3], screening[3], N;
         gp_coulomb_frame_parameters(el.Ma, T.mass, kinetic, kinetic0, fCM);
         const int np = gp_coulomb_screening(
-            el, T.mass, kinetic, kinetic0, amplitude, screening);
+            el, T.mass, kinetic, kinetic0, amplitude, screening, N);
         const int n = np - 1;
         double A = screening[0];
         for (int i = 1; i < 3; i++) {
@@ -2189,7 +2192,7 @@ static __device__ __forceinline__ void gp_do_ehs(const gp_tables & T, const gp_c
                         if (k >= n) break;
                         ratio += amplitude[k] * (A + mu1) / (screening[k] + mu1);
                 }
-                ratio *= gp_coulomb_nuclear_form_factor(mu1, screening[n]);
+                ratio *= gp_coulomb_nuclear_form_factor(mu1, N);
                 ratio *= ratio * (1. - fspin * mu1);
                 if (gp_random(e) <= ratio) break;
         }
