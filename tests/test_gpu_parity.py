@@ -7,16 +7,18 @@ Tolerance: 1E-09 relative on energy, distance, grammage, time, weight,
 position and direction (absolute floor of 1E-09 near zero), identical end
 events, media and status. At least 99.9 % of all golden events within
 tolerance, all of them for deterministic CSDA; in every stochastic case at
-least 98 % within 1E-09, every event but at most one within 1E-06 (no other
-trajectory differs), and KS / chi-square tests (p > 0.01) on the final
-states. The fraction of each case is printed at the end of the run.
+least 99.9 % within 1E-09 and every event within 1E-06, and KS / chi-square
+tests (p > 0.01) on the final states. The inputs are fixed and the device
+results deterministic, so these gates do not flake. The fraction of each
+case is printed at the end of the run.
 
-Why a case can miss 1E-09 without any fault: the device's libm (log, exp,
-sincos) and its products round differently from glibc in the last bit now
-and then; such differences stay at 1e-16 relative along a track, except for
-a muon that ranges out, whose last step is the difference of two nearly
-equal ranges and amplifies them to 1e-8 (water_grammage_limit and
-water_time_limit have one and three such events).
+Why an event could miss 1E-09 without any fault: CUDA's pow, sin, cos and
+atan can round differently from glibc's in the last bit; such differences
+stay at 1e-16 relative along a track, unless a rejection test flips on
+one. Every product and sum is otherwise rounded as in the reference (the
+build does not fuse multiply-adds, table lookups divide as the reference
+does): a muon that ranges out, whose last step is the difference of two
+nearly equal ranges, would otherwise amplify a last bit to 1e-8.
 
 Backward weights included: the backward DEL weight multiplies single
 precision DCS interpolations (pumas.c:6036-6093, 6214-6230, 11276-11346),
@@ -40,9 +42,9 @@ RTOL = 1E-09
 # Fraction of the events of one stochastic case that must agree within
 # RTOL; events of a case allowed beyond LOOSE; fraction of all golden
 # events within RTOL.
-CASE_FRACTION = 0.98
+CASE_FRACTION = 0.999
 LOOSE = 1E-06
-CASE_BEYOND_LOOSE = 1
+CASE_BEYOND_LOOSE = 0
 AGGREGATE_FRACTION = 0.999
 
 
