@@ -305,7 +305,7 @@ def test_gpu_carry_requires_results(gpu_physics):
         ctx._ptr, 2) == pg.RETURN_VALUE_ERROR
 
 
-def test_gpu_statistics_north_star_size(gpu_physics, port):
+def test_gpu_statistics_rock_slab_1e7(gpu_physics, port):
     """The rock slab workload at its full size, 1e7 events, on the GPU;
     the C restatement over all host cores on a seeded subset of 1e6 of
     them (event ids 0 .. 999 999: initial states are drawn per event id,
