@@ -40,7 +40,7 @@ sys.path.insert(0, ROOT)
 # workload: FP64 flops (DADD, DMUL: 1, DFMA: 2, per thread) counted by ncu
 # on the one thread per event restatement of the algorithm (gp_kernel_plain)
 # over 20 000 rock slab events (5 482 614 steps), frozen here. The pool
-# engine's own executed count over the same events (its four kernels) is
+# engine's own executed count over the same events (its kernels) is
 # reported beside it.
 F_STEP = 680.4
 F_STEP_EXECUTED = 681.7
