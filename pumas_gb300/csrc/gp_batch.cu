@@ -9,30 +9,36 @@
  * start to end makes a warp wait on its slowest lane at every such branch.
  *
  * This engine keeps a pool of P event slots in device memory (structure of
- * arrays, sized to stay resident in L2) and advances all of them one
- * iteration at a time with one kernel per step kind:
+ * arrays) and advances all of them one iteration at a time with one kernel
+ * per step kind:
  *
- *   0. gp_pool_drain: clears the previous iteration's lists and, once the
- *      queue is empty and few slots remain active, runs their events to
- *      the end in one launch (otherwise it returns at once).
- *   1. gp_pool_step: every slot makes its continuous step(s). Empty slots are
- *      first refilled from the input (a device work queue: an atomic cursor
- *      over the events of every job). Slots whose step ended on a DEL or an
- *      EHS are appended to the DEL or EHS list with warp aggregated atomics
- *      (a ballot and prefix count per warp), so that the lists are compact.
- *   2. gp_pool_del: one thread per listed DEL, full warps; photonuclear
+ *   0. gp_pool_drain: clears the consumed lists and, once the queue is
+ *      empty and few slots remain active, runs their events to the end in
+ *      one launch (otherwise it returns at once).
+ *   1. gp_pool_fill: slot turnover. Events that ended in the last step
+ *      kernel are written back to the caller's arrays at their input index;
+ *      empty slots are refilled from the input (a device work queue: an
+ *      atomic cursor over the events of every job).
+ *   2. gp_pool_step: every slot in the step phase makes its continuous
+ *      step(s). Slots whose step ended on a DEL or an EHS are appended to
+ *      the DEL or EHS list with warp aggregated atomics (a ballot and prefix
+ *      count per warp), so that the lists are compact.
+ *   3. gp_pool_del: one thread per listed DEL, full warps; photonuclear
  *      polar angles are deferred to
- *   3. gp_pool_polar: Brent search and rejection in lockstep, with refill;
- *   4. gp_pool_ehs: one thread per listed EHS, full warps.
+ *   4. gp_pool_polar: Brent search and rejection in lockstep, with refill,
+ *      on a second graph stream beside the next kernels;
+ *   5. gp_pool_ehs: one thread per listed EHS, full warps.
  *
- * Finished events are written back to the caller's arrays at their input
- * index and their slot is refilled at the next iteration. Per event results
- * are identical to the one thread per event kernel: the random stream of an
- * event depends only on (seed, event id), and an event's draws are consumed
- * in the same order whichever slot, warp or kernel executes them.
+ * Each kernel is built twice (template <int LOC>): without the code of the
+ * media's local properties, and with it for jobs whose geometry has them.
+ * Per event results are identical to the one thread per event kernel: the
+ * random stream of an event depends only on (seed, event id), and an
+ * event's draws are consumed in the same order whichever slot, warp or
+ * kernel executes them.
  *
  * The host runs the iterations in batches captured in a CUDA graph and reads
- * two counters (input cursor, active slots) after each batch to stop.
+ * the counters (input cursor, active slots, completed jobs) after each
+ * batch to stop or to report completions.
  */
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
