@@ -129,6 +129,30 @@ def test_port_matches_reference_fresh_events(request, reference, name):
     assert np.array_equal(ra["draws"], rb["draws"])
 
 
+@pytest.mark.parametrize("name", ["rock_slab", "stack_backward_mixed",
+                                  "water_time_limit"])
+def test_coulomb_in_double_changes_no_event(name):
+    """The reference evaluates the Coulomb functions of hard scatters in long
+    double (pumas.c:7524-7683); the copy of the port built with double
+    there (timed beside the CPU baseline) transports the same events to the
+    same final states, bit for bit, on this host."""
+    import oracle
+    from cases import physics_dump
+    oracle.build_port()
+    dump = physics_dump("muon")
+    case = CASES[name]
+    s0 = make_states(name, n=600, first_event=4242)
+    out = []
+    for cls in (oracle.Port, oracle.PortDouble):
+        o = cls(dump, private=True)
+        geo = oracle_geometry(o, case["geometry"])
+        cfg = oracle_config(case["config"], case["seed"])
+        out.append(o.transport(cfg, geo, s0, 4242, 4))
+    (a, ra), (b, rb) = out
+    assert a.tobytes() == b.tobytes()
+    assert ra.tobytes() == rb.tobytes()
+
+
 def test_port_edge_cases(port):
     """Empty batches, bad directions, start outside the geometry and
     decayed states follow pumas.c:3135-3192."""
