@@ -158,6 +158,19 @@ def test_atmosphere_workload_on_the_oracle():
     assert cpu["value"] > 0. and cpu["kind"] == "port"
 
 
+def test_cpu_baseline_explains_itself():
+    """The CPU baseline of the bench line reports the host's cores, the
+    OpenMP threads, the one thread rate, the thread scaling and the rate
+    with the Coulomb functions in double, on the same events."""
+    import bench
+    cpu = bench.cpu_baseline(400, 7)
+    for key in ("value", "cores", "nproc", "omp_max_threads", "one_thread",
+                "thread_scaling", "one_thread_coulomb_double"):
+        assert key in cpu, key
+    assert cpu["kind"] == "port" and cpu["value"] > 0.
+    assert cpu["one_thread_coulomb_double"]["same_steps"]
+
+
 def test_atmosphere_geometry_descriptor():
     """The bench's device geometry: the ctypes descriptor carries the
     locals of both media."""
