@@ -1,6 +1,6 @@
 """gpumas_physics_upload: the device physics from a live struct
 pumas_physics, the path a C program that created or loaded its physics
-with the reference takes (include/gpumas.h; INTEGRATION.md section 2).
+with the reference takes (include/gpumas.h).
 
 A live struct is the dump's blob whose pointers have been moved to the
 addresses of this process (pumas_physics_load, pumas.c:2096-2122).
