@@ -1099,19 +1099,29 @@ def main():
                             first_event=first)
     # The batched-jobs and serving targets, measured once after the timed
     # region on this rank's GPU.
+    # A failure of one of them is recorded in its object; the line of the
+    # timed region above is printed all the same.
     c3 = c4 = None
     if rank == 0 and not args.no_c3:
-        c3 = measure_slab_jobs(args, physics, dev, args.c3_scale, 1, 1,
-                               baseline=not args.no_baseline)
-        c3["workload"] = ("slab_jobs: %d uneven jobs, 1-8 slabs of rock / "
-                          "water / iron, 50/50 forward / backward, "
-                          "straggled + mixed, events per job x %g"
-                          % (c3["jobs"], c3["event_scale"]))
+        try:
+            c3 = measure_slab_jobs(args, physics, dev, args.c3_scale, 1, 1,
+                                   baseline=not args.no_baseline)
+            c3["workload"] = ("slab_jobs: %d uneven jobs, 1-8 slabs of "
+                              "rock / water / iron, 50/50 forward / "
+                              "backward, straggled + mixed, events per job "
+                              "x %g" % (c3["jobs"], c3["event_scale"]))
+        except (RuntimeError, MemoryError, pg.PumasError) as err:
+            c3 = {"error": "%s: %s" % (type(err).__name__, err)}
+        torch.cuda.empty_cache()
     if rank == 0 and not args.no_c4:
         from pumas_gb300 import serving
-        c4 = serving.sweep(physics, [float(x) for x in
-                                     args.rates.split(",")],
-                           args.serve_seconds, args.serve_scale, args.seed)
+        try:
+            c4 = serving.sweep(physics, [float(x) for x in
+                                         args.rates.split(",")],
+                               args.serve_seconds, args.serve_scale,
+                               args.seed)
+        except (RuntimeError, MemoryError, pg.PumasError) as err:
+            c4 = {"error": "%s: %s" % (type(err).__name__, err)}
     if rank != 0:
         return
     line = {
